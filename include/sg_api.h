@@ -1,0 +1,265 @@
+/*
+ * sg_api.h - C ABI of sgmd, a GB300 (sm_103a) implementation of the SurfaceGrowthConsole
+ * per-timestep force and integration path.
+ *
+ * Two layers are exported by libsgmd.so:
+ *
+ *  1. The reference's own wrapper ABI (sg_refcompat.h): CudaInitW, SetParametersW,
+ *     InitCoordsW, DoComputationsW, with the reference's SimParams bytes
+ *     (SurfaceGrowthConsole/SurfaceGrowth.h:217-235), so the reference's host program links
+ *     against this library unchanged.
+ *
+ *  2. The finer sg_* API below.  Every call returns an int status (SG_OK == 0), never calls
+ *     exit(), keeps no global simulation state (everything hangs off an sg_ctx) and takes
+ *     plain pointers and sizes.  Host arrays use the reference's layouts: positions are
+ *     float4 {x,y,z,U} (U = per-atom potential energy, written by the force pass), velocities
+ *     and accelerations float3, all in the reference's atom order (metal atoms first).
+ *
+ * A context holds one or more independent replicas (systems).  Each replica is described by
+ * one sg_simparams, i.e. exactly what the reference's SetParams() derives from sugr_in.txt;
+ * all replicas of a context advance together and share one launch per kernel phase.
+ *
+ * Status codes other than SG_OK leave a message retrievable with sg_last_error().
+ */
+#ifndef SG_API_H
+#define SG_API_H
+
+#include "sg_simparams.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SG_API_VERSION 1
+
+/* ---- status codes -------------------------------------------------------------------- */
+enum {
+    SG_OK = 0,
+    SG_ERR_INVALID = 1,        /* bad argument or inconsistent parameters */
+    SG_ERR_CUDA = 2,           /* CUDA runtime error */
+    SG_ERR_NOMEM = 3,          /* device or host allocation failed */
+    SG_ERR_NO_DEVICE = 4,      /* no CUDA device, or not an sm_103 device */
+    SG_ERR_NEBR_OVERFLOW = 5,  /* an atom had more than iNebrMax neighbours (list truncated) */
+    SG_ERR_CELL_RANGE = 6,     /* an atom mapped outside the cell grid (left out of the lists) */
+    SG_ERR_RDF_RANGE = 7,      /* an RDF bin index reached sizeHistRdf (sample dropped) */
+    SG_ERR_TIMEOUT = 8,        /* a bounded device-side wait gave up */
+    SG_ERR_IO = 9,             /* output file could not be written */
+    SG_ERR_UNSUPPORTED = 10,   /* feature not available in this mode */
+    SG_ERR_CELL_OVERFLOW = 11, /* more than blockSize (64) atoms in one cell (reference cap) */
+    SG_ERR_BAD_FILE = 12       /* malformed input or checkpoint file */
+};
+
+/* ---- modes ------------------------------------------------------------------------------ */
+enum {
+    /* FP32 throughout, arithmetic in the reference's operation order without FMA
+     * contraction, reductions in the reference's tree order.  Integer outputs (cell
+     * assignment, neighbour lists, RDF counts) are bit-exact with the reference; forces
+     * agree to within the accuracy of the CUDA/libm transcendental functions. */
+    SG_MODE_PLAIN = 0,
+    /* FP32 pair arithmetic with FMA, tabulated EAM in shared memory, FP64 accumulation of
+     * energy/virial/momentum sums, FP64 thermostat factor and MSD accumulators, and
+     * positions carried as a float hi/lo pair. */
+    SG_MODE_MIXED = 1
+};
+
+typedef struct sg_options {
+    int mode;              /* SG_MODE_PLAIN or SG_MODE_MIXED */
+    int force_rebuild;     /* 1: rebuild cell and neighbour lists every step */
+    int use_graphs;        /* 1: capture each step variant in a CUDA graph (default) */
+    int device;            /* CUDA device ordinal */
+    void *stream;          /* cudaStream_t to run on; NULL: the context creates its own */
+    int rdf_ext_bins;      /* >0: also accumulate an all-pairs metal-metal RDF */
+    float rdf_ext_range;   /* its range, dimensionless length */
+    int eam_table_knots;   /* MIXED: knots per tabulated EAM function (0: 2048) */
+    int tune_force_tpa;    /* threads per atom in the carbon force pass (0: auto) */
+    int tune_block;        /* block size of the per-atom passes (0: auto) */
+    int reserved[8];
+} sg_options;
+
+/* Initialise *opt with the defaults (PLAIN mode, graphs on, device 0). */
+void sg_default_options(sg_options *opt);
+
+typedef struct sg_ctx sg_ctx;
+
+/* Last error message of the calling thread ("" if none). */
+const char *sg_last_error(void);
+int sg_version(void);
+
+/* ---- context ------------------------------------------------------------------------------
+ * Replaces the allocation and upload half of DoComputationsW
+ * (SurfaceGrowthConsole/SurfaceGrowth.cu:2040-2126) and SetParametersW (cu:2639-2650).
+ * params points to n_replicas consecutive sg_simparams. */
+int sg_create(const sg_simparams *params, int n_replicas, const sg_options *opt, sg_ctx **out);
+int sg_destroy(sg_ctx *ctx);
+int sg_num_replicas(const sg_ctx *ctx);
+/* Number of atoms of replica rep (rep < 0: all replicas). */
+int sg_num_atoms(const sg_ctx *ctx, int rep);
+
+/* Upload / download state of one replica (rep >= 0) or of all replicas concatenated
+ * (rep == -1).  Any pointer may be NULL to skip that array.  Layouts as the reference's
+ * host arrays hr/hv/ha (SurfaceGrowth.cpp:95-96).  A download first applies a pending
+ * thermostat rescale, so it returns exactly the reference's end-of-step velocities. */
+int sg_set_state(sg_ctx *ctx, int rep, const sg_float4 *r, const sg_float3 *v, const sg_float3 *a);
+int sg_get_state(sg_ctx *ctx, int rep, sg_float4 *r, sg_float3 *v, sg_float3 *a);
+
+/* The replica's parameter block with the mutable fields (stepCount, Props, nebrNow,
+ * dispHi, shear, countRdf, ...) as the reference would hold them after the last step. */
+int sg_get_params(sg_ctx *ctx, int rep, sg_simparams *out);
+
+/* ---- stepping ------------------------------------------------------------------------------
+ * One timestep is the body of the reference loop DoComputationsW
+ * (SurfaceGrowth.cu:2141-2489) without file output: Verlet part 1 + wrap, cell/neighbour
+ * rebuild when nebrNow, EAM density, forces, friction sum, Verlet part 2, tribology
+ * reductions, nanoparticle diffusion sample, momentum/max-v2/Sum mv2, Berendsen thermostat,
+ * potential energy, rebuild criterion, shear, RDF sample, property accumulation. */
+int sg_step(sg_ctx *ctx, int nsteps);
+
+typedef struct sg_thermo {
+    int stepCount;
+    int nebrNow;            /* lists will be rebuilt at the next step */
+    int rebuilds;           /* rebuilds performed since creation */
+    int countRdf;
+    float kinEnergy, potEnergy, totEnergy; /* per-atom means, reference definition */
+    float vvSum, vvMax, uSum, dispHi;
+    sg_float3 vSum;                        /* total impulse (metal x mass-weighted) */
+    sg_float3 centerOfMass;                /* metal centre of mass (wrapped coordinates) */
+    sg_float3 cmVel;                       /* metal centre-of-mass velocity */
+    float frictForce;                      /* x force of carbon on metal */
+    sg_float3 particleSize;
+    float shear, totalShear;
+    double kinEnergy64, potEnergy64;       /* FP64 sums / nMol (MIXED; PLAIN: promoted) */
+    double virial64;                       /* pair virial sum (MIXED; 0 in PLAIN) */
+    sg_prop props[7];  /* totEnergy, potEnergy, kinEnergy, oneStep, centerOfMass, cmVel, frictForce */
+} sg_thermo;
+int sg_get_thermo(sg_ctx *ctx, int rep, sg_thermo *out);
+
+/* ---- single phases on the current state (parity checks, harness) ---------------------- */
+/* Cell binning + neighbour list from the current positions
+ * (BinAtomsIntoCellsK cu:547-609 + BuildNebrListK cu:612-711). */
+int sg_build_lists(sg_ctx *ctx);
+/* EAM density and forces on the current state (EamComputeRhoK cu:716-773,
+ * ComputeForcesK cu:776-1091): writes a, r.w and the metal friction array. */
+int sg_compute_forces(sg_ctx *ctx);
+/* One RDF sample (EvalRdfK cu:1895-1999) over the last-built cells, current positions. */
+int sg_eval_rdf(sg_ctx *ctx);
+int sg_reset_rdf(sg_ctx *ctx);
+
+/* Counting-sort result, local atom indices: cell_of_atom[nMol] (linear cell index, -1 if the
+ * atom fell outside the grid), cell_start[ncells+1], cell_atoms[nMol] (atoms grouped by cell,
+ * ascending index inside a cell). */
+int sg_get_cells(sg_ctx *ctx, int rep, int *cell_of_atom, int *cell_start, int *cell_atoms);
+int sg_num_cells(const sg_ctx *ctx, int rep);
+/* Neighbour list in the reference layout: nn[nMol], nbl[iNebrMax * nMol] column-major
+ * (entry j of atom i at nbl[j*nMol + i]), local indices, unused entries -1. */
+int sg_get_nebr(sg_ctx *ctx, int rep, int *nn, int *nbl);
+int sg_get_rho(sg_ctx *ctx, int rep, float *rho);          /* nMolMe values */
+int sg_get_friction(sg_ctx *ctx, int rep, float *fric);    /* nMolMe values */
+int sg_get_rdf(sg_ctx *ctx, int rep, unsigned int *hist);  /* sizeHistRdf counts */
+int sg_get_rdf_ext(sg_ctx *ctx, int rep, unsigned long long *hist); /* rdf_ext_bins counts */
+/* Diffusion accumulators (TBuf/rrDiffuseAv of SurfaceGrowth.cu:2021-2032): rr_av[nValDiffuse]
+ * as currently accumulated, counts[nBuffDiffuse]. */
+int sg_get_diffusion(sg_ctx *ctx, int rep, float *rr_av, int *counts, int *count_av);
+
+typedef struct sg_diag {
+    int max_neighbours;      /* largest neighbour count seen */
+    int max_cell_occupancy;  /* largest atoms-per-cell seen */
+    int nebr_overflow;       /* atoms whose list was truncated */
+    int cell_range;          /* atoms left out of the grid */
+    int cell_overflow;       /* cells above blockSize atoms */
+    int rdf_range;           /* RDF samples dropped at the top bin */
+    int timeouts;            /* bounded waits that gave up */
+    int reserved[9];
+} sg_diag;
+int sg_get_diag(sg_ctx *ctx, int rep, sg_diag *out);
+
+/* ---- whole run with the reference's outputs ------------------------------------------------
+ * Runs replica 0 to stepLimit exactly as DoComputationsW does, writing the sg_* summary rows
+ * to fResults (a FILE*), rdf_* files, sugr_*.pdb snapshots (name prefix pdb_prefix),
+ * Diffuse.txt (regime 2) and bckup0/1.sugr backups, in the reference's formats. */
+int sg_run(sg_ctx *ctx, void *fResults, const char *pdb_prefix);
+
+/* ---- configuration (host) --------------------------------------------------------------- */
+/* The 22 positional rows of sugr_in.txt (SurfaceGrowth.cpp:633-785). */
+typedef struct sg_input {
+    int iRegime, iMaterial;
+    int ucx, ucy, ucz;
+    float temperatureK;
+    int nMolMe;
+    float epsilonEv, sigmaA;
+    int stepLimit;
+    float deltaT;
+    int stepAvg, stepEquil;
+    float deltaFpN;
+    int stepCool;
+    float deposEnergyEv;
+    int nMolToDeposit, stepDeposit, stepPdb, stepRdf, bBckup, bStartBckup;
+    /* compiled-in globals of the reference that sugr_in.txt cannot set
+     * (SurfaceGrowth.cpp:35-90); sg_default_input() gives the reference values */
+    float rNebrShell;
+    int iNebrMax, stepThermostat;
+    float gammaBerendsen;
+    int limitRdf, sizeHistRdf, nValDiffuse, nBuffDiffuse, stepDiffuse, limitDiffuseAv;
+    int stepBckup, randSeed;   /* randSeed 0: time-based like the reference */
+    int bPdb, bResult, bRdf;
+} sg_input;
+void sg_default_input(sg_input *in);
+/* Parse sugr_in.txt semantics; returns SG_ERR_IO if the file cannot be opened. */
+int sg_read_input_file(const char *path, sg_input *in);
+/* SetParams (SurfaceGrowth.cpp:189-396) with EamInit/GrapheneInit (cpp:480-545). */
+int sg_set_params(const sg_input *in, sg_simparams *p);
+/* Initial coordinates (InitCoordsW cu:2532-2609 and its lattice kernels), nMol entries. */
+int sg_init_coords(sg_simparams *p, sg_float4 *r);
+/* Initial velocities with the reference's generator (InitVels cpp:596-621). */
+int sg_init_vels(sg_simparams *p, sg_float3 *v);
+
+/* Synthetic nanoparticle-on-graphene workload: a ucx x ucy graphene sheet (32*ucx*ucy C)
+ * with n_clusters fcc metal clusters (atom-centred spheres of the given sizes) placed at
+ * seeded random non-overlapping x-y positions, lowest atom clearance_A above the sheet,
+ * Maxwell-Boltzmann velocities at temperatureK (FP64 counter-based generator, zero net
+ * momentum).  Call with r == NULL to get the atom count in p->nMol. */
+typedef struct sg_workload {
+    int ucx, ucy, iMaterial;
+    int n_clusters;
+    const int *cluster_sizes;
+    float temperatureK;
+    float clearance_A;
+    unsigned long long seed;
+    int stepLimit, stepAvg, stepEquil, stepCool, stepRdf, limitRdf;
+    int stepDiffuse, nValDiffuse, nBuffDiffuse, limitDiffuseAv;
+    float deltaT;
+} sg_workload;
+int sg_build_workload(const sg_workload *w, sg_simparams *p, sg_float4 *r, sg_float3 *v);
+
+/* ---- output writers (host), in the reference's formats --------------------------------------
+ * These are what sg_run uses; exported so that a caller driving sg_step itself writes the
+ * same files.  All take the parameter block with the Props as the step loop holds them. */
+/* AccumProps (SurfaceGrowth.cu:2659-2686): icode 0 zero, 1 accumulate val, 2 average. */
+void sg_accum_props(sg_simparams *p, int icode);
+/* One summary row (PrintSummary, cu:2689-2731); Props must already be averaged. */
+int sg_print_summary(void *fp, const sg_simparams *p);
+/* Result-file name (sg + regime suffix + metal + .txt) and its header line
+ * (SetupJob, SurfaceGrowth.cpp:420-469). */
+int sg_result_file_name(const sg_simparams *p, char *out, int out_len);
+int sg_print_result_header(void *fp, const sg_simparams *p, float deposEnergyEv);
+/* sugr_<i>.pdb snapshot (CreatePdbFile, cu:2734-2810). */
+int sg_create_pdb(const char *prefix, const sg_simparams *p, const sg_float4 *r);
+/* rdf_stepCount_<n>_<metal>.txt (PrintRdf, cu:2812-2844); p->countRdf must equal the number
+ * of samples in hist. */
+int sg_print_rdf(const sg_simparams *p, const unsigned int *hist);
+/* One "diffusion" table (PrintDiffusion, cu:2884-2895). */
+int sg_print_diffusion(void *fp, const sg_simparams *p, const float *table);
+/* Backup file bckup0/1.sugr (cu:2456-2481) and its reader (the reference parses the restart
+ * flag but has no reader).  r/v/a may be NULL on read to query nMol from *p. */
+int sg_write_backup(const char *path, const sg_simparams *p, const sg_float4 *r, const sg_float3 *v,
+                    const sg_float3 *a);
+int sg_read_backup(const char *path, sg_simparams *p, sg_float4 *r, sg_float3 *v, sg_float3 *a);
+
+/* ---- tuning ------------------------------------------------------------------------------- */
+/* Times the candidate launch shapes of the tunable passes on the context's own state for
+ * `steps` steps each, keeps the fastest; state is restored afterwards. */
+int sg_autotune(sg_ctx *ctx, int steps, char *report, int report_len);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SG_API_H */

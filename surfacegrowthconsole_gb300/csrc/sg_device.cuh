@@ -1,0 +1,167 @@
+// sg_device.cuh - device-side data layout shared by the sgmd kernels.
+//
+// Layout in HBM (all replicas of a context concatenated, replica r owning the global atom
+// range [atomOff, atomOff + nMol) with its metal atoms first, as in the reference):
+//   pos   float4[Ntot]  x, y, z, U (U = per-atom potential energy, written by the force pass)
+//   vel   float4[Ntot]  vx, vy, vz, -
+//   acc   float4[Ntot]  ax, ay, az, -            (acceleration = force / mass)
+//   posLo float4[Ntot]  low words of the hi/lo position pair (MIXED mode only)
+//   cellOf int[Ntot]    local cell of the atom at the last rebuild (-1: outside the grid)
+//   slot   int[Ntot]    arrival slot inside the cell (scratch of the counting sort)
+//   cellCount int[Ctot], cellStart int[Ctot + R] (per-replica, tile-padded cell ranges)
+//   sortIdx int[Ntot], sortPos float4[Ntot]  atoms grouped by cell, ascending index per cell
+//   nn int[Ntot], nbl int[nebrMax * Ntot]   neighbour list, entry j of atom g at nbl[j*Ntot+g]
+//   ns int[Ntot], sl int[kShortMax * Ntot]  short list: neighbours within (rCutC+skin) at build
+//   rho/dF/Fv float[Ntot]   EAM density, F'(rho), F(rho) (metal atoms)
+//   fric float[Ntot]       x force of carbon on each metal atom
+// Per-replica constants live in RepConst, mutable per-replica scalars in RepState.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sg {
+
+constexpr int kShortMax = 8;      // short-list capacity per atom
+constexpr int kRedThreads = 512;  // reduction block: 512 threads x 2 elements (reference shape)
+constexpr int kRedElems = 1024;
+constexpr int kCellTile = 2048;   // cells per scan tile (cell ranges are padded to this)
+constexpr int kNumRed = 16;       // values reduced per element in the step reduction
+
+// Values of the step reduction (slot indices into a 16-float record).
+enum RedSlot {
+  RS_VSUM_X = 0, RS_VSUM_Y, RS_VSUM_Z,  // total impulse
+  RS_VVMAX,                             // max v^2
+  RS_VVSUM,                             // Sum m v^2 (metal v.x - V_cm in regime 2)
+  RS_USUM,                              // Sum U
+  RS_CM_X, RS_CM_Y, RS_CM_Z,            // Sum r (metal)
+  RS_MIN_X, RS_MIN_Y, RS_MIN_Z,         // min r (metal, with the reference's zero padding)
+  RS_MAX_X, RS_MAX_Y, RS_MAX_Z,
+  RS_FRICT                              // Sum friction (metal)
+};
+
+struct RepConst {
+  // geometry and bookkeeping
+  float region[3], invWidth[3];
+  int cells[3], ncells, ncellsPad;
+  int atomOff, nMol, nMolMe, cellOff;
+  int nRedBlocks;  // ceil(nMol / 1024)
+  // integrator
+  float deltaT, rrNebr, rNebrShell, rrShort;
+  float xLeft, xRight, yBottom, yTop;
+  // EAM
+  float rei, rhoei, rhoe, fe, alpha, beta, A, B, kappa, lambda, Fn[4], F[4], eta, Fe, massMe;
+  float rrCutEam;
+  // graphene and LJ
+  float rrCutC, mu_r, theta_0, mu_theta, mu_p, z_0, sigmaLJ, epsLJ, rrCutLJ;
+  // thermostat, shear, deposition
+  float temperature, kB, gammaBerendsen, deltaF, velMagDepos;
+  int iRegime, stepEquil, stepCool, stepThermostat, stepDeposit, nMolToDeposit;
+  int hasFric;
+  // RDF
+  float rangeRdf, intervalRdf;
+  int sizeHistRdf, bRdf;
+  // diffusion
+  int nValDiffuse, nBuffDiffuse, stepDiffuse, limitDiffuseAv;
+  int stepAvg;
+  // MIXED mode: tabulated EAM (offset of this replica's tables in the table buffer)
+  int tabOff;
+  float rTabMin, rTabInv, rhoTabInv;
+  int nTab;
+};
+
+struct RepState {
+  int stepCount;       // steps completed
+  int nebrNow;         // rebuild at the next step
+  int rebuilds;
+  int thermoPending;   // 1: rescale velocities at the start of the next step
+  float betaC, betaM;  // factors of the pending rescale
+  int thermoMetal;     // pending rescale includes metal atoms
+  float dispHi;
+  float shear, totalShear;
+  unsigned shearCount;
+  int nMolDeposited;
+  int countRdf;
+  float cmVal, cmVelVal, frictVal;  // centerOfMass.val, cmVel.val, frictForce.val
+  float ke, pe, te;
+  float red[kNumRed];               // last step's reduced values
+  float cmVel[3];                   // Sum v over metal (from the cmVel pass)
+  double ke64, pe64, virial64;
+  double red64[kNumRed];
+  float props[7][3];                // totEnergy, potEnergy, kinEnergy, oneStep, cm, cmVel, frict
+  float propsSnap[7][3];            // sums at the last stepAvg boundary (before averaging)
+  int snapStep;
+  int countDiffuseAv;
+  int diffPrints;                   // number of Diffuse.txt tables produced
+  unsigned redCounter;              // last-block counters
+  unsigned cmvCounter;
+  unsigned shearCounter;
+  int flags;                        // sticky error bits (SG_ERR_* as 1 << code)
+  int maxNeighbours, maxCellOcc, nebrOverflow, cellRange, cellOverflow, rdfRange, shortStale;
+  int pad[4];
+};
+
+// Block-to-replica tables: block b of a launch covers [start[b], start[b] + bs) clipped to its
+// replica's range; start is a global index (atoms) or local index (cells, reductions).
+struct BlockTab {
+  const int *rep;
+  const int *start;
+  int nblocks;
+};
+
+// Device diffusion buffers of one replica live in a flat float array:
+//   tb[nBuff] {count, orgR.xyz, rTrue.xyz} as 7 floats, rr[nBuff][nVal], av[nVal],
+//   print[nVal] (last finished table).
+struct DiffLayout {
+  static __host__ __device__ size_t floatsPerRep(int nBuff, int nVal) {
+    return (size_t)nBuff * 7 + (size_t)nBuff * nVal + 2 * (size_t)nVal;
+  }
+};
+
+// Offsets of the 27 neighbour cells in the reference's visiting order
+// (SurfaceGrowthConsole/ComputeDefs.h:221-231), packed as (dx+1) + 3(dy+1) + 9(dz+1).
+__device__ __constant__ static const signed char kOff27[27][3] = {
+    {0, 0, 0},  {0, 0, 1},  {0, 0, -1},  {0, 1, 0},  {0, 1, 1},  {0, 1, -1},  {0, -1, 0},
+    {0, -1, 1}, {0, -1, -1}, {1, 0, 0},  {1, 0, 1},  {1, 0, -1}, {1, 1, 0},   {1, 1, 1},
+    {1, 1, -1}, {1, -1, 0}, {1, -1, 1},  {1, -1, -1}, {-1, 0, 0}, {-1, 0, 1}, {-1, 0, -1},
+    {-1, 1, 0}, {-1, 1, 1}, {-1, 1, -1}, {-1, -1, 0}, {-1, -1, 1}, {-1, -1, -1}};
+
+// Neighbour cell of local cell c at stencil offset o with the periodic shift
+// (BuildNebrListK, SurfaceGrowth.cu:641-674).
+__device__ __forceinline__ int stencilCell(const RepConst &P, int c, int o, float &sx, float &sy,
+                                           float &sz) {
+  int ccz = c / (P.cells[0] * P.cells[1]);
+  int ccy = (c - ccz * P.cells[0] * P.cells[1]) / P.cells[0];
+  int ccx = c - (ccz * P.cells[1] + ccy) * P.cells[0];
+  int mx = ccx + kOff27[o][0], my = ccy + kOff27[o][1], mz = ccz + kOff27[o][2];
+  sx = 0.f; sy = 0.f; sz = 0.f;
+  if (mx >= P.cells[0]) { mx = 0; sx = P.region[0]; }
+  else if (mx < 0) { mx = P.cells[0] - 1; sx = -P.region[0]; }
+  if (my >= P.cells[1]) { my = 0; sy = P.region[1]; }
+  else if (my < 0) { my = P.cells[1] - 1; sy = -P.region[1]; }
+  if (mz >= P.cells[2]) { mz = 0; sz = P.region[2]; }
+  else if (mz < 0) { mz = P.cells[2] - 1; sz = -P.region[2]; }
+  return (mz * P.cells[1] + my) * P.cells[0] + mx;
+}
+
+// Cell of a position (BinAtomsIntoCellsK, SurfaceGrowth.cu:594-600); -1 when the linear index
+// falls outside the grid (the reference then never bins the atom).
+__device__ __forceinline__ int cellIndex(const RepConst &P, float x, float y, float z) {
+  int cx = (int)((x + 0.5f * P.region[0]) * P.invWidth[0]);
+  int cy = (int)((y + 0.5f * P.region[1]) * P.invWidth[1]);
+  int cz = (int)((z + 0.5f * P.region[2]) * P.invWidth[2]);
+  long long c = ((long long)cz * P.cells[1] + cy) * P.cells[0] + cx;
+  return (c < 0 || c >= P.ncells) ? -1 : (int)c;
+}
+
+// Minimum image of one component as the force kernels do it (SurfaceGrowth.cu:750-759).
+__device__ __forceinline__ float minImg(float d, float L) {
+  if (d >= 0.5f * L) d -= L;
+  else if (d < -0.5f * L) d += L;
+  return d;
+}
+
+__device__ __forceinline__ void setFlag(RepState *st, int code) {
+  atomicOr(&st->flags, 1 << code);
+}
+
+}  // namespace sg

@@ -1,0 +1,841 @@
+// sg_engine.cu - context, device memory, step sequencing (CUDA graphs) and the sg_* C ABI.
+//
+// One step is a fixed sequence of launches, each covering every replica of the context:
+//   integrate_first  (Verlet part 1 + wrap + pending thermostat + deposition + cell histogram)
+//   [scan_tiles, scan_tile_prefix, scan_final, scatter, rank, build_nebr]  (rebuild; a
+//        replica whose nebrNow flag is clear leaves these kernels at once)
+//   rho, force_metal, force_carbon
+//   cmvel, step_reduce (Verlet part 2 + all reductions + per-replica step control)
+//   [shear] [rdf]    (only on steps where the host-known schedule asks for them)
+// The sequence is captured once per variant into a CUDA graph and replayed, so a step costs
+// one graph launch and no host synchronisation; the host reads results only at output
+// points.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "sg_api.h"
+#include "sg_device.cuh"
+#include "sg_engine.h"
+#include "sg_kernels.h"
+
+using namespace sg;
+
+// ---- error plumbing ----------------------------------------------------------------------
+static thread_local std::string g_err;
+int sg_fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+#define CK(call)                                                                              \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess)                                                                    \
+      return sg_fail(e_ == cudaErrorMemoryAllocation ? SG_ERR_NOMEM : SG_ERR_CUDA, "%s: %s (%s:%d)", \
+                     #call, cudaGetErrorString(e_), __FILE__, __LINE__);                      \
+  } while (0)
+
+extern "C" const char *sg_last_error(void) { return g_err.c_str(); }
+extern "C" int sg_version(void) { return SG_API_VERSION; }
+
+extern "C" void sg_default_options(sg_options *o) {
+  memset(o, 0, sizeof(*o));
+  o->mode = SG_MODE_PLAIN;
+  o->use_graphs = 1;
+  o->rdf_ext_range = 0.f;
+}
+
+static int devAlloc(sg_ctx *c, void **p, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) return sg_fail(SG_ERR_NOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+  c->allocs.push_back(*p);
+  e = cudaMemsetAsync(*p, 0, bytes, c->stream);
+  if (e != cudaSuccess) return sg_fail(SG_ERR_CUDA, "cudaMemset: %s", cudaGetErrorString(e));
+  return SG_OK;
+}
+template <class T> static int devAllocT(sg_ctx *c, T **p, size_t n) {
+  return devAlloc(c, (void **)p, n * sizeof(T));
+}
+
+static int uploadTab(sg_ctx *c, DevTab &t, const std::vector<int> &rep, const std::vector<int> &start) {
+  t.n = (int)rep.size();
+  int rc;
+  if ((rc = devAllocT(c, &t.rep, std::max<size_t>(rep.size(), 1)))) return rc;
+  if ((rc = devAllocT(c, &t.start, std::max<size_t>(start.size(), 1)))) return rc;
+  if (t.n) {
+    CK(cudaMemcpyAsync(t.rep, rep.data(), rep.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(t.start, start.data(), start.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  }
+  return SG_OK;
+}
+// blocks of bs over [b, e) of each replica
+static int makeRangeTab(sg_ctx *c, DevTab &t, int bs, int which) {
+  std::vector<int> rep, start;
+  for (int r = 0; r < c->nrep; r++) {
+    const RepConst &P = c->hrc[r];
+    int b = P.atomOff, e = P.atomOff + P.nMol;
+    if (which == 1) e = P.atomOff + P.nMolMe;
+    if (which == 2) b = P.atomOff + P.nMolMe;
+    for (int s = b; s < e; s += bs) { rep.push_back(r); start.push_back(s); }
+  }
+  return uploadTab(c, t, rep, start);
+}
+
+// Parameters of one replica as the kernels read them.
+static RepConst makeConst(const sg_simparams &p) {
+  RepConst P;
+  memset(&P, 0, sizeof(P));
+  P.region[0] = p.region.x; P.region[1] = p.region.y; P.region[2] = p.region.z;
+  P.invWidth[0] = p.invWidth.x; P.invWidth[1] = p.invWidth.y; P.invWidth[2] = p.invWidth.z;
+  P.cells[0] = p.cells.x; P.cells[1] = p.cells.y; P.cells[2] = p.cells.z;
+  P.ncells = p.cells.x * p.cells.y * p.cells.z;
+  P.ncellsPad = ((P.ncells + 1 + kCellTile - 1) / kCellTile) * kCellTile;
+  P.nMol = p.nMol;
+  P.nMolMe = p.nMolMe;
+  P.nRedBlocks = (p.nMol + kRedElems - 1) / kRedElems;
+  P.deltaT = p.deltaT;
+  P.rrNebr = p.rrNebr;
+  P.rNebrShell = p.rNebrShell;
+  const float rs = p.rCutC + p.rNebrShell;
+  P.rrShort = rs * rs;
+  const float c30 = (float)cos(M_PI / 6.f);  // LeapfrogStepK, SurfaceGrowth.cu:416-421
+  P.xLeft = 0.5f * (c30 - p.region.x);
+  P.xRight = 0.5f * (p.region.x - c30);
+  P.yBottom = 0.5f * (1.f - p.region.y);
+  P.yTop = 0.5f * (p.region.y - 1.f);
+  P.rei = p.rei; P.rhoei = p.rhoei; P.rhoe = p.rhoe; P.fe = p.fe; P.alpha = p.alpha;
+  P.beta = p.beta; P.A = p.A; P.B = p.B; P.kappa = p.kappa; P.lambda = p.lambda;
+  for (int i = 0; i < 4; i++) { P.Fn[i] = p.Fn[i]; P.F[i] = p.F[i]; }
+  P.eta = p.eta; P.Fe = p.Fe; P.massMe = p.massMe; P.rrCutEam = p.rrCutEam;
+  P.rrCutC = p.rrCutC; P.mu_r = p.mu_r; P.theta_0 = p.theta_0; P.mu_theta = p.mu_theta;
+  P.mu_p = p.mu_p; P.z_0 = p.z_0; P.sigmaLJ = p.sigmaLJ; P.epsLJ = p.epsLJ; P.rrCutLJ = p.rrCutLJ;
+  P.temperature = p.temperature; P.kB = p.kB; P.gammaBerendsen = p.gammaBerendsen;
+  P.deltaF = p.deltaF; P.velMagDepos = p.velMagDepos;
+  P.iRegime = p.iRegime; P.stepEquil = p.stepEquil; P.stepCool = p.stepCool;
+  P.stepThermostat = p.stepThermostat > 0 ? p.stepThermostat : 1;
+  P.stepDeposit = p.stepDeposit > 0 ? p.stepDeposit : 1;
+  P.nMolToDeposit = p.nMolToDeposit;
+  P.hasFric = (p.iRegime != 0 && p.nMolMe != 0) ? 1 : 0;
+  P.rangeRdf = p.rangeRdf; P.intervalRdf = p.intervalRdf; P.sizeHistRdf = p.sizeHistRdf;
+  P.bRdf = p.bRdf;
+  P.nValDiffuse = p.nValDiffuse; P.nBuffDiffuse = p.nBuffDiffuse;
+  P.stepDiffuse = p.stepDiffuse > 0 ? p.stepDiffuse : 1;
+  P.limitDiffuseAv = p.limitDiffuseAv;
+  P.stepAvg = p.stepAvg > 0 ? p.stepAvg : 1;
+  return P;
+}
+
+static int validate(const sg_simparams *p, int n) {
+  for (int r = 0; r < n; r++) {
+    const sg_simparams &q = p[r];
+    if (q.nMol <= 0 || q.nMolMe < 0 || q.nMolMe > q.nMol)
+      return sg_fail(SG_ERR_INVALID, "replica %d: bad atom counts nMol=%d nMolMe=%d", r, q.nMol, q.nMolMe);
+    if (q.cells.x < 1 || q.cells.y < 1 || q.cells.z < 1)
+      return sg_fail(SG_ERR_INVALID, "replica %d: bad cell grid", r);
+    if (q.iNebrMax < 1) return sg_fail(SG_ERR_INVALID, "replica %d: iNebrMax < 1", r);
+    if (q.bRdf && (q.sizeHistRdf < 1 || q.stepRdf < 1 || q.limitRdf < 1))
+      return sg_fail(SG_ERR_INVALID, "replica %d: bad RDF settings", r);
+    if (q.iRegime == 2 && (q.nBuffDiffuse < 1 || q.nValDiffuse < 1 || q.limitDiffuseAv < 1 || q.nBuffDiffuse > 4096))
+      return sg_fail(SG_ERR_INVALID, "replica %d: bad diffusion settings", r);
+    if (r > 0) {  // one host-side schedule drives all replicas
+      const sg_simparams &z = p[0];
+      if (q.stepRdf != z.stepRdf || q.limitRdf != z.limitRdf || q.bRdf != z.bRdf ||
+          q.stepCount != z.stepCount || q.stepAvg != z.stepAvg || q.iNebrMax != z.iNebrMax)
+        return sg_fail(SG_ERR_INVALID, "replica %d: schedule differs from replica 0", r);
+    }
+  }
+  return SG_OK;
+}
+
+static void destroyGraphs(sg_ctx *c) {
+  for (auto &kv : c->graphs) cudaGraphExecDestroy(kv.second);
+  c->graphs.clear();
+}
+
+extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_options *opt, sg_ctx **out) {
+  if (!params || n_replicas < 1 || !out) return sg_fail(SG_ERR_INVALID, "sg_create: bad arguments");
+  *out = nullptr;
+  int rc = validate(params, n_replicas);
+  if (rc) return rc;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return sg_fail(SG_ERR_NO_DEVICE, "no CUDA device available");
+  sg_ctx *c = new sg_ctx;
+  if (opt) c->opt = *opt;
+  else sg_default_options(&c->opt);
+  if (c->opt.mode != SG_MODE_PLAIN && c->opt.mode != SG_MODE_MIXED) {
+    delete c;
+    return sg_fail(SG_ERR_INVALID, "unknown mode %d", c->opt.mode);
+  }
+  if (cudaSetDevice(c->opt.device) != cudaSuccess) {
+    delete c;
+    return sg_fail(SG_ERR_NO_DEVICE, "cannot select device %d", c->opt.device);
+  }
+  cudaDeviceProp prop;
+  cudaGetDeviceProperties(&prop, c->opt.device);
+  if (prop.major != 10 || prop.minor != 3) {
+    delete c;
+    return sg_fail(SG_ERR_NO_DEVICE, "device %d is sm_%d%d; this build targets sm_103 (GB300)",
+                   c->opt.device, prop.major, prop.minor);
+  }
+  if (c->opt.stream) c->stream = (cudaStream_t)c->opt.stream;
+  else {
+    cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    c->ownStream = true;
+  }
+  c->nrep = n_replicas;
+  c->hp.assign(params, params + n_replicas);
+  c->nebrMax = params[0].iNebrMax;
+  c->stepCount = params[0].stepCount;
+  c->countRdf = params[0].countRdf;
+  c->oneStep.resize(n_replicas);
+  for (int r = 0; r < n_replicas; r++) c->oneStep[r] = params[r].oneStep;
+  // layout of replicas
+  int atomOff = 0, cellOff = 0, redOff = 0, cmvOff = 0;
+  size_t diffOff = 0;
+  for (int r = 0; r < n_replicas; r++) {
+    RepConst P = makeConst(params[r]);
+    P.atomOff = atomOff;
+    P.cellOff = cellOff;
+    c->redFirst.push_back(redOff);
+    c->cmvFirst.push_back(cmvOff);
+    c->diffOffH.push_back(diffOff);
+    atomOff += P.nMol;
+    cellOff += P.ncellsPad;
+    redOff += P.nRedBlocks;
+    cmvOff += (P.nMolMe + kRedElems - 1) / kRedElems;
+    if (params[r].iRegime == 2) diffOff += DiffLayout::floatsPerRep(P.nBuffDiffuse, P.nValDiffuse);
+    c->hrc.push_back(P);
+    c->anyMetal |= (P.nMolMe > 0);
+    c->anyCarbon |= (P.nMol > P.nMolMe);
+    c->maxHist = std::max(c->maxHist, params[r].bRdf ? params[r].sizeHistRdf : 0);
+  }
+  c->ntot = atomOff;
+  c->ctot = cellOff;
+  const size_t N = c->ntot;
+#define AL(ptr, n)                          \
+  if ((rc = devAllocT(c, &ptr, (n)))) {     \
+    sg_destroy(c);                          \
+    return rc;                              \
+  }
+  AL(c->rc, n_replicas);
+  AL(c->st, n_replicas);
+  AL(c->pos, N); AL(c->vel, N); AL(c->acc, N); AL(c->sortPos, N);
+  if (c->opt.mode == SG_MODE_MIXED) AL(c->posLo, N);
+  AL(c->cellOf, N); AL(c->slot, N); AL(c->tmpIdx, N); AL(c->sortIdx, N);
+  AL(c->cellCount, (size_t)c->ctot); AL(c->cellStart, (size_t)c->ctot);
+  AL(c->nn, N); AL(c->ns, N);
+  AL(c->nbl, N * c->nebrMax);
+  AL(c->sl, N * kShortMax);
+  AL(c->rho, N); AL(c->dF, N); AL(c->Fv, N); AL(c->fric, N);
+  AL(c->partial, (size_t)std::max(redOff, 1) * kNumRed);
+  AL(c->partialCmv, (size_t)std::max(cmvOff, 1) * 3);
+  AL(c->dRedFirst, n_replicas); AL(c->dCmvFirst, n_replicas);
+  c->histStride = std::max(c->maxHist, 1);
+  AL(c->hist, (size_t)n_replicas * c->histStride);
+  if (c->opt.rdf_ext_bins > 0) AL(c->histExt, (size_t)n_replicas * c->opt.rdf_ext_bins);
+  AL(c->diffBuf, std::max<size_t>(diffOff, 1));
+  AL(c->dDiffOff, n_replicas);
+#undef AL
+  // tables
+  if ((rc = makeRangeTab(c, c->atomTab, 128, 0)) || (rc = makeRangeTab(c, c->metalTab, 128, 1)) ||
+      (rc = makeRangeTab(c, c->carbonTab, 128, 2))) {
+    sg_destroy(c);
+    return rc;
+  }
+  {
+    std::vector<int> rr, ss, cr, cs, tr, ts;
+    for (int r = 0; r < n_replicas; r++) {
+      const RepConst &P = c->hrc[r];
+      for (int b = 0; b < P.nRedBlocks; b++) { rr.push_back(r); ss.push_back(b); }
+      for (int b = 0; b < (P.nMolMe + kRedElems - 1) / kRedElems; b++) { cr.push_back(r); cs.push_back(b); }
+      c->tileFirst.push_back((int)tr.size());
+      for (int t = 0; t < P.ncellsPad; t += kCellTile) { tr.push_back(r); ts.push_back(t); }
+    }
+    c->ntiles = (int)tr.size();
+    if ((rc = uploadTab(c, c->redTab, rr, ss)) || (rc = uploadTab(c, c->cmvTab, cr, cs)) ||
+        (rc = uploadTab(c, c->tileTab, tr, ts))) {
+      sg_destroy(c);
+      return rc;
+    }
+    if ((rc = devAllocT(c, &c->tileSum, std::max<size_t>(tr.size(), 1))) ||
+        (rc = devAllocT(c, &c->dTileFirst, n_replicas))) {
+      sg_destroy(c);
+      return rc;
+    }
+  }
+  // constants, initial state
+  std::vector<RepState> hs(n_replicas);
+  for (int r = 0; r < n_replicas; r++) {
+    const sg_simparams &p = params[r];
+    RepState &S = hs[r];
+    memset(&S, 0, sizeof(S));
+    S.stepCount = p.stepCount;
+    S.nebrNow = 1;  // lists do not exist yet
+    S.dispHi = p.dispHi;
+    S.shear = p.shear;
+    S.totalShear = p.totalShear;
+    S.nMolDeposited = p.nMolDeposited;
+    S.countRdf = p.countRdf;
+    const sg_prop *pp[7] = {&p.totEnergy, &p.potEnergy, &p.kinEnergy, &p.oneStep,
+                            &p.centerOfMass, &p.cmVel, &p.frictForce};
+    for (int k = 0; k < 7; k++) {
+      S.props[k][0] = pp[k]->val; S.props[k][1] = pp[k]->sum; S.props[k][2] = pp[k]->sum2;
+    }
+    S.countDiffuseAv = p.countDiffuseAv;
+  }
+  cudaError_t e = cudaMemcpyAsync(c->rc, c->hrc.data(), sizeof(RepConst) * n_replicas, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(c->st, hs.data(), sizeof(RepState) * n_replicas, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(c->dRedFirst, c->redFirst.data(), sizeof(int) * n_replicas, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(c->dCmvFirst, c->cmvFirst.data(), sizeof(int) * n_replicas, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(c->dTileFirst, c->tileFirst.data(), sizeof(int) * n_replicas, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(c->dDiffOff, c->diffOffH.data(), sizeof(size_t) * n_replicas, cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) {
+    sg_destroy(c);
+    return sg_fail(SG_ERR_CUDA, "upload: %s", cudaGetErrorString(e));
+  }
+  // diffusion buffer counts start staggered (InitDiffusion, SurfaceGrowth.cu:2868-2871)
+  for (int r = 0; r < n_replicas; r++) {
+    const sg_simparams &p = params[r];
+    if (p.iRegime != 2) continue;
+    std::vector<float> tb((size_t)p.nBuffDiffuse * 7, 0.f);
+    for (int nb = 0; nb < p.nBuffDiffuse; nb++) {
+      int cnt = -nb * p.nValDiffuse / p.nBuffDiffuse;
+      memcpy(&tb[7 * nb], &cnt, sizeof(int));
+    }
+    e = cudaMemcpyAsync(c->diffBuf + c->diffOffH[r], tb.data(), tb.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) {
+      sg_destroy(c);
+      return sg_fail(SG_ERR_CUDA, "upload: %s", cudaGetErrorString(e));
+    }
+  }
+  if (c->opt.mode == SG_MODE_MIXED) {
+    rc = sg_mixed_init(c);
+    if (rc) {
+      sg_destroy(c);
+      return rc;
+    }
+  }
+  e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    sg_destroy(c);
+    return sg_fail(SG_ERR_CUDA, "create: %s", cudaGetErrorString(e));
+  }
+  *out = c;
+  return SG_OK;
+}
+
+extern "C" int sg_destroy(sg_ctx *c) {
+  if (!c) return SG_OK;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  destroyGraphs(c);
+  sg_mixed_free(c);
+  for (void *p : c->allocs) cudaFree(p);
+  if (c->ownStream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return SG_OK;
+}
+
+extern "C" int sg_num_replicas(const sg_ctx *c) { return c ? c->nrep : 0; }
+extern "C" int sg_num_atoms(const sg_ctx *c, int rep) {
+  if (!c) return 0;
+  if (rep < 0) return c->ntot;
+  return (rep < c->nrep) ? c->hrc[rep].nMol : 0;
+}
+extern "C" int sg_num_cells(const sg_ctx *c, int rep) {
+  return (c && rep >= 0 && rep < c->nrep) ? c->hrc[rep].ncells : 0;
+}
+
+static int repRange(sg_ctx *c, int rep, int &off, int &n) {
+  if (rep < 0) { off = 0; n = c->ntot; return SG_OK; }
+  if (rep >= c->nrep) return sg_fail(SG_ERR_INVALID, "replica %d out of range", rep);
+  off = c->hrc[rep].atomOff;
+  n = c->hrc[rep].nMol;
+  return SG_OK;
+}
+
+extern "C" int sg_set_state(sg_ctx *c, int rep, const sg_float4 *r, const sg_float3 *v, const sg_float3 *a) {
+  if (!c) return sg_fail(SG_ERR_INVALID, "null context");
+  int off, n, rc;
+  if ((rc = repRange(c, rep, off, n))) return rc;
+  std::vector<float4> buf(n);
+  if (r) {
+    for (int i = 0; i < n; i++) buf[i] = make_float4(r[i].x, r[i].y, r[i].z, r[i].w);
+    CK(cudaMemcpyAsync(c->pos + off, buf.data(), n * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
+    if (c->posLo) CK(cudaMemsetAsync(c->posLo + off, 0, n * sizeof(float4), c->stream));
+  }
+  if (v) {
+    for (int i = 0; i < n; i++) buf[i] = make_float4(v[i].x, v[i].y, v[i].z, 0.f);
+    CK(cudaMemcpyAsync(c->vel + off, buf.data(), n * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
+  }
+  if (a) {
+    for (int i = 0; i < n; i++) buf[i] = make_float4(a[i].x, a[i].y, a[i].z, 0.f);
+    CK(cudaMemcpyAsync(c->acc + off, buf.data(), n * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
+  }
+  // a new state cancels any thermostat rescale still pending from the previous step
+  k_clear_pending<<<(c->nrep + 127) / 128, 128, 0, c->stream>>>(c->st, c->nrep);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->stream));
+  return SG_OK;
+}
+
+static int applyPending(sg_ctx *c) {
+  if (c->atomTab.n) {
+    k_apply_pending<<<c->atomTab.n, 128, 0, c->stream>>>(c->atomTab.view(), c->rc, c->st, c->vel);
+    k_clear_pending<<<(c->nrep + 127) / 128, 128, 0, c->stream>>>(c->st, c->nrep);
+    CK(cudaGetLastError());
+  }
+  return SG_OK;
+}
+
+extern "C" int sg_get_state(sg_ctx *c, int rep, sg_float4 *r, sg_float3 *v, sg_float3 *a) {
+  if (!c) return sg_fail(SG_ERR_INVALID, "null context");
+  int off, n, rc;
+  if ((rc = repRange(c, rep, off, n))) return rc;
+  if (v && (rc = applyPending(c))) return rc;
+  std::vector<float4> buf(n);
+  if (r) {
+    CK(cudaMemcpyAsync(buf.data(), c->pos + off, n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int i = 0; i < n; i++) r[i] = sg_float4{buf[i].x, buf[i].y, buf[i].z, buf[i].w};
+  }
+  if (v) {
+    CK(cudaMemcpyAsync(buf.data(), c->vel + off, n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int i = 0; i < n; i++) v[i] = sg_float3{buf[i].x, buf[i].y, buf[i].z};
+  }
+  if (a) {
+    CK(cudaMemcpyAsync(buf.data(), c->acc + off, n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int i = 0; i < n; i++) a[i] = sg_float3{buf[i].x, buf[i].y, buf[i].z};
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return SG_OK;
+}
+
+// ---- launch sequences ---------------------------------------------------------------------
+enum { V_SHEAR = 1, V_RDF = 2, V_RDF_ZERO = 4 };
+
+#define LAUNCH_OK() CK(cudaGetLastError())
+
+static int enqueueRebuild(sg_ctx *c, int force) {
+  const int fr = force;
+  if (c->ntiles) {
+    k_scan_tiles<<<c->tileTab.n, 256, 0, c->stream>>>(c->tileTab.view(), c->rc, c->st, c->cellCount, c->tileSum, fr);
+    k_scan_tile_prefix<<<c->nrep, 1024, 0, c->stream>>>(c->rc, c->st, c->dTileFirst, c->tileSum, fr);
+    k_scan_final<<<c->tileTab.n, 256, 0, c->stream>>>(c->tileTab.view(), c->rc, c->st, c->cellCount, c->tileSum,
+                                                       c->cellStart, (int)c->hp[0].blockSize, fr);
+    LAUNCH_OK();
+  }
+  k_scatter<<<c->atomTab.n, 128, 0, c->stream>>>(c->atomTab.view(), c->rc, c->st, c->cellOf, c->slot, c->cellStart,
+                                                 c->tmpIdx, c->nn, c->ns, fr);
+  k_rank<<<c->atomTab.n, 128, 0, c->stream>>>(c->atomTab.view(), c->rc, c->st, c->cellOf, c->cellStart, c->tmpIdx,
+                                              c->pos, c->sortIdx, c->sortPos, fr);
+  k_build_nebr<<<c->atomTab.n, 128, 0, c->stream>>>(c->atomTab.view(), c->rc, c->st, c->cellOf, c->cellStart,
+                                                    c->sortPos, c->nn, c->nbl, c->ns, c->sl, c->ntot,
+                                                    c->nebrMax, fr);
+  LAUNCH_OK();
+  return SG_OK;
+}
+
+static int enqueueForces(sg_ctx *c) {
+  if (c->opt.mode == SG_MODE_MIXED) return sg_mixed_enqueue_forces(c);
+  if (c->metalTab.n) {
+    k_rho<<<c->metalTab.n, 128, 0, c->stream>>>(c->metalTab.view(), c->rc, c->pos, c->nn, c->nbl, c->rho, c->dF,
+                                                c->Fv, c->ntot);
+    k_force_metal<<<c->metalTab.n, 128, 0, c->stream>>>(c->metalTab.view(), c->rc, c->pos, c->acc, c->nn, c->nbl,
+                                                        c->dF, c->Fv, c->fric, c->ntot);
+  }
+  if (c->carbonTab.n)
+    k_force_carbon<<<c->carbonTab.n, 128, 0, c->stream>>>(c->carbonTab.view(), c->rc, c->pos, c->acc, c->nn,
+                                                          c->nbl, c->ns, c->sl, c->st, c->ntot);
+  LAUNCH_OK();
+  return SG_OK;
+}
+
+static int enqueueRdf(sg_ctx *c, bool zero) {
+  if (zero) {
+    CK(cudaMemsetAsync(c->hist, 0, sizeof(unsigned) * c->nrep * c->histStride, c->stream));
+    if (c->histExt)
+      CK(cudaMemsetAsync(c->histExt, 0, sizeof(unsigned long long) * c->nrep * c->opt.rdf_ext_bins, c->stream));
+  }
+  if (c->metalTab.n && c->maxHist > 0) {
+    k_rdf<<<c->metalTab.n, 128, c->maxHist * sizeof(unsigned), c->stream>>>(
+        c->metalTab.view(), c->rc, c->st, c->pos, c->cellOf, c->cellStart, c->sortIdx, c->hist, c->histStride);
+    LAUNCH_OK();
+  }
+  if (c->histExt && c->metalTab.n) {
+    k_rdf_ext<<<c->metalTab.n, 128, c->opt.rdf_ext_bins * sizeof(unsigned), c->stream>>>(
+        c->rc, c->pos, c->metalTab.rep, c->metalTab.start, c->histExt, c->opt.rdf_ext_bins, c->opt.rdf_ext_range);
+    LAUNCH_OK();
+  }
+  return SG_OK;
+}
+
+static int enqueueStep(sg_ctx *c, int variant) {
+  int rc;
+  const int fr = c->opt.force_rebuild ? 1 : 0;
+  if (c->opt.mode == SG_MODE_MIXED) {
+    if ((rc = sg_mixed_enqueue_integrate(c, fr))) return rc;
+  } else {
+    k_integrate_first<<<c->atomTab.n, 128, 0, c->stream>>>(c->atomTab.view(), c->rc, c->st, c->pos, c->vel, c->acc,
+                                                           c->cellOf, c->slot, c->cellCount, fr);
+    LAUNCH_OK();
+  }
+  if ((rc = enqueueRebuild(c, fr))) return rc;
+  if ((rc = enqueueForces(c))) return rc;
+  if (c->opt.mode == SG_MODE_MIXED) {
+    if ((rc = sg_mixed_enqueue_reduce(c, fr))) return rc;
+  } else {
+    if (c->cmvTab.n)
+      k_cmvel<<<c->cmvTab.n, kRedThreads, 0, c->stream>>>(c->cmvTab.view(), c->rc, c->st, c->vel, c->acc,
+                                                           c->partialCmv, c->dCmvFirst);
+    k_step_reduce<<<c->redTab.n, kRedThreads, 0, c->stream>>>(c->redTab.view(), c->rc, c->st, c->pos, c->vel, c->acc,
+                                                              c->fric, c->partial, c->dRedFirst, c->diffBuf,
+                                                              c->dDiffOff, fr);
+    LAUNCH_OK();
+  }
+  if ((variant & V_SHEAR) && c->metalTab.n) {
+    k_shear<<<c->metalTab.n, 128, 0, c->stream>>>(c->metalTab.view(), c->rc, c->st, c->pos, c->acc);
+    LAUNCH_OK();
+  }
+  if (variant & V_RDF) {
+    if ((rc = enqueueRdf(c, (variant & V_RDF_ZERO) != 0))) return rc;
+  }
+  return SG_OK;
+}
+
+// Which optional phases the coming step needs (host-known schedule, SurfaceGrowth.cu:2398-2429).
+static int stepVariant(sg_ctx *c) {
+  const int sc = c->stepCount + 1;
+  int v = 0;
+  for (int r = 0; r < c->nrep; r++) {
+    const sg_simparams &p = c->hp[r];
+    if (p.iRegime == 2 && p.nMolMe != 0 && sc > p.stepEquil + p.stepCool) v |= V_SHEAR;
+  }
+  const sg_simparams &p0 = c->hp[0];
+  if (p0.bRdf && (sc % p0.stepRdf == 0)) {
+    v |= V_RDF;
+    if (c->countRdf == 0) v |= V_RDF_ZERO;
+  }
+  return v;
+}
+
+static void advanceSchedule(sg_ctx *c, int variant, bool *rdfPrint) {
+  c->stepCount++;
+  if (rdfPrint) *rdfPrint = false;
+  if (variant & V_RDF) {
+    c->countRdf++;
+    if (c->countRdf == c->hp[0].limitRdf) {
+      if (rdfPrint) *rdfPrint = true;
+      c->countRdf = 0;
+    }
+  }
+}
+
+static int launchStep(sg_ctx *c, int variant) {
+  if (!c->opt.use_graphs) return enqueueStep(c, variant);
+  auto it = c->graphs.find(variant);
+  if (it == c->graphs.end()) {
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueueStep(c, variant);
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (rc) return rc;
+    if (e != cudaSuccess) return sg_fail(SG_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    cudaGraphExec_t ex;
+    e = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return sg_fail(SG_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    it = c->graphs.emplace(variant, ex).first;
+  }
+  CK(cudaGraphLaunch(it->second, c->stream));
+  return SG_OK;
+}
+
+// Sticky device error bits -> status code (first set bit wins).
+static int checkFlags(sg_ctx *c) {
+  std::vector<RepState> hs(c->nrep);
+  CK(cudaMemcpyAsync(hs.data(), c->st, sizeof(RepState) * c->nrep, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  int flags = 0;
+  for (auto &s : hs) flags |= s.flags;
+  if (!flags) return SG_OK;
+  // report once, then clear
+  for (int r = 0; r < c->nrep; r++) hs[r].flags = 0;
+  int zero = 0;
+  for (int r = 0; r < c->nrep; r++)
+    CK(cudaMemcpyAsync(&c->st[r].flags, &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  for (int code = 1; code < 31; code++)
+    if (flags & (1 << code))
+      return sg_fail(code, "device reported condition %d (see sg_get_diag)", code);
+  return SG_OK;
+}
+
+extern "C" int sg_step(sg_ctx *c, int nsteps) {
+  if (!c) return sg_fail(SG_ERR_INVALID, "null context");
+  for (int s = 0; s < nsteps; s++) {
+    const int v = stepVariant(c);
+    int rc = launchStep(c, v);
+    if (rc) return rc;
+    advanceSchedule(c, v, nullptr);
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return checkFlags(c);
+}
+
+// Launch-only stepping for timing loops (no synchronisation, no flag check).
+int sg_step_async(sg_ctx *c, int nsteps) {
+  for (int s = 0; s < nsteps; s++) {
+    const int v = stepVariant(c);
+    int rc = launchStep(c, v);
+    if (rc) return rc;
+    advanceSchedule(c, v, nullptr);
+  }
+  return SG_OK;
+}
+
+extern "C" int sg_build_lists(sg_ctx *c) {
+  if (!c) return sg_fail(SG_ERR_INVALID, "null context");
+  k_cell_count<<<c->atomTab.n, 128, 0, c->stream>>>(c->atomTab.view(), c->rc, c->pos, c->cellOf, c->slot, c->cellCount);
+  LAUNCH_OK();
+  int rc = enqueueRebuild(c, 1);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return checkFlags(c);
+}
+
+extern "C" int sg_compute_forces(sg_ctx *c) {
+  if (!c) return sg_fail(SG_ERR_INVALID, "null context");
+  int rc = enqueueForces(c);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return checkFlags(c);
+}
+
+extern "C" int sg_eval_rdf(sg_ctx *c) {
+  if (!c) return sg_fail(SG_ERR_INVALID, "null context");
+  int rc = enqueueRdf(c, false);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return checkFlags(c);
+}
+
+extern "C" int sg_reset_rdf(sg_ctx *c) {
+  if (!c) return sg_fail(SG_ERR_INVALID, "null context");
+  CK(cudaMemsetAsync(c->hist, 0, sizeof(unsigned) * c->nrep * c->histStride, c->stream));
+  if (c->histExt)
+    CK(cudaMemsetAsync(c->histExt, 0, sizeof(unsigned long long) * c->nrep * c->opt.rdf_ext_bins, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return SG_OK;
+}
+
+// ---- read-back ---------------------------------------------------------------------------
+int sg_read_state(sg_ctx *c, int rep, RepState *out) {
+  CK(cudaMemcpyAsync(out, c->st + rep, sizeof(RepState), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return SG_OK;
+}
+
+extern "C" int sg_get_thermo(sg_ctx *c, int rep, sg_thermo *t) {
+  if (!c || !t || rep < 0 || rep >= c->nrep) return sg_fail(SG_ERR_INVALID, "sg_get_thermo: bad arguments");
+  RepState S;
+  int rc = sg_read_state(c, rep, &S);
+  if (rc) return rc;
+  memset(t, 0, sizeof(*t));
+  t->stepCount = S.stepCount;
+  t->nebrNow = S.nebrNow;
+  t->rebuilds = S.rebuilds;
+  t->countRdf = c->countRdf;
+  t->kinEnergy = S.ke; t->potEnergy = S.pe; t->totEnergy = S.te;
+  t->vvSum = S.red[RS_VVSUM]; t->vvMax = S.red[RS_VVMAX]; t->uSum = S.red[RS_USUM]; t->dispHi = S.dispHi;
+  t->vSum = sg_float3{S.red[RS_VSUM_X], S.red[RS_VSUM_Y], S.red[RS_VSUM_Z]};
+  t->centerOfMass = sg_float3{S.red[RS_CM_X], S.red[RS_CM_Y], S.red[RS_CM_Z]};
+  t->cmVel = sg_float3{S.cmVel[0], S.cmVel[1], S.cmVel[2]};
+  t->frictForce = S.frictVal;
+  const sg_simparams &p = c->hp[rep];
+  if (p.nMolMe != 0)
+    t->particleSize = sg_float3{S.red[RS_MAX_X] - S.red[RS_MIN_X], S.red[RS_MAX_Y] - S.red[RS_MIN_Y],
+                                S.red[RS_MAX_Z] - S.red[RS_MIN_Z]};
+  t->shear = S.shear;
+  t->totalShear = S.totalShear;
+  t->kinEnergy64 = S.ke64;
+  t->potEnergy64 = S.pe64;
+  t->virial64 = S.virial64;
+  for (int k = 0; k < 7; k++) t->props[k] = sg_prop{S.props[k][0], S.props[k][1], S.props[k][2]};
+  t->props[3] = c->oneStep[rep];
+  return SG_OK;
+}
+
+extern "C" int sg_get_params(sg_ctx *c, int rep, sg_simparams *out) {
+  if (!c || !out || rep < 0 || rep >= c->nrep) return sg_fail(SG_ERR_INVALID, "sg_get_params: bad arguments");
+  sg_thermo t;
+  int rc = sg_get_thermo(c, rep, &t);
+  if (rc) return rc;
+  RepState S;
+  if ((rc = sg_read_state(c, rep, &S))) return rc;
+  sg_simparams p = c->hp[rep];
+  p.stepCount = t.stepCount;
+  p.nebrNow = t.nebrNow;
+  p.dispHi = t.dispHi;
+  p.vSum = t.vSum;
+  p.totEnergy = t.props[0]; p.potEnergy = t.props[1]; p.kinEnergy = t.props[2];
+  p.oneStep = t.props[3]; p.centerOfMass = t.props[4]; p.cmVel = t.props[5]; p.frictForce = t.props[6];
+  p.particleSize = t.particleSize;
+  p.shear = t.shear;
+  p.totalShear = t.totalShear;
+  p.countRdf = c->countRdf;
+  p.countDiffuseAv = S.countDiffuseAv;
+  p.nMolDeposited = S.nMolDeposited;
+  p.moreCycles = (p.stepCount >= p.stepLimit) ? 0 : 1;
+  *out = p;
+  return SG_OK;
+}
+
+template <class T> static int readArr(sg_ctx *c, T *dst, const T *src, size_t n) {
+  CK(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return SG_OK;
+}
+
+extern "C" int sg_get_cells(sg_ctx *c, int rep, int *cellOfOut, int *cellStartOut, int *cellAtomsOut) {
+  if (!c || rep < 0 || rep >= c->nrep) return sg_fail(SG_ERR_INVALID, "sg_get_cells: bad arguments");
+  const RepConst &P = c->hrc[rep];
+  int rc;
+  if (cellOfOut && (rc = readArr(c, cellOfOut, c->cellOf + P.atomOff, P.nMol))) return rc;
+  std::vector<int> cs(P.ncells + 1);
+  if ((rc = readArr(c, cs.data(), c->cellStart + P.cellOff, P.ncells + 1))) return rc;
+  if (cellStartOut)
+    for (int i = 0; i <= P.ncells; i++) cellStartOut[i] = cs[i] - P.atomOff;
+  if (cellAtomsOut) {
+    const int nb = cs[P.ncells] - P.atomOff;
+    std::vector<int> idx(std::max(nb, 1));
+    if (nb > 0 && (rc = readArr(c, idx.data(), c->sortIdx + P.atomOff, nb))) return rc;
+    for (int i = 0; i < P.nMol; i++) cellAtomsOut[i] = (i < nb) ? idx[i] - P.atomOff : -1;
+  }
+  return SG_OK;
+}
+
+extern "C" int sg_get_nebr(sg_ctx *c, int rep, int *nnOut, int *nblOut) {
+  if (!c || rep < 0 || rep >= c->nrep) return sg_fail(SG_ERR_INVALID, "sg_get_nebr: bad arguments");
+  const RepConst &P = c->hrc[rep];
+  std::vector<int> nn(P.nMol);
+  int rc;
+  if ((rc = readArr(c, nn.data(), c->nn + P.atomOff, P.nMol))) return rc;
+  if (nnOut) memcpy(nnOut, nn.data(), sizeof(int) * P.nMol);
+  if (nblOut) {
+    std::vector<int> col(P.nMol);
+    for (int j = 0; j < c->nebrMax; j++) {
+      if ((rc = readArr(c, col.data(), c->nbl + (size_t)j * c->ntot + P.atomOff, P.nMol))) return rc;
+      for (int i = 0; i < P.nMol; i++)
+        nblOut[(size_t)j * P.nMol + i] = (j < nn[i]) ? col[i] - P.atomOff : -1;
+    }
+  }
+  return SG_OK;
+}
+
+static int getMetalArr(sg_ctx *c, int rep, float *out, const float *src) {
+  if (!c || rep < 0 || rep >= c->nrep || !out) return sg_fail(SG_ERR_INVALID, "bad arguments");
+  const RepConst &P = c->hrc[rep];
+  if (P.nMolMe == 0) return SG_OK;
+  return readArr(c, out, src + P.atomOff, P.nMolMe);
+}
+extern "C" int sg_get_rho(sg_ctx *c, int rep, float *rho) { return getMetalArr(c, rep, rho, c ? c->rho : nullptr); }
+extern "C" int sg_get_friction(sg_ctx *c, int rep, float *f) { return getMetalArr(c, rep, f, c ? c->fric : nullptr); }
+
+extern "C" int sg_get_rdf(sg_ctx *c, int rep, unsigned int *hist) {
+  if (!c || rep < 0 || rep >= c->nrep || !hist) return sg_fail(SG_ERR_INVALID, "bad arguments");
+  return readArr(c, hist, c->hist + (size_t)rep * c->histStride, (size_t)c->hp[rep].sizeHistRdf);
+}
+extern "C" int sg_get_rdf_ext(sg_ctx *c, int rep, unsigned long long *hist) {
+  if (!c || rep < 0 || rep >= c->nrep || !hist) return sg_fail(SG_ERR_INVALID, "bad arguments");
+  if (!c->histExt) return sg_fail(SG_ERR_UNSUPPORTED, "extended RDF not enabled (rdf_ext_bins)");
+  return readArr(c, hist, c->histExt + (size_t)rep * c->opt.rdf_ext_bins, (size_t)c->opt.rdf_ext_bins);
+}
+
+extern "C" int sg_get_diffusion(sg_ctx *c, int rep, float *rr_av, int *counts, int *count_av) {
+  if (!c || rep < 0 || rep >= c->nrep) return sg_fail(SG_ERR_INVALID, "bad arguments");
+  const sg_simparams &p = c->hp[rep];
+  if (p.iRegime != 2) return sg_fail(SG_ERR_UNSUPPORTED, "diffusion is measured in regime 2 only");
+  const size_t nf = DiffLayout::floatsPerRep(p.nBuffDiffuse, p.nValDiffuse);
+  std::vector<float> buf(nf);
+  int rc;
+  if ((rc = readArr(c, buf.data(), c->diffBuf + c->diffOffH[rep], nf))) return rc;
+  const float *av = buf.data() + (size_t)p.nBuffDiffuse * 7 + (size_t)p.nBuffDiffuse * p.nValDiffuse;
+  if (rr_av) memcpy(rr_av, av, sizeof(float) * p.nValDiffuse);
+  if (counts)
+    for (int nb = 0; nb < p.nBuffDiffuse; nb++) memcpy(&counts[nb], &buf[7 * nb], sizeof(int));
+  if (count_av) {
+    RepState S;
+    if ((rc = sg_read_state(c, rep, &S))) return rc;
+    *count_av = S.countDiffuseAv;
+  }
+  return SG_OK;
+}
+
+// The last finished diffusion table (what PrintDiffusion writes) and the number produced.
+int sg_get_diffusion_print(sg_ctx *c, int rep, float *table, int *nprints) {
+  const sg_simparams &p = c->hp[rep];
+  const size_t nf = DiffLayout::floatsPerRep(p.nBuffDiffuse, p.nValDiffuse);
+  int rc;
+  if (table && (rc = readArr(c, table, c->diffBuf + c->diffOffH[rep] + nf - p.nValDiffuse, (size_t)p.nValDiffuse)))
+    return rc;
+  if (nprints) {
+    RepState S;
+    if ((rc = sg_read_state(c, rep, &S))) return rc;
+    *nprints = S.diffPrints;
+  }
+  return SG_OK;
+}
+
+extern "C" int sg_get_diag(sg_ctx *c, int rep, sg_diag *d) {
+  if (!c || !d || rep < 0 || rep >= c->nrep) return sg_fail(SG_ERR_INVALID, "bad arguments");
+  RepState S;
+  int rc = sg_read_state(c, rep, &S);
+  if (rc) return rc;
+  memset(d, 0, sizeof(*d));
+  d->max_neighbours = S.maxNeighbours;
+  d->max_cell_occupancy = S.maxCellOcc;
+  d->nebr_overflow = S.nebrOverflow;
+  d->cell_range = S.cellRange;
+  d->cell_overflow = S.cellOverflow;
+  d->rdf_range = S.rdfRange;
+  d->reserved[0] = S.shortStale;
+  return SG_OK;
+}
+
+// Accessors for the other translation units of the library.
+cudaStream_t sg_stream(sg_ctx *c) { return c->stream; }
+const sg_simparams &sg_host_params(sg_ctx *c, int rep) { return c->hp[rep]; }
+int sg_host_step_count(sg_ctx *c) { return c->stepCount; }
+int sg_next_variant(sg_ctx *c) { return stepVariant(c); }
+int sg_launch_step(sg_ctx *c, int variant, bool *rdfPrint) {
+  int rc = launchStep(c, variant);
+  if (rc) return rc;
+  advanceSchedule(c, variant, rdfPrint);
+  return SG_OK;
+}
+sg_prop &sg_one_step_prop(sg_ctx *c, int rep) { return c->oneStep[rep]; }
+int sg_check_flags(sg_ctx *c) { return checkFlags(c); }
+
+// ---- autotuner ----------------------------------------------------------------------------
+// Placeholder: PLAIN mode has no tunable launch shape yet.
+extern "C" int sg_autotune(sg_ctx *c, int, char *report, int report_len) {
+  if (!c) return sg_fail(SG_ERR_INVALID, "null context");
+  if (report && report_len > 0) snprintf(report, report_len, "{}");
+  return SG_OK;
+}

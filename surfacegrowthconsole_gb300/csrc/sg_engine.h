@@ -1,0 +1,73 @@
+// sg_engine.h - internal: the context structure and the functions the translation units of
+// libsgmd share.  Not part of the public C ABI (that is include/sg_api.h).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "sg_api.h"
+#include "sg_device.cuh"
+
+using sg::BlockTab;
+using sg::RepConst;
+using sg::RepState;
+
+// ---- host-side tables ----------------------------------------------------------------------
+struct DevTab {
+  int *rep = nullptr, *start = nullptr;
+  int n = 0;
+  BlockTab view() const { return BlockTab{rep, start, n}; }
+};
+
+struct sg_ctx {
+  int nrep = 0, ntot = 0, ctot = 0, nebrMax = 128, ntiles = 0;
+  sg_options opt;
+  std::vector<sg_simparams> hp;  // parameters as given (mutable fields refreshed on demand)
+  std::vector<RepConst> hrc;
+  std::vector<int> tileFirst, redFirst, cmvFirst;
+  std::vector<size_t> diffOffH;
+  cudaStream_t stream = nullptr;
+  bool ownStream = false;
+  std::vector<void *> allocs;
+  // device arrays
+  RepConst *rc = nullptr;
+  RepState *st = nullptr;
+  float4 *pos = nullptr, *vel = nullptr, *acc = nullptr, *posLo = nullptr, *sortPos = nullptr;
+  int *cellOf = nullptr, *slot = nullptr, *cellCount = nullptr, *cellStart = nullptr;
+  int *tmpIdx = nullptr, *sortIdx = nullptr, *nn = nullptr, *nbl = nullptr, *ns = nullptr, *sl = nullptr;
+  float *rho = nullptr, *dF = nullptr, *Fv = nullptr, *fric = nullptr;
+  float *partial = nullptr, *partialCmv = nullptr;
+  int *dRedFirst = nullptr, *dCmvFirst = nullptr, *tileSum = nullptr, *dTileFirst = nullptr;
+  unsigned *hist = nullptr;
+  unsigned long long *histExt = nullptr;
+  int histStride = 0;
+  float *diffBuf = nullptr;
+  size_t *dDiffOff = nullptr;
+  DevTab atomTab, metalTab, carbonTab, redTab, cmvTab, tileTab;
+  int anyMetal = 0, anyCarbon = 0, maxHist = 0;
+  // graphs keyed by variant bits
+  std::map<int, cudaGraphExec_t> graphs;
+  // host mirror of the schedule
+  int stepCount = 0;
+  int countRdf = 0;
+  std::vector<sg_prop> oneStep;  // per replica, host-accumulated step times
+  void *mixed = nullptr;         // MIXED-mode buffers (sg_kernels_mixed.cu)
+};
+
+
+int sg_fail(int code, const char *fmt, ...);
+int sg_step_async(sg_ctx *c, int nsteps);
+int sg_read_state(sg_ctx *c, int rep, sg::RepState *out);
+int sg_get_diffusion_print(sg_ctx *c, int rep, float *table, int *nprints);
+int sg_next_variant(sg_ctx *c);
+int sg_launch_step(sg_ctx *c, int variant, bool *rdfPrint);
+int sg_check_flags(sg_ctx *c);
+
+// MIXED mode (sg_kernels_mixed.cu)
+int sg_mixed_init(sg_ctx *c);
+void sg_mixed_free(sg_ctx *c);
+int sg_mixed_enqueue_integrate(sg_ctx *c, int forceRebuild);
+int sg_mixed_enqueue_forces(sg_ctx *c);
+int sg_mixed_enqueue_reduce(sg_ctx *c, int forceRebuild);

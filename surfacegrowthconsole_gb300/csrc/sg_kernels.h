@@ -1,0 +1,55 @@
+// sg_kernels.h - kernel entry points of sgmd (device code in sg_kernels_plain.cu and
+// sg_kernels_mixed.cu), launched by sg_engine.cu.
+#pragma once
+#include "sg_device.cuh"
+
+namespace sg {
+
+// ---- shared list building (PLAIN TU, also used by MIXED) ----
+__global__ void k_integrate_first(BlockTab tab, const RepConst *rc, RepState *st, float4 *pos,
+                                  float4 *vel, const float4 *acc, int *cellOf, int *slot,
+                                  int *cellCount, int forceRebuild);
+__global__ void k_cell_count(BlockTab tab, const RepConst *rc, const float4 *pos, int *cellOf,
+                             int *slot, int *cellCount);
+__global__ void k_scan_tiles(BlockTab tab, const RepConst *rc, const RepState *st,
+                             const int *cellCount, int *tileSum, int forceRebuild);
+__global__ void k_scan_tile_prefix(const RepConst *rc, const RepState *st, const int *tileFirst,
+                                   int *tileSum, int forceRebuild);
+__global__ void k_scan_final(BlockTab tab, const RepConst *rc, RepState *st, int *cellCount,
+                             const int *tileSum, int *cellStart, int blockSizeCap, int forceRebuild);
+__global__ void k_scatter(BlockTab tab, const RepConst *rc, RepState *st, const int *cellOf,
+                          const int *slot, const int *cellStart, int *tmpIdx, int *nn, int *ns,
+                          int forceRebuild);
+__global__ void k_rank(BlockTab tab, const RepConst *rc, const RepState *st, const int *cellOf,
+                       const int *cellStart, const int *tmpIdx, const float4 *pos, int *sortIdx,
+                       float4 *sortPos, int forceRebuild);
+__global__ void k_build_nebr(BlockTab tab, const RepConst *rc, RepState *st, const int *cellOf,
+                             const int *cellStart, const float4 *sortPos, int *nn, int *nbl,
+                             int *ns, int *sl, int ntot, int nebrMax, int forceRebuild);
+
+// ---- PLAIN force and step kernels ----
+__global__ void k_rho(BlockTab tab, const RepConst *rc, const float4 *pos, const int *nn,
+                      const int *nbl, float *rho, float *dF, float *Fv, int ntot);
+__global__ void k_force_metal(BlockTab tab, const RepConst *rc, float4 *pos, float4 *acc,
+                              const int *nn, const int *nbl, const float *dF, const float *Fv,
+                              float *fric, int ntot);
+__global__ void k_force_carbon(BlockTab tab, const RepConst *rc, float4 *pos, float4 *acc,
+                               const int *nn, const int *nbl, const int *ns, const int *sl,
+                               RepState *st, int ntot);
+__global__ void k_cmvel(BlockTab tab, const RepConst *rc, RepState *st, const float4 *vel,
+                        const float4 *acc, float *partial, const int *redFirst);
+__global__ void k_step_reduce(BlockTab tab, const RepConst *rc, RepState *st, const float4 *pos,
+                              float4 *vel, const float4 *acc, const float *fric, float *partial,
+                              const int *redFirst, float *diffBuf, const size_t *diffOff,
+                              int forceRebuild);
+__global__ void k_shear(BlockTab tab, const RepConst *rc, RepState *st, const float4 *pos,
+                        float4 *acc);
+__global__ void k_rdf(BlockTab tab, const RepConst *rc, RepState *st, const float4 *pos,
+                      const int *cellOf, const int *cellStart, const int *sortIdx, unsigned *hist,
+                      int histStride);
+__global__ void k_rdf_ext(const RepConst *rc, const float4 *pos, const int *tileRep,
+                          const int *tileStart, unsigned long long *hist, int nbins, float range);
+__global__ void k_apply_pending(BlockTab tab, const RepConst *rc, RepState *st, float4 *vel);
+__global__ void k_clear_pending(RepState *st, int nrep);
+
+}  // namespace sg

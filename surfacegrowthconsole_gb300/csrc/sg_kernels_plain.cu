@@ -1,0 +1,1177 @@
+// sg_kernels_plain.cu - PLAIN-mode (FP32 parity) kernels and the list-building kernels
+// shared by both modes.  Compiled with -fmad=false: every expression below is evaluated in the
+// reference's source order with separately rounded multiplies and adds, so integer results
+// (cell assignment, neighbour lists, RDF counts) and all arithmetic not involving a
+// transcendental function are bit-identical to the reference built without FMA contraction
+// and to the CPU oracle built with -ffp-contract=off.
+//
+// All kernels are batched: blocks are assigned to replicas through BlockTab tables and never
+// straddle two replicas, so per-replica constants are block-uniform.
+#include "sg_device.cuh"
+#include "sg_kernels.h"
+
+namespace sg {
+
+// ============================================================================================
+// Integrator, part 1 (LeapfrogStepK part==1 + ApplyBoundaryCondK, SurfaceGrowth.cu:397-453),
+// fused with: the Berendsen rescale decided at the end of the previous step
+// (ApplyBerendsenThermostat, cu:455-485), regime-1 deposition (InsertAtomsK, cu:488-514,
+// schedule cu:2148-2168) and, on rebuild steps, the histogram pass of the cell counting sort
+// (cell index as BinAtomsIntoCellsK, cu:594-600).
+// ============================================================================================
+__device__ __forceinline__ bool isFrozen(const RepConst &P, int local, float x, float y) {
+  if (local < P.nMolMe) return false;
+  return !((x != P.xLeft) && (x < P.xRight) && (y != P.yTop) && (y != P.yBottom));
+}
+
+__device__ __forceinline__ void depositionPlan(const RepConst &P, const RepState &S, int sc,
+                                               int &nDep, int &nTo, bool &act) {
+  nDep = S.nMolDeposited;
+  nTo = 0;
+  act = false;
+  if (P.iRegime != 1) return;
+  if (sc <= P.stepEquil) {
+    act = true;
+  } else if (nDep < P.nMolMe) {
+    act = true;
+    if ((sc - P.stepEquil) % P.stepDeposit == 0) nTo = P.nMolToDeposit;
+  }
+}
+
+__global__ void k_integrate_first(BlockTab tab, const RepConst *__restrict__ rc, RepState *st,
+                                  float4 *__restrict__ pos, float4 *__restrict__ vel,
+                                  const float4 *__restrict__ acc, int *__restrict__ cellOf,
+                                  int *__restrict__ slot, int *__restrict__ cellCount,
+                                  int forceRebuild) {
+  const int rep = tab.rep[blockIdx.x];
+  const RepConst &P = rc[rep];
+  RepState *S = st + rep;
+  const int g = tab.start[blockIdx.x] + threadIdx.x;
+  const int end = P.atomOff + P.nMol;
+  if (g >= end) return;
+  const int local = g - P.atomOff;
+  const int sc = S->stepCount + 1;
+  float4 r = pos[g];
+  float4 v = vel[g];
+  const float4 a = acc[g];
+  // pending thermostat rescale of the previous step
+  if (S->thermoPending) {
+    if (local >= P.nMolMe) {
+      const float b = S->betaC;
+      v.x = b * v.x; v.y = b * v.y; v.z = b * v.z;
+    } else if (S->thermoMetal) {
+      const float b = S->betaM;
+      v.x = b * v.x; v.y = b * v.y; v.z = b * v.z;
+    }
+  }
+  // deposition (regime 1)
+  if (local < P.nMolMe && P.iRegime == 1) {
+    int nDep, nTo;
+    bool act;
+    depositionPlan(P, *S, sc, nDep, nTo, act);
+    if (act) {
+      if (local >= nDep && local < nDep + nTo) {
+        r.z = 0.49f * P.region[2];
+        v.z = -P.velMagDepos;
+      }
+      if (local >= nDep + nTo) {
+        r.z = 1.5f * P.region[2] + 0.5f * (float)(local + 1) * P.region[2];
+        v.x = 0.f; v.y = 0.f; v.z = 0.f;
+      }
+    }
+  }
+  // Verlet: half kick and drift, unless a frozen graphene edge atom
+  if (!isFrozen(P, local, r.x, r.y)) {
+    const float h = 0.5f * P.deltaT;
+    v.x = v.x + h * a.x;
+    v.y = v.y + h * a.y;
+    v.z = v.z + h * a.z;
+    r.x = r.x + P.deltaT * v.x;
+    r.y = r.y + P.deltaT * v.y;
+    r.z = r.z + P.deltaT * v.z;
+  }
+  // periodic wrap, one image per axis
+  if (r.x >= 0.5f * P.region[0]) r.x -= P.region[0];
+  else if (r.x < -0.5f * P.region[0]) r.x += P.region[0];
+  if (r.y >= 0.5f * P.region[1]) r.y -= P.region[1];
+  else if (r.y < -0.5f * P.region[1]) r.y += P.region[1];
+  if (r.z >= 0.5f * P.region[2]) r.z -= P.region[2];
+  else if (r.z < -0.5f * P.region[2]) r.z += P.region[2];
+  pos[g] = r;
+  vel[g] = v;
+  if (forceRebuild || S->nebrNow) {
+    const int c = cellIndex(P, r.x, r.y, r.z);
+    cellOf[g] = c;
+    if (c >= 0) slot[g] = atomicAdd(&cellCount[P.cellOff + c], 1);
+  }
+}
+
+// Histogram pass alone (used when lists are rebuilt outside a step).
+__global__ void k_cell_count(BlockTab tab, const RepConst *__restrict__ rc,
+                             const float4 *__restrict__ pos, int *__restrict__ cellOf,
+                             int *__restrict__ slot, int *__restrict__ cellCount) {
+  const int rep = tab.rep[blockIdx.x];
+  const RepConst &P = rc[rep];
+  const int g = tab.start[blockIdx.x] + threadIdx.x;
+  if (g >= P.atomOff + P.nMol) return;
+  const float4 r = pos[g];
+  const int c = cellIndex(P, r.x, r.y, r.z);
+  cellOf[g] = c;
+  if (c >= 0) slot[g] = atomicAdd(&cellCount[P.cellOff + c], 1);
+}
+
+__device__ __forceinline__ bool rebuilding(const RepState *S, int forceRebuild) {
+  return forceRebuild || S->nebrNow;
+}
+
+// ============================================================================================
+// Counting sort of atoms by cell: exclusive scan of the per-cell counts, in three passes
+// (tile sums, per-replica tile prefix, in-tile scan), then scatter and in-cell ordering.
+// ============================================================================================
+__global__ void k_scan_tiles(BlockTab tab, const RepConst *__restrict__ rc, const RepState *st,
+                             const int *__restrict__ cellCount, int *__restrict__ tileSum,
+                             int forceRebuild) {
+  const int rep = tab.rep[blockIdx.x];
+  if (!rebuilding(st + rep, forceRebuild)) return;
+  const RepConst &P = rc[rep];
+  const int c0 = tab.start[blockIdx.x];  // local cell index of the tile start
+  int s = 0;
+  for (int c = c0 + threadIdx.x; c < c0 + kCellTile; c += blockDim.x) s += cellCount[P.cellOff + c];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  __shared__ int ws[32];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    int v = (threadIdx.x < (blockDim.x >> 5)) ? ws[threadIdx.x] : 0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) tileSum[blockIdx.x] = v;
+  }
+}
+
+// One block per replica: exclusive prefix over the replica's tiles (tiles of a replica are
+// consecutive blocks of the tile table starting at tileFirst[rep]).
+__global__ void k_scan_tile_prefix(const RepConst *__restrict__ rc, const RepState *st,
+                                   const int *__restrict__ tileFirst, int *__restrict__ tileSum,
+                                   int forceRebuild) {
+  const int rep = blockIdx.x;
+  if (!rebuilding(st + rep, forceRebuild)) return;
+  const RepConst &P = rc[rep];
+  const int t0 = tileFirst[rep];
+  const int nt = P.ncellsPad / kCellTile;
+  __shared__ int carry;
+  __shared__ int ws[32];
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < nt; base += blockDim.x) {
+    const int t = base + threadIdx.x;
+    int v = (t < nt) ? tileSum[t0 + t] : 0;
+    // inclusive warp scan
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, x, o);
+      if ((threadIdx.x & 31) >= o) x += y;
+    }
+    if ((threadIdx.x & 31) == 31) ws[threadIdx.x >> 5] = x;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      int w = (threadIdx.x < (blockDim.x >> 5)) ? ws[threadIdx.x] : 0;
+      for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, w, o);
+        if (threadIdx.x >= o) w += y;
+      }
+      ws[threadIdx.x] = w;
+    }
+    __syncthreads();
+    const int warpPrefix = (threadIdx.x >= 32) ? ws[(threadIdx.x >> 5) - 1] : 0;
+    const int excl = carry + warpPrefix + x - v;
+    if (t < nt) tileSum[t0 + t] = excl;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = excl + v;
+    __syncthreads();
+  }
+}
+
+// In-tile exclusive scan; writes global cellStart (index into the sorted arrays) and clears
+// the counts for the next rebuild.  Also records the largest cell occupancy.
+__global__ void k_scan_final(BlockTab tab, const RepConst *__restrict__ rc, RepState *st,
+                             int *__restrict__ cellCount, const int *__restrict__ tileSum,
+                             int *__restrict__ cellStart, int blockSizeCap, int forceRebuild) {
+  const int rep = tab.rep[blockIdx.x];
+  RepState *S = st + rep;
+  if (!rebuilding(S, forceRebuild)) return;
+  const RepConst &P = rc[rep];
+  const int c0 = tab.start[blockIdx.x];
+  constexpr int kPer = kCellTile / 256;  // launched with 256 threads
+  int v[kPer];
+  int sum = 0, occ = 0, over = 0;
+  const int cb = P.cellOff + c0 + threadIdx.x * kPer;
+#pragma unroll
+  for (int i = 0; i < kPer; i++) {
+    v[i] = cellCount[cb + i];
+    occ = max(occ, v[i]);
+    over += (v[i] > blockSizeCap) ? 1 : 0;
+    sum += v[i];
+  }
+  __shared__ int ws[8];
+  int x = sum;
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) >= o) x += y;
+  }
+  if ((threadIdx.x & 31) == 31) ws[threadIdx.x >> 5] = x;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    int w = (threadIdx.x < 8) ? ws[threadIdx.x] : 0;
+    for (int o = 1; o < 8; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, w, o);
+      if (threadIdx.x >= o) w += y;
+    }
+    if (threadIdx.x < 8) ws[threadIdx.x] = w;
+  }
+  __syncthreads();
+  int run = P.atomOff + tileSum[blockIdx.x] + ((threadIdx.x >= 32) ? ws[(threadIdx.x >> 5) - 1] : 0) + x - sum;
+#pragma unroll
+  for (int i = 0; i < kPer; i++) {
+    cellStart[cb + i] = run;
+    run += v[i];
+    cellCount[cb + i] = 0;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    occ = max(occ, __shfl_xor_sync(0xffffffffu, occ, o));
+    over += __shfl_xor_sync(0xffffffffu, over, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (occ > 0) atomicMax(&S->maxCellOcc, occ);
+    if (over > 0) {
+      atomicAdd(&S->cellOverflow, over);
+      setFlag(S, 11 /*SG_ERR_CELL_OVERFLOW*/);
+    }
+  }
+}
+
+// Scatter atoms into their cell segments in arrival order.
+__global__ void k_scatter(BlockTab tab, const RepConst *__restrict__ rc, RepState *st,
+                          const int *__restrict__ cellOf, const int *__restrict__ slot,
+                          const int *__restrict__ cellStart, int *__restrict__ tmpIdx,
+                          int *__restrict__ nn, int *__restrict__ ns, int forceRebuild) {
+  const int rep = tab.rep[blockIdx.x];
+  RepState *S = st + rep;
+  if (!rebuilding(S, forceRebuild)) return;
+  const RepConst &P = rc[rep];
+  const int g = tab.start[blockIdx.x] + threadIdx.x;
+  if (g >= P.atomOff + P.nMol) return;
+  const int c = cellOf[g];
+  if (c >= 0) {
+    tmpIdx[cellStart[P.cellOff + c] + slot[g]] = g;
+  } else {
+    nn[g] = 0;  // an atom outside the grid has no neighbours (the reference clears NN)
+    ns[g] = 0;
+    atomicAdd(&S->cellRange, 1);
+  }
+}
+
+// Order each cell by ascending atom index: the rank of an atom is the number of atoms of its
+// cell with a smaller index.  Writes the sorted index and a sorted position copy whose w holds
+// the atom index (as int bits) for the neighbour search.
+__global__ void k_rank(BlockTab tab, const RepConst *__restrict__ rc, const RepState *st,
+                       const int *__restrict__ cellOf, const int *__restrict__ cellStart,
+                       const int *__restrict__ tmpIdx, const float4 *__restrict__ pos,
+                       int *__restrict__ sortIdx, float4 *__restrict__ sortPos, int forceRebuild) {
+  const int rep = tab.rep[blockIdx.x];
+  if (!rebuilding(st + rep, forceRebuild)) return;
+  const RepConst &P = rc[rep];
+  const int g = tab.start[blockIdx.x] + threadIdx.x;
+  if (g >= P.atomOff + P.nMol) return;
+  const int c = cellOf[g];
+  if (c < 0) return;
+  const int b = cellStart[P.cellOff + c], e = cellStart[P.cellOff + c + 1];
+  int rank = 0;
+  for (int q = b; q < e; q++) rank += (tmpIdx[q] < g) ? 1 : 0;
+  sortIdx[b + rank] = g;
+  float4 r = pos[g];
+  r.w = __int_as_float(g);
+  sortPos[b + rank] = r;
+}
+
+// ============================================================================================
+// Neighbour list (BuildNebrListK, SurfaceGrowth.cu:612-711): one thread per sorted slot, so a
+// warp mostly shares one home cell and walks the same 27 segments.  Entries are emitted in
+// stencil order, ascending atom index inside a cell.  Also emits the short list: the
+// neighbours within (rCutC + skin) in list order, used by the graphene second-neighbour walk.
+// ============================================================================================
+__global__ void k_build_nebr(BlockTab tab, const RepConst *__restrict__ rc, RepState *st,
+                             const int *__restrict__ cellOf, const int *__restrict__ cellStart,
+                             const float4 *__restrict__ sortPos, int *__restrict__ nn,
+                             int *__restrict__ nbl, int *__restrict__ ns, int *__restrict__ sl,
+                             int ntot, int nebrMax, int forceRebuild) {
+  const int rep = tab.rep[blockIdx.x];
+  RepState *S = st + rep;
+  if (!rebuilding(S, forceRebuild)) return;
+  const RepConst &P = rc[rep];
+  const int s = tab.start[blockIdx.x] + threadIdx.x;
+  const int binnedEnd = cellStart[P.cellOff + P.ncells];
+  int want = 0, over = 0;
+  if (s < binnedEnd) {
+    const float4 A = sortPos[s];
+    const int g = __float_as_int(A.w);
+    const int c = cellOf[g];
+    int n = 0, m = 0;
+    for (int o = 0; o < 27; o++) {
+      float sx, sy, sz;
+      const int C = stencilCell(P, c, o, sx, sy, sz);
+      const int qb = cellStart[P.cellOff + C], qe = cellStart[P.cellOff + C + 1];
+      for (int q = qb; q < qe; q++) {
+        const float4 B = sortPos[q];
+        const int k = __float_as_int(B.w);
+        float dx = A.x - B.x, dy = A.y - B.y, dz = A.z - B.z;
+        dx = dx - sx; dy = dy - sy; dz = dz - sz;
+        const float rr = dx * dx + dy * dy + dz * dz;
+        if ((rr < P.rrNebr) && (g != k)) {
+          if (n < nebrMax) nbl[(size_t)n * ntot + g] = k;
+          n++;
+          if (rr < P.rrShort) {
+            if (m < kShortMax) sl[(size_t)m * ntot + g] = k;
+            m++;
+          }
+        }
+      }
+    }
+    want = n;
+    if (n > nebrMax) over = 1;
+    nn[g] = min(n, nebrMax);
+    ns[g] = (m > kShortMax || n > nebrMax) ? -1 : m;  // -1: walk the full list instead
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    want = max(want, __shfl_xor_sync(0xffffffffu, want, o));
+    over += __shfl_xor_sync(0xffffffffu, over, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (want > 0) atomicMax(&S->maxNeighbours, want);
+    if (over > 0) {
+      atomicAdd(&S->nebrOverflow, over);
+      setFlag(S, 5 /*SG_ERR_NEBR_OVERFLOW*/);
+    }
+  }
+}
+
+// ============================================================================================
+// EAM (Zhou-Wadley-Johnson analytic forms, SurfaceGrowth.cu:46-210).  The pair functions
+// share their exponentials and powers; each value is the one the reference's separate
+// function calls produce for the same argument.
+// ============================================================================================
+struct EamPair {
+  float phi, dphi, df;
+};
+__device__ __forceinline__ EamPair eamPair(const RepConst &P, float r) {
+  const float x = r * P.rei;
+  const float xm1 = x - 1.f;
+  const float eA = expf(-P.alpha * xm1);
+  const float eB = expf(-P.beta * xm1);
+  const float pk = x - P.kappa, pl = x - P.lambda;
+  const float dA = 1.f + powf(pk, 20.f);
+  const float dB = 1.f + powf(pl, 20.f);
+  const float tA = P.alpha + 20.f * powf(pk, 19.f) / dA;
+  const float tB = P.beta + 20.f * powf(pl, 19.f) / dB;
+  EamPair e;
+  e.phi = P.A * eA / dA - P.B * eB / dB;
+  e.dphi = (-P.A * eA * tA / dA + P.B * eB * tB / dB) * P.rei;
+  e.df = -P.fe * P.rei * eB * tB / dB;
+  return e;
+}
+__device__ __forceinline__ float eamDensity(const RepConst &P, float r) {
+  const float x = r * P.rei;
+  return P.fe * expf(-P.beta * (x - 1.f)) / (1.f + powf(x - P.lambda, 20.f));
+}
+__device__ __forceinline__ float eamEmbed(const RepConst &P, float rho) {
+  const float rhon = 0.85f * P.rhoe;
+  if (rho < rhon) {
+    const float rhoni = P.rhoei * 1.176471f;
+    const float x = rho * rhoni - 1.f;
+    return P.Fn[0] + P.Fn[1] * x + P.Fn[2] * x * x + P.Fn[3] * x * x * x;
+  }
+  const float rhoo = 1.15f * P.rhoe;
+  if ((rho >= rhon) && (rho < rhoo)) {
+    const float x = rho * P.rhoei - 1.f;
+    return P.F[0] + P.F[1] * x + P.F[2] * x * x + P.F[3] * x * x * x;
+  }
+  if (rho >= rhoo) {
+    const float x = rho * P.rhoei;
+    return P.Fe * (1.f - logf(powf(x, P.eta))) * powf(x, P.eta);
+  }
+  return 0.f;
+}
+__device__ __forceinline__ float eamEmbedDeriv(const RepConst &P, float rho) {
+  const float rhon = 0.85f * P.rhoe;
+  if (rho < rhon) {
+    const float rhoni = P.rhoei * 1.176471f;
+    const float x = rho * rhoni - 1.f;
+    return rhoni * (P.Fn[1] + 2.f * P.Fn[2] * x + 3.f * P.Fn[3] * x * x);
+  }
+  const float rhoo = 1.15f * P.rhoe;
+  if ((rho >= rhon) && (rho < rhoo)) {
+    const float y = rho * P.rhoei;
+    return P.rhoei * (P.F[1] + 2.f * P.F[2] * (y - 1.f) + 3.f * P.F[3] * (y - 1.f) * (y - 1.f));
+  }
+  if (rho >= rhoo) {
+    const float y = rho * P.rhoei;
+    return -P.Fe * P.eta * P.rhoei * powf(y, (P.eta - 1.f)) * logf(powf(y, P.eta));
+  }
+  return 0.f;
+}
+
+// Electron density of each metal atom (EamComputeRhoK, cu:716-773), plus F(rho) and F'(rho),
+// which the reference re-evaluates per pair in the force kernel.
+__global__ void k_rho(BlockTab tab, const RepConst *__restrict__ rc, const float4 *__restrict__ pos,
+                      const int *__restrict__ nn, const int *__restrict__ nbl,
+                      float *__restrict__ rho, float *__restrict__ dF, float *__restrict__ Fv,
+                      int ntot) {
+  const int rep = tab.rep[blockIdx.x];
+  const RepConst &P = rc[rep];
+  const int i = tab.start[blockIdx.x] + threadIdx.x;
+  const int metalEnd = P.atomOff + P.nMolMe;
+  if (i >= metalEnd) return;
+  const float4 A = pos[i];
+  const int n = nn[i];
+  float sum = 0.f;
+  for (int j = 0; j < n; j++) {
+    const int k = nbl[(size_t)j * ntot + i];
+    const float4 B = pos[k];
+    const float dx = minImg(A.x - B.x, P.region[0]);
+    const float dy = minImg(A.y - B.y, P.region[1]);
+    const float dz = minImg(A.z - B.z, P.region[2]);
+    const float rr = dx * dx + dy * dy + dz * dz;
+    if ((rr < P.rrCutEam) && (k < metalEnd)) sum += eamDensity(P, sqrtf(rr));
+  }
+  rho[i] = sum;
+  dF[i] = eamEmbedDeriv(P, sum);
+  Fv[i] = eamEmbed(P, sum);
+}
+
+// Lennard-Jones metal-carbon term (cu:880-884).
+__device__ __forceinline__ void ljTerms(const RepConst &P, float rr, float &fc, float &u) {
+  const float rri = P.sigmaLJ * P.sigmaLJ / rr;
+  const float rri3 = rri * rri * rri;
+  fc = 48.f * P.epsLJ * rri3 * (rri3 - 0.5f) * rri / (P.sigmaLJ * P.sigmaLJ);
+  u = 4.f * P.epsLJ * rri3 * (rri3 - 1.f);
+}
+
+// Forces on metal atoms: EAM pair + embedding with metal neighbours, LJ with carbon neighbours
+// (ComputeForcesK case 0, cu:856-897, epilogue cu:1069-1082).
+__global__ void k_force_metal(BlockTab tab, const RepConst *__restrict__ rc, float4 *__restrict__ pos,
+                              float4 *__restrict__ acc, const int *__restrict__ nn,
+                              const int *__restrict__ nbl, const float *__restrict__ dF,
+                              const float *__restrict__ Fv, float *__restrict__ fric, int ntot) {
+  const int rep = tab.rep[blockIdx.x];
+  const RepConst &P = rc[rep];
+  const int i = tab.start[blockIdx.x] + threadIdx.x;
+  const int metalEnd = P.atomOff + P.nMolMe;
+  if (i >= metalEnd) return;
+  const float4 A = pos[i];
+  const int n = nn[i];
+  const float dFi = dF[i];
+  float fx = 0.f, fy = 0.f, fz = 0.f, rx = 0.f, ry = 0.f, rz = 0.f, u = 0.f;
+  for (int j = 0; j < n; j++) {
+    const int k = nbl[(size_t)j * ntot + i];
+    const float4 B = pos[k];
+    const float dx = minImg(A.x - B.x, P.region[0]);
+    const float dy = minImg(A.y - B.y, P.region[1]);
+    const float dz = minImg(A.z - B.z, P.region[2]);
+    const float rr = dx * dx + dy * dy + dz * dz;
+    if (k < metalEnd) {
+      if (rr >= P.rrCutEam) continue;  // the reference computes and then zeroes the term
+      const float r = sqrtf(rr);
+      const EamPair e = eamPair(P, r);
+      float fc = -e.dphi;
+      fc = fc - e.df * (dFi + dF[k]);
+      fc = fc / r;
+      fx = fx + fc * dx; fy = fy + fc * dy; fz = fz + fc * dz;
+      u += e.phi;
+    } else {
+      if (rr >= P.rrCutLJ) continue;
+      float fc, ul;
+      ljTerms(P, rr, fc, ul);
+      u += ul;
+      fx = fx + fc * dx; fy = fy + fc * dy; fz = fz + fc * dz;
+      rx = rx + fc * dx; ry = ry + fc * dy; rz = rz + fc * dz;
+    }
+  }
+  acc[i] = make_float4(fx / P.massMe, fy / P.massMe, fz / P.massMe, 0.f);
+  pos[i].w = 0.5f * u + Fv[i];
+  if (P.hasFric) fric[i] = rx;
+}
+
+// Forces on carbon atoms: LJ with metal neighbours and the harmonic graphene terms over the
+// first three carbon neighbours within rCutC, including the second-neighbour angle terms
+// (ComputeForcesK case 1, cu:899-1063, epilogue cu:1083-1088).  The second-neighbour walk
+// uses the neighbour's short list, which holds every entry of its full list that can be
+// within rCutC before the next rebuild, in the same order.
+__global__ void k_force_carbon(BlockTab tab, const RepConst *__restrict__ rc,
+                               float4 *__restrict__ pos, float4 *__restrict__ acc,
+                               const int *__restrict__ nn, const int *__restrict__ nbl,
+                               const int *__restrict__ ns, const int *__restrict__ sl,
+                               RepState *st, int ntot) {
+  const int rep = tab.rep[blockIdx.x];
+  const RepConst &P = rc[rep];
+  const int i = tab.start[blockIdx.x] + threadIdx.x;
+  const int metalEnd = P.atomOff + P.nMolMe;
+  if (i >= P.atomOff + P.nMol) return;
+  const float4 A = pos[i];
+  const int nNeigh = nn[i];
+  float fx = 0.f, fy = 0.f, fz = 0.f, u = 0.f;
+  float rnx[3], rny[3], rnz[3], absR[3], dzs[3];
+  int counti = 0;
+  // own short-list pointer, to check that the list still holds every close neighbour
+  const int myNs = ns[i];
+  int sp = 0, stale = 0, checked = -1;
+  for (int j = 0; j < nNeigh; j++) {
+    const int k = nbl[(size_t)j * ntot + i];
+    const float4 B = pos[k];
+    const float dx = minImg(A.x - B.x, P.region[0]);
+    const float dy = minImg(A.y - B.y, P.region[1]);
+    const float dz = minImg(A.z - B.z, P.region[2]);
+    const float rr = dx * dx + dy * dy + dz * dz;
+    if (j > checked) {  // first visit of this entry (the walk may resume at entry 4)
+      checked = j;
+      if (rr < P.rrCutC && myNs >= 0) {
+        while (sp < myNs && sl[(size_t)sp * ntot + i] != k) sp++;
+        if (sp >= myNs) stale = 1;
+        else sp++;
+      }
+    }
+    if (k < metalEnd) {
+      if (rr >= P.rrCutLJ) continue;
+      float fc, ul;
+      ljTerms(P, rr, fc, ul);
+      u += ul;
+      fx = fx + fc * dx; fy = fy + fc * dy; fz = fz + fc * dz;
+      continue;
+    }
+    if ((rr < P.rrCutC) && (counti < 3)) {
+      absR[counti] = sqrtf(rr);
+      dzs[counti] = B.z - P.z_0;
+      rnx[counti] = dx; rny[counti] = dy; rnz[counti] = dz;
+      const int nk = ns[k];
+      const bool full = nk < 0;
+      const int lim = full ? nn[k] : nk;
+      int countk = 0;
+      for (int l = 0; l < lim; l++) {
+        const int m = full ? nbl[(size_t)l * ntot + k] : sl[(size_t)l * ntot + k];
+        const float4 rm = pos[m];
+        float ex = minImg(B.x - rm.x, P.region[0]);
+        float ey = minImg(B.y - rm.y, P.region[1]);
+        float ez = minImg(B.z - rm.z, P.region[2]);
+        const float rr2 = ex * ex + ey * ey + ez * ez;
+        if ((rr2 < P.rrCutC) && (m != i)) {
+          ex = ex * (-1.f); ey = ey * (-1.f); ez = ez * (-1.f);
+          const float cs = (rnx[counti] * ex + rny[counti] * ey + rnz[counti] * ez) / (absR[counti] * rr2);
+          const float th = acosf(cs);
+          const float dth = th - P.theta_0;
+          const float tmp = P.mu_theta * dth / sqrtf(1.f - cs * cs);
+          float fc = tmp / (absR[counti] * rr2);
+          fx = fx + fc * ex; fy = fy + fc * ey; fz = fz + fc * ez;
+          fc = -tmp * cs / (absR[counti] * absR[counti]);
+          fx = fx + fc * rnx[counti]; fy = fy + fc * rny[counti]; fz = fz + fc * rnz[counti];
+          fc = -P.mu_p * (rm.z - P.z_0) / 9.f;
+          fx = fx + 0.f; fy = fy + 0.f; fz = fz + fc;
+          ++countk;
+        }
+        if (countk == 2) break;
+      }
+      ++counti;
+    }
+    if (counti == 3) {
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        const float fc = -P.mu_r * (absR[q] - 1.f) / absR[q];
+        fx = fx + fc * rnx[q]; fy = fy + fc * rny[q]; fz = fz + fc * rnz[q];
+        u += P.mu_r * (absR[q] - 1.f) * (absR[q] - 1.f);
+      }
+      float dZ = 2.f * (A.z - P.z_0) - (dzs[0] + dzs[1] + dzs[2]);
+      const float fcz = -0.666666667f * P.mu_p * dZ;
+      fx = fx + 0.f; fy = fy + 0.f; fz = fz + fcz;
+      dZ = (A.z - P.z_0) - 0.33333333f * (dzs[0] + dzs[1] + dzs[2]);
+      u += P.mu_p * dZ * dZ;
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        const int p0 = (q == 0) ? 0 : (q == 1) ? 1 : 2;
+        const int p1 = (q == 0) ? 1 : (q == 1) ? 2 : 0;
+        const float cs = (rnx[p0] * rnx[p1] + rny[p0] * rny[p1] + rnz[p0] * rnz[p1]) / (absR[p0] * absR[p1]);
+        const float th = acosf(cs);
+        const float dth = th - P.theta_0;
+        const float tmp = P.mu_theta * dth / sqrtf(1.f - cs * cs);
+        float fc = tmp * (1.f - absR[p0] * cs / absR[p1]) / (absR[p0] * absR[p1]);
+        fx = fx + fc * rnx[p1]; fy = fy + fc * rny[p1]; fz = fz + fc * rnz[p1];
+        fc = tmp * (1.f - absR[p1] * cs / absR[p0]) / (absR[p0] * absR[p1]);
+        fx = fx + fc * rnx[p0]; fy = fy + fc * rny[p0]; fz = fz + fc * rnz[p0];
+        u += P.mu_theta * dth * dth;
+      }
+      // The reference's radial loop reuses the neighbour-loop counter (cu:989): the walk
+      // resumes at list entry 4.
+      j = 3;
+      counti = 4;
+    }
+  }
+  acc[i] = make_float4(fx, fy, fz, 0.f);
+  pos[i].w = 0.5f * u;
+  if (stale) atomicAdd(&st[rep].shortStale, 1);
+}
+
+// ============================================================================================
+// Reductions in the reference's tree order (cu:1101-1892): a block of 512 threads reduces the
+// 1024 elements [1024 b, 1024 b + 1024) with the stride-halving tree, the last block of the
+// replica reduces the block partials in a zero-padded 1024-slot tree.
+// ============================================================================================
+__device__ __forceinline__ int slotOp(int s) {  // 0 add, 1 max, 2 min
+  return (s == RS_VVMAX || (s >= RS_MAX_X && s <= RS_MAX_Z)) ? 1 : (s >= RS_MIN_X && s <= RS_MIN_Z) ? 2 : 0;
+}
+__device__ __forceinline__ float combine(int op, float a, float b) {
+  if (op == 0) return a + b;
+  if (op == 1) return (a < b) ? b : a;
+  return (a > b) ? b : a;
+}
+
+// Tree over 512 per-thread values (after the first level, done in registers), for NV values
+// per element; strides 256..32 through shared memory, 16..1 with shuffles in warp 0 (the same
+// pairing as the reference's shared-memory tree).  Result valid in thread 0.
+template <int NV>
+__device__ __forceinline__ void blockTree512(float (&x)[NV], const int *ops, float (*sh)[kRedThreads]) {
+  const int t = threadIdx.x;
+#pragma unroll
+  for (int v = 0; v < NV; v++) sh[v][t] = x[v];
+  __syncthreads();
+  for (int s = 256; s >= 32; s >>= 1) {
+    if (t < s) {
+#pragma unroll
+      for (int v = 0; v < NV; v++) sh[v][t] = combine(ops[v], sh[v][t], sh[v][t + s]);
+    }
+    __syncthreads();
+  }
+  if (t < 32) {
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+      float y = sh[v][t];
+      for (int s = 16; s >= 1; s >>= 1) {
+        const float o = __shfl_down_sync(0xffffffffu, y, s);
+        y = combine(ops[v], y, o);
+      }
+      x[v] = y;
+    }
+  }
+}
+
+// Centre-of-mass velocity of the metal (ComputeCmVelK, cu:1560-1638) on the velocities after
+// the second half kick, which k_step_reduce applies; launched over the metal reduction blocks.
+__global__ void __launch_bounds__(kRedThreads) k_cmvel(BlockTab tab, const RepConst *__restrict__ rc,
+                                                       RepState *st, const float4 *__restrict__ vel,
+                                                       const float4 *__restrict__ acc,
+                                                       float *__restrict__ partial,
+                                                       const int *__restrict__ redFirst) {
+  const int rep = tab.rep[blockIdx.x];
+  const RepConst &P = rc[rep];
+  RepState *S = st + rep;
+  const int b = tab.start[blockIdx.x];  // local reduction block index
+  const int t = threadIdx.x;
+  const float h = 0.5f * P.deltaT;
+  float e[2][3];
+#pragma unroll
+  for (int half = 0; half < 2; half++) {
+    const int local = kRedElems * b + half * kRedThreads + t;
+    if (local < P.nMolMe) {
+      const float4 v = vel[P.atomOff + local];
+      const float4 a = acc[P.atomOff + local];
+      e[half][0] = v.x + h * a.x;
+      e[half][1] = v.y + h * a.y;
+      e[half][2] = v.z + h * a.z;
+    } else {
+      e[half][0] = e[half][1] = e[half][2] = 0.f;
+    }
+  }
+  float x[3] = {e[0][0] + e[1][0], e[0][1] + e[1][1], e[0][2] + e[1][2]};
+  __shared__ float sh[3][kRedThreads];
+  const int ops[3] = {0, 0, 0};
+  blockTree512<3>(x, ops, sh);
+  __shared__ bool last;
+  float *part = partial + (size_t)redFirst[rep] * 3;
+  const int nMetalBlocks = (P.nMolMe + kRedElems - 1) / kRedElems;
+  if (t == 0) {
+    part[3 * b + 0] = x[0]; part[3 * b + 1] = x[1]; part[3 * b + 2] = x[2];
+    __threadfence();
+    const unsigned prev = atomicAdd(&S->cmvCounter, 1u);
+    last = (prev == (unsigned)nMetalBlocks - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  // final tree over the block partials (slots beyond the metal blocks are zero, as the
+  // reference's non-metal blocks contribute zero sums)
+  float y[3] = {0.f, 0.f, 0.f};
+  float carry[3] = {0.f, 0.f, 0.f};
+  for (int base = 0; base < nMetalBlocks; base += kRedElems) {
+    float lo[3], hi[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      lo[c] = (base + t < nMetalBlocks) ? __ldcg(part + 3 * (base + t) + c) : 0.f;
+      hi[c] = (base + kRedThreads + t < nMetalBlocks) ? __ldcg(part + 3 * (base + kRedThreads + t) + c) : 0.f;
+      y[c] = lo[c] + hi[c];
+    }
+    __syncthreads();
+    blockTree512<3>(y, ops, sh);
+    if (t == 0) {
+#pragma unroll
+      for (int c = 0; c < 3; c++) carry[c] = (base == 0) ? y[c] : carry[c] + y[c];
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
+    S->cmVel[0] = carry[0]; S->cmVel[1] = carry[1]; S->cmVel[2] = carry[2];
+    S->cmvCounter = 0;
+  }
+}
+
+// Per-element values of the step reduction for local atom index `local`.
+__device__ __forceinline__ void stepElem(const RepConst &P, int local, const float4 &r,
+                                         const float4 &v, float frc, float cmVelX,
+                                         float (&e)[kNumRed]) {
+  if (local >= P.nMol) {
+#pragma unroll
+    for (int s = 0; s < kNumRed; s++) e[s] = 0.f;
+    return;
+  }
+  const bool metal = local < P.nMolMe;
+  e[RS_VSUM_X] = metal ? P.massMe * v.x : v.x;  // cu:1123-1126
+  e[RS_VSUM_Y] = v.y;
+  e[RS_VSUM_Z] = v.z;
+  e[RS_VVMAX] = v.x * v.x + v.y * v.y + v.z * v.z;
+  float vx = v.x;
+  if (P.iRegime == 2 && metal) vx = vx - cmVelX;  // cu:1230-1234
+  float vv = vx * vx + v.y * v.y + v.z * v.z;
+  if (metal) vv = P.massMe * vv;
+  e[RS_VVSUM] = vv;
+  e[RS_USUM] = r.w;
+  e[RS_CM_X] = metal ? r.x : 0.f;
+  e[RS_CM_Y] = metal ? r.y : 0.f;
+  e[RS_CM_Z] = metal ? r.z : 0.f;
+  e[RS_MIN_X] = e[RS_CM_X]; e[RS_MIN_Y] = e[RS_CM_Y]; e[RS_MIN_Z] = e[RS_CM_Z];
+  e[RS_MAX_X] = e[RS_CM_X]; e[RS_MAX_Y] = e[RS_CM_Y]; e[RS_MAX_Z] = e[RS_CM_Z];
+  e[RS_FRICT] = metal ? frc : 0.f;
+}
+
+__device__ void stepControl(const RepConst &P, RepState *S, const float (&red)[kNumRed],
+                            float *diff, int forceRebuild);
+
+// Verlet part 2 (LeapfrogStepK part==2, cu:2253) fused with all property reductions of the
+// step; the last block of each replica runs the step's scalar control (stepControl).
+__global__ void __launch_bounds__(kRedThreads) k_step_reduce(
+    BlockTab tab, const RepConst *__restrict__ rc, RepState *st, const float4 *__restrict__ pos,
+    float4 *__restrict__ vel, const float4 *__restrict__ acc, const float *__restrict__ fric,
+    float *__restrict__ partial, const int *__restrict__ redFirst, float *__restrict__ diffBuf,
+    const size_t *__restrict__ diffOff, int forceRebuild) {
+  const int rep = tab.rep[blockIdx.x];
+  const RepConst &P = rc[rep];
+  RepState *S = st + rep;
+  const int b = tab.start[blockIdx.x];
+  const int t = threadIdx.x;
+  const float h = 0.5f * P.deltaT;
+  const float cmVelX = (P.nMolMe != 0) ? S->cmVel[0] / (float)P.nMolMe : 0.f;
+  float e0[kNumRed], e1[kNumRed];
+#pragma unroll
+  for (int half = 0; half < 2; half++) {
+    const int local = kRedElems * b + half * kRedThreads + t;
+    float4 r = make_float4(0.f, 0.f, 0.f, 0.f), v = r;
+    float frc = 0.f;
+    if (local < P.nMol) {
+      const int g = P.atomOff + local;
+      r = pos[g];
+      v = vel[g];
+      if (!isFrozen(P, local, r.x, r.y)) {
+        const float4 a = acc[g];
+        v.x = v.x + h * a.x;
+        v.y = v.y + h * a.y;
+        v.z = v.z + h * a.z;
+        vel[g] = v;
+      }
+      if (local < P.nMolMe && P.hasFric) frc = fric[g];
+    }
+    if (half == 0) stepElem(P, local, r, v, frc, cmVelX, e0);
+    else stepElem(P, local, r, v, frc, cmVelX, e1);
+  }
+  int ops[kNumRed];
+  float x[kNumRed];
+#pragma unroll
+  for (int s = 0; s < kNumRed; s++) {
+    ops[s] = slotOp(s);
+    x[s] = combine(ops[s], e0[s], e1[s]);
+  }
+  __shared__ float sh[kNumRed][kRedThreads];
+  blockTree512<kNumRed>(x, ops, sh);
+  __shared__ bool last;
+  float *part = partial + (size_t)redFirst[rep] * kNumRed;
+  if (t == 0) {
+#pragma unroll
+    for (int s = 0; s < kNumRed; s++) part[kNumRed * b + s] = x[s];
+    __threadfence();
+    const unsigned prev = atomicAdd(&S->redCounter, 1u);
+    last = (prev == (unsigned)P.nRedBlocks - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  float y[kNumRed], carry[kNumRed];
+  for (int base = 0; base < P.nRedBlocks; base += kRedElems) {
+#pragma unroll
+    for (int s = 0; s < kNumRed; s++) {
+      const float lo = (base + t < P.nRedBlocks) ? __ldcg(part + kNumRed * (base + t) + s) : 0.f;
+      const float hi = (base + kRedThreads + t < P.nRedBlocks) ? __ldcg(part + kNumRed * (base + kRedThreads + t) + s) : 0.f;
+      y[s] = combine(ops[s], lo, hi);
+    }
+    __syncthreads();
+    blockTree512<kNumRed>(y, ops, sh);
+    if (t == 0) {
+#pragma unroll
+      for (int s = 0; s < kNumRed; s++) carry[s] = (base == 0) ? y[s] : combine(ops[s], carry[s], y[s]);
+    }
+    __syncthreads();
+  }
+  __shared__ float red[kNumRed];
+  if (t == 0) {
+#pragma unroll
+    for (int s = 0; s < kNumRed; s++) red[s] = carry[s];
+    S->redCounter = 0;
+  }
+  __syncthreads();
+  float redv[kNumRed];
+#pragma unroll
+  for (int s = 0; s < kNumRed; s++) redv[s] = red[s];
+  stepControl(P, S, redv, diffBuf ? diffBuf + diffOff[rep] : nullptr, forceRebuild);
+}
+
+// Nint of ComputeDefs.h:70-71 (evaluated in double because of the 0.5 literal).
+__device__ __forceinline__ int nintRef(float x) {
+  return (x < 0.) ? (-(int)(0.5 - (double)x)) : ((int)(0.5 + (double)x));
+}
+
+// Scalar control of one step, run by the whole last block of the replica: the host-side
+// statements of the reference step loop (cu:2305-2395, 2398-2414 bookkeeping, 2439-2445),
+// the nanoparticle diffusion sample (EvalDiffusion/AccumDiffusion, cu:2898-2952), the
+// thermostat decision (cu:2362-2373) and the rebuild criterion (cu:2389-2391).
+__device__ void stepControl(const RepConst &P, RepState *S, const float (&red)[kNumRed],
+                            float *diff, int forceRebuild) {
+  const int t = threadIdx.x;
+  const int sc = S->stepCount + 1;
+  __shared__ int diffDue, accumNb[16], printNow;
+  __shared__ float cmc[3];
+  if (t == 0) {
+#pragma unroll
+    for (int s = 0; s < kNumRed; s++) S->red[s] = red[s];
+    diffDue = 0;
+    if (P.nMolMe != 0) {
+      S->cmVal = red[RS_CM_X] / P.nMolMe;
+      S->cmVelVal = S->cmVel[0] / P.nMolMe;
+      S->frictVal = P.hasFric ? red[RS_FRICT] : 0.f;
+      if (P.iRegime == 2 && sc > P.stepEquil && ((sc - P.stepEquil) % P.stepDiffuse == 0) && diff) {
+        diffDue = 1;
+        cmc[0] = red[RS_CM_X] / P.nMolMe;
+        cmc[1] = red[RS_CM_Y] / P.nMolMe;
+        cmc[2] = red[RS_CM_Z] / P.nMolMe;
+      }
+    } else {
+      S->cmVal = 0.f; S->cmVelVal = 0.f; S->frictVal = 0.f;
+    }
+    const float vvMax = red[RS_VVMAX], vvSum = red[RS_VVSUM], uSum = red[RS_USUM];
+    const bool thermo = ((P.iRegime == 2) && (sc > P.stepEquil) && (sc % P.stepThermostat == 0)) ||
+                        ((P.iRegime == 1) && (sc % P.stepThermostat == 0));
+    if (thermo) {
+      const float kin = vvSum * 0.5f / P.nMol;
+      S->betaC = sqrtf(1.f + P.gammaBerendsen * (P.temperature * 1.5f * P.kB / kin - 1.f));
+      S->betaM = sqrtf(1.f + P.gammaBerendsen * (P.temperature * P.kB / kin - 1.f));
+      S->thermoMetal = (P.iRegime == 2) && (sc > P.stepEquil) && (sc < P.stepEquil + P.stepCool);
+      S->thermoPending = 1;
+    } else {
+      S->thermoPending = 0;
+    }
+    if (forceRebuild || S->nebrNow) {
+      S->nebrNow = 0;
+      S->dispHi = 0.f;
+      S->rebuilds++;
+    }
+    S->dispHi += sqrtf(vvMax) * P.deltaT;
+    if (S->dispHi > 0.5f * P.rNebrShell) S->nebrNow = 1;
+    S->ke = 0.5f * vvSum / P.nMol;
+    S->pe = uSum / P.nMol;
+    S->te = S->ke + S->pe;
+    S->ke64 = (double)S->ke;
+    S->pe64 = (double)S->pe;
+    if (P.iRegime == 2 && P.nMolMe != 0 && sc > P.stepEquil + P.stepCool) {
+      if (S->cmVelVal < 0.005f) S->shear += P.deltaF;
+      S->shearCount = 0;
+    }
+    if (P.iRegime == 1) {
+      int nDep, nTo;
+      bool act;
+      depositionPlan(P, *S, sc, nDep, nTo, act);
+      if (act) S->nMolDeposited = nDep + nTo;
+    }
+    // AccumProps(1) for every property but oneStep (host-side)
+    const float vals[7] = {S->te, S->pe, S->ke, 0.f, S->cmVal, S->cmVelVal, S->frictVal};
+#pragma unroll
+    for (int p = 0; p < 7; p++) {
+      if (p == 3) continue;
+      S->props[p][0] = vals[p];
+      S->props[p][1] += vals[p];
+      S->props[p][2] += vals[p] * vals[p];
+    }
+    if (sc % P.stepAvg == 0) {
+#pragma unroll
+      for (int p = 0; p < 7; p++) {
+        S->propsSnap[p][0] = S->props[p][0];
+        S->propsSnap[p][1] = S->props[p][1];
+        S->propsSnap[p][2] = S->props[p][2];
+        S->props[p][1] = 0.f;
+        S->props[p][2] = 0.f;
+      }
+      S->snapStep = sc;
+    }
+    S->stepCount = sc;
+  }
+  __syncthreads();
+  if (!diffDue) return;
+  // ---- diffusion sample (device copy of TBuf/rrDiffuseAv) ----
+  const int nB = P.nBuffDiffuse, nV = P.nValDiffuse;
+  float *tb = diff;                        // 7 floats per buffer
+  float *rr = diff + (size_t)nB * 7;       // nB x nV
+  float *av = rr + (size_t)nB * nV;        // nV
+  float *pr = av + nV;                     // nV (last finished table)
+  if (t == 0) {
+    for (int nb = 0; nb < nB; nb++) {
+      float *b = tb + 7 * nb;
+      int count = __float_as_int(b[0]);
+      if (count == 0) {
+        b[1] = cmc[0]; b[2] = cmc[1]; b[3] = cmc[2];
+        b[4] = cmc[0]; b[5] = cmc[1]; b[6] = cmc[2];
+      }
+      if (count >= 0) {
+        const int ni = count;
+        float *rrb = rr + (size_t)nb * nV;
+        rrb[ni] = 0.f;
+        float dx = b[4] - cmc[0], dy = b[5] - cmc[1], dz = b[6] - cmc[2];
+        dx = dx / P.region[0]; dy = dy / P.region[1]; dz = dz / P.region[2];
+        dx = (float)nintRef(dx); dy = (float)nintRef(dy); dz = (float)nintRef(dz);
+        dx = dx * P.region[0]; dy = dy * P.region[1]; dz = dz * P.region[2];
+        b[4] = cmc[0] + dx; b[5] = cmc[1] + dy; b[6] = cmc[2] + dz;
+        dx = b[4] - b[1]; dy = b[5] - b[2]; dz = b[6] - b[3];
+        rrb[ni] += dx * dx + dy * dy + dz * dz;
+      }
+      b[0] = __int_as_float(count + 1);
+    }
+  }
+  __syncthreads();
+  for (int nb = 0; nb < nB; nb++) {
+    if (t == 0) {
+      accumNb[0] = (__float_as_int(tb[7 * nb]) == nV);
+      printNow = 0;
+    }
+    __syncthreads();
+    if (accumNb[0]) {
+      const float *rrb = rr + (size_t)nb * nV;
+      for (int j = t; j < nV; j += blockDim.x) av[j] += rrb[j];
+      __syncthreads();
+      if (t == 0) {
+        tb[7 * nb] = __int_as_float(0);
+        S->countDiffuseAv++;
+        printNow = (S->countDiffuseAv == P.limitDiffuseAv);
+      }
+      __syncthreads();
+      if (printNow) {
+        const int ia = 3 * 2 * P.stepDiffuse;
+        const float fa = (float)ia * P.deltaT * (float)P.limitDiffuseAv;
+        const float fac = (float)(1. / (double)fa);
+        for (int j = t; j < nV; j += blockDim.x) {
+          float vj = av[j];
+          if (j >= 1) vj *= fac / j;
+          pr[j] = vj;
+          av[j] = 0.f;
+        }
+        __syncthreads();
+        if (t == 0) {
+          S->countDiffuseAv = 0;
+          S->diffPrints++;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Shear drive (ApplyShearK, cu:517-534; schedule cu:2398-2413): after the step's control has
+// updated the shear value, add it to a.x of metal atoms left of the centre of mass.
+__global__ void k_shear(BlockTab tab, const RepConst *__restrict__ rc, RepState *st,
+                        const float4 *__restrict__ pos, float4 *__restrict__ acc) {
+  const int rep = tab.rep[blockIdx.x];
+  const RepConst &P = rc[rep];
+  RepState *S = st + rep;
+  const int i = tab.start[blockIdx.x] + threadIdx.x;
+  const int metalEnd = P.atomOff + P.nMolMe;
+  const int sc = S->stepCount;  // already advanced by the control
+  const bool active = (P.iRegime == 2) && (P.nMolMe != 0) && (sc > P.stepEquil + P.stepCool);
+  if (!active) return;
+  unsigned hit = 0;
+  if (i < metalEnd) {
+    const float dR = S->cmVal - pos[i].x;
+    if (dR > 0.f) {
+      acc[i].x += S->shear;
+      hit = 1;
+    }
+  }
+  unsigned cnt = __popc(__ballot_sync(0xffffffffu, hit));
+  __shared__ unsigned bc;
+  if (threadIdx.x == 0) bc = 0;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(&bc, cnt);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (bc) atomicAdd(&S->shearCount, bc);
+    __threadfence();
+    const int nblk = (P.nMolMe + blockDim.x - 1) / blockDim.x;
+    const unsigned prev = atomicAdd(&S->shearCounter, 1u);
+    if (prev == (unsigned)nblk - 1) {
+      __threadfence();
+      S->totalShear = atomicAdd(&S->shearCount, 0u) * S->shear;
+      S->shearCounter = 0;
+    }
+  }
+}
+
+// ============================================================================================
+// RDF sample (EvalRdfK, cu:1895-1999): ordered metal pairs in the 27-cell stencil of the
+// last-built cells, current positions, warp-aggregated shared-memory histogram.
+// ============================================================================================
+__global__ void k_rdf(BlockTab tab, const RepConst *__restrict__ rc, RepState *st,
+                      const float4 *__restrict__ pos, const int *__restrict__ cellOf,
+                      const int *__restrict__ cellStart, const int *__restrict__ sortIdx,
+                      unsigned *__restrict__ hist, int histStride) {
+  extern __shared__ unsigned shist[];
+  const int rep = tab.rep[blockIdx.x];
+  const RepConst &P = rc[rep];
+  RepState *S = st + rep;
+  const int nb = P.sizeHistRdf;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) shist[b] = 0u;
+  __syncthreads();
+  const int i = tab.start[blockIdx.x] + threadIdx.x;
+  const int metalEnd = P.atomOff + P.nMolMe;
+  const float range2 = P.rangeRdf * P.rangeRdf;
+  const int lane = threadIdx.x & 31;
+  int dropped = 0;
+  const bool active = (i < metalEnd) && (cellOf[i] >= 0);
+  const float4 A = active ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const int c = active ? cellOf[i] : 0;
+  for (int o = 0; o < 27; o++) {
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    int qb = 0, len = 0;
+    if (active) {
+      const int C = stencilCell(P, c, o, sx, sy, sz);
+      qb = cellStart[P.cellOff + C];
+      len = cellStart[P.cellOff + C + 1] - qb;
+    }
+    // every lane runs the same trip count, so the warp is converged at the match below
+    const int maxLen = __reduce_max_sync(0xffffffffu, len);
+    for (int q = 0; q < maxLen; q++) {
+      int bin = -1;
+      if (q < len) {
+        const int k = sortIdx[qb + q];
+        if (k < metalEnd && k != i) {
+          const float4 B = pos[k];
+          float dx = A.x - B.x, dy = A.y - B.y, dz = A.z - B.z;
+          dx = dx - sx; dy = dy - sy; dz = dz - sz;
+          const float rr = dx * dx + dy * dy + dz * dz;
+          if (rr < range2) {
+            bin = (int)(sqrtf(rr) * P.intervalRdf);
+            if (bin < 0 || bin >= nb) {
+              dropped++;
+              bin = -1;
+            }
+          }
+        }
+      }
+      const unsigned same = __match_any_sync(0xffffffffu, bin);
+      if (bin >= 0 && lane == __ffs(same) - 1) atomicAdd(&shist[bin], (unsigned)__popc(same));
+    }
+  }
+  __syncthreads();
+  unsigned *h = hist + (size_t)rep * histStride;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x)
+    if (shist[b]) atomicAdd(&h[b], shist[b]);
+  if (dropped) {
+    atomicAdd(&S->rdfRange, dropped);
+    setFlag(S, 7 /*SG_ERR_RDF_RANGE*/);
+  }
+}
+
+// All-pairs metal-metal histogram with minimum image (an extension beyond the stencil-limited
+// reference RDF): tiles of 128 atoms staged in shared memory.
+__global__ void k_rdf_ext(const RepConst *__restrict__ rc, const float4 *__restrict__ pos,
+                          const int *__restrict__ tileRep, const int *__restrict__ tileStart,
+                          unsigned long long *__restrict__ hist, int nbins, float range) {
+  extern __shared__ unsigned eh[];
+  __shared__ float4 tileB[128];
+  const int rep = tileRep[blockIdx.x];
+  const RepConst &P = rc[rep];
+  for (int b = threadIdx.x; b < nbins; b += blockDim.x) eh[b] = 0u;
+  const int i = tileStart[blockIdx.x] + threadIdx.x;
+  const int mb = P.atomOff, me = P.atomOff + P.nMolMe;
+  const float4 A = (i < me) ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float scale = nbins / range;
+  const float r2max = range * range;
+  for (int j0 = mb; j0 < me; j0 += 128) {
+    __syncthreads();
+    if (j0 + threadIdx.x < me) tileB[threadIdx.x] = pos[j0 + threadIdx.x];
+    __syncthreads();
+    if (i < me) {
+      const int nj = min(128, me - j0);
+      for (int jj = 0; jj < nj; jj++) {
+        if (j0 + jj == i) continue;
+        const float4 B = tileB[jj];
+        float dx = A.x - B.x, dy = A.y - B.y, dz = A.z - B.z;
+        dx -= P.region[0] * rintf(dx / P.region[0]);
+        dy -= P.region[1] * rintf(dy / P.region[1]);
+        dz -= P.region[2] * rintf(dz / P.region[2]);
+        const float rr = dx * dx + dy * dy + dz * dz;
+        if (rr < r2max) {
+          const int bin = (int)(sqrtf(rr) * scale);
+          if (bin < nbins) atomicAdd(&eh[bin], 1u);
+        }
+      }
+    }
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < nbins; b += blockDim.x)
+    if (eh[b]) atomicAdd(&hist[(size_t)rep * nbins + b], (unsigned long long)eh[b]);
+}
+
+// Apply a pending thermostat rescale now (before the state is read back).
+__global__ void k_apply_pending(BlockTab tab, const RepConst *__restrict__ rc, RepState *st,
+                                float4 *__restrict__ vel) {
+  const int rep = tab.rep[blockIdx.x];
+  const RepConst &P = rc[rep];
+  const RepState *S = st + rep;
+  const int g = tab.start[blockIdx.x] + threadIdx.x;
+  if (g >= P.atomOff + P.nMol || !S->thermoPending) return;
+  const int local = g - P.atomOff;
+  float4 v = vel[g];
+  if (local >= P.nMolMe) {
+    const float b = S->betaC;
+    v.x = b * v.x; v.y = b * v.y; v.z = b * v.z;
+  } else if (S->thermoMetal) {
+    const float b = S->betaM;
+    v.x = b * v.x; v.y = b * v.y; v.z = b * v.z;
+  } else {
+    return;
+  }
+  vel[g] = v;
+}
+
+__global__ void k_clear_pending(RepState *st, int nrep) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < nrep) st[r].thermoPending = 0;
+}
+
+}  // namespace sg

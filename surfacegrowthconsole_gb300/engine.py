@@ -1,0 +1,242 @@
+"""Python face of sgmd: configuration helpers and the `Simulation` class over the C ABI.
+
+This mirrors the reference's host interface for the timestep path: the reference derives a
+SimParams from sugr_in.txt (ReadInputFile/SetParams, SurfaceGrowth.cpp:189-396, 633-785),
+fills initial coordinates and velocities (InitCoordsW/InitVels) and hands everything to
+DoComputationsW (SurfaceGrowth.cu:2013-2529).  Here the same steps are `read_input_file`,
+`set_params`, `init_coords`, `init_vels` and `Simulation(...).run(...)`, with the finer
+per-phase calls (`build_lists`, `compute_forces`, `eval_rdf`, ...) used by the parity tests.
+Arrays are numpy, in the reference's host layouts: positions (N, 4) float32 {x, y, z, U},
+velocities and accelerations (N, 3) float32, metal atoms first.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Sequence
+
+import numpy as np
+
+from ._lib import (MODE_MIXED, MODE_PLAIN, Diag, Input, Options, SimParams, Thermo, Workload,
+                   check, lib, libc)
+
+__all__ = ["Simulation", "read_input_file", "default_input", "set_params", "init_coords", "init_vels",
+           "build_workload", "SimParams", "Input", "MODE_PLAIN", "MODE_MIXED"]
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def default_input() -> Input:
+    inp = Input()
+    lib().sg_default_input(C.byref(inp))
+    return inp
+
+
+def read_input_file(path: str, inp: Input | None = None) -> Input:
+    """sugr_in.txt semantics: 22 positional rows on top of the compiled-in defaults."""
+    inp = inp or default_input()
+    check(lib().sg_read_input_file(str(path).encode(), C.byref(inp)))
+    return inp
+
+
+def set_params(inp: Input) -> SimParams:
+    p = SimParams()
+    check(lib().sg_set_params(C.byref(inp), C.byref(p)))
+    return p
+
+
+def init_coords(p: SimParams) -> np.ndarray:
+    """Initial lattice of the regime (advances p's random seed in regime 1, sets initUcellMe*)."""
+    r = np.zeros((p.nMol, 4), np.float32)
+    check(lib().sg_init_coords(C.byref(p), _ptr(r)))
+    return r
+
+
+def init_vels(p: SimParams) -> np.ndarray:
+    v = np.zeros((p.nMol, 3), np.float32)
+    check(lib().sg_init_vels(C.byref(p), _ptr(v)))
+    return v
+
+
+def build_workload(ucx: int, ucy: int, cluster_sizes: Sequence[int], temperature_K: float, seed: int,
+                   material: int = 3, clearance_A: float = 2.5, step_limit: int = 1000, step_avg: int = 100,
+                   step_equil: int = 0, step_cool: int | None = None, step_rdf: int = 100, limit_rdf: int = 100,
+                   step_diffuse: int = 0, n_val_diffuse: int = 0, n_buff_diffuse: int = 0,
+                   limit_diffuse_av: int = 0, delta_t: float = 0.005):
+    """Graphene sheet (32*ucx*ucy C) with fcc metal clusters; returns (params, r, v)."""
+    sizes = (C.c_int * max(1, len(cluster_sizes)))(*cluster_sizes)
+    w = Workload(ucx=ucx, ucy=ucy, iMaterial=material, n_clusters=len(cluster_sizes),
+                 cluster_sizes=C.cast(sizes, C.POINTER(C.c_int)), temperatureK=temperature_K,
+                 clearance_A=clearance_A, seed=seed, stepLimit=step_limit, stepAvg=step_avg,
+                 stepEquil=step_equil, stepCool=step_limit if step_cool is None else step_cool,
+                 stepRdf=step_rdf, limitRdf=limit_rdf, stepDiffuse=step_diffuse, nValDiffuse=n_val_diffuse,
+                 nBuffDiffuse=n_buff_diffuse, limitDiffuseAv=limit_diffuse_av, deltaT=delta_t)
+    p = SimParams()
+    check(lib().sg_build_workload(C.byref(w), C.byref(p), None, None))
+    r = np.zeros((p.nMol, 4), np.float32)
+    v = np.zeros((p.nMol, 3), np.float32)
+    check(lib().sg_build_workload(C.byref(w), C.byref(p), _ptr(r), _ptr(v)))
+    return p, r, v
+
+
+class Simulation:
+    """One sgmd context: one or more replicas stepped together on one GPU."""
+
+    def __init__(self, params: SimParams | Sequence[SimParams], mode: int = MODE_PLAIN, force_rebuild: bool = False,
+                 use_graphs: bool = True, device: int = 0, rdf_ext_bins: int = 0, rdf_ext_range: float = 0.0,
+                 eam_table_knots: int = 0):
+        plist = [params] if isinstance(params, SimParams) else list(params)
+        arr = (SimParams * len(plist))(*plist)
+        opt = Options()
+        lib().sg_default_options(C.byref(opt))
+        opt.mode = mode
+        opt.force_rebuild = int(force_rebuild)
+        opt.use_graphs = int(use_graphs)
+        opt.device = device
+        opt.rdf_ext_bins = rdf_ext_bins
+        opt.rdf_ext_range = rdf_ext_range
+        opt.eam_table_knots = eam_table_knots
+        h = C.c_void_p()
+        check(lib().sg_create(arr, len(plist), C.byref(opt), C.byref(h)))
+        self._h = h
+        self.params0 = [q.copy() for q in plist]
+        self.nrep = len(plist)
+
+    # -- lifetime
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().sg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def natoms(self, rep: int = -1) -> int:
+        return lib().sg_num_atoms(self._h, rep)
+
+    # -- state
+    def set_state(self, r: np.ndarray | None, v: np.ndarray | None = None, a: np.ndarray | None = None,
+                  rep: int = -1) -> None:
+        n = self.natoms(rep)
+        def prep(x, w):
+            if x is None:
+                return None
+            x = np.ascontiguousarray(x, dtype=np.float32)
+            if x.shape != (n, w):
+                raise ValueError(f"expected shape {(n, w)}, got {x.shape}")
+            return x
+        r_, v_, a_ = prep(r, 4), prep(v, 3), prep(a, 3)
+        check(lib().sg_set_state(self._h, rep, _ptr(r_), _ptr(v_), _ptr(a_)))
+
+    def get_state(self, rep: int = -1):
+        n = self.natoms(rep)
+        r = np.zeros((n, 4), np.float32)
+        v = np.zeros((n, 3), np.float32)
+        a = np.zeros((n, 3), np.float32)
+        check(lib().sg_get_state(self._h, rep, _ptr(r), _ptr(v), _ptr(a)))
+        return r, v, a
+
+    def params(self, rep: int = 0) -> SimParams:
+        p = SimParams()
+        check(lib().sg_get_params(self._h, rep, C.byref(p)))
+        return p
+
+    # -- stepping and phases
+    def step(self, n: int = 1) -> None:
+        check(lib().sg_step(self._h, n))
+
+    def thermo(self, rep: int = 0) -> Thermo:
+        t = Thermo()
+        check(lib().sg_get_thermo(self._h, rep, C.byref(t)))
+        return t
+
+    def build_lists(self) -> None:
+        check(lib().sg_build_lists(self._h))
+
+    def compute_forces(self) -> None:
+        check(lib().sg_compute_forces(self._h))
+
+    def eval_rdf(self) -> None:
+        check(lib().sg_eval_rdf(self._h))
+
+    def reset_rdf(self) -> None:
+        check(lib().sg_reset_rdf(self._h))
+
+    # -- read-back
+    def cells(self, rep: int = 0):
+        p = self.params0[rep]
+        nc = lib().sg_num_cells(self._h, rep)
+        co = np.zeros(p.nMol, np.int32)
+        cs = np.zeros(nc + 1, np.int32)
+        ca = np.zeros(p.nMol, np.int32)
+        check(lib().sg_get_cells(self._h, rep, _ptr(co), _ptr(cs), _ptr(ca)))
+        return co, cs, ca
+
+    def nebr(self, rep: int = 0):
+        p = self.params0[rep]
+        nn = np.zeros(p.nMol, np.int32)
+        nbl = np.zeros((p.iNebrMax, p.nMol), np.int32)
+        check(lib().sg_get_nebr(self._h, rep, _ptr(nn), _ptr(nbl)))
+        return nn, nbl
+
+    def rho(self, rep: int = 0) -> np.ndarray:
+        out = np.zeros(self.params0[rep].nMolMe, np.float32)
+        check(lib().sg_get_rho(self._h, rep, _ptr(out)))
+        return out
+
+    def friction(self, rep: int = 0) -> np.ndarray:
+        out = np.zeros(self.params0[rep].nMolMe, np.float32)
+        check(lib().sg_get_friction(self._h, rep, _ptr(out)))
+        return out
+
+    def rdf(self, rep: int = 0) -> np.ndarray:
+        out = np.zeros(self.params0[rep].sizeHistRdf, np.uint32)
+        check(lib().sg_get_rdf(self._h, rep, _ptr(out)))
+        return out
+
+    def rdf_ext(self, rep: int, nbins: int) -> np.ndarray:
+        out = np.zeros(nbins, np.uint64)
+        check(lib().sg_get_rdf_ext(self._h, rep, _ptr(out)))
+        return out
+
+    def diffusion(self, rep: int = 0):
+        p = self.params0[rep]
+        rr = np.zeros(p.nValDiffuse, np.float32)
+        counts = np.zeros(p.nBuffDiffuse, np.int32)
+        cav = C.c_int()
+        check(lib().sg_get_diffusion(self._h, rep, _ptr(rr), _ptr(counts), C.byref(cav)))
+        return rr, counts, cav.value
+
+    def diag(self, rep: int = 0) -> Diag:
+        d = Diag()
+        check(lib().sg_get_diag(self._h, rep, C.byref(d)))
+        return d
+
+    def run(self, result_path: str | None, pdb_prefix: str = "sugr") -> None:
+        """The whole simulation with the reference's output files (replica 0)."""
+        L = libc()
+        f = L.fopen(str(result_path).encode(), b"a") if result_path else None
+        try:
+            check(lib().sg_run(self._h, f, pdb_prefix.encode()))
+        finally:
+            if f:
+                L.fclose(f)
+
+    def autotune(self, steps: int = 20) -> str:
+        buf = C.create_string_buffer(4096)
+        check(lib().sg_autotune(self._h, steps, buf, len(buf)))
+        return buf.value.decode()
