@@ -1,0 +1,289 @@
+#!/usr/bin/env python3
+"""Benchmark of the SurfaceGrowth timestep on GB300: atom-steps/s.
+
+Workload (the production-size configuration): a 40,000-atom graphene sheet with 8 Ni clusters of
+300-1,000 atoms (seeded), 700 K, cell and neighbour lists rebuilt every step, RDF and
+centre-of-mass diffusion on.  One step = one full timestep of every atom (Verlet, lists, EAM,
+LJ, graphene, reductions, thermostat, RDF/diffusion when due).
+
+  value : atom-steps/s with the state resident in HBM, each step timed with CUDA events on the
+          library's stream; the L2 is flushed (a 512 MB write) between timed steps because the
+          whole state fits in the 129 MB L2.
+  e2e   : the same metric through the public C ABI with host buffers: every step uploads the
+          state (r, v, a) from pinned host memory, steps, and reads the step's thermo record.
+  roofline : the carbon-force kernel (the largest share of the step), algorithmic bytes per
+          launch / its mean duration in the timed region, against the measured HBM copy peak.
+  cpu_baseline : the FP32 CPU restatement of the same step on all host cores (the reference has
+          no CPU implementation of this path).
+--impl reference times that CPU restatement on the same workload and prints its own line.
+Multi-GPU (torchrun): replicas only -- each rank runs its own seeded system, no collective on
+the data path; value is the sum over ranks over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+L2_FLUSH_BYTES = 512 << 20
+RDF_EXT_BINS = 300
+RDF_EXT_RANGE = 15.0 / 1.42  # 0-15 A
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="sgmd", choices=["sgmd", "reference"])
+    ap.add_argument("--mode", default="plain", choices=["plain", "mixed"])
+    ap.add_argument("--cpu-sample-steps", type=int, default=300)
+    ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def workload(rank: int):
+    from surfacegrowthconsole_gb300 import workloads
+    return workloads.production(seed=2 + rank)
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.dev = device
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.p = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        time.sleep(0.2)
+        if self.p:
+            self.p.terminate()
+            self.p.wait()
+
+    def summary(self):
+        self.f.flush()
+        rows = [r.split(",") for r in Path(self.f.name).read_text().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, n in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].strip() == "Active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def measured_peaks():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def carbon_force_bytes(p, nn: np.ndarray, ns: np.ndarray) -> float:
+    """Compulsory bytes of one carbon-force launch: per carbon atom its position (16), list
+    length (4), list entries (4 each), own short-list length + entries, the acceleration and
+    energy it writes (16 + 4); plus one read of every metal position gathered (16)."""
+    c = slice(p.nMolMe, p.nMol)
+    nc = p.nMol - p.nMolMe
+    entries = float(nn[c].sum())
+    short = float(np.clip(ns[c], 0, 8).sum())
+    return nc * (16 + 4 + 4 + 16 + 4) + 4 * entries + 4 * short + 16 * p.nMolMe
+
+
+def cpu_baseline(p, r, v, sample_steps: int):
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle  # the CPU restatement, as the reported baseline only
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    o = oracle.OracleSim(p, 32, force_rebuild=True)
+    o.set_state(r, v, np.zeros((p.nMol, 3), np.float32))
+    o.step(2)  # warm
+    t0 = time.perf_counter()
+    o.step(sample_steps)
+    dt = time.perf_counter() - t0
+    return {"value": p.nMol * sample_steps / dt, "unit": "atom-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{sample_steps} steps of the same {p.nMol}-atom workload (FP32 CPU restatement, "
+                      f"OpenMP over atoms, lists rebuilt every step)"}
+
+
+def run_reference(args, rank: int, world: int):
+    if rank != 0:
+        return
+    p, r, v = workload(0)
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    o = oracle.OracleSim(p, 32, force_rebuild=True)
+    o.set_state(r, v, np.zeros((p.nMol, 3), np.float32))
+    o.step(args.warmup)
+    t0 = time.perf_counter()
+    o.step(args.steps)
+    dt = time.perf_counter() - t0
+    val = p.nMol * args.steps / dt
+    line = {"metric": "atom-steps/s", "value": val, "unit": "atom-steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)", "impl": "reference",
+            "config": {"workload": f"graphene 40000 C + 8 Ni clusters ({p.nMolMe} Ni), {p.nMol} atoms, 700 K, "
+                                   "lists rebuilt every step", "atoms": p.nMol},
+            "cpu_baseline": {"value": val, "unit": "atom-steps/s", "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} steps of the full workload, FP32 CPU restatement of the "
+                                       "reference step (the reference has no CPU path)"},
+            "e2e": {"value": val, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line, default=float))
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from surfacegrowthconsole_gb300 import MODE_MIXED, MODE_PLAIN
+    from surfacegrowthconsole_gb300.engine import Simulation
+
+    p, r, v = workload(rank)
+    a = np.zeros((p.nMol, 3), np.float32)
+    stream = torch.cuda.Stream(device=local)
+    mode = MODE_MIXED if args.mode == "mixed" else MODE_PLAIN
+    sim = Simulation(p, mode=mode, force_rebuild=True, device=local, stream=stream.cuda_stream, phase_timing=True,
+                     rdf_ext_bins=RDF_EXT_BINS, rdf_ext_range=RDF_EXT_RANGE)
+    sim.set_state(r, v, a)
+    sim.step(args.warmup)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    phases = []
+    launches = 0
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    barrier()
+    with Clocks(local) as clk:
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                flush.zero_()
+                ev[k][0].record(stream)
+                sim.step_async(1)
+                ev[k][1].record(stream)
+                phases.append(sim.phase_times())  # waits for this step
+                launches += sim.kernels_per_step()
+        barrier()
+    sim.step(0)  # collects device status (overflow flags)
+    step_ms = [e0.elapsed_time(e1) for e0, e1 in ev]
+    total_s = sum(step_ms) * 1e-3
+    if dist:
+        t = torch.tensor([total_s], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t.item())
+        n_all = torch.tensor([float(p.nMol)], device=f"cuda:{local}")
+        dist.all_reduce(n_all)
+        atoms_all = float(n_all.item())
+    else:
+        atoms_all = float(p.nMol)
+    value = atoms_all * args.steps / total_s
+    ph = np.mean(np.array(phases), axis=0)  # integrate, rebuild, metal, carbon, reduce, extra
+
+    # roofline of the carbon-force kernel
+    nn, _ = sim.nebr()
+    ns = np.zeros(p.nMol, np.int32)  # short-list lengths are not read back; bound by 3 per atom
+    ns[p.nMolMe:] = 3
+    bytes_launch = carbon_force_bytes(p, nn, ns)
+    peak, peak_kind = measured_peaks()
+    achieved = bytes_launch / (ph[3] * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": "k_force_carbon", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+            "algorithmic_bytes_per_launch": bytes_launch, "mean_launch_ms": float(ph[3]),
+            "phase_ms": {"integrate": float(ph[0]), "rebuild": float(ph[1]), "metal_forces": float(ph[2]),
+                         "carbon_forces": float(ph[3]), "reduce": float(ph[4]), "rdf_shear": float(ph[5])}}
+    prof = ROOT / "profiles" / "bench_carbon_force_traffic.json"
+    if prof.exists():
+        roof["traffic"] = json.loads(prof.read_text()).get("dram_bytes_per_launch")
+
+    # end to end through the C ABI with pinned host buffers
+    hr = torch.empty((p.nMol, 4), dtype=torch.float32, pin_memory=True).numpy()
+    hv = torch.empty((p.nMol, 3), dtype=torch.float32, pin_memory=True).numpy()
+    ha = torch.empty((p.nMol, 3), dtype=torch.float32, pin_memory=True).numpy()
+    hr[:], hv[:], ha[:] = sim.get_state()
+    e2e_steps = max(1, min(args.e2e_steps, args.steps))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sim.set_state(hr, hv, ha)
+        sim.step(1)
+        th = sim.thermo()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    import ctypes
+    e2e = {"value": atoms_all * e2e_steps / e2e_s, "unit": "atom-steps/s",
+           "h2d_bytes_per_step": p.nMol * (16 + 12 + 12), "d2h_bytes_per_step": ctypes.sizeof(th), "steps": e2e_steps}
+
+    if rank == 0:
+        cpu = None if args.no_cpu or world > 1 else cpu_baseline(p, r, v, args.cpu_sample_steps)
+        line = {"metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded graphene + fcc Ni clusters, Maxwell velocities)",
+                "config": {"workload": f"graphene 40000 C + 8 Ni clusters ({p.nMolMe} Ni), {p.nMol} atoms per "
+                                       "GPU, 700 K, dt 1 fs, lists rebuilt every step, RDF + diffusion on",
+                           "atoms_per_gpu": p.nMol, "mode": args.mode, "l2": "flushed between timed steps",
+                           "parallelism": f"replicas x{world}"},
+                "clocks": clk.summary(), "gpu_launches": launches, "roofline": roof, "e2e": e2e,
+                "cpu_baseline": cpu}
+        print(json.dumps(line, default=float))
+    sim.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -73,7 +73,8 @@ typedef struct sg_options {
     int eam_table_knots;   /* MIXED: knots per tabulated EAM function (0: 2048) */
     int tune_force_tpa;    /* threads per atom in the carbon force pass (0: auto) */
     int tune_block;        /* block size of the per-atom passes (0: auto) */
-    int reserved[8];
+    int phase_timing;      /* 1: record CUDA events between the phases of every step */
+    int reserved[7];
 } sg_options;
 
 /* Initialise *opt with the defaults (PLAIN mode, graphs on, device 0). */
@@ -113,6 +114,16 @@ int sg_get_params(sg_ctx *ctx, int rep, sg_simparams *out);
  * reductions, nanoparticle diffusion sample, momentum/max-v2/Sum mv2, Berendsen thermostat,
  * potential energy, rebuild criterion, shear, RDF sample, property accumulation. */
 int sg_step(sg_ctx *ctx, int nsteps);
+/* The same steps, launched on the context's stream without waiting for them (no status from
+ * the device is checked; call sg_step(ctx, 0) to synchronise and collect it). */
+int sg_step_async(sg_ctx *ctx, int nsteps);
+/* Kernel launches one step issues (for the step variant that ran last). */
+int sg_kernels_per_step(sg_ctx *ctx);
+/* With phase_timing on: durations in ms of the phases of the last step, in the order
+ * integrate, rebuild, metal forces (density + EAM/LJ), carbon forces, reduce, extra
+ * (shear/RDF).  Returns the number of phases, or
+ * minus a status code. */
+int sg_get_phase_times(sg_ctx *ctx, float *ms, int n);
 
 typedef struct sg_thermo {
     int stepCount;

@@ -88,7 +88,7 @@ class Options(C.Structure):
         ("mode", C.c_int), ("force_rebuild", C.c_int), ("use_graphs", C.c_int), ("device", C.c_int),
         ("stream", C.c_void_p), ("rdf_ext_bins", C.c_int), ("rdf_ext_range", C.c_float),
         ("eam_table_knots", C.c_int), ("tune_force_tpa", C.c_int), ("tune_block", C.c_int),
-        ("reserved", C.c_int * 8),
+        ("phase_timing", C.c_int), ("reserved", C.c_int * 7),
     ]
 
 
@@ -170,6 +170,9 @@ _SIGS = {
     "sg_get_state": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "sg_get_params": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(SimParams)]),
     "sg_step": (C.c_int, [C.c_void_p, C.c_int]),
+    "sg_step_async": (C.c_int, [C.c_void_p, C.c_int]),
+    "sg_kernels_per_step": (C.c_int, [C.c_void_p]),
+    "sg_get_phase_times": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
     "sg_get_thermo": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Thermo)]),
     "sg_build_lists": (C.c_int, [C.c_void_p]),
     "sg_compute_forces": (C.c_int, [C.c_void_p]),

@@ -249,7 +249,10 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
   if (c->opt.rdf_ext_bins > 0) AL(c->histExt, (size_t)n_replicas * c->opt.rdf_ext_bins);
   AL(c->diffBuf, std::max<size_t>(diffOff, 1));
   AL(c->dDiffOff, n_replicas);
+  AL(c->stage, 3 * N);
 #undef AL
+  if (c->opt.phase_timing)
+    for (auto &e : c->phaseEv) cudaEventCreate(&e);
   // tables
   if ((rc = makeRangeTab(c, c->atomTab, 128, 0)) || (rc = makeRangeTab(c, c->metalTab, 128, 1)) ||
       (rc = makeRangeTab(c, c->carbonTab, 128, 2))) {
@@ -343,6 +346,8 @@ extern "C" int sg_destroy(sg_ctx *c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   destroyGraphs(c);
   sg_mixed_free(c);
+  for (auto &e : c->phaseEv)
+    if (e) cudaEventDestroy(e);
   for (void *p : c->allocs) cudaFree(p);
   if (c->ownStream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -367,24 +372,34 @@ static int repRange(sg_ctx *c, int rep, int &off, int &n) {
   return SG_OK;
 }
 
+// Host float4 arrays have the device layout and are copied directly; float3 arrays go through
+// a device staging buffer and a widening kernel.  With pinned host buffers every copy is a
+// single DMA transfer.
+static int upload3(sg_ctx *c, const sg_float3 *h, float4 *d, int n) {
+  CK(cudaMemcpyAsync(c->stage, h, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  k_unpack3<<<(n + 255) / 256, 256, 0, c->stream>>>(c->stage, d, n);
+  CK(cudaGetLastError());
+  return SG_OK;
+}
+static int download3(sg_ctx *c, const float4 *d, sg_float3 *h, int n) {
+  k_pack3<<<(n + 255) / 256, 256, 0, c->stream>>>(d, c->stage, n);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(h, c->stage, (size_t)n * 3 * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return SG_OK;
+}
+
 extern "C" int sg_set_state(sg_ctx *c, int rep, const sg_float4 *r, const sg_float3 *v, const sg_float3 *a) {
   if (!c) return sg_fail(SG_ERR_INVALID, "null context");
   int off, n, rc;
   if ((rc = repRange(c, rep, off, n))) return rc;
-  std::vector<float4> buf(n);
   if (r) {
-    for (int i = 0; i < n; i++) buf[i] = make_float4(r[i].x, r[i].y, r[i].z, r[i].w);
-    CK(cudaMemcpyAsync(c->pos + off, buf.data(), n * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
-    if (c->posLo) CK(cudaMemsetAsync(c->posLo + off, 0, n * sizeof(float4), c->stream));
+    CK(cudaMemcpyAsync(c->pos + off, r, (size_t)n * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
+    if (c->posLo) CK(cudaMemsetAsync(c->posLo + off, 0, (size_t)n * sizeof(float4), c->stream));
   }
-  if (v) {
-    for (int i = 0; i < n; i++) buf[i] = make_float4(v[i].x, v[i].y, v[i].z, 0.f);
-    CK(cudaMemcpyAsync(c->vel + off, buf.data(), n * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
-  }
-  if (a) {
-    for (int i = 0; i < n; i++) buf[i] = make_float4(a[i].x, a[i].y, a[i].z, 0.f);
-    CK(cudaMemcpyAsync(c->acc + off, buf.data(), n * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
-  }
+  if (v && (rc = upload3(c, v, c->vel + off, n))) return rc;
+  if (v) CK(cudaStreamSynchronize(c->stream));  // the staging buffer is reused below
+  if (a && (rc = upload3(c, a, c->acc + off, n))) return rc;
   // a new state cancels any thermostat rescale still pending from the previous step
   k_clear_pending<<<(c->nrep + 127) / 128, 128, 0, c->stream>>>(c->st, c->nrep);
   CK(cudaGetLastError());
@@ -406,22 +421,9 @@ extern "C" int sg_get_state(sg_ctx *c, int rep, sg_float4 *r, sg_float3 *v, sg_f
   int off, n, rc;
   if ((rc = repRange(c, rep, off, n))) return rc;
   if (v && (rc = applyPending(c))) return rc;
-  std::vector<float4> buf(n);
-  if (r) {
-    CK(cudaMemcpyAsync(buf.data(), c->pos + off, n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    for (int i = 0; i < n; i++) r[i] = sg_float4{buf[i].x, buf[i].y, buf[i].z, buf[i].w};
-  }
-  if (v) {
-    CK(cudaMemcpyAsync(buf.data(), c->vel + off, n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    for (int i = 0; i < n; i++) v[i] = sg_float3{buf[i].x, buf[i].y, buf[i].z};
-  }
-  if (a) {
-    CK(cudaMemcpyAsync(buf.data(), c->acc + off, n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    for (int i = 0; i < n; i++) a[i] = sg_float3{buf[i].x, buf[i].y, buf[i].z};
-  }
+  if (r) CK(cudaMemcpyAsync(r, c->pos + off, (size_t)n * sizeof(float4), cudaMemcpyDeviceToHost, c->stream));
+  if (v && (rc = download3(c, c->vel + off, v, n))) return rc;
+  if (a && (rc = download3(c, c->acc + off, a, n))) return rc;
   CK(cudaStreamSynchronize(c->stream));
   return SG_OK;
 }
@@ -459,6 +461,7 @@ static int enqueueForces(sg_ctx *c) {
     k_force_metal<<<c->metalTab.n, 128, 0, c->stream>>>(c->metalTab.view(), c->rc, c->pos, c->acc, c->nn, c->nbl,
                                                         c->dF, c->Fv, c->fric, c->ntot);
   }
+  if (c->opt.phase_timing) cudaEventRecordWithFlags(c->phaseEv[3], c->stream, cudaEventRecordExternal);
   if (c->carbonTab.n)
     k_force_carbon<<<c->carbonTab.n, 128, 0, c->stream>>>(c->carbonTab.view(), c->rc, c->pos, c->acc, c->nn,
                                                           c->nbl, c->ns, c->sl, c->st, c->ntot);
@@ -485,9 +488,16 @@ static int enqueueRdf(sg_ctx *c, bool zero) {
   return SG_OK;
 }
 
+// External records: inside a stream capture they become event-record nodes of the graph
+// (a plain record would only express a dependency between captured streams).
+static void phaseMark(sg_ctx *c, int k) {
+  if (c->opt.phase_timing) cudaEventRecordWithFlags(c->phaseEv[k], c->stream, cudaEventRecordExternal);
+}
+
 static int enqueueStep(sg_ctx *c, int variant) {
   int rc;
   const int fr = c->opt.force_rebuild ? 1 : 0;
+  phaseMark(c, 0);
   if (c->opt.mode == SG_MODE_MIXED) {
     if ((rc = sg_mixed_enqueue_integrate(c, fr))) return rc;
   } else {
@@ -495,8 +505,11 @@ static int enqueueStep(sg_ctx *c, int variant) {
                                                            c->cellOf, c->slot, c->cellCount, fr);
     LAUNCH_OK();
   }
+  phaseMark(c, 1);
   if ((rc = enqueueRebuild(c, fr))) return rc;
+  phaseMark(c, 2);
   if ((rc = enqueueForces(c))) return rc;
+  phaseMark(c, 4);
   if (c->opt.mode == SG_MODE_MIXED) {
     if ((rc = sg_mixed_enqueue_reduce(c, fr))) return rc;
   } else {
@@ -508,6 +521,7 @@ static int enqueueStep(sg_ctx *c, int variant) {
                                                               c->dDiffOff, fr);
     LAUNCH_OK();
   }
+  phaseMark(c, 5);
   if ((variant & V_SHEAR) && c->metalTab.n) {
     k_shear<<<c->metalTab.n, 128, 0, c->stream>>>(c->metalTab.view(), c->rc, c->st, c->pos, c->acc);
     LAUNCH_OK();
@@ -515,7 +529,22 @@ static int enqueueStep(sg_ctx *c, int variant) {
   if (variant & V_RDF) {
     if ((rc = enqueueRdf(c, (variant & V_RDF_ZERO) != 0))) return rc;
   }
+  phaseMark(c, 6);
   return SG_OK;
+}
+
+// Kernel launches of one step variant, counted from the graph that holds it.
+static int countKernels(cudaGraph_t g) {
+  size_t n = 0;
+  if (cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess) return -1;
+  std::vector<cudaGraphNode_t> nodes(n);
+  cudaGraphGetNodes(g, nodes.data(), &n);
+  int k = 0;
+  for (auto nd : nodes) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) k++;
+  }
+  return k;
 }
 
 // Which optional phases the coming step needs (host-known schedule, SurfaceGrowth.cu:2398-2429).
@@ -556,6 +585,7 @@ static int launchStep(sg_ctx *c, int variant) {
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     if (rc) return rc;
     if (e != cudaSuccess) return sg_fail(SG_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    c->kernelsPerVariant[variant] = countKernels(g);
     cudaGraphExec_t ex;
     e = cudaGraphInstantiate(&ex, g, 0);
     cudaGraphDestroy(g);
@@ -563,6 +593,7 @@ static int launchStep(sg_ctx *c, int variant) {
     it = c->graphs.emplace(variant, ex).first;
   }
   CK(cudaGraphLaunch(it->second, c->stream));
+  c->lastVariant = variant;
   return SG_OK;
 }
 
@@ -598,8 +629,30 @@ extern "C" int sg_step(sg_ctx *c, int nsteps) {
   return checkFlags(c);
 }
 
+extern "C" int sg_kernels_per_step(sg_ctx *c) {
+  if (!c) return -1;
+  auto it = c->kernelsPerVariant.find(c->lastVariant);
+  return it == c->kernelsPerVariant.end() ? -1 : it->second;
+}
+
+// Returns the number of phases, or minus a status code.
+extern "C" int sg_get_phase_times(sg_ctx *c, float *ms, int n) {
+  if (!c || !c->opt.phase_timing) return -sg_fail(SG_ERR_UNSUPPORTED, "phase_timing is off");
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return -sg_fail(SG_ERR_CUDA, "%s", cudaGetErrorString(e));
+  const int np = 6;
+  for (int k = 0; k < np && k < n; k++) {
+    float t = 0.f;
+    e = cudaEventElapsedTime(&t, c->phaseEv[k], c->phaseEv[k + 1]);
+    if (e != cudaSuccess) return -sg_fail(SG_ERR_CUDA, "%s", cudaGetErrorString(e));
+    ms[k] = t;
+  }
+  return np;
+}
+
 // Launch-only stepping for timing loops (no synchronisation, no flag check).
-int sg_step_async(sg_ctx *c, int nsteps) {
+extern "C" int sg_step_async(sg_ctx *c, int nsteps) {
+  if (!c) return sg_fail(SG_ERR_INVALID, "null context");
   for (int s = 0; s < nsteps; s++) {
     const int v = stepVariant(c);
     int rc = launchStep(c, v);

@@ -54,11 +54,16 @@ struct sg_ctx {
   int countRdf = 0;
   std::vector<sg_prop> oneStep;  // per replica, host-accumulated step times
   void *mixed = nullptr;         // MIXED-mode buffers (sg_kernels_mixed.cu)
+  float *stage = nullptr;        // 3 floats per atom: host float3 arrays in transit
+  cudaEvent_t phaseEv[7] = {};   // phase boundaries of a step (phase_timing)
+  int launchCount = 0;           // kernel launches counted while enqueueing a step
+  std::map<int, int> kernelsPerVariant;
+  int lastVariant = 0;
 };
 
 
 int sg_fail(int code, const char *fmt, ...);
-int sg_step_async(sg_ctx *c, int nsteps);
+
 int sg_read_state(sg_ctx *c, int rep, sg::RepState *out);
 int sg_get_diffusion_print(sg_ctx *c, int rep, float *table, int *nprints);
 int sg_next_variant(sg_ctx *c);

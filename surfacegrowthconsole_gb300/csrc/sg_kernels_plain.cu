@@ -1169,6 +1169,19 @@ __global__ void k_apply_pending(BlockTab tab, const RepConst *__restrict__ rc, R
   vel[g] = v;
 }
 
+// float3 host layout <-> float4 device layout
+__global__ void k_unpack3(const float *src, float4 *dst, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = make_float4(src[3 * i], src[3 * i + 1], src[3 * i + 2], 0.f);
+}
+__global__ void k_pack3(const float4 *src, float *dst, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const float4 v = src[i];
+    dst[3 * i] = v.x; dst[3 * i + 1] = v.y; dst[3 * i + 2] = v.z;
+  }
+}
+
 __global__ void k_clear_pending(RepState *st, int nrep) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r < nrep) st[r].thermoPending = 0;

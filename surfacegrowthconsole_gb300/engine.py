@@ -85,7 +85,7 @@ class Simulation:
 
     def __init__(self, params: SimParams | Sequence[SimParams], mode: int = MODE_PLAIN, force_rebuild: bool = False,
                  use_graphs: bool = True, device: int = 0, rdf_ext_bins: int = 0, rdf_ext_range: float = 0.0,
-                 eam_table_knots: int = 0):
+                 eam_table_knots: int = 0, stream: int = 0, phase_timing: bool = False):
         plist = [params] if isinstance(params, SimParams) else list(params)
         arr = (SimParams * len(plist))(*plist)
         opt = Options()
@@ -97,6 +97,8 @@ class Simulation:
         opt.rdf_ext_bins = rdf_ext_bins
         opt.rdf_ext_range = rdf_ext_range
         opt.eam_table_knots = eam_table_knots
+        opt.stream = stream or None
+        opt.phase_timing = int(phase_timing)
         h = C.c_void_p()
         check(lib().sg_create(arr, len(plist), C.byref(opt), C.byref(h)))
         self._h = h
@@ -158,6 +160,21 @@ class Simulation:
     # -- stepping and phases
     def step(self, n: int = 1) -> None:
         check(lib().sg_step(self._h, n))
+
+    def step_async(self, n: int = 1) -> None:
+        """Launch n steps without waiting for them."""
+        check(lib().sg_step_async(self._h, n))
+
+    def kernels_per_step(self) -> int:
+        return lib().sg_kernels_per_step(self._h)
+
+    def phase_times(self) -> np.ndarray:
+        """ms of the phases of the last step: integrate, rebuild, forces, reduce, extra."""
+        out = np.zeros(8, np.float32)
+        n = lib().sg_get_phase_times(self._h, _ptr(out), 8)
+        if n < 0:
+            check(-n)
+        return out[:n]
 
     def thermo(self, rep: int = 0) -> Thermo:
         t = Thermo()
