@@ -265,6 +265,26 @@ int sg_write_backup(const char *path, const sg_simparams *p, const sg_float4 *r,
                     const sg_float3 *a);
 int sg_read_backup(const char *path, sg_simparams *p, sg_float4 *r, sg_float3 *v, sg_float3 *a);
 
+/* ---- force evaluation without device allocation ---------------------------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc: code running
+ * under another framework's memory manager that owns the device heap, code that must not
+ * stall the device with the implicit synchronisation of cudaMalloc/cudaFree, plugins that may
+ * not grow the device footprint per call.  Same work as sg_build_lists + sg_compute_forces on
+ * one system: d_pos (nMol float4 {x,y,z,U}, device) is read and its .w receives the per-atom
+ * potential energy, d_acc (nMol float4, device) receives the accelerations.  Everything else
+ * lives in one static device array of SG_NOALLOC_SCRATCH_BYTES that every GPU loading the
+ * library holds until the process exits; systems above the SG_NOALLOC_MAX_* limits are
+ * rejected with SG_ERR_INVALID.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress), so make it before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU (other streams, other host threads) race and corrupt
+ * each other's results.  The call synchronises `stream` (a cudaStream_t, NULL: the default
+ * stream) to report device-side conditions.  It calls no cudaMalloc/cudaFree. */
+#define SG_NOALLOC_MAX_ATOMS 16384
+#define SG_NOALLOC_MAX_CELLS 65536   /* cell grid padded to whole scan tiles of 2048 cells */
+#define SG_NOALLOC_MAX_NEBR 128      /* iNebrMax */
+#define SG_NOALLOC_SCRATCH_BYTES (12u << 20)
+int sg_compute_forces_noalloc(const sg_simparams *p, sg_float4 *d_pos, sg_float4 *d_acc, void *stream);
+
 /* ---- tuning ------------------------------------------------------------------------------- */
 /* Times the candidate launch shapes of the tunable passes on the context's own state for
  * `steps` steps each, keeps the fastest; state is restored afterwards. */

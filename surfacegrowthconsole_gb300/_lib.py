@@ -202,6 +202,7 @@ _SIGS = {
     "sg_print_diffusion": (C.c_int, [C.c_void_p, C.POINTER(SimParams), C.c_void_p]),
     "sg_write_backup": (C.c_int, [C.c_char_p, C.POINTER(SimParams), C.c_void_p, C.c_void_p, C.c_void_p]),
     "sg_read_backup": (C.c_int, [C.c_char_p, C.POINTER(SimParams), C.c_void_p, C.c_void_p, C.c_void_p]),
+    "sg_compute_forces_noalloc": (C.c_int, [C.POINTER(SimParams), C.c_void_p, C.c_void_p, C.c_void_p]),
     "sg_autotune": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p, C.c_int]),
     "CudaInitW": (None, [C.c_int, C.c_void_p]),
     "SetParametersW": (None, [C.POINTER(SimParams)]),

@@ -36,6 +36,7 @@ CUDA_UNITS = [
     ("sg_kernels_mixed.cu", []),
     ("sg_engine.cu", []),
     ("sg_run.cu", []),
+    ("sg_noalloc.cu", []),
 ]
 CXX_UNITS = ["sg_host.cpp", "sg_refcompat.cpp"]
 
