@@ -227,7 +227,7 @@ def main():
     else:
         atoms_all = float(p.nMol)
     value = atoms_all * args.steps / total_s
-    ph = np.mean(np.array(phases), axis=0)  # integrate, rebuild, metal, carbon, reduce, extra
+    ph = np.mean(np.array(phases), axis=0)  # integrate, rebuild, metal chain, carbon, forces, reduce, extra
 
     # roofline of the carbon-force kernel
     nn, _ = sim.nebr()
@@ -239,8 +239,9 @@ def main():
     roof = {"bound": "hbm", "kernel": "k_force_carbon", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
             "algorithmic_bytes_per_launch": bytes_launch, "mean_launch_ms": float(ph[3]),
-            "phase_ms": {"integrate": float(ph[0]), "rebuild": float(ph[1]), "metal_forces": float(ph[2]),
-                         "carbon_forces": float(ph[3]), "reduce": float(ph[4]), "rdf_shear": float(ph[5])}}
+            "phase_ms": {"integrate": float(ph[0]), "rebuild": float(ph[1]), "metal_chain_side_stream": float(ph[2]),
+                         "carbon_forces": float(ph[3]), "forces_fork_to_join": float(ph[4]), "reduce": float(ph[5]),
+                         "rdf_shear": float(ph[6])}}
     prof = ROOT / "profiles" / "bench_carbon_force_traffic.json"
     if prof.exists():
         roof["traffic"] = json.loads(prof.read_text()).get("dram_bytes_per_launch")

@@ -119,10 +119,10 @@ int sg_step(sg_ctx *ctx, int nsteps);
 int sg_step_async(sg_ctx *ctx, int nsteps);
 /* Kernel launches one step issues (for the step variant that ran last). */
 int sg_kernels_per_step(sg_ctx *ctx);
-/* With phase_timing on: durations in ms of the phases of the last step, in the order
- * integrate, rebuild, metal forces (density + EAM/LJ), carbon forces, reduce, extra
- * (shear/RDF).  Returns the number of phases, or
- * minus a status code. */
+/* With phase_timing on: durations in ms of the phases of the last step: integrate, rebuild,
+ * metal chain (density, metal forces, metal centre-of-mass velocity; runs beside the carbon
+ * pass), carbon pass, forces (fork to join), reduce, extra (shear/RDF).  Returns the number
+ * of phases (7), or minus a status code. */
 int sg_get_phase_times(sg_ctx *ctx, float *ms, int n);
 
 typedef struct sg_thermo {
@@ -282,7 +282,7 @@ int sg_read_backup(const char *path, sg_simparams *p, sg_float4 *r, sg_float3 *v
 #define SG_NOALLOC_MAX_ATOMS 16384
 #define SG_NOALLOC_MAX_CELLS 65536   /* cell grid padded to whole scan tiles of 2048 cells */
 #define SG_NOALLOC_MAX_NEBR 128      /* iNebrMax */
-#define SG_NOALLOC_SCRATCH_BYTES (12u << 20)
+#define SG_NOALLOC_SCRATCH_BYTES (20u << 20)
 int sg_compute_forces_noalloc(const sg_simparams *p, sg_float4 *d_pos, sg_float4 *d_acc, void *stream);
 
 /* ---- tuning ------------------------------------------------------------------------------- */

@@ -10,8 +10,13 @@
 //   slot   int[Ntot]    arrival slot inside the cell (scratch of the counting sort)
 //   cellCount int[Ctot], cellStart int[Ctot + R] (per-replica, tile-padded cell ranges)
 //   sortIdx int[Ntot], sortPos float4[Ntot]  atoms grouped by cell, ascending index per cell
-//   nn int[Ntot], nbl int[nebrMax * Ntot]   neighbour list, entry j of atom g at nbl[j*Ntot+g]
-//   ns int[Ntot], sl int[kShortMax * Ntot]  short list: neighbours within (rCutC+skin) at build
+//   nn int[Ntot], nbl int[Ntot * rowStride] neighbour list, entry j of atom g at
+//                                           nbl[g * rowStride + j] (rowStride = nebrMax rounded
+//                                           up to a multiple of 4: 16-byte aligned rows)
+//   ns int[Ntot], sl int[Ntot * kShortMax]  short list: neighbours within (rCutC+skin) at build
+//   nrl int[Ntot], rl int2[Ntot * kRelMax]  relevant list of a carbon atom: its metal entries
+//                                           and entries within (rCutC+skin), {index, position
+//                                           in the full list}
 //   rho/dF/Fv float[Ntot]   EAM density, F'(rho), F(rho) (metal atoms)
 //   fric float[Ntot]       x force of carbon on each metal atom
 // Per-replica constants live in RepConst, mutable per-replica scalars in RepState.
@@ -26,6 +31,14 @@ constexpr int kRedThreads = 512;  // reduction block: 512 threads x 2 elements (
 constexpr int kRedElems = 1024;
 constexpr int kCellTile = 2048;   // cells per scan tile (cell ranges are padded to this)
 constexpr int kNumRed = 16;       // values reduced per element in the step reduction
+constexpr int kMT = 16;           // lanes per metal atom in the density and metal-force passes
+constexpr int kCT = 4;            // lanes per carbon atom in the carbon-force pass
+constexpr int kNebrWarps = 4;     // warps per block in the neighbour-list build (one home cell each)
+constexpr int kWin = 512;         // candidates per shared-memory window of the list build
+constexpr int kHomeMax = 64;      // home atoms handled per window pass
+constexpr int kRelMax = 48;       // relevant-list capacity per carbon atom
+constexpr int kMetalPerBlock = 128 / kMT;   // atoms per 128-thread block
+constexpr int kCarbonPerBlock = 128 / kCT;
 
 // Values of the step reduction (slot indices into a 16-float record).
 enum RedSlot {

@@ -186,6 +186,7 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
   }
   cudaDeviceProp prop;
   cudaGetDeviceProperties(&prop, c->opt.device);
+  const int numSMs = prop.multiProcessorCount;
   if (prop.major != 10 || prop.minor != 3) {
     delete c;
     return sg_fail(SG_ERR_NO_DEVICE, "device %d is sm_%d%d; this build targets sm_103 (GB300)",
@@ -196,9 +197,13 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
     cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     c->ownStream = true;
   }
+  cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+  cudaEventCreateWithFlags(&c->evFork, cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&c->evJoin, cudaEventDisableTiming);
   c->nrep = n_replicas;
   c->hp.assign(params, params + n_replicas);
   c->nebrMax = params[0].iNebrMax;
+  c->rowStride = (c->nebrMax + 3) & ~3;
   c->stepCount = params[0].stepCount;
   c->countRdf = params[0].countRdf;
   c->oneStep.resize(n_replicas);
@@ -225,6 +230,8 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
   }
   c->ntot = atomOff;
   c->ctot = cellOff;
+  // list build: one warp per home cell, a grid of a few resident blocks per SM walking the cells
+  c->nebrGrid = std::max(1, std::min((c->ctot + kNebrWarps - 1) / kNebrWarps, numSMs * 8));
   const size_t N = c->ntot;
 #define AL(ptr, n)                          \
   if ((rc = devAllocT(c, &ptr, (n)))) {     \
@@ -238,8 +245,12 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
   AL(c->cellOf, N); AL(c->slot, N); AL(c->tmpIdx, N); AL(c->sortIdx, N);
   AL(c->cellCount, (size_t)c->ctot); AL(c->cellStart, (size_t)c->ctot);
   AL(c->nn, N); AL(c->ns, N);
-  AL(c->nbl, N * c->nebrMax);
+  AL(c->nbl, N * c->rowStride);
   AL(c->sl, N * kShortMax);
+  AL(c->nrl, N);
+  AL(c->rl, N * kRelMax);
+  AL(c->activeCells, (size_t)c->ctot);
+  AL(c->nebrWork, 2);
   AL(c->rho, N); AL(c->dF, N); AL(c->Fv, N); AL(c->fric, N);
   AL(c->partial, (size_t)std::max(redOff, 1) * kNumRed);
   AL(c->partialCmv, (size_t)std::max(cmvOff, 1) * 3);
@@ -255,7 +266,8 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
     for (auto &e : c->phaseEv) cudaEventCreate(&e);
   // tables
   if ((rc = makeRangeTab(c, c->atomTab, 128, 0)) || (rc = makeRangeTab(c, c->metalTab, 128, 1)) ||
-      (rc = makeRangeTab(c, c->carbonTab, 128, 2))) {
+      (rc = makeRangeTab(c, c->carbonTab, 128, 2)) || (rc = makeRangeTab(c, c->metalTabT, kMetalPerBlock, 1)) ||
+      (rc = makeRangeTab(c, c->carbonTabT, kCarbonPerBlock, 2))) {
     sg_destroy(c);
     return rc;
   }
@@ -349,6 +361,10 @@ extern "C" int sg_destroy(sg_ctx *c) {
   for (auto &e : c->phaseEv)
     if (e) cudaEventDestroy(e);
   for (void *p : c->allocs) cudaFree(p);
+  if (c->side) cudaStreamSynchronize(c->side);
+  if (c->evFork) cudaEventDestroy(c->evFork);
+  if (c->evJoin) cudaEventDestroy(c->evJoin);
+  if (c->side) cudaStreamDestroy(c->side);
   if (c->ownStream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return SG_OK;
@@ -435,37 +451,57 @@ enum { V_SHEAR = 1, V_RDF = 2, V_RDF_ZERO = 4 };
 
 static int enqueueRebuild(sg_ctx *c, int force) {
   const int fr = force;
+  CK(cudaMemsetAsync(c->nebrWork, 0, 2 * sizeof(int), c->stream));
   if (c->ntiles) {
     k_scan_tiles<<<c->tileTab.n, 256, 0, c->stream>>>(c->tileTab.view(), c->rc, c->st, c->cellCount, c->tileSum, fr);
     k_scan_tile_prefix<<<c->nrep, 1024, 0, c->stream>>>(c->rc, c->st, c->dTileFirst, c->tileSum, fr);
     k_scan_final<<<c->tileTab.n, 256, 0, c->stream>>>(c->tileTab.view(), c->rc, c->st, c->cellCount, c->tileSum,
-                                                       c->cellStart, (int)c->hp[0].blockSize, fr);
+                                                       c->cellStart, (int)c->hp[0].blockSize, fr, c->activeCells,
+                                                       c->nebrWork);
     LAUNCH_OK();
   }
   k_scatter<<<c->atomTab.n, 128, 0, c->stream>>>(c->atomTab.view(), c->rc, c->st, c->cellOf, c->slot, c->cellStart,
                                                  c->tmpIdx, c->nn, c->ns, fr);
   k_rank<<<c->atomTab.n, 128, 0, c->stream>>>(c->atomTab.view(), c->rc, c->st, c->cellOf, c->cellStart, c->tmpIdx,
                                               c->pos, c->sortIdx, c->sortPos, fr);
-  k_build_nebr<<<c->atomTab.n, 128, 0, c->stream>>>(c->atomTab.view(), c->rc, c->st, c->cellOf, c->cellStart,
-                                                    c->sortPos, c->nn, c->nbl, c->ns, c->sl, c->ntot,
-                                                    c->nebrMax, fr);
+  k_build_nebr<<<c->nebrGrid, kNebrWarps * 32, 0, c->stream>>>(c->tileTab.rep, c->activeCells, c->nebrWork, c->rc,
+                                                                 c->st, c->cellStart, c->sortPos, c->nn, c->nbl,
+                                                                 c->ns, c->sl, c->nrl, c->rl, c->rowStride,
+                                                                 c->nebrMax);
   LAUNCH_OK();
   return SG_OK;
 }
 
-static int enqueueForces(sg_ctx *c) {
+// Forces: the carbon pass on the main stream, the metal chain (density, metal forces and, in
+// a step, the metal centre-of-mass velocity) on the side stream; both join before the
+// reduction.  Inside a capture the fork and join become graph edges.
+static int enqueueForces(sg_ctx *c, bool withCmVel) {
   if (c->opt.mode == SG_MODE_MIXED) return sg_mixed_enqueue_forces(c);
-  if (c->metalTab.n) {
-    k_rho<<<c->metalTab.n, 128, 0, c->stream>>>(c->metalTab.view(), c->rc, c->pos, c->nn, c->nbl, c->rho, c->dF,
-                                                c->Fv, c->ntot);
-    k_force_metal<<<c->metalTab.n, 128, 0, c->stream>>>(c->metalTab.view(), c->rc, c->pos, c->acc, c->nn, c->nbl,
-                                                        c->dF, c->Fv, c->fric, c->ntot);
+  const bool fork = c->metalTabT.n > 0;
+  if (fork) {
+    CK(cudaEventRecord(c->evFork, c->stream));
+    CK(cudaStreamWaitEvent(c->side, c->evFork, 0));
+    k_rho<<<c->metalTabT.n, 128, 0, c->side>>>(c->metalTabT.view(), c->rc, c->pos, c->nn, c->nbl, c->rho, c->dF,
+                                               c->Fv, c->rowStride);
+    k_force_metal<<<c->metalTabT.n, 128, 0, c->side>>>(c->metalTabT.view(), c->rc, c->pos, c->acc, c->nn, c->nbl,
+                                                       c->dF, c->Fv, c->fric, c->rowStride);
+    if (withCmVel && c->cmvTab.n)
+      k_cmvel<<<c->cmvTab.n, kRedThreads, 0, c->side>>>(c->cmvTab.view(), c->rc, c->st, c->vel, c->acc,
+                                                        c->partialCmv, c->dCmvFirst);
+    if (c->opt.phase_timing) cudaEventRecordWithFlags(c->phaseEv[7], c->side, cudaEventRecordExternal);
+    LAUNCH_OK();
   }
+  if (c->carbonTabT.n)
+    k_force_carbon<<<c->carbonTabT.n, 128, 0, c->stream>>>(c->carbonTabT.view(), c->rc, c->pos, c->acc, c->nn,
+                                                           c->nbl, c->ns, c->sl, c->nrl, c->rl, c->rowStride);
   if (c->opt.phase_timing) cudaEventRecordWithFlags(c->phaseEv[3], c->stream, cudaEventRecordExternal);
-  if (c->carbonTab.n)
-    k_force_carbon<<<c->carbonTab.n, 128, 0, c->stream>>>(c->carbonTab.view(), c->rc, c->pos, c->acc, c->nn,
-                                                          c->nbl, c->ns, c->sl, c->st, c->ntot);
   LAUNCH_OK();
+  if (fork) {
+    CK(cudaEventRecord(c->evJoin, c->side));
+    CK(cudaStreamWaitEvent(c->stream, c->evJoin, 0));
+  } else if (c->opt.phase_timing) {
+    cudaEventRecordWithFlags(c->phaseEv[7], c->stream, cudaEventRecordExternal);
+  }
   return SG_OK;
 }
 
@@ -508,14 +544,11 @@ static int enqueueStep(sg_ctx *c, int variant) {
   phaseMark(c, 1);
   if ((rc = enqueueRebuild(c, fr))) return rc;
   phaseMark(c, 2);
-  if ((rc = enqueueForces(c))) return rc;
+  if ((rc = enqueueForces(c, true))) return rc;
   phaseMark(c, 4);
   if (c->opt.mode == SG_MODE_MIXED) {
     if ((rc = sg_mixed_enqueue_reduce(c, fr))) return rc;
   } else {
-    if (c->cmvTab.n)
-      k_cmvel<<<c->cmvTab.n, kRedThreads, 0, c->stream>>>(c->cmvTab.view(), c->rc, c->st, c->vel, c->acc,
-                                                           c->partialCmv, c->dCmvFirst);
     k_step_reduce<<<c->redTab.n, kRedThreads, 0, c->stream>>>(c->redTab.view(), c->rc, c->st, c->pos, c->vel, c->acc,
                                                               c->fric, c->partial, c->dRedFirst, c->diffBuf,
                                                               c->dDiffOff, fr);
@@ -640,10 +673,13 @@ extern "C" int sg_get_phase_times(sg_ctx *c, float *ms, int n) {
   if (!c || !c->opt.phase_timing) return -sg_fail(SG_ERR_UNSUPPORTED, "phase_timing is off");
   cudaError_t e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return -sg_fail(SG_ERR_CUDA, "%s", cudaGetErrorString(e));
-  const int np = 6;
+  // integrate, rebuild, metal chain (side stream), carbon pass, forces (fork to join),
+  // reduce, extra
+  const int from[7] = {0, 1, 2, 2, 2, 4, 5}, to[7] = {1, 2, 7, 3, 4, 5, 6};
+  const int np = 7;
   for (int k = 0; k < np && k < n; k++) {
     float t = 0.f;
-    e = cudaEventElapsedTime(&t, c->phaseEv[k], c->phaseEv[k + 1]);
+    e = cudaEventElapsedTime(&t, c->phaseEv[from[k]], c->phaseEv[to[k]]);
     if (e != cudaSuccess) return -sg_fail(SG_ERR_CUDA, "%s", cudaGetErrorString(e));
     ms[k] = t;
   }
@@ -674,7 +710,7 @@ extern "C" int sg_build_lists(sg_ctx *c) {
 
 extern "C" int sg_compute_forces(sg_ctx *c) {
   if (!c) return sg_fail(SG_ERR_INVALID, "null context");
-  int rc = enqueueForces(c);
+  int rc = enqueueForces(c, false);
   if (rc) return rc;
   CK(cudaStreamSynchronize(c->stream));
   return checkFlags(c);
@@ -791,12 +827,11 @@ extern "C" int sg_get_nebr(sg_ctx *c, int rep, int *nnOut, int *nblOut) {
   if ((rc = readArr(c, nn.data(), c->nn + P.atomOff, P.nMol))) return rc;
   if (nnOut) memcpy(nnOut, nn.data(), sizeof(int) * P.nMol);
   if (nblOut) {
-    std::vector<int> col(P.nMol);
-    for (int j = 0; j < c->nebrMax; j++) {
-      if ((rc = readArr(c, col.data(), c->nbl + (size_t)j * c->ntot + P.atomOff, P.nMol))) return rc;
+    std::vector<int> rows((size_t)P.nMol * c->rowStride);
+    if ((rc = readArr(c, rows.data(), c->nbl + (size_t)P.atomOff * c->rowStride, rows.size()))) return rc;
+    for (int j = 0; j < c->nebrMax; j++)
       for (int i = 0; i < P.nMol; i++)
-        nblOut[(size_t)j * P.nMol + i] = (j < nn[i]) ? col[i] - P.atomOff : -1;
-    }
+        nblOut[(size_t)j * P.nMol + i] = (j < nn[i]) ? rows[(size_t)i * c->rowStride + j] - P.atomOff : -1;
   }
   return SG_OK;
 }

@@ -22,7 +22,7 @@ struct DevTab {
 };
 
 struct sg_ctx {
-  int nrep = 0, ntot = 0, ctot = 0, nebrMax = 128, ntiles = 0;
+  int nrep = 0, ntot = 0, ctot = 0, nebrMax = 128, rowStride = 128, ntiles = 0;
   sg_options opt;
   std::vector<sg_simparams> hp;  // parameters as given (mutable fields refreshed on demand)
   std::vector<RepConst> hrc;
@@ -37,6 +37,10 @@ struct sg_ctx {
   float4 *pos = nullptr, *vel = nullptr, *acc = nullptr, *posLo = nullptr, *sortPos = nullptr;
   int *cellOf = nullptr, *slot = nullptr, *cellCount = nullptr, *cellStart = nullptr;
   int *tmpIdx = nullptr, *sortIdx = nullptr, *nn = nullptr, *nbl = nullptr, *ns = nullptr, *sl = nullptr;
+  int *nrl = nullptr;
+  int2 *rl = nullptr;
+  int nebrGrid = 0;
+  int *activeCells = nullptr, *nebrWork = nullptr;
   float *rho = nullptr, *dF = nullptr, *Fv = nullptr, *fric = nullptr;
   float *partial = nullptr, *partialCmv = nullptr;
   int *dRedFirst = nullptr, *dCmvFirst = nullptr, *tileSum = nullptr, *dTileFirst = nullptr;
@@ -46,6 +50,7 @@ struct sg_ctx {
   float *diffBuf = nullptr;
   size_t *dDiffOff = nullptr;
   DevTab atomTab, metalTab, carbonTab, redTab, cmvTab, tileTab;
+  DevTab metalTabT, carbonTabT;  // blocks of kMetalPerBlock / kCarbonPerBlock atoms
   int anyMetal = 0, anyCarbon = 0, maxHist = 0;
   // graphs keyed by variant bits
   std::map<int, cudaGraphExec_t> graphs;
@@ -55,7 +60,9 @@ struct sg_ctx {
   std::vector<sg_prop> oneStep;  // per replica, host-accumulated step times
   void *mixed = nullptr;         // MIXED-mode buffers (sg_kernels_mixed.cu)
   float *stage = nullptr;        // 3 floats per atom: host float3 arrays in transit
-  cudaEvent_t phaseEv[7] = {};   // phase boundaries of a step (phase_timing)
+  cudaEvent_t phaseEv[8] = {};   // phase boundaries of a step (phase_timing)
+  cudaStream_t side = nullptr;   // second stream: the metal force chain runs beside the carbon pass
+  cudaEvent_t evFork = nullptr, evJoin = nullptr;
   int launchCount = 0;           // kernel launches counted while enqueueing a step
   std::map<int, int> kernelsPerVariant;
   int lastVariant = 0;

@@ -16,26 +16,29 @@ __global__ void k_scan_tiles(BlockTab tab, const RepConst *rc, const RepState *s
 __global__ void k_scan_tile_prefix(const RepConst *rc, const RepState *st, const int *tileFirst,
                                    int *tileSum, int forceRebuild);
 __global__ void k_scan_final(BlockTab tab, const RepConst *rc, RepState *st, int *cellCount,
-                             const int *tileSum, int *cellStart, int blockSizeCap, int forceRebuild);
+                             const int *tileSum, int *cellStart, int blockSizeCap, int forceRebuild,
+                             int *active, int *work);
 __global__ void k_scatter(BlockTab tab, const RepConst *rc, RepState *st, const int *cellOf,
                           const int *slot, const int *cellStart, int *tmpIdx, int *nn, int *ns,
                           int forceRebuild);
 __global__ void k_rank(BlockTab tab, const RepConst *rc, const RepState *st, const int *cellOf,
                        const int *cellStart, const int *tmpIdx, const float4 *pos, int *sortIdx,
                        float4 *sortPos, int forceRebuild);
-__global__ void k_build_nebr(BlockTab tab, const RepConst *rc, RepState *st, const int *cellOf,
-                             const int *cellStart, const float4 *sortPos, int *nn, int *nbl,
-                             int *ns, int *sl, int ntot, int nebrMax, int forceRebuild);
+// work[0]: next entry of the active-cell list to take, work[1]: its length (both reset before
+// the scan of every rebuild)
+__global__ void k_build_nebr(const int *tileRep, const int *active, int *work, const RepConst *rc,
+                             RepState *st, const int *cellStart, const float4 *sortPos, int *nn,
+                             int *nbl, int *ns, int *sl, int *nrl, int2 *rl, int rowStride, int nebrMax);
 
 // ---- PLAIN force and step kernels ----
 __global__ void k_rho(BlockTab tab, const RepConst *rc, const float4 *pos, const int *nn,
-                      const int *nbl, float *rho, float *dF, float *Fv, int ntot);
+                      const int *nbl, float *rho, float *dF, float *Fv, int rowStride);
 __global__ void k_force_metal(BlockTab tab, const RepConst *rc, float4 *pos, float4 *acc,
                               const int *nn, const int *nbl, const float *dF, const float *Fv,
-                              float *fric, int ntot);
+                              float *fric, int rowStride);
 __global__ void k_force_carbon(BlockTab tab, const RepConst *rc, float4 *pos, float4 *acc,
                                const int *nn, const int *nbl, const int *ns, const int *sl,
-                               RepState *st, int ntot);
+                               const int *nrl, const int2 *rl, int rowStride);
 __global__ void k_cmvel(BlockTab tab, const RepConst *rc, RepState *st, const float4 *vel,
                         const float4 *acc, float *partial, const int *redFirst);
 __global__ void k_step_reduce(BlockTab tab, const RepConst *rc, RepState *st, const float4 *pos,

@@ -195,7 +195,8 @@ __global__ void k_scan_tile_prefix(const RepConst *__restrict__ rc, const RepSta
 // the counts for the next rebuild.  Also records the largest cell occupancy.
 __global__ void k_scan_final(BlockTab tab, const RepConst *__restrict__ rc, RepState *st,
                              int *__restrict__ cellCount, const int *__restrict__ tileSum,
-                             int *__restrict__ cellStart, int blockSizeCap, int forceRebuild) {
+                             int *__restrict__ cellStart, int blockSizeCap, int forceRebuild,
+                             int *__restrict__ active, int *__restrict__ work) {
   const int rep = tab.rep[blockIdx.x];
   RepState *S = st + rep;
   if (!rebuilding(S, forceRebuild)) return;
@@ -236,6 +237,23 @@ __global__ void k_scan_final(BlockTab tab, const RepConst *__restrict__ rc, RepS
     run += v[i];
     cellCount[cb + i] = 0;
   }
+  // compact the non-empty cells (any order) for the list build
+  int nonEmpty = 0;
+#pragma unroll
+  for (int i = 0; i < kPer; i++) nonEmpty += (v[i] > 0 && c0 + threadIdx.x * kPer + i < P.ncells) ? 1 : 0;
+  int pre = nonEmpty;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, pre, o);
+    if ((threadIdx.x & 31) >= o) pre += y;
+  }
+  const int wsum = __shfl_sync(0xffffffffu, pre, 31);
+  int wbase = 0;
+  if ((threadIdx.x & 31) == 31 && wsum > 0) wbase = atomicAdd(&work[1], wsum);
+  wbase = __shfl_sync(0xffffffffu, wbase, 31);
+  int slotOut = wbase + pre - nonEmpty;
+#pragma unroll
+  for (int i = 0; i < kPer; i++)
+    if (v[i] > 0 && c0 + threadIdx.x * kPer + i < P.ncells) active[slotOut++] = cb + i;
   for (int o = 16; o > 0; o >>= 1) {
     occ = max(occ, __shfl_xor_sync(0xffffffffu, occ, o));
     over += __shfl_xor_sync(0xffffffffu, over, o);
@@ -294,63 +312,162 @@ __global__ void k_rank(BlockTab tab, const RepConst *__restrict__ rc, const RepS
 }
 
 // ============================================================================================
-// Neighbour list (BuildNebrListK, SurfaceGrowth.cu:612-711): one thread per sorted slot, so a
-// warp mostly shares one home cell and walks the same 27 segments.  Entries are emitted in
-// stencil order, ascending atom index inside a cell.  Also emits the short list: the
-// neighbours within (rCutC + skin) in list order, used by the graphene second-neighbour walk.
+// Neighbour list (BuildNebrListK, SurfaceGrowth.cu:612-711), cell-centric.  Warps take non-empty
+// home cells from the list k_scan_final compacted, through an atomic work counter.  Lanes
+// 0..26 look up the 27 stencil cells (reference visiting order); their segments form a
+// shared-memory window of candidates in stencil order.  Per chunk of 32 candidates (held in
+// registers, one per lane), the warp streams the home atoms (up to 32 at a time, lane a holding
+// home atom a and its counters): every lane tests its candidate against the broadcast home
+// atom, and a ballot ranks the matches, so entries land in the atom's row nbl[g*rowStride + j]
+// in stencil order and ascending atom index inside a cell: the order of the reference's
+// one-thread walk.  The same pass emits
+//  - the short list: entries within rCutC + skin (graphene second-neighbour walk), and
+//  - for carbon atoms the relevant list: every metal entry and every entry within
+//    rCutC + skin, each with its position in the full list, which is all the carbon-force
+//    pass needs.
+// Both rest on the skin, as the neighbour list itself does: no pair closes in by more than
+// rNebrShell between rebuilds.
 // ============================================================================================
-__global__ void k_build_nebr(BlockTab tab, const RepConst *__restrict__ rc, RepState *st,
-                             const int *__restrict__ cellOf, const int *__restrict__ cellStart,
-                             const float4 *__restrict__ sortPos, int *__restrict__ nn,
-                             int *__restrict__ nbl, int *__restrict__ ns, int *__restrict__ sl,
-                             int ntot, int nebrMax, int forceRebuild) {
-  const int rep = tab.rep[blockIdx.x];
-  RepState *S = st + rep;
-  if (!rebuilding(S, forceRebuild)) return;
-  const RepConst &P = rc[rep];
-  const int s = tab.start[blockIdx.x] + threadIdx.x;
-  const int binnedEnd = cellStart[P.cellOff + P.ncells];
-  int want = 0, over = 0;
-  if (s < binnedEnd) {
-    const float4 A = sortPos[s];
-    const int g = __float_as_int(A.w);
-    const int c = cellOf[g];
-    int n = 0, m = 0;
-    for (int o = 0; o < 27; o++) {
-      float sx, sy, sz;
-      const int C = stencilCell(P, c, o, sx, sy, sz);
-      const int qb = cellStart[P.cellOff + C], qe = cellStart[P.cellOff + C + 1];
-      for (int q = qb; q < qe; q++) {
-        const float4 B = sortPos[q];
-        const int k = __float_as_int(B.w);
-        float dx = A.x - B.x, dy = A.y - B.y, dz = A.z - B.z;
-        dx = dx - sx; dy = dy - sy; dz = dz - sz;
-        const float rr = dx * dx + dy * dy + dz * dz;
-        if ((rr < P.rrNebr) && (g != k)) {
-          if (n < nebrMax) nbl[(size_t)n * ntot + g] = k;
-          n++;
-          if (rr < P.rrShort) {
-            if (m < kShortMax) sl[(size_t)m * ntot + g] = k;
-            m++;
+__global__ void __launch_bounds__(128) k_build_nebr(const int *__restrict__ tileRep, const int *__restrict__ active,
+                                                    int *work, const RepConst *__restrict__ rc, RepState *st,
+                                                    const int *__restrict__ cellStart,
+                                                    const float4 *__restrict__ sortPos, int *__restrict__ nn,
+                                                    int *__restrict__ nbl, int *__restrict__ ns,
+                                                    int *__restrict__ sl, int *__restrict__ nrl,
+                                                    int2 *__restrict__ rl, int rowStride, int nebrMax) {
+  __shared__ int sBuf[kNebrWarps][kWin];
+  __shared__ float sSh[kNebrWarps][27][3];
+  __shared__ int sQb[kNebrWarps][27], sQe[kNebrWarps][27];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned lower = (1u << lane) - 1;
+  const int nActive = work[1];
+  while (true) {
+    int idx = 0;
+    if (lane == 0) idx = atomicAdd(&work[0], 1);
+    idx = __shfl_sync(0xffffffffu, idx, 0);
+    if (idx >= nActive) break;
+    const int gc = active[idx];
+    const int rep = tileRep[gc / kCellTile];
+    RepState *S = st + rep;
+    const RepConst &P = rc[rep];
+    const int c = gc - P.cellOff;
+    const int hb = cellStart[gc], he = cellStart[gc + 1];
+    const int metalEnd = P.atomOff + P.nMolMe;
+    if (lane < 27) {
+      const int cxy = P.cells[0] * P.cells[1];
+      const int ccz = c / cxy;
+      const int ccy = (c - ccz * cxy) / P.cells[0];
+      const int ccx = c - (ccz * P.cells[1] + ccy) * P.cells[0];
+      int mx = ccx + kOff27[lane][0], my = ccy + kOff27[lane][1], mz = ccz + kOff27[lane][2];
+      float sx = 0.f, sy = 0.f, sz = 0.f;
+      if (mx >= P.cells[0]) { mx = 0; sx = P.region[0]; }
+      else if (mx < 0) { mx = P.cells[0] - 1; sx = -P.region[0]; }
+      if (my >= P.cells[1]) { my = 0; sy = P.region[1]; }
+      else if (my < 0) { my = P.cells[1] - 1; sy = -P.region[1]; }
+      if (mz >= P.cells[2]) { mz = 0; sz = P.region[2]; }
+      else if (mz < 0) { mz = P.cells[2] - 1; sz = -P.region[2]; }
+      const int C = P.cellOff + (mz * P.cells[1] + my) * P.cells[0] + mx;
+      sQb[w][lane] = cellStart[C];
+      sQe[w][lane] = cellStart[C + 1];
+      sSh[w][lane][0] = sx; sSh[w][lane][1] = sy; sSh[w][lane][2] = sz;
+    }
+    __syncwarp();
+    int want = 0, over = 0;
+    for (int h0 = hb; h0 < he; h0 += 32) {
+      const int nh = min(32, he - h0);
+      // lane a holds home atom a of this pass and its three counters
+      float4 Ah = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (lane < nh) Ah = sortPos[h0 + lane];
+      int n = 0, m = 0, r = 0;
+      int o = 0, qpos = sQb[w][0];
+      while (o < 27) {
+        int fill = 0;
+        while (o < 27 && fill < kWin) {
+          const int take = min(sQe[w][o] - qpos, kWin - fill);
+          for (int t = lane; t < take; t += 32) sBuf[w][fill + t] = ((qpos + t) << 5) | o;
+          fill += take;
+          qpos += take;
+          if (qpos >= sQe[w][o]) {
+            o++;
+            if (o < 27) qpos = sQb[w][o];
           }
         }
+        __syncwarp();
+        for (int e0 = 0; e0 < fill; e0 += 32) {
+          // this lane's candidate, shifted into the home cell's image
+          const int e = e0 + lane;
+          const bool have = e < fill;
+          float bx = 0.f, by = 0.f, bz = 0.f;
+          int k = -1, oo = 0;
+          if (have) {
+            const int code = sBuf[w][e];
+            oo = code & 31;
+            const float4 B = sortPos[code >> 5];
+            k = __float_as_int(B.w);
+            bx = B.x; by = B.y; bz = B.z;
+          }
+          // the reference subtracts the cell shift after the difference: both roundings kept
+          const float sx = sSh[w][oo][0], sy = sSh[w][oo][1], sz = sSh[w][oo][2];
+          for (int a = 0; a < nh; a++) {
+            const float ax = __shfl_sync(0xffffffffu, Ah.x, a);
+            const float ay = __shfl_sync(0xffffffffu, Ah.y, a);
+            const float az = __shfl_sync(0xffffffffu, Ah.z, a);
+            const int g = __shfl_sync(0xffffffffu, __float_as_int(Ah.w), a);
+            float dx = ax - bx, dy = ay - by, dz = az - bz;
+            dx = dx - sx; dy = dy - sy; dz = dz - sz;
+            const float rr = dx * dx + dy * dy + dz * dz;
+            const bool hit = have && (rr < P.rrNebr) && (g != k);
+            const unsigned mh = __ballot_sync(0xffffffffu, hit);
+            if (mh == 0) continue;
+            const bool close = hit && (rr < P.rrShort);
+            const bool rel = (g >= metalEnd) && (close || (hit && k < metalEnd));
+            const unsigned mc = __ballot_sync(0xffffffffu, close);
+            const unsigned mr = __ballot_sync(0xffffffffu, rel);
+            const int na = __shfl_sync(0xffffffffu, n, a);
+            const int ma = __shfl_sync(0xffffffffu, m, a);
+            const int ra = __shfl_sync(0xffffffffu, r, a);
+            if (hit) {
+              const int j = na + __popc(mh & lower);
+              if (j < nebrMax) nbl[(size_t)g * rowStride + j] = k;
+              if (rel) {
+                const int jr = ra + __popc(mr & lower);
+                if (jr < kRelMax) rl[(size_t)g * kRelMax + jr] = make_int2(k, j);
+              }
+            }
+            if (close) {
+              const int j = ma + __popc(mc & lower);
+              if (j < kShortMax) sl[(size_t)g * kShortMax + j] = k;
+            }
+            if (lane == a) {
+              n += __popc(mh);
+              m += __popc(mc);
+              r += __popc(mr);
+            }
+          }
+        }
+        __syncwarp();
+      }
+      if (lane < nh) {
+        const int g = __float_as_int(Ah.w);
+        nn[g] = min(n, nebrMax);
+        ns[g] = (m > kShortMax || n > nebrMax) ? -1 : m;   // -1: walk the full list instead
+        nrl[g] = (r > kRelMax || n > nebrMax) ? -1 : r;    // -1: carbon pass walks the full list
+        want = max(want, n);
+        over += (n > nebrMax) ? 1 : 0;
       }
     }
-    want = n;
-    if (n > nebrMax) over = 1;
-    nn[g] = min(n, nebrMax);
-    ns[g] = (m > kShortMax || n > nebrMax) ? -1 : m;  // -1: walk the full list instead
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    want = max(want, __shfl_xor_sync(0xffffffffu, want, o));
-    over += __shfl_xor_sync(0xffffffffu, over, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    if (want > 0) atomicMax(&S->maxNeighbours, want);
-    if (over > 0) {
-      atomicAdd(&S->nebrOverflow, over);
-      setFlag(S, 5 /*SG_ERR_NEBR_OVERFLOW*/);
+    for (int off = 16; off > 0; off >>= 1) {
+      want = max(want, __shfl_xor_sync(0xffffffffu, want, off));
+      over += __shfl_xor_sync(0xffffffffu, over, off);
     }
+    if (lane == 0) {
+      atomicMax(&S->maxNeighbours, want);
+      if (over > 0) {
+        atomicAdd(&S->nebrOverflow, over);
+        setFlag(S, 5 /*SG_ERR_NEBR_OVERFLOW*/);
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -420,31 +537,41 @@ __device__ __forceinline__ float eamEmbedDeriv(const RepConst &P, float rho) {
 }
 
 // Electron density of each metal atom (EamComputeRhoK, cu:716-773), plus F(rho) and F'(rho),
-// which the reference re-evaluates per pair in the force kernel.
-__global__ void k_rho(BlockTab tab, const RepConst *__restrict__ rc, const float4 *__restrict__ pos,
-                      const int *__restrict__ nn, const int *__restrict__ nbl,
-                      float *__restrict__ rho, float *__restrict__ dF, float *__restrict__ Fv,
-                      int ntot) {
+// which the reference re-evaluates per pair in the force kernel.  kMT lanes share one metal
+// atom: lane l takes list entries l, l + kMT, ...; the partial sums meet in a shuffle tree.
+__global__ void __launch_bounds__(128) k_rho(BlockTab tab, const RepConst *__restrict__ rc,
+                                             const float4 *__restrict__ pos, const int *__restrict__ nn,
+                                             const int *__restrict__ nbl, float *__restrict__ rho,
+                                             float *__restrict__ dF, float *__restrict__ Fv, int rowStride) {
   const int rep = tab.rep[blockIdx.x];
   const RepConst &P = rc[rep];
-  const int i = tab.start[blockIdx.x] + threadIdx.x;
+  const int sub = threadIdx.x & (kMT - 1);
+  const unsigned gmask = ((1u << kMT) - 1) << (threadIdx.x & 31 & ~(kMT - 1));
+  const int i = tab.start[blockIdx.x] + threadIdx.x / kMT;
   const int metalEnd = P.atomOff + P.nMolMe;
-  if (i >= metalEnd) return;
-  const float4 A = pos[i];
-  const int n = nn[i];
+  const bool valid = i < metalEnd;
   float sum = 0.f;
-  for (int j = 0; j < n; j++) {
-    const int k = nbl[(size_t)j * ntot + i];
-    const float4 B = pos[k];
-    const float dx = minImg(A.x - B.x, P.region[0]);
-    const float dy = minImg(A.y - B.y, P.region[1]);
-    const float dz = minImg(A.z - B.z, P.region[2]);
-    const float rr = dx * dx + dy * dy + dz * dz;
-    if ((rr < P.rrCutEam) && (k < metalEnd)) sum += eamDensity(P, sqrtf(rr));
+  if (valid) {
+    const float4 A = pos[i];
+    const int n = nn[i];
+    const int *row = nbl + (size_t)i * rowStride;
+    for (int j = sub; j < n; j += kMT) {
+      const int k = row[j];
+      const float4 B = pos[k];
+      const float dx = minImg(A.x - B.x, P.region[0]);
+      const float dy = minImg(A.y - B.y, P.region[1]);
+      const float dz = minImg(A.z - B.z, P.region[2]);
+      const float rr = dx * dx + dy * dy + dz * dz;
+      if ((rr < P.rrCutEam) && (k < metalEnd)) sum += eamDensity(P, sqrtf(rr));
+    }
   }
-  rho[i] = sum;
-  dF[i] = eamEmbedDeriv(P, sum);
-  Fv[i] = eamEmbed(P, sum);
+#pragma unroll
+  for (int o = kMT / 2; o > 0; o >>= 1) sum += __shfl_xor_sync(gmask, sum, o);
+  if (valid && sub == 0) {
+    rho[i] = sum;
+    dF[i] = eamEmbedDeriv(P, sum);
+    Fv[i] = eamEmbed(P, sum);
+  }
 }
 
 // Lennard-Jones metal-carbon term (cu:880-884).
@@ -456,164 +583,252 @@ __device__ __forceinline__ void ljTerms(const RepConst &P, float rr, float &fc, 
 }
 
 // Forces on metal atoms: EAM pair + embedding with metal neighbours, LJ with carbon neighbours
-// (ComputeForcesK case 0, cu:856-897, epilogue cu:1069-1082).
-__global__ void k_force_metal(BlockTab tab, const RepConst *__restrict__ rc, float4 *__restrict__ pos,
-                              float4 *__restrict__ acc, const int *__restrict__ nn,
-                              const int *__restrict__ nbl, const float *__restrict__ dF,
-                              const float *__restrict__ Fv, float *__restrict__ fric, int ntot) {
+// (ComputeForcesK case 0, cu:856-897, epilogue cu:1069-1082); kMT lanes per atom.
+__global__ void __launch_bounds__(128) k_force_metal(BlockTab tab, const RepConst *__restrict__ rc,
+                                                     float4 *__restrict__ pos, float4 *__restrict__ acc,
+                                                     const int *__restrict__ nn, const int *__restrict__ nbl,
+                                                     const float *__restrict__ dF, const float *__restrict__ Fv,
+                                                     float *__restrict__ fric, int rowStride) {
   const int rep = tab.rep[blockIdx.x];
   const RepConst &P = rc[rep];
-  const int i = tab.start[blockIdx.x] + threadIdx.x;
+  const int sub = threadIdx.x & (kMT - 1);
+  const unsigned gmask = ((1u << kMT) - 1) << (threadIdx.x & 31 & ~(kMT - 1));
+  const int i = tab.start[blockIdx.x] + threadIdx.x / kMT;
   const int metalEnd = P.atomOff + P.nMolMe;
-  if (i >= metalEnd) return;
-  const float4 A = pos[i];
-  const int n = nn[i];
-  const float dFi = dF[i];
-  float fx = 0.f, fy = 0.f, fz = 0.f, rx = 0.f, ry = 0.f, rz = 0.f, u = 0.f;
-  for (int j = 0; j < n; j++) {
-    const int k = nbl[(size_t)j * ntot + i];
-    const float4 B = pos[k];
-    const float dx = minImg(A.x - B.x, P.region[0]);
-    const float dy = minImg(A.y - B.y, P.region[1]);
-    const float dz = minImg(A.z - B.z, P.region[2]);
-    const float rr = dx * dx + dy * dy + dz * dz;
-    if (k < metalEnd) {
-      if (rr >= P.rrCutEam) continue;  // the reference computes and then zeroes the term
-      const float r = sqrtf(rr);
-      const EamPair e = eamPair(P, r);
-      float fc = -e.dphi;
-      fc = fc - e.df * (dFi + dF[k]);
-      fc = fc / r;
-      fx = fx + fc * dx; fy = fy + fc * dy; fz = fz + fc * dz;
-      u += e.phi;
-    } else {
-      if (rr >= P.rrCutLJ) continue;
-      float fc, ul;
-      ljTerms(P, rr, fc, ul);
-      u += ul;
-      fx = fx + fc * dx; fy = fy + fc * dy; fz = fz + fc * dz;
-      rx = rx + fc * dx; ry = ry + fc * dy; rz = rz + fc * dz;
+  const bool valid = i < metalEnd;
+  float fx = 0.f, fy = 0.f, fz = 0.f, rx = 0.f, u = 0.f;
+  if (valid) {
+    const float4 A = pos[i];
+    const int n = nn[i];
+    const float dFi = dF[i];
+    const int *row = nbl + (size_t)i * rowStride;
+    for (int j = sub; j < n; j += kMT) {
+      const int k = row[j];
+      const float4 B = pos[k];
+      const float dx = minImg(A.x - B.x, P.region[0]);
+      const float dy = minImg(A.y - B.y, P.region[1]);
+      const float dz = minImg(A.z - B.z, P.region[2]);
+      const float rr = dx * dx + dy * dy + dz * dz;
+      if (k < metalEnd) {
+        if (rr >= P.rrCutEam) continue;  // the reference computes and then zeroes the term
+        const float r = sqrtf(rr);
+        const EamPair e = eamPair(P, r);
+        float fc = -e.dphi;
+        fc = fc - e.df * (dFi + dF[k]);
+        fc = fc / r;
+        fx = fx + fc * dx; fy = fy + fc * dy; fz = fz + fc * dz;
+        u += e.phi;
+      } else {
+        if (rr >= P.rrCutLJ) continue;
+        float fc, ul;
+        ljTerms(P, rr, fc, ul);
+        u += ul;
+        fx = fx + fc * dx; fy = fy + fc * dy; fz = fz + fc * dz;
+        rx = rx + fc * dx;
+      }
     }
   }
-  acc[i] = make_float4(fx / P.massMe, fy / P.massMe, fz / P.massMe, 0.f);
-  pos[i].w = 0.5f * u + Fv[i];
-  if (P.hasFric) fric[i] = rx;
+#pragma unroll
+  for (int o = kMT / 2; o > 0; o >>= 1) {
+    fx += __shfl_xor_sync(gmask, fx, o);
+    fy += __shfl_xor_sync(gmask, fy, o);
+    fz += __shfl_xor_sync(gmask, fz, o);
+    rx += __shfl_xor_sync(gmask, rx, o);
+    u += __shfl_xor_sync(gmask, u, o);
+  }
+  if (valid && sub == 0) {
+    acc[i] = make_float4(fx / P.massMe, fy / P.massMe, fz / P.massMe, 0.f);
+    pos[i].w = 0.5f * u + Fv[i];
+    if (P.hasFric) fric[i] = rx;
+  }
 }
 
-// Forces on carbon atoms: LJ with metal neighbours and the harmonic graphene terms over the
-// first three carbon neighbours within rCutC, including the second-neighbour angle terms
-// (ComputeForcesK case 1, cu:899-1063, epilogue cu:1083-1088).  The second-neighbour walk
-// uses the neighbour's short list, which holds every entry of its full list that can be
-// within rCutC before the next rebuild, in the same order.
-__global__ void k_force_carbon(BlockTab tab, const RepConst *__restrict__ rc,
-                               float4 *__restrict__ pos, float4 *__restrict__ acc,
-                               const int *__restrict__ nn, const int *__restrict__ nbl,
-                               const int *__restrict__ ns, const int *__restrict__ sl,
-                               RepState *st, int ntot) {
+// Forces on carbon atoms (ComputeForcesK case 1, cu:899-1063, epilogue cu:1083-1088): LJ with
+// metal neighbours and the harmonic graphene terms over the first three carbon neighbours
+// within rCutC in list order, with the second-neighbour angle and out-of-plane terms of each.
+// kCT = 4 lanes share one carbon atom.  The walk goes over the atom's relevant list (metal
+// entries and close entries with their full-list positions; the full list when the relevant
+// list overflowed), four entries at a time; a ballot finds, in list order, the first three
+// close carbons (their data go to shared memory) and the full-list position p2 of the third.
+// The reference reuses its list counter for the bonded loop (cu:989), so after the third close
+// carbon its walk resumes at entry 4: metal entries at positions 4..p2 contribute their LJ term
+// twice, and entry 3 is skipped when p2 == 2.  After the walk, lane q < 3 adds the
+// second-neighbour terms of close carbon q (walking that neighbour's short list) and lane 3 the
+// radial, out-of-plane and angle terms; the four partial sums meet in a shuffle tree.
+__device__ __forceinline__ void relEntry(bool full, const int *row, const int2 *rrow, int e, int &k, int &j) {
+  if (full) { k = row[e]; j = e; }
+  else { const int2 v = rrow[e]; k = v.x; j = v.y; }
+}
+
+__global__ void __launch_bounds__(128) k_force_carbon(BlockTab tab, const RepConst *__restrict__ rc,
+                                                      float4 *__restrict__ pos, float4 *__restrict__ acc,
+                                                      const int *__restrict__ nn, const int *__restrict__ nbl,
+                                                      const int *__restrict__ ns, const int *__restrict__ sl,
+                                                      const int *__restrict__ nrl, const int2 *__restrict__ rl,
+                                                      int rowStride) {
+  __shared__ float sD[128 / kCT][3][4];  // dx, dy, dz, |d| of close carbon q
+  __shared__ float sZ[128 / kCT][3];     // its z - z_0
+  __shared__ int sK[128 / kCT][3];       // its index
   const int rep = tab.rep[blockIdx.x];
   const RepConst &P = rc[rep];
-  const int i = tab.start[blockIdx.x] + threadIdx.x;
+  const int sub = threadIdx.x & (kCT - 1);
+  const int a = threadIdx.x / kCT;  // atom slot in the block
+  const int glane = threadIdx.x & 31 & ~(kCT - 1);
+  const unsigned gmask = ((1u << kCT) - 1) << glane;
+  const int i = tab.start[blockIdx.x] + a;
   const int metalEnd = P.atomOff + P.nMolMe;
-  if (i >= P.atomOff + P.nMol) return;
-  const float4 A = pos[i];
-  const int nNeigh = nn[i];
+  const bool valid = i < P.atomOff + P.nMol;
   float fx = 0.f, fy = 0.f, fz = 0.f, u = 0.f;
-  float rnx[3], rny[3], rnz[3], absR[3], dzs[3];
-  int counti = 0;
-  // own short-list pointer, to check that the list still holds every close neighbour
-  const int myNs = ns[i];
-  int sp = 0, stale = 0, checked = -1;
-  for (int j = 0; j < nNeigh; j++) {
-    const int k = nbl[(size_t)j * ntot + i];
-    const float4 B = pos[k];
-    const float dx = minImg(A.x - B.x, P.region[0]);
-    const float dy = minImg(A.y - B.y, P.region[1]);
-    const float dz = minImg(A.z - B.z, P.region[2]);
-    const float rr = dx * dx + dy * dy + dz * dz;
-    if (j > checked) {  // first visit of this entry (the walk may resume at entry 4)
-      checked = j;
-      if (rr < P.rrCutC && myNs >= 0) {
-        while (sp < myNs && sl[(size_t)sp * ntot + i] != k) sp++;
-        if (sp >= myNs) stale = 1;
-        else sp++;
-      }
-    }
-    if (k < metalEnd) {
-      if (rr >= P.rrCutLJ) continue;
-      float fc, ul;
-      ljTerms(P, rr, fc, ul);
-      u += ul;
-      fx = fx + fc * dx; fy = fy + fc * dy; fz = fz + fc * dz;
-      continue;
-    }
-    if ((rr < P.rrCutC) && (counti < 3)) {
-      absR[counti] = sqrtf(rr);
-      dzs[counti] = B.z - P.z_0;
-      rnx[counti] = dx; rny[counti] = dy; rnz[counti] = dz;
-      const int nk = ns[k];
-      const bool full = nk < 0;
-      const int lim = full ? nn[k] : nk;
-      int countk = 0;
-      for (int l = 0; l < lim; l++) {
-        const int m = full ? nbl[(size_t)l * ntot + k] : sl[(size_t)l * ntot + k];
-        const float4 rm = pos[m];
-        float ex = minImg(B.x - rm.x, P.region[0]);
-        float ey = minImg(B.y - rm.y, P.region[1]);
-        float ez = minImg(B.z - rm.z, P.region[2]);
-        const float rr2 = ex * ex + ey * ey + ez * ez;
-        if ((rr2 < P.rrCutC) && (m != i)) {
-          ex = ex * (-1.f); ey = ey * (-1.f); ez = ez * (-1.f);
-          const float cs = (rnx[counti] * ex + rny[counti] * ey + rnz[counti] * ez) / (absR[counti] * rr2);
-          const float th = acosf(cs);
-          const float dth = th - P.theta_0;
-          const float tmp = P.mu_theta * dth / sqrtf(1.f - cs * cs);
-          float fc = tmp / (absR[counti] * rr2);
-          fx = fx + fc * ex; fy = fy + fc * ey; fz = fz + fc * ez;
-          fc = -tmp * cs / (absR[counti] * absR[counti]);
-          fx = fx + fc * rnx[counti]; fy = fy + fc * rny[counti]; fz = fz + fc * rnz[counti];
-          fc = -P.mu_p * (rm.z - P.z_0) / 9.f;
-          fx = fx + 0.f; fy = fy + 0.f; fz = fz + fc;
-          ++countk;
+  int counti = 0, p2 = -1;
+  const float4 A = valid ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const int nr = valid ? nrl[i] : 0;
+  const bool full = nr < 0;
+  const int nEnt = full ? nn[i] : nr;
+  const int *row = nbl + (size_t)i * rowStride;
+  const int2 *rrow = rl + (size_t)i * kRelMax;
+  for (int base = 0; base < nEnt; base += kCT) {
+    const int e = base + sub;
+    bool closeC = false;
+    float lx = 0.f, ly = 0.f, lz = 0.f, lu = 0.f;
+    float dx = 0.f, dy = 0.f, dz = 0.f, rr = 0.f, bz = 0.f;
+    int k = -1, j = -1;
+    if (e < nEnt) {
+      relEntry(full, row, rrow, e, k, j);
+      const float4 B = pos[k];
+      bz = B.z;
+      dx = minImg(A.x - B.x, P.region[0]);
+      dy = minImg(A.y - B.y, P.region[1]);
+      dz = minImg(A.z - B.z, P.region[2]);
+      rr = dx * dx + dy * dy + dz * dz;
+      if (k < metalEnd) {
+        if (rr < P.rrCutLJ) {
+          float fc;
+          ljTerms(P, rr, fc, lu);
+          lx = fc * dx; ly = fc * dy; lz = fc * dz;
         }
-        if (countk == 2) break;
+      } else {
+        closeC = rr < P.rrCutC;
       }
-      ++counti;
     }
-    if (counti == 3) {
-#pragma unroll
-      for (int q = 0; q < 3; q++) {
-        const float fc = -P.mu_r * (absR[q] - 1.f) / absR[q];
-        fx = fx + fc * rnx[q]; fy = fy + fc * rny[q]; fz = fz + fc * rnz[q];
-        u += P.mu_r * (absR[q] - 1.f) * (absR[q] - 1.f);
+    const unsigned bal = (__ballot_sync(gmask, closeC) >> glane) & ((1u << kCT) - 1);
+    if (counti < 3) {
+      if (closeC) {
+        const int rank = counti + __popc(bal & ((1u << sub) - 1));
+        if (rank < 3) {
+          sD[a][rank][0] = dx; sD[a][rank][1] = dy; sD[a][rank][2] = dz; sD[a][rank][3] = sqrtf(rr);
+          sZ[a][rank] = bz - P.z_0;
+          sK[a][rank] = k;
+        }
       }
-      float dZ = 2.f * (A.z - P.z_0) - (dzs[0] + dzs[1] + dzs[2]);
-      const float fcz = -0.666666667f * P.mu_p * dZ;
-      fx = fx + 0.f; fy = fy + 0.f; fz = fz + fcz;
-      dZ = (A.z - P.z_0) - 0.33333333f * (dzs[0] + dzs[1] + dzs[2]);
-      u += P.mu_p * dZ * dZ;
-#pragma unroll
-      for (int q = 0; q < 3; q++) {
-        const int p0 = (q == 0) ? 0 : (q == 1) ? 1 : 2;
-        const int p1 = (q == 0) ? 1 : (q == 1) ? 2 : 0;
-        const float cs = (rnx[p0] * rnx[p1] + rny[p0] * rny[p1] + rnz[p0] * rnz[p1]) / (absR[p0] * absR[p1]);
+      const int c2 = counti + __popc(bal);
+      if (c2 >= 3) {  // the third close carbon is in this group of entries
+        unsigned b = bal;
+        for (int r = counti; r < 2; r++) b &= b - 1;  // drop the set bits of ranks counti..1
+        p2 = __shfl_sync(gmask, j, glane + __ffs(b) - 1);
+      }
+      counti = min(c2, 3);
+    }
+    if (!(j == 3 && p2 == 2)) {  // entry 3 is never visited when the third NN sits at 2
+      fx += lx; fy += ly; fz += lz; u += lu;
+    }
+  }
+  // entries 4..p2 of the full list are walked a second time: their LJ terms repeat
+  if (counti == 3 && p2 >= 4) {
+    for (int e = sub; e < nEnt; e += kCT) {
+      int k, j;
+      relEntry(full, row, rrow, e, k, j);
+      if (j > p2) break;
+      if (j < 4 || k >= metalEnd) continue;
+      const float4 B = pos[k];
+      const float dx = minImg(A.x - B.x, P.region[0]);
+      const float dy = minImg(A.y - B.y, P.region[1]);
+      const float dz = minImg(A.z - B.z, P.region[2]);
+      const float rr = dx * dx + dy * dy + dz * dz;
+      if (rr < P.rrCutLJ) {
+        float fc, ul;
+        ljTerms(P, rr, fc, ul);
+        fx += fc * dx; fy += fc * dy; fz += fc * dz; u += ul;
+      }
+    }
+  }
+  __syncwarp(gmask);
+  if (sub < 3 && sub < counti) {
+    // second-neighbour terms of close carbon q = sub (cu:929-981)
+    const int q = sub;
+    const int k = sK[a][q];
+    const float rnx = sD[a][q][0], rny = sD[a][q][1], rnz = sD[a][q][2], absR = sD[a][q][3];
+    const float4 B = pos[k];
+    const int nk = ns[k];
+    const bool fullk = nk < 0;
+    const int lim = fullk ? nn[k] : nk;
+    const int *src = fullk ? nbl + (size_t)k * rowStride : sl + (size_t)k * kShortMax;
+    int countk = 0;
+    for (int l = 0; l < lim; l++) {
+      const int m = src[l];
+      const float4 rm = pos[m];
+      float ex = minImg(B.x - rm.x, P.region[0]);
+      float ey = minImg(B.y - rm.y, P.region[1]);
+      float ez = minImg(B.z - rm.z, P.region[2]);
+      const float rr2 = ex * ex + ey * ey + ez * ez;
+      if ((rr2 < P.rrCutC) && (m != i)) {
+        ex = ex * (-1.f); ey = ey * (-1.f); ez = ez * (-1.f);
+        const float cs = (rnx * ex + rny * ey + rnz * ez) / (absR * rr2);
         const float th = acosf(cs);
         const float dth = th - P.theta_0;
         const float tmp = P.mu_theta * dth / sqrtf(1.f - cs * cs);
-        float fc = tmp * (1.f - absR[p0] * cs / absR[p1]) / (absR[p0] * absR[p1]);
-        fx = fx + fc * rnx[p1]; fy = fy + fc * rny[p1]; fz = fz + fc * rnz[p1];
-        fc = tmp * (1.f - absR[p1] * cs / absR[p0]) / (absR[p0] * absR[p1]);
-        fx = fx + fc * rnx[p0]; fy = fy + fc * rny[p0]; fz = fz + fc * rnz[p0];
-        u += P.mu_theta * dth * dth;
+        float f = tmp / (absR * rr2);
+        fx = fx + f * ex; fy = fy + f * ey; fz = fz + f * ez;
+        f = -tmp * cs / (absR * absR);
+        fx = fx + f * rnx; fy = fy + f * rny; fz = fz + f * rnz;
+        f = -P.mu_p * (rm.z - P.z_0) / 9.f;
+        fz = fz + f;
+        ++countk;
       }
-      // The reference's radial loop reuses the neighbour-loop counter (cu:989): the walk
-      // resumes at list entry 4.
-      j = 3;
-      counti = 4;
+      if (countk == 2) break;
+    }
+  } else if (sub == 3 && counti == 3) {
+    // radial, out-of-plane and own-angle terms (cu:985-1061)
+    float rnx[3], rny[3], rnz[3], absR[3], dzs[3];
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      rnx[q] = sD[a][q][0]; rny[q] = sD[a][q][1]; rnz[q] = sD[a][q][2]; absR[q] = sD[a][q][3];
+      dzs[q] = sZ[a][q];
+    }
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      const float f = -P.mu_r * (absR[q] - 1.f) / absR[q];
+      fx = fx + f * rnx[q]; fy = fy + f * rny[q]; fz = fz + f * rnz[q];
+      u += P.mu_r * (absR[q] - 1.f) * (absR[q] - 1.f);
+    }
+    float dZ = 2.f * (A.z - P.z_0) - (dzs[0] + dzs[1] + dzs[2]);
+    fz = fz + -0.666666667f * P.mu_p * dZ;
+    dZ = (A.z - P.z_0) - 0.33333333f * (dzs[0] + dzs[1] + dzs[2]);
+    u += P.mu_p * dZ * dZ;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      const int p0 = q, p1 = (q == 2) ? 0 : q + 1;
+      const float cs = (rnx[p0] * rnx[p1] + rny[p0] * rny[p1] + rnz[p0] * rnz[p1]) / (absR[p0] * absR[p1]);
+      const float th = acosf(cs);
+      const float dth = th - P.theta_0;
+      const float tmp = P.mu_theta * dth / sqrtf(1.f - cs * cs);
+      float f = tmp * (1.f - absR[p0] * cs / absR[p1]) / (absR[p0] * absR[p1]);
+      fx = fx + f * rnx[p1]; fy = fy + f * rny[p1]; fz = fz + f * rnz[p1];
+      f = tmp * (1.f - absR[p1] * cs / absR[p0]) / (absR[p0] * absR[p1]);
+      fx = fx + f * rnx[p0]; fy = fy + f * rny[p0]; fz = fz + f * rnz[p0];
+      u += P.mu_theta * dth * dth;
     }
   }
-  acc[i] = make_float4(fx, fy, fz, 0.f);
-  pos[i].w = 0.5f * u;
-  if (stale) atomicAdd(&st[rep].shortStale, 1);
+#pragma unroll
+  for (int o = kCT / 2; o > 0; o >>= 1) {
+    fx += __shfl_xor_sync(gmask, fx, o);
+    fy += __shfl_xor_sync(gmask, fy, o);
+    fz += __shfl_xor_sync(gmask, fz, o);
+    u += __shfl_xor_sync(gmask, u, o);
+  }
+  if (valid && sub == 0) {
+    acc[i] = make_float4(fx, fy, fz, 0.f);
+    pos[i].w = 0.5f * u;
+  }
 }
 
 // ============================================================================================
@@ -630,33 +845,42 @@ __device__ __forceinline__ float combine(int op, float a, float b) {
   return (a > b) ? b : a;
 }
 
-// Tree over 512 per-thread values (after the first level, done in registers), for NV values
-// per element; strides 256..32 through shared memory, 16..1 with shuffles in warp 0 (the same
-// pairing as the reference's shared-memory tree).  Result valid in thread 0.
+// Tree over 512 per-thread values (after the first level, done in registers), for NV <= 16
+// values per element, in the reference's pairing (x[t] += x[t + s] for s = 256 ... 1).  The
+// values go through shared memory once; warp v then owns value v, its lane l holding the
+// entries t = l + 32 k, k = 0..15, so the strides s >= 32 pair registers of the same lane and
+// the strides 16..1 are shuffles.  Result valid in lane 0 of warp v (returned to thread 0 via
+// shared memory in x[] of thread 0).
 template <int NV>
 __device__ __forceinline__ void blockTree512(float (&x)[NV], const int *ops, float (*sh)[kRedThreads]) {
   const int t = threadIdx.x;
+  const int w = t >> 5, l = t & 31;
 #pragma unroll
   for (int v = 0; v < NV; v++) sh[v][t] = x[v];
   __syncthreads();
-  for (int s = 256; s >= 32; s >>= 1) {
-    if (t < s) {
+  __shared__ float res[16];
+  if (w < NV) {
+    const int op = ops[w];
+    float e[16];
 #pragma unroll
-      for (int v = 0; v < NV; v++) sh[v][t] = combine(ops[v], sh[v][t], sh[v][t + s]);
-    }
-    __syncthreads();
-  }
-  if (t < 32) {
+    for (int k = 0; k < 16; k++) e[k] = sh[w][l + 32 * k];
 #pragma unroll
-    for (int v = 0; v < NV; v++) {
-      float y = sh[v][t];
-      for (int s = 16; s >= 1; s >>= 1) {
-        const float o = __shfl_down_sync(0xffffffffu, y, s);
-        y = combine(ops[v], y, o);
-      }
-      x[v] = y;
-    }
+    for (int k = 0; k < 8; k++) e[k] = combine(op, e[k], e[k + 8]);  // s = 256
+#pragma unroll
+    for (int k = 0; k < 4; k++) e[k] = combine(op, e[k], e[k + 4]);  // s = 128
+#pragma unroll
+    for (int k = 0; k < 2; k++) e[k] = combine(op, e[k], e[k + 2]);  // s = 64
+    float y = combine(op, e[0], e[1]);                              // s = 32
+#pragma unroll
+    for (int s = 16; s >= 1; s >>= 1) y = combine(op, y, __shfl_down_sync(0xffffffffu, y, s));
+    if (l == 0) res[w] = y;
   }
+  __syncthreads();
+  if (t == 0) {
+#pragma unroll
+    for (int v = 0; v < NV; v++) x[v] = res[v];
+  }
+  __syncthreads();
 }
 
 // Centre-of-mass velocity of the metal (ComputeCmVelK, cu:1560-1638) on the velocities after

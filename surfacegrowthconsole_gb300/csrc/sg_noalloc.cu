@@ -29,6 +29,8 @@ namespace {
 constexpr size_t kScratchBytes = SG_NOALLOC_SCRATCH_BYTES;
 constexpr int kBs = 128;
 constexpr int kMaxBlocks = (SG_NOALLOC_MAX_ATOMS + kBs - 1) / kBs;
+// table capacity: the metal pass has the smallest blocks (kMetalPerBlock atoms)
+constexpr int kMaxTabBlocks = (SG_NOALLOC_MAX_ATOMS + kMetalPerBlock - 1) / kMetalPerBlock;
 constexpr int kMaxTiles = SG_NOALLOC_MAX_CELLS / kCellTile;
 
 // The scratch of every call on this device.  Host code must not take its address directly:
@@ -38,7 +40,7 @@ static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 // Carving of the scratch array (offsets in bytes, each 256-byte aligned).
 struct Carve {
   size_t rc, st, tabRep, tabStart, tileRep, tileStart, tileFirst, tileSum, cellCount, cellStart;
-  size_t cellOf, slot, tmpIdx, sortIdx, nn, ns, sortPos, rho, dF, Fv, fric, nbl, sl, total;
+  size_t cellOf, slot, tmpIdx, sortIdx, nn, ns, sortPos, rho, dF, Fv, fric, nbl, sl, nrl, rl, active, work, total;
 };
 constexpr size_t up(size_t x) { return (x + 255) & ~size_t(255); }
 constexpr Carve carve() {
@@ -47,8 +49,8 @@ constexpr Carve carve() {
   const size_t N = SG_NOALLOC_MAX_ATOMS;
   c.rc = o; o += up(sizeof(RepConst));
   c.st = o; o += up(sizeof(RepState));
-  c.tabRep = o; o += up(3 * kMaxBlocks * sizeof(int));    // atom, metal, carbon tables
-  c.tabStart = o; o += up(3 * kMaxBlocks * sizeof(int));
+  c.tabRep = o; o += up(3 * kMaxTabBlocks * sizeof(int));    // atom, metal, carbon tables
+  c.tabStart = o; o += up(3 * kMaxTabBlocks * sizeof(int));
   c.tileRep = o; o += up(kMaxTiles * sizeof(int));
   c.tileStart = o; o += up(kMaxTiles * sizeof(int));
   c.tileFirst = o; o += up(sizeof(int));
@@ -68,6 +70,10 @@ constexpr Carve carve() {
   c.fric = o; o += up(N * sizeof(float));
   c.nbl = o; o += up(N * SG_NOALLOC_MAX_NEBR * sizeof(int));
   c.sl = o; o += up(N * kShortMax * sizeof(int));
+  c.nrl = o; o += up(N * sizeof(int));
+  c.rl = o; o += up(N * kRelMax * sizeof(int2));
+  c.active = o; o += up(SG_NOALLOC_MAX_CELLS * sizeof(int));
+  c.work = o; o += up(2 * sizeof(int));
   c.total = o;
   return c;
 }
@@ -82,7 +88,7 @@ std::mutex g_mu;
 // Writes the parameter block, clears the state block and the cell counts, and fills the
 // block tables of a single system: everything that must start fresh on every call.
 __global__ void k_noalloc_setup(RepConst P, RepState *st, RepConst *rc, int *tabRep, int *tabStart,
-                                int *tileRep, int *tileStart, int *tileFirst, int *cellCount) {
+                                int *tileRep, int *tileStart, int *tileFirst, int *cellCount, int *work) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int stride = gridDim.x * blockDim.x;
   if (t == 0) {
@@ -91,16 +97,17 @@ __global__ void k_noalloc_setup(RepConst P, RepState *st, RepConst *rc, int *tab
     st->nebrNow = 1;
     *tileFirst = 0;
   }
-  for (int b = t; b < kMaxBlocks; b += stride) {
-    tabRep[b] = 0; tabStart[b] = b * kBs;
-    tabRep[kMaxBlocks + b] = 0; tabStart[kMaxBlocks + b] = b * kBs;
-    tabRep[2 * kMaxBlocks + b] = 0; tabStart[2 * kMaxBlocks + b] = P.nMolMe + b * kBs;
+  for (int b = t; b < kMaxTabBlocks; b += stride) {
+    tabRep[b] = 0; tabStart[b] = b * kBs;                                   // atoms, 128 per block
+    tabRep[kMaxTabBlocks + b] = 0; tabStart[kMaxTabBlocks + b] = b * kMetalPerBlock;
+    tabRep[2 * kMaxTabBlocks + b] = 0; tabStart[2 * kMaxTabBlocks + b] = P.nMolMe + b * kCarbonPerBlock;
   }
   for (int k = t; k < P.ncellsPad / kCellTile; k += stride) {
     tileRep[k] = 0;
     tileStart[k] = k * kCellTile;
   }
   for (int c = t; c < P.ncellsPad; c += stride) cellCount[c] = 0;
+  if (t < 2) work[t] = 0;
 }
 
 RepConst constFor(const sg_simparams &p) {
@@ -170,34 +177,39 @@ extern "C" int sg_compute_forces_noalloc(const sg_simparams *p, sg_float4 *d_pos
   float4 *sortPos = (float4 *)(base + K.sortPos);
   float *rho = (float *)(base + K.rho), *dF = (float *)(base + K.dF), *Fv = (float *)(base + K.Fv);
   float *fric = (float *)(base + K.fric);
-  int *nbl = (int *)(base + K.nbl), *sl = (int *)(base + K.sl);
+  int *nbl = (int *)(base + K.nbl), *sl = (int *)(base + K.sl), *nrl = (int *)(base + K.nrl);
+  int2 *rl = (int2 *)(base + K.rl);
+  int *active = (int *)(base + K.active), *work = (int *)(base + K.work);
   float4 *pos = (float4 *)d_pos, *acc = (float4 *)d_acc;
 
   const RepConst P = constFor(*p);
   const int N = p->nMol;
   const int nAtomBlk = (N + kBs - 1) / kBs;
-  const int nMetalBlk = (p->nMolMe + kBs - 1) / kBs;
-  const int nCarbBlk = (N - p->nMolMe + kBs - 1) / kBs;
+  const int nMetalBlk = (p->nMolMe + kMetalPerBlock - 1) / kMetalPerBlock;
+  const int nCarbBlk = (N - p->nMolMe + kCarbonPerBlock - 1) / kCarbonPerBlock;
   const int nTiles = ncellsPad / kCellTile;
   BlockTab atomTab{tabRep, tabStart, nAtomBlk};
-  BlockTab metalTab{tabRep + kMaxBlocks, tabStart + kMaxBlocks, nMetalBlk};
-  BlockTab carbTab{tabRep + 2 * kMaxBlocks, tabStart + 2 * kMaxBlocks, nCarbBlk};
+  BlockTab metalTab{tabRep + kMaxTabBlocks, tabStart + kMaxTabBlocks, nMetalBlk};
+  BlockTab carbTab{tabRep + 2 * kMaxTabBlocks, tabStart + 2 * kMaxTabBlocks, nCarbBlk};
   BlockTab tileTab{tileRep, tileStart, nTiles};
 
-  k_noalloc_setup<<<64, 256, 0, s>>>(P, st, rc, tabRep, tabStart, tileRep, tileStart, tileFirst, cellCount);
+
+  k_noalloc_setup<<<64, 256, 0, s>>>(P, st, rc, tabRep, tabStart, tileRep, tileStart, tileFirst, cellCount, work);
   k_cell_count<<<nAtomBlk, kBs, 0, s>>>(atomTab, rc, pos, cellOf, slot, cellCount);
   k_scan_tiles<<<nTiles, 256, 0, s>>>(tileTab, rc, st, cellCount, tileSum, 1);
   k_scan_tile_prefix<<<1, 1024, 0, s>>>(rc, st, tileFirst, tileSum, 1);
-  k_scan_final<<<nTiles, 256, 0, s>>>(tileTab, rc, st, cellCount, tileSum, cellStart, (int)p->blockSize, 1);
+  k_scan_final<<<nTiles, 256, 0, s>>>(tileTab, rc, st, cellCount, tileSum, cellStart, (int)p->blockSize, 1, active,
+                                      work);
   k_scatter<<<nAtomBlk, kBs, 0, s>>>(atomTab, rc, st, cellOf, slot, cellStart, tmpIdx, nn, ns, 1);
   k_rank<<<nAtomBlk, kBs, 0, s>>>(atomTab, rc, st, cellOf, cellStart, tmpIdx, pos, sortIdx, sortPos, 1);
-  k_build_nebr<<<nAtomBlk, kBs, 0, s>>>(atomTab, rc, st, cellOf, cellStart, sortPos, nn, nbl, ns, sl, N,
-                                        p->iNebrMax, 1);
+  const int rowStride = (p->iNebrMax + 3) & ~3;
+  k_build_nebr<<<256, kNebrWarps * 32, 0, s>>>(tileRep, active, work, rc, st, cellStart, sortPos, nn, nbl, ns, sl,
+                                               nrl, rl, rowStride, p->iNebrMax);
   if (nMetalBlk) {
-    k_rho<<<nMetalBlk, kBs, 0, s>>>(metalTab, rc, pos, nn, nbl, rho, dF, Fv, N);
-    k_force_metal<<<nMetalBlk, kBs, 0, s>>>(metalTab, rc, pos, acc, nn, nbl, dF, Fv, fric, N);
+    k_rho<<<nMetalBlk, kBs, 0, s>>>(metalTab, rc, pos, nn, nbl, rho, dF, Fv, rowStride);
+    k_force_metal<<<nMetalBlk, kBs, 0, s>>>(metalTab, rc, pos, acc, nn, nbl, dF, Fv, fric, rowStride);
   }
-  if (nCarbBlk) k_force_carbon<<<nCarbBlk, kBs, 0, s>>>(carbTab, rc, pos, acc, nn, nbl, ns, sl, st, N);
+  if (nCarbBlk) k_force_carbon<<<nCarbBlk, kBs, 0, s>>>(carbTab, rc, pos, acc, nn, nbl, ns, sl, nrl, rl, rowStride);
   e = cudaGetLastError();
   if (e != cudaSuccess) return sg_fail(SG_ERR_CUDA, "sg_compute_forces_noalloc launch: %s", cudaGetErrorString(e));
   int flags = 0;
