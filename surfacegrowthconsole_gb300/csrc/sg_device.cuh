@@ -13,10 +13,9 @@
 //   nn int[Ntot], nbl int[Ntot * rowStride] neighbour list, entry j of atom g at
 //                                           nbl[g * rowStride + j] (rowStride = nebrMax rounded
 //                                           up to a multiple of 4: 16-byte aligned rows)
-//   ns int[Ntot], sl int[Ntot * kShortMax]  short list: neighbours within (rCutC+skin) at build
 //   nrl int[Ntot], rl int2[Ntot * kRelMax]  relevant list of a carbon atom: its metal entries
 //                                           and entries within (rCutC+skin), {index, position
-//                                           in the full list}
+//                                           in the full list | kRelClose if within rCutC+skin}
 //   rho/dF/Fv float[Ntot]   EAM density, F'(rho), F(rho) (metal atoms)
 //   fric float[Ntot]       x force of carbon on each metal atom
 // Per-replica constants live in RepConst, mutable per-replica scalars in RepState.
@@ -26,7 +25,6 @@
 
 namespace sg {
 
-constexpr int kShortMax = 8;      // short-list capacity per atom
 constexpr int kRedThreads = 512;  // reduction block: 512 threads x 2 elements (reference shape)
 constexpr int kRedElems = 1024;
 constexpr int kCellTile = 2048;   // cells per scan tile (cell ranges are padded to this)
@@ -35,8 +33,10 @@ constexpr int kMT = 16;           // lanes per metal atom in the density and met
 constexpr int kCT = 4;            // lanes per carbon atom in the carbon-force pass
 constexpr int kNebrWarps = 4;     // warps per block in the neighbour-list build (one home cell each)
 constexpr int kWin = 512;         // candidates per shared-memory window of the list build
-constexpr int kHomeMax = 64;      // home atoms handled per window pass
 constexpr int kRelMax = 48;       // relevant-list capacity per carbon atom
+constexpr int kRelClose = 1 << 30;  // flag on a relevant-list position: entry within rCutC + skin
+constexpr int kHeavyCell = 16;    // list build: cells above this many atoms are split into items
+constexpr int kHeavyChunk = 8;    // of this many home atoms
 constexpr int kMetalPerBlock = 128 / kMT;   // atoms per 128-thread block
 constexpr int kCarbonPerBlock = 128 / kCT;
 

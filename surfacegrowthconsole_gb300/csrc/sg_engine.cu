@@ -244,13 +244,14 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
   if (c->opt.mode == SG_MODE_MIXED) AL(c->posLo, N);
   AL(c->cellOf, N); AL(c->slot, N); AL(c->tmpIdx, N); AL(c->sortIdx, N);
   AL(c->cellCount, (size_t)c->ctot); AL(c->cellStart, (size_t)c->ctot);
-  AL(c->nn, N); AL(c->ns, N);
+  AL(c->nn, N);
   AL(c->nbl, N * c->rowStride);
-  AL(c->sl, N * kShortMax);
   AL(c->nrl, N);
   AL(c->rl, N * kRelMax);
   AL(c->activeCells, (size_t)c->ctot);
-  AL(c->nebrWork, 2);
+  // every crowded cell (> kHeavyCell atoms) adds at most one partial chunk
+  AL(c->heavyItems, (size_t)N / kHeavyChunk + (size_t)N / (kHeavyCell + 1) + 16);
+  AL(c->nebrWork, 3);
   AL(c->rho, N); AL(c->dF, N); AL(c->Fv, N); AL(c->fric, N);
   AL(c->partial, (size_t)std::max(redOff, 1) * kNumRed);
   AL(c->partialCmv, (size_t)std::max(cmvOff, 1) * 3);
@@ -451,23 +452,23 @@ enum { V_SHEAR = 1, V_RDF = 2, V_RDF_ZERO = 4 };
 
 static int enqueueRebuild(sg_ctx *c, int force) {
   const int fr = force;
-  CK(cudaMemsetAsync(c->nebrWork, 0, 2 * sizeof(int), c->stream));
+  CK(cudaMemsetAsync(c->nebrWork, 0, 3 * sizeof(int), c->stream));
   if (c->ntiles) {
     k_scan_tiles<<<c->tileTab.n, 256, 0, c->stream>>>(c->tileTab.view(), c->rc, c->st, c->cellCount, c->tileSum, fr);
     k_scan_tile_prefix<<<c->nrep, 1024, 0, c->stream>>>(c->rc, c->st, c->dTileFirst, c->tileSum, fr);
     k_scan_final<<<c->tileTab.n, 256, 0, c->stream>>>(c->tileTab.view(), c->rc, c->st, c->cellCount, c->tileSum,
                                                        c->cellStart, (int)c->hp[0].blockSize, fr, c->activeCells,
-                                                       c->nebrWork);
+                                                       c->heavyItems, c->nebrWork);
     LAUNCH_OK();
   }
   k_scatter<<<c->atomTab.n, 128, 0, c->stream>>>(c->atomTab.view(), c->rc, c->st, c->cellOf, c->slot, c->cellStart,
-                                                 c->tmpIdx, c->nn, c->ns, fr);
+                                                 c->tmpIdx, c->nn, c->nrl, fr);
   k_rank<<<c->atomTab.n, 128, 0, c->stream>>>(c->atomTab.view(), c->rc, c->st, c->cellOf, c->cellStart, c->tmpIdx,
                                               c->pos, c->sortIdx, c->sortPos, fr);
-  k_build_nebr<<<c->nebrGrid, kNebrWarps * 32, 0, c->stream>>>(c->tileTab.rep, c->activeCells, c->nebrWork, c->rc,
-                                                                 c->st, c->cellStart, c->sortPos, c->nn, c->nbl,
-                                                                 c->ns, c->sl, c->nrl, c->rl, c->rowStride,
-                                                                 c->nebrMax);
+  k_build_nebr<<<c->nebrGrid, kNebrWarps * 32, 0, c->stream>>>(c->tileTab.rep, c->activeCells, c->heavyItems,
+                                                                c->nebrWork, c->rc, c->st, c->cellStart, c->sortPos,
+                                                                c->nn, c->nbl, c->nrl, c->rl, c->rowStride,
+                                                                c->nebrMax);
   LAUNCH_OK();
   return SG_OK;
 }
@@ -493,7 +494,7 @@ static int enqueueForces(sg_ctx *c, bool withCmVel) {
   }
   if (c->carbonTabT.n)
     k_force_carbon<<<c->carbonTabT.n, 128, 0, c->stream>>>(c->carbonTabT.view(), c->rc, c->pos, c->acc, c->nn,
-                                                           c->nbl, c->ns, c->sl, c->nrl, c->rl, c->rowStride);
+                                                           c->nbl, c->nrl, c->rl, c->rowStride);
   if (c->opt.phase_timing) cudaEventRecordWithFlags(c->phaseEv[3], c->stream, cudaEventRecordExternal);
   LAUNCH_OK();
   if (fork) {

@@ -36,11 +36,12 @@ struct sg_ctx {
   RepState *st = nullptr;
   float4 *pos = nullptr, *vel = nullptr, *acc = nullptr, *posLo = nullptr, *sortPos = nullptr;
   int *cellOf = nullptr, *slot = nullptr, *cellCount = nullptr, *cellStart = nullptr;
-  int *tmpIdx = nullptr, *sortIdx = nullptr, *nn = nullptr, *nbl = nullptr, *ns = nullptr, *sl = nullptr;
+  int *tmpIdx = nullptr, *sortIdx = nullptr, *nn = nullptr, *nbl = nullptr;
   int *nrl = nullptr;
   int2 *rl = nullptr;
   int nebrGrid = 0;
   int *activeCells = nullptr, *nebrWork = nullptr;
+  int2 *heavyItems = nullptr;
   float *rho = nullptr, *dF = nullptr, *Fv = nullptr, *fric = nullptr;
   float *partial = nullptr, *partialCmv = nullptr;
   int *dRedFirst = nullptr, *dCmvFirst = nullptr, *tileSum = nullptr, *dTileFirst = nullptr;

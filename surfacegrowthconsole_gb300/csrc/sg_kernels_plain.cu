@@ -196,7 +196,7 @@ __global__ void k_scan_tile_prefix(const RepConst *__restrict__ rc, const RepSta
 __global__ void k_scan_final(BlockTab tab, const RepConst *__restrict__ rc, RepState *st,
                              int *__restrict__ cellCount, const int *__restrict__ tileSum,
                              int *__restrict__ cellStart, int blockSizeCap, int forceRebuild,
-                             int *__restrict__ active, int *__restrict__ work) {
+                             int *__restrict__ active, int2 *__restrict__ heavy, int *__restrict__ work) {
   const int rep = tab.rep[blockIdx.x];
   RepState *S = st + rep;
   if (!rebuilding(S, forceRebuild)) return;
@@ -237,23 +237,41 @@ __global__ void k_scan_final(BlockTab tab, const RepConst *__restrict__ rc, RepS
     run += v[i];
     cellCount[cb + i] = 0;
   }
-  // compact the non-empty cells (any order) for the list build
-  int nonEmpty = 0;
+  // work items of the list build (any order): a cell of up to kHeavyCell atoms is one item;
+  // a larger one is split into items of kHeavyChunk home atoms, queued apart so that the list
+  // build takes them first
+  int nLight = 0, nHeavy = 0;
 #pragma unroll
-  for (int i = 0; i < kPer; i++) nonEmpty += (v[i] > 0 && c0 + threadIdx.x * kPer + i < P.ncells) ? 1 : 0;
-  int pre = nonEmpty;
-  for (int o = 1; o < 32; o <<= 1) {
-    const int y = __shfl_up_sync(0xffffffffu, pre, o);
-    if ((threadIdx.x & 31) >= o) pre += y;
+  for (int i = 0; i < kPer; i++) {
+    if (v[i] > 0 && c0 + threadIdx.x * kPer + i < P.ncells) {
+      if (v[i] > kHeavyCell) nHeavy += (v[i] + kHeavyChunk - 1) / kHeavyChunk;
+      else nLight++;
+    }
   }
-  const int wsum = __shfl_sync(0xffffffffu, pre, 31);
-  int wbase = 0;
-  if ((threadIdx.x & 31) == 31 && wsum > 0) wbase = atomicAdd(&work[1], wsum);
-  wbase = __shfl_sync(0xffffffffu, wbase, 31);
-  int slotOut = wbase + pre - nonEmpty;
+  int preL = nLight, preH = nHeavy;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int yl = __shfl_up_sync(0xffffffffu, preL, o);
+    const int yh = __shfl_up_sync(0xffffffffu, preH, o);
+    if ((threadIdx.x & 31) >= o) { preL += yl; preH += yh; }
+  }
+  const int sumL = __shfl_sync(0xffffffffu, preL, 31), sumH = __shfl_sync(0xffffffffu, preH, 31);
+  int baseL = 0, baseH = 0;
+  if ((threadIdx.x & 31) == 31) {
+    if (sumL > 0) baseL = atomicAdd(&work[1], sumL);
+    if (sumH > 0) baseH = atomicAdd(&work[2], sumH);
+  }
+  int outL = __shfl_sync(0xffffffffu, baseL, 31) + preL - nLight;
+  int outH = __shfl_sync(0xffffffffu, baseH, 31) + preH - nHeavy;
 #pragma unroll
-  for (int i = 0; i < kPer; i++)
-    if (v[i] > 0 && c0 + threadIdx.x * kPer + i < P.ncells) active[slotOut++] = cb + i;
+  for (int i = 0; i < kPer; i++) {
+    if (v[i] > 0 && c0 + threadIdx.x * kPer + i < P.ncells) {
+      if (v[i] > kHeavyCell) {
+        for (int h = 0; h < v[i]; h += kHeavyChunk) heavy[outH++] = make_int2(cb + i, h);
+      } else {
+        active[outL++] = cb + i;
+      }
+    }
+  }
   for (int o = 16; o > 0; o >>= 1) {
     occ = max(occ, __shfl_xor_sync(0xffffffffu, occ, o));
     over += __shfl_xor_sync(0xffffffffu, over, o);
@@ -271,7 +289,7 @@ __global__ void k_scan_final(BlockTab tab, const RepConst *__restrict__ rc, RepS
 __global__ void k_scatter(BlockTab tab, const RepConst *__restrict__ rc, RepState *st,
                           const int *__restrict__ cellOf, const int *__restrict__ slot,
                           const int *__restrict__ cellStart, int *__restrict__ tmpIdx,
-                          int *__restrict__ nn, int *__restrict__ ns, int forceRebuild) {
+                          int *__restrict__ nn, int *__restrict__ nrl, int forceRebuild) {
   const int rep = tab.rep[blockIdx.x];
   RepState *S = st + rep;
   if (!rebuilding(S, forceRebuild)) return;
@@ -283,7 +301,7 @@ __global__ void k_scatter(BlockTab tab, const RepConst *__restrict__ rc, RepStat
     tmpIdx[cellStart[P.cellOff + c] + slot[g]] = g;
   } else {
     nn[g] = 0;  // an atom outside the grid has no neighbours (the reference clears NN)
-    ns[g] = 0;
+    nrl[g] = 0;
     atomicAdd(&S->cellRange, 1);
   }
 }
@@ -312,153 +330,202 @@ __global__ void k_rank(BlockTab tab, const RepConst *__restrict__ rc, const RepS
 }
 
 // ============================================================================================
-// Neighbour list (BuildNebrListK, SurfaceGrowth.cu:612-711), cell-centric.  Warps take non-empty
-// home cells from the list k_scan_final compacted, through an atomic work counter.  Lanes
-// 0..26 look up the 27 stencil cells (reference visiting order); their segments form a
-// shared-memory window of candidates in stencil order.  Per chunk of 32 candidates (held in
-// registers, one per lane), the warp streams the home atoms (up to 32 at a time, lane a holding
-// home atom a and its counters): every lane tests its candidate against the broadcast home
-// atom, and a ballot ranks the matches, so entries land in the atom's row nbl[g*rowStride + j]
-// in stencil order and ascending atom index inside a cell: the order of the reference's
-// one-thread walk.  The same pass emits
-//  - the short list: entries within rCutC + skin (graphene second-neighbour walk), and
-//  - for carbon atoms the relevant list: every metal entry and every entry within
-//    rCutC + skin, each with its position in the full list, which is all the carbon-force
-//    pass needs.
-// Both rest on the skin, as the neighbour list itself does: no pair closes in by more than
-// rNebrShell between rebuilds.
+// Neighbour list (BuildNebrListK, SurfaceGrowth.cu:612-711), cell-centric.  Warps take work
+// items from the lists k_scan_final wrote, through an atomic work counter: first the chunks of
+// kHeavyChunk home atoms of the crowded cells, then the other non-empty cells whole.  Lanes
+// 0..26 look up the 27 stencil cells (reference visiting order); their segments, in that order
+// and ascending atom index inside each, form the cell's window of candidates: exactly the
+// order in which the reference's one-thread walk meets them.  A lane finds the segment of its
+// window position by binary search over the segment offsets.
+//  Test pass: per 32-candidate word of the window (one candidate per lane, in registers) the
+//    warp runs through the home atoms (positions broadcast from shared memory); two ballots
+//    give the word's "within the list radius" and "within rCutC + skin" masks of each home
+//    atom, kept in shared memory with the word's "metal candidate" mask.  Words without a
+//    periodic shift that cannot hold a home atom take a loop without the shift and the
+//    self-pair test (subtracting a zero shift changes no bit).
+//  Emit pass: per home atom and word with hits, lane l places candidate l at its rank among
+//    the word's set bits, so consecutive entries of the atom's row nbl[g*rowStride + j] come
+//    from one coalesced store; for a carbon atom the same ranks place its relevant list (every
+//    metal entry and every entry within rCutC + skin, with its position in the full list:
+//    all the carbon-force pass needs; kRelClose marks the entries within rCutC + skin).  The
+//    running lengths are uniform across the warp; stores are predicated, not branched.
+// A window pass holds kWin candidates; larger stencils take several passes, the lengths
+// carrying over in the lane of each home atom.  The relevant list rests on the skin, as the
+// neighbour list itself does: no pair closes in by more than rNebrShell between rebuilds.
 // ============================================================================================
-__global__ void __launch_bounds__(128) k_build_nebr(const int *__restrict__ tileRep, const int *__restrict__ active,
-                                                    int *work, const RepConst *__restrict__ rc, RepState *st,
-                                                    const int *__restrict__ cellStart,
-                                                    const float4 *__restrict__ sortPos, int *__restrict__ nn,
-                                                    int *__restrict__ nbl, int *__restrict__ ns,
-                                                    int *__restrict__ sl, int *__restrict__ nrl,
-                                                    int2 *__restrict__ rl, int rowStride, int nebrMax) {
-  __shared__ int sBuf[kNebrWarps][kWin];
-  __shared__ float sSh[kNebrWarps][27][3];
-  __shared__ int sQb[kNebrWarps][27], sQe[kNebrWarps][27];
+__device__ __forceinline__ void stIf(bool p, int *a, int v) {
+  asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %0, 0;\n\t@q st.global.u32 [%1], %2;\n\t}" ::"r"((unsigned)p), "l"(a),
+               "r"(v)
+               : "memory");
+}
+__device__ __forceinline__ void stIf2(bool p, int2 *a, int x, int y) {
+  asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %0, 0;\n\t@q st.global.v2.u32 [%1], {%2, %3};\n\t}" ::"r"((unsigned)p),
+               "l"(a), "r"(x), "r"(y)
+               : "memory");
+}
+
+__global__ void __launch_bounds__(kNebrWarps * 32) k_build_nebr(const int *__restrict__ tileRep,
+                                                                const int *__restrict__ active,
+                                                                const int2 *__restrict__ heavy, int *work,
+                                                                const RepConst *__restrict__ rc, RepState *st,
+                                                                const int *__restrict__ cellStart,
+                                                                const float4 *__restrict__ sortPos,
+                                                                int *__restrict__ nn, int *__restrict__ nbl,
+                                                                int *__restrict__ nrl, int2 *__restrict__ rl,
+                                                                int rowStride, int nebrMax) {
+  __shared__ int sK[kNebrWarps][kWin];                 // atom index of each window position
+  __shared__ uint2 sMask[kNebrWarps][kWin / 32][32];   // [word][home atom]: {hit, close}
+  __shared__ unsigned sMetal[kNebrWarps][kWin / 32];   // [word]: candidate is a metal atom
+  __shared__ float4 sHome[kNebrWarps][32];
+  __shared__ float4 sSh[kNebrWarps][27];               // periodic shift, w = 1 when non-zero
+  __shared__ int sQb[kNebrWarps][27], sOff[kNebrWarps][27];
+  const unsigned full = 0xffffffffu;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const unsigned lower = (1u << lane) - 1;
-  const int nActive = work[1];
+  const unsigned lower = (1u << lane) - 1u, laneBit = 1u << lane;
+  const int nLight = work[1], nHeavy = work[2];
   while (true) {
     int idx = 0;
     if (lane == 0) idx = atomicAdd(&work[0], 1);
-    idx = __shfl_sync(0xffffffffu, idx, 0);
-    if (idx >= nActive) break;
-    const int gc = active[idx];
+    idx = __shfl_sync(full, idx, 0);
+    if (idx >= nHeavy + nLight) break;
+    int gc, hOff = 0, hCnt = 1 << 30;
+    if (idx < nHeavy) {
+      const int2 it = heavy[idx];
+      gc = it.x;
+      hOff = it.y;
+      hCnt = kHeavyChunk;
+    } else {
+      gc = active[idx - nHeavy];
+    }
     const int rep = tileRep[gc / kCellTile];
     RepState *S = st + rep;
     const RepConst &P = rc[rep];
     const int c = gc - P.cellOff;
     const int hb = cellStart[gc], he = cellStart[gc + 1];
+    const int hFirst = hb + hOff, hLast = min(he, hFirst + hCnt);  // home atoms of this item
     const int metalEnd = P.atomOff + P.nMolMe;
+    const float rrNebr = P.rrNebr, rrShort = P.rrShort;
+    int len = 0;
     if (lane < 27) {
-      const int cxy = P.cells[0] * P.cells[1];
-      const int ccz = c / cxy;
-      const int ccy = (c - ccz * cxy) / P.cells[0];
-      const int ccx = c - (ccz * P.cells[1] + ccy) * P.cells[0];
-      int mx = ccx + kOff27[lane][0], my = ccy + kOff27[lane][1], mz = ccz + kOff27[lane][2];
-      float sx = 0.f, sy = 0.f, sz = 0.f;
-      if (mx >= P.cells[0]) { mx = 0; sx = P.region[0]; }
-      else if (mx < 0) { mx = P.cells[0] - 1; sx = -P.region[0]; }
-      if (my >= P.cells[1]) { my = 0; sy = P.region[1]; }
-      else if (my < 0) { my = P.cells[1] - 1; sy = -P.region[1]; }
-      if (mz >= P.cells[2]) { mz = 0; sz = P.region[2]; }
-      else if (mz < 0) { mz = P.cells[2] - 1; sz = -P.region[2]; }
-      const int C = P.cellOff + (mz * P.cells[1] + my) * P.cells[0] + mx;
-      sQb[w][lane] = cellStart[C];
-      sQe[w][lane] = cellStart[C + 1];
-      sSh[w][lane][0] = sx; sSh[w][lane][1] = sy; sSh[w][lane][2] = sz;
+      float sx, sy, sz;
+      const int C = P.cellOff + stencilCell(P, c, lane, sx, sy, sz);
+      const int qb = cellStart[C];
+      len = cellStart[C + 1] - qb;
+      sQb[w][lane] = qb;
+      sSh[w][lane] = make_float4(sx, sy, sz, (sx != 0.f || sy != 0.f || sz != 0.f) ? 1.f : 0.f);
     }
+    int incl = len;  // inclusive prefix of the segment lengths
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int v = __shfl_up_sync(full, incl, d);
+      if (lane >= d) incl += v;
+    }
+    if (lane < 27) sOff[w][lane] = incl - len;
+    const int total = __shfl_sync(full, incl, 26);
+    const int homeLen = he - hb;  // stencil cell 0 is the home cell: window positions [0, homeLen)
     __syncwarp();
     int want = 0, over = 0;
-    for (int h0 = hb; h0 < he; h0 += 32) {
-      const int nh = min(32, he - h0);
-      // lane a holds home atom a of this pass and its three counters
-      float4 Ah = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int h0 = hFirst; h0 < hLast; h0 += 32) {
+      const int nh = min(32, hLast - h0);
+      float4 Ah = make_float4(0.f, 0.f, 0.f, __int_as_float(-2));
       if (lane < nh) Ah = sortPos[h0 + lane];
-      int n = 0, m = 0, r = 0;
-      int o = 0, qpos = sQb[w][0];
-      while (o < 27) {
-        int fill = 0;
-        while (o < 27 && fill < kWin) {
-          const int take = min(sQe[w][o] - qpos, kWin - fill);
-          for (int t = lane; t < take; t += 32) sBuf[w][fill + t] = ((qpos + t) << 5) | o;
-          fill += take;
-          qpos += take;
-          if (qpos >= sQe[w][o]) {
-            o++;
-            if (o < 27) qpos = sQb[w][o];
+      sHome[w][lane] = Ah;
+      const int ga = __float_as_int(Ah.w);
+      int nMy = 0, rMy = 0;  // list and relevant-list lengths of home atom `lane`
+      __syncwarp();
+      for (int base = 0; base < total; base += kWin) {
+        const int nw = (min(kWin, total - base) + 31) >> 5;
+        // ---- test pass
+        for (int i = 0; i < nw; i++) {
+          const int e = base + 32 * i + lane;
+          // this lane's candidate; past the window end it sits at 1e30 and never matches
+          float bx = 1e30f, by = 1e30f, bz = 1e30f, sx = 0.f, sy = 0.f, sz = 0.f;
+          int k = -1;
+          bool shifted = false;
+          if (e < total) {
+            int o = 0;  // the last stencil cell whose segment starts at or before e
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1)
+              if (o + step < 27 && sOff[w][o + step] <= e) o += step;
+            const float4 B = sortPos[sQb[w][o] + e - sOff[w][o]];
+            k = __float_as_int(B.w);
+            bx = B.x; by = B.y; bz = B.z;
+            const float4 sh = sSh[w][o];
+            sx = sh.x; sy = sh.y; sz = sh.z;
+            shifted = sh.w != 0.f;
+            sK[w][32 * i + lane] = k;
+          }
+          sMetal[w][i] = __ballot_sync(full, k >= 0 && k < metalEnd);
+          if (!__any_sync(full, shifted) && base + 32 * i >= homeLen) {
+#pragma unroll 4
+            for (int a = 0; a < nh; a++) {
+              const float4 H = sHome[w][a];
+              const float dx = H.x - bx, dy = H.y - by, dz = H.z - bz;
+              const float rr = dx * dx + dy * dy + dz * dz;
+              const unsigned mh = __ballot_sync(full, rr < rrNebr);
+              const unsigned mc = __ballot_sync(full, rr < rrShort);
+              sMask[w][i][a] = make_uint2(mh, mc);
+            }
+          } else {
+#pragma unroll 4
+            for (int a = 0; a < nh; a++) {
+              const float4 H = sHome[w][a];
+              // the reference subtracts the cell shift after the difference: both roundings kept
+              float dx = H.x - bx, dy = H.y - by, dz = H.z - bz;
+              dx = dx - sx; dy = dy - sy; dz = dz - sz;
+              const float rr = dx * dx + dy * dy + dz * dz;
+              const bool hit = (rr < rrNebr) && (__float_as_int(H.w) != k);
+              const unsigned mh = __ballot_sync(full, hit);
+              const unsigned mc = __ballot_sync(full, rr < rrShort);
+              sMask[w][i][a] = make_uint2(mh, mc);
+            }
           }
         }
         __syncwarp();
-        for (int e0 = 0; e0 < fill; e0 += 32) {
-          // this lane's candidate, shifted into the home cell's image
-          const int e = e0 + lane;
-          const bool have = e < fill;
-          float bx = 0.f, by = 0.f, bz = 0.f;
-          int k = -1, oo = 0;
-          if (have) {
-            const int code = sBuf[w][e];
-            oo = code & 31;
-            const float4 B = sortPos[code >> 5];
-            k = __float_as_int(B.w);
-            bx = B.x; by = B.y; bz = B.z;
-          }
-          // the reference subtracts the cell shift after the difference: both roundings kept
-          const float sx = sSh[w][oo][0], sy = sSh[w][oo][1], sz = sSh[w][oo][2];
-          for (int a = 0; a < nh; a++) {
-            const float ax = __shfl_sync(0xffffffffu, Ah.x, a);
-            const float ay = __shfl_sync(0xffffffffu, Ah.y, a);
-            const float az = __shfl_sync(0xffffffffu, Ah.z, a);
-            const int g = __shfl_sync(0xffffffffu, __float_as_int(Ah.w), a);
-            float dx = ax - bx, dy = ay - by, dz = az - bz;
-            dx = dx - sx; dy = dy - sy; dz = dz - sz;
-            const float rr = dx * dx + dy * dy + dz * dz;
-            const bool hit = have && (rr < P.rrNebr) && (g != k);
-            const unsigned mh = __ballot_sync(0xffffffffu, hit);
-            if (mh == 0) continue;
-            const bool close = hit && (rr < P.rrShort);
-            const bool rel = (g >= metalEnd) && (close || (hit && k < metalEnd));
-            const unsigned mc = __ballot_sync(0xffffffffu, close);
-            const unsigned mr = __ballot_sync(0xffffffffu, rel);
-            const int na = __shfl_sync(0xffffffffu, n, a);
-            const int ma = __shfl_sync(0xffffffffu, m, a);
-            const int ra = __shfl_sync(0xffffffffu, r, a);
-            if (hit) {
-              const int j = na + __popc(mh & lower);
-              if (j < nebrMax) nbl[(size_t)g * rowStride + j] = k;
-              if (rel) {
-                const int jr = ra + __popc(mr & lower);
-                if (jr < kRelMax) rl[(size_t)g * kRelMax + jr] = make_int2(k, j);
-              }
-            }
-            if (close) {
-              const int j = ma + __popc(mc & lower);
-              if (j < kShortMax) sl[(size_t)g * kShortMax + j] = k;
-            }
-            if (lane == a) {
-              n += __popc(mh);
-              m += __popc(mc);
+        // ---- emit pass
+        for (int a = 0; a < nh; a++) {
+          const int g = __float_as_int(sHome[w][a].w);
+          int n = __shfl_sync(full, nMy, a);
+          int *row = nbl + (size_t)g * rowStride;
+          if (g >= metalEnd) {
+            int r = __shfl_sync(full, rMy, a);
+            int2 *rrow = rl + (size_t)g * kRelMax;
+            for (int i = 0; i < nw; i++) {
+              const uint2 hc = sMask[w][i][a];
+              const int k = sK[w][32 * i + lane];
+              const int j = n + __popc(hc.x & lower);
+              stIf((hc.x & laneBit) && j < nebrMax, row + j, k);
+              const unsigned mr = hc.x & (hc.y | sMetal[w][i]);
+              const int jr = r + __popc(mr & lower);
+              stIf2((mr & laneBit) && jr < kRelMax, rrow + jr, k, (hc.y & laneBit) ? (j | kRelClose) : j);
               r += __popc(mr);
+              n += __popc(hc.x);
+            }
+            rMy = (lane == a) ? r : rMy;
+          } else {
+            for (int i = 0; i < nw; i++) {
+              const unsigned hx = sMask[w][i][a].x;
+              const int k = sK[w][32 * i + lane];
+              const int j = n + __popc(hx & lower);
+              stIf((hx & laneBit) && j < nebrMax, row + j, k);
+              n += __popc(hx);
             }
           }
+          nMy = (lane == a) ? n : nMy;
         }
         __syncwarp();
       }
       if (lane < nh) {
-        const int g = __float_as_int(Ah.w);
-        nn[g] = min(n, nebrMax);
-        ns[g] = (m > kShortMax || n > nebrMax) ? -1 : m;   // -1: walk the full list instead
-        nrl[g] = (r > kRelMax || n > nebrMax) ? -1 : r;    // -1: carbon pass walks the full list
-        want = max(want, n);
-        over += (n > nebrMax) ? 1 : 0;
+        nn[ga] = min(nMy, nebrMax);
+        // -1: the carbon pass walks the full list instead
+        nrl[ga] = (ga < metalEnd) ? 0 : (rMy > kRelMax || nMy > nebrMax) ? -1 : rMy;
+        want = max(want, nMy);
+        over += (nMy > nebrMax) ? 1 : 0;
       }
     }
     for (int off = 16; off > 0; off >>= 1) {
-      want = max(want, __shfl_xor_sync(0xffffffffu, want, off));
-      over += __shfl_xor_sync(0xffffffffu, over, off);
+      want = max(want, __shfl_xor_sync(full, want, off));
+      over += __shfl_xor_sync(full, over, off);
     }
     if (lane == 0) {
       atomicMax(&S->maxNeighbours, want);
@@ -653,17 +720,16 @@ __global__ void __launch_bounds__(128) k_force_metal(BlockTab tab, const RepCons
 // The reference reuses its list counter for the bonded loop (cu:989), so after the third close
 // carbon its walk resumes at entry 4: metal entries at positions 4..p2 contribute their LJ term
 // twice, and entry 3 is skipped when p2 == 2.  After the walk, lane q < 3 adds the
-// second-neighbour terms of close carbon q (walking that neighbour's short list) and lane 3 the
+// second-neighbour terms of close carbon q (walking that neighbour's relevant list) and lane 3 the
 // radial, out-of-plane and angle terms; the four partial sums meet in a shuffle tree.
 __device__ __forceinline__ void relEntry(bool full, const int *row, const int2 *rrow, int e, int &k, int &j) {
   if (full) { k = row[e]; j = e; }
-  else { const int2 v = rrow[e]; k = v.x; j = v.y; }
+  else { const int2 v = rrow[e]; k = v.x; j = v.y & (kRelClose - 1); }
 }
 
 __global__ void __launch_bounds__(128) k_force_carbon(BlockTab tab, const RepConst *__restrict__ rc,
                                                       float4 *__restrict__ pos, float4 *__restrict__ acc,
                                                       const int *__restrict__ nn, const int *__restrict__ nbl,
-                                                      const int *__restrict__ ns, const int *__restrict__ sl,
                                                       const int *__restrict__ nrl, const int2 *__restrict__ rl,
                                                       int rowStride) {
   __shared__ float sD[128 / kCT][3][4];  // dx, dy, dz, |d| of close carbon q
@@ -758,33 +824,58 @@ __global__ void __launch_bounds__(128) k_force_carbon(BlockTab tab, const RepCon
     const int k = sK[a][q];
     const float rnx = sD[a][q][0], rny = sD[a][q][1], rnz = sD[a][q][2], absR = sD[a][q][3];
     const float4 B = pos[k];
-    const int nk = ns[k];
+    // the entries of the neighbour's relevant list marked kRelClose are, in list order, every
+    // entry that can pass the rCutC test below
+    const int nk = nrl[k];
     const bool fullk = nk < 0;
     const int lim = fullk ? nn[k] : nk;
-    const int *src = fullk ? nbl + (size_t)k * rowStride : sl + (size_t)k * kShortMax;
+    const int *krow = nbl + (size_t)k * rowStride;
+    const int2 *krel = rl + (size_t)k * kRelMax;
     int countk = 0;
-    for (int l = 0; l < lim; l++) {
-      const int m = src[l];
-      const float4 rm = pos[m];
-      float ex = minImg(B.x - rm.x, P.region[0]);
-      float ey = minImg(B.y - rm.y, P.region[1]);
-      float ez = minImg(B.z - rm.z, P.region[2]);
-      const float rr2 = ex * ex + ey * ey + ez * ez;
-      if ((rr2 < P.rrCutC) && (m != i)) {
-        ex = ex * (-1.f); ey = ey * (-1.f); ez = ez * (-1.f);
-        const float cs = (rnx * ex + rny * ey + rnz * ez) / (absR * rr2);
-        const float th = acosf(cs);
-        const float dth = th - P.theta_0;
-        const float tmp = P.mu_theta * dth / sqrtf(1.f - cs * cs);
-        float f = tmp / (absR * rr2);
-        fx = fx + f * ex; fy = fy + f * ey; fz = fz + f * ez;
-        f = -tmp * cs / (absR * absR);
-        fx = fx + f * rnx; fy = fy + f * rny; fz = fz + f * rnz;
-        f = -P.mu_p * (rm.z - P.z_0) / 9.f;
-        fz = fz + f;
-        ++countk;
+    // four entries per load (a relevant-list row holds kRelMax entries, 32-byte aligned, so the
+    // group of the last entry stays inside it); positions are loaded for close entries only
+    for (int l0 = 0; l0 < lim && countk < 2; l0 += 4) {
+      int mm[4];
+      bool use[4];
+      if (fullk) {
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+          use[t] = l0 + t < lim;
+          mm[t] = use[t] ? krow[l0 + t] : 0;
+        }
+      } else {
+        const int4 u = *reinterpret_cast<const int4 *>(krel + l0);
+        const int4 v = *reinterpret_cast<const int4 *>(krel + l0 + 2);
+        mm[0] = u.x; mm[1] = u.z; mm[2] = v.x; mm[3] = v.z;
+        use[0] = (u.y & kRelClose) != 0;
+        use[1] = l0 + 1 < lim && (u.w & kRelClose) != 0;
+        use[2] = l0 + 2 < lim && (v.y & kRelClose) != 0;
+        use[3] = l0 + 3 < lim && (v.w & kRelClose) != 0;
       }
-      if (countk == 2) break;
+      for (int t = 0; t < 4; t++) {
+        if (!use[t]) continue;
+        const int m = mm[t];
+        const float4 rm = pos[m];
+        float ex = minImg(B.x - rm.x, P.region[0]);
+        float ey = minImg(B.y - rm.y, P.region[1]);
+        float ez = minImg(B.z - rm.z, P.region[2]);
+        const float rr2 = ex * ex + ey * ey + ez * ez;
+        if ((rr2 < P.rrCutC) && (m != i)) {
+          ex = ex * (-1.f); ey = ey * (-1.f); ez = ez * (-1.f);
+          const float cs = (rnx * ex + rny * ey + rnz * ez) / (absR * rr2);
+          const float th = acosf(cs);
+          const float dth = th - P.theta_0;
+          const float tmp = P.mu_theta * dth / sqrtf(1.f - cs * cs);
+          float f = tmp / (absR * rr2);
+          fx = fx + f * ex; fy = fy + f * ey; fz = fz + f * ez;
+          f = -tmp * cs / (absR * absR);
+          fx = fx + f * rnx; fy = fy + f * rny; fz = fz + f * rnz;
+          f = -P.mu_p * (rm.z - P.z_0) / 9.f;
+          fz = fz + f;
+          ++countk;
+        }
+        if (countk == 2) break;
+      }
     }
   } else if (sub == 3 && counti == 3) {
     // radial, out-of-plane and own-angle terms (cu:985-1061)

@@ -40,7 +40,7 @@ static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 // Carving of the scratch array (offsets in bytes, each 256-byte aligned).
 struct Carve {
   size_t rc, st, tabRep, tabStart, tileRep, tileStart, tileFirst, tileSum, cellCount, cellStart;
-  size_t cellOf, slot, tmpIdx, sortIdx, nn, ns, sortPos, rho, dF, Fv, fric, nbl, sl, nrl, rl, active, work, total;
+  size_t cellOf, slot, tmpIdx, sortIdx, nn, sortPos, rho, dF, Fv, fric, nbl, nrl, rl, active, heavy, work, total;
 };
 constexpr size_t up(size_t x) { return (x + 255) & ~size_t(255); }
 constexpr Carve carve() {
@@ -62,18 +62,17 @@ constexpr Carve carve() {
   c.tmpIdx = o; o += up(N * sizeof(int));
   c.sortIdx = o; o += up(N * sizeof(int));
   c.nn = o; o += up(N * sizeof(int));
-  c.ns = o; o += up(N * sizeof(int));
   c.sortPos = o; o += up(N * sizeof(float4));
   c.rho = o; o += up(N * sizeof(float));
   c.dF = o; o += up(N * sizeof(float));
   c.Fv = o; o += up(N * sizeof(float));
   c.fric = o; o += up(N * sizeof(float));
   c.nbl = o; o += up(N * SG_NOALLOC_MAX_NEBR * sizeof(int));
-  c.sl = o; o += up(N * kShortMax * sizeof(int));
   c.nrl = o; o += up(N * sizeof(int));
   c.rl = o; o += up(N * kRelMax * sizeof(int2));
   c.active = o; o += up(SG_NOALLOC_MAX_CELLS * sizeof(int));
-  c.work = o; o += up(2 * sizeof(int));
+  c.heavy = o; o += up(((size_t)N / kHeavyChunk + (size_t)N / (kHeavyCell + 1) + 16) * sizeof(int2));
+  c.work = o; o += up(3 * sizeof(int));
   c.total = o;
   return c;
 }
@@ -107,7 +106,7 @@ __global__ void k_noalloc_setup(RepConst P, RepState *st, RepConst *rc, int *tab
     tileStart[k] = k * kCellTile;
   }
   for (int c = t; c < P.ncellsPad; c += stride) cellCount[c] = 0;
-  if (t < 2) work[t] = 0;
+  if (t < 3) work[t] = 0;
 }
 
 RepConst constFor(const sg_simparams &p) {
@@ -173,13 +172,14 @@ extern "C" int sg_compute_forces_noalloc(const sg_simparams *p, sg_float4 *d_pos
   int *tileFirst = (int *)(base + K.tileFirst), *tileSum = (int *)(base + K.tileSum);
   int *cellCount = (int *)(base + K.cellCount), *cellStart = (int *)(base + K.cellStart);
   int *cellOf = (int *)(base + K.cellOf), *slot = (int *)(base + K.slot), *tmpIdx = (int *)(base + K.tmpIdx);
-  int *sortIdx = (int *)(base + K.sortIdx), *nn = (int *)(base + K.nn), *ns = (int *)(base + K.ns);
+  int *sortIdx = (int *)(base + K.sortIdx), *nn = (int *)(base + K.nn);
   float4 *sortPos = (float4 *)(base + K.sortPos);
   float *rho = (float *)(base + K.rho), *dF = (float *)(base + K.dF), *Fv = (float *)(base + K.Fv);
   float *fric = (float *)(base + K.fric);
-  int *nbl = (int *)(base + K.nbl), *sl = (int *)(base + K.sl), *nrl = (int *)(base + K.nrl);
+  int *nbl = (int *)(base + K.nbl), *nrl = (int *)(base + K.nrl);
   int2 *rl = (int2 *)(base + K.rl);
   int *active = (int *)(base + K.active), *work = (int *)(base + K.work);
+  int2 *heavy = (int2 *)(base + K.heavy);
   float4 *pos = (float4 *)d_pos, *acc = (float4 *)d_acc;
 
   const RepConst P = constFor(*p);
@@ -199,17 +199,17 @@ extern "C" int sg_compute_forces_noalloc(const sg_simparams *p, sg_float4 *d_pos
   k_scan_tiles<<<nTiles, 256, 0, s>>>(tileTab, rc, st, cellCount, tileSum, 1);
   k_scan_tile_prefix<<<1, 1024, 0, s>>>(rc, st, tileFirst, tileSum, 1);
   k_scan_final<<<nTiles, 256, 0, s>>>(tileTab, rc, st, cellCount, tileSum, cellStart, (int)p->blockSize, 1, active,
-                                      work);
-  k_scatter<<<nAtomBlk, kBs, 0, s>>>(atomTab, rc, st, cellOf, slot, cellStart, tmpIdx, nn, ns, 1);
+                                      heavy, work);
+  k_scatter<<<nAtomBlk, kBs, 0, s>>>(atomTab, rc, st, cellOf, slot, cellStart, tmpIdx, nn, nrl, 1);
   k_rank<<<nAtomBlk, kBs, 0, s>>>(atomTab, rc, st, cellOf, cellStart, tmpIdx, pos, sortIdx, sortPos, 1);
   const int rowStride = (p->iNebrMax + 3) & ~3;
-  k_build_nebr<<<256, kNebrWarps * 32, 0, s>>>(tileRep, active, work, rc, st, cellStart, sortPos, nn, nbl, ns, sl,
-                                               nrl, rl, rowStride, p->iNebrMax);
+  k_build_nebr<<<256, kNebrWarps * 32, 0, s>>>(tileRep, active, heavy, work, rc, st, cellStart, sortPos, nn, nbl, nrl,
+                                               rl, rowStride, p->iNebrMax);
   if (nMetalBlk) {
     k_rho<<<nMetalBlk, kBs, 0, s>>>(metalTab, rc, pos, nn, nbl, rho, dF, Fv, rowStride);
     k_force_metal<<<nMetalBlk, kBs, 0, s>>>(metalTab, rc, pos, acc, nn, nbl, dF, Fv, fric, rowStride);
   }
-  if (nCarbBlk) k_force_carbon<<<nCarbBlk, kBs, 0, s>>>(carbTab, rc, pos, acc, nn, nbl, ns, sl, nrl, rl, rowStride);
+  if (nCarbBlk) k_force_carbon<<<nCarbBlk, kBs, 0, s>>>(carbTab, rc, pos, acc, nn, nbl, nrl, rl, rowStride);
   e = cudaGetLastError();
   if (e != cudaSuccess) return sg_fail(SG_ERR_CUDA, "sg_compute_forces_noalloc launch: %s", cudaGetErrorString(e));
   int flags = 0;

@@ -20,6 +20,15 @@ FORCE_ATOL = 1e-6
 ENERGY_RTOL = 2e-5
 
 
+def angle_atol(p):
+    """Absolute force difference that acosf alone can cause on a carbon atom: CUDA's and libm's
+    acosf differ by up to 2 ulp, and each of the atom's angle terms (3 own, up to 6 with second
+    neighbours) turns one ulp of theta into mu_theta * ulp / sin(theta_0) of force.  In a flat
+    sheet (theta = theta_0) these differences do not shrink with the force itself."""
+    ulp = float(np.spacing(np.float32(p.theta_0)))
+    return 2 * 9 * p.mu_theta * ulp / np.sin(p.theta_0)
+
+
 def perturbed_small(seed=21, jitter=0.05):
     p, r, v = workloads.small(seed=seed)
     rng = np.random.RandomState(seed)
@@ -56,6 +65,36 @@ def test_cells_and_neighbours_bit_exact():
     assert np.array_equal(nbl_g, nbl_o)  # same entries in the same order
     d = sim.diag()
     assert d.max_neighbours == nn_o.max() and d.nebr_overflow == 0
+    sim.close()
+
+
+def test_neighbours_bit_exact_production_workload():
+    """The full graphene + Ni-cluster system: 149 cells of the clusters hold more than 16 atoms
+    and are split into home-atom chunks by the list build; lists and forces as on the oracle."""
+    p, r, v = workloads.production(seed=2, steps=10)
+    a = np.zeros((p.nMol, 3), np.float32)
+    sim, orc = make_pair(p, r, v, a)
+    sim.build_lists()
+    orc.build_lists()
+    co_g, cs_g, ca_g = sim.cells()
+    co_o, cs_o, ca_o = orc.cells()
+    assert np.diff(cs_o).max() > 16
+    assert np.array_equal(co_g, co_o) and np.array_equal(cs_g, cs_o) and np.array_equal(ca_g, ca_o)
+    nn_g, nbl_g = sim.nebr()
+    nn_o, nbl_o = orc.nebr()
+    assert np.array_equal(nn_g, nn_o)
+    assert np.array_equal(nbl_g, nbl_o)
+    sim.compute_forces()
+    orc.compute_forces()
+    rg, _, ag = sim.get_state()
+    ro, _, ao = orc.get_state()
+    m = p.nMolMe
+    ok, rel = close(ag[:m], ao[:m])
+    assert ok, f"metal accelerations rel err {rel:.3g}"
+    ok, rel = close(ag[m:], ao[m:], atol=angle_atol(p))
+    assert ok, f"carbon accelerations rel err {rel:.3g}"
+    ok, rel = close(rg[:, 3], ro[:, 3], rtol=ENERGY_RTOL)
+    assert ok, f"per-atom energies rel err {rel:.3g}"
     sim.close()
 
 
