@@ -15,7 +15,9 @@
 //                                           up to a multiple of 4: 16-byte aligned rows)
 //   nrl int[Ntot], rl int2[Ntot * kRelMax]  relevant list of a carbon atom: its metal entries
 //                                           and entries within (rCutC+skin), {index, position
-//                                           in the full list | kRelClose if within rCutC+skin}
+//                                           in the full list}
+//   ns int[Ntot], sl int[Ntot * kShortMax]  close list of a carbon atom: its entries within
+//                                           (rCutC+skin), in list order
 //   rho/dF/Fv float[Ntot]   EAM density, F'(rho), F(rho) (metal atoms)
 //   fric float[Ntot]       x force of carbon on each metal atom
 // Per-replica constants live in RepConst, mutable per-replica scalars in RepState.
@@ -34,7 +36,7 @@ constexpr int kCT = 4;            // lanes per carbon atom in the carbon-force p
 constexpr int kNebrWarps = 4;     // warps per block in the neighbour-list build (one home cell each)
 constexpr int kWin = 512;         // candidates per shared-memory window of the list build
 constexpr int kRelMax = 48;       // relevant-list capacity per carbon atom
-constexpr int kRelClose = 1 << 30;  // flag on a relevant-list position: entry within rCutC + skin
+constexpr int kShortMax = 8;      // close-list capacity per carbon atom (a multiple of 4)
 constexpr int kHeavyCell = 16;    // list build: cells above this many atoms are split into items
 constexpr int kHeavyChunk = 8;    // of this many home atoms
 constexpr int kMetalPerBlock = 128 / kMT;   // atoms per 128-thread block

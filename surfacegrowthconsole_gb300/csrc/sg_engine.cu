@@ -244,7 +244,8 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
   if (c->opt.mode == SG_MODE_MIXED) AL(c->posLo, N);
   AL(c->cellOf, N); AL(c->slot, N); AL(c->tmpIdx, N); AL(c->sortIdx, N);
   AL(c->cellCount, (size_t)c->ctot); AL(c->cellStart, (size_t)c->ctot);
-  AL(c->nn, N);
+  AL(c->nn, N); AL(c->ns, N);
+  AL(c->sl, N * kShortMax);
   AL(c->nbl, N * c->rowStride);
   AL(c->nrl, N);
   AL(c->rl, N * kRelMax);
@@ -462,13 +463,13 @@ static int enqueueRebuild(sg_ctx *c, int force) {
     LAUNCH_OK();
   }
   k_scatter<<<c->atomTab.n, 128, 0, c->stream>>>(c->atomTab.view(), c->rc, c->st, c->cellOf, c->slot, c->cellStart,
-                                                 c->tmpIdx, c->nn, c->nrl, fr);
+                                                 c->tmpIdx, c->nn, c->ns, c->nrl, fr);
   k_rank<<<c->atomTab.n, 128, 0, c->stream>>>(c->atomTab.view(), c->rc, c->st, c->cellOf, c->cellStart, c->tmpIdx,
                                               c->pos, c->sortIdx, c->sortPos, fr);
   k_build_nebr<<<c->nebrGrid, kNebrWarps * 32, 0, c->stream>>>(c->tileTab.rep, c->activeCells, c->heavyItems,
                                                                 c->nebrWork, c->rc, c->st, c->cellStart, c->sortPos,
-                                                                c->nn, c->nbl, c->nrl, c->rl, c->rowStride,
-                                                                c->nebrMax);
+                                                                c->nn, c->nbl, c->ns, c->sl, c->nrl, c->rl,
+                                                                c->rowStride, c->nebrMax);
   LAUNCH_OK();
   return SG_OK;
 }
@@ -494,7 +495,7 @@ static int enqueueForces(sg_ctx *c, bool withCmVel) {
   }
   if (c->carbonTabT.n)
     k_force_carbon<<<c->carbonTabT.n, 128, 0, c->stream>>>(c->carbonTabT.view(), c->rc, c->pos, c->acc, c->nn,
-                                                           c->nbl, c->nrl, c->rl, c->rowStride);
+                                                           c->nbl, c->ns, c->sl, c->nrl, c->rl, c->rowStride);
   if (c->opt.phase_timing) cudaEventRecordWithFlags(c->phaseEv[3], c->stream, cudaEventRecordExternal);
   LAUNCH_OK();
   if (fork) {

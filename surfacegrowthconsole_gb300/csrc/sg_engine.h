@@ -36,7 +36,7 @@ struct sg_ctx {
   RepState *st = nullptr;
   float4 *pos = nullptr, *vel = nullptr, *acc = nullptr, *posLo = nullptr, *sortPos = nullptr;
   int *cellOf = nullptr, *slot = nullptr, *cellCount = nullptr, *cellStart = nullptr;
-  int *tmpIdx = nullptr, *sortIdx = nullptr, *nn = nullptr, *nbl = nullptr;
+  int *tmpIdx = nullptr, *sortIdx = nullptr, *nn = nullptr, *nbl = nullptr, *ns = nullptr, *sl = nullptr;
   int *nrl = nullptr;
   int2 *rl = nullptr;
   int nebrGrid = 0;

@@ -19,7 +19,7 @@ __global__ void k_scan_final(BlockTab tab, const RepConst *rc, RepState *st, int
                              const int *tileSum, int *cellStart, int blockSizeCap, int forceRebuild,
                              int *active, int2 *heavy, int *work);
 __global__ void k_scatter(BlockTab tab, const RepConst *rc, RepState *st, const int *cellOf,
-                          const int *slot, const int *cellStart, int *tmpIdx, int *nn, int *nrl,
+                          const int *slot, const int *cellStart, int *tmpIdx, int *nn, int *ns, int *nrl,
                           int forceRebuild);
 __global__ void k_rank(BlockTab tab, const RepConst *rc, const RepState *st, const int *cellOf,
                        const int *cellStart, const int *tmpIdx, const float4 *pos, int *sortIdx,
@@ -27,8 +27,8 @@ __global__ void k_rank(BlockTab tab, const RepConst *rc, const RepState *st, con
 // work[0]: next work item to take, work[1]: length of the cell list `active`, work[2]: length
 // of the home-chunk list `heavy` (all reset before the scan of every rebuild).
 __global__ void k_build_nebr(const int *tileRep, const int *active, const int2 *heavy, int *work, const RepConst *rc, RepState *st,
-                             const int *cellStart, const float4 *sortPos, int *nn, int *nbl, int *nrl, int2 *rl,
-                             int rowStride, int nebrMax);
+                             const int *cellStart, const float4 *sortPos, int *nn, int *nbl, int *ns, int *sl,
+                             int *nrl, int2 *rl, int rowStride, int nebrMax);
 
 // ---- PLAIN force and step kernels ----
 __global__ void k_rho(BlockTab tab, const RepConst *rc, const float4 *pos, const int *nn,
@@ -37,7 +37,7 @@ __global__ void k_force_metal(BlockTab tab, const RepConst *rc, float4 *pos, flo
                               const int *nn, const int *nbl, const float *dF, const float *Fv,
                               float *fric, int rowStride);
 __global__ void k_force_carbon(BlockTab tab, const RepConst *rc, float4 *pos, float4 *acc,
-                               const int *nn, const int *nbl,
+                               const int *nn, const int *nbl, const int *ns, const int *sl,
                                const int *nrl, const int2 *rl, int rowStride);
 __global__ void k_cmvel(BlockTab tab, const RepConst *rc, RepState *st, const float4 *vel,
                         const float4 *acc, float *partial, const int *redFirst);

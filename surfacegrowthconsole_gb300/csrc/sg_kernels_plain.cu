@@ -289,7 +289,8 @@ __global__ void k_scan_final(BlockTab tab, const RepConst *__restrict__ rc, RepS
 __global__ void k_scatter(BlockTab tab, const RepConst *__restrict__ rc, RepState *st,
                           const int *__restrict__ cellOf, const int *__restrict__ slot,
                           const int *__restrict__ cellStart, int *__restrict__ tmpIdx,
-                          int *__restrict__ nn, int *__restrict__ nrl, int forceRebuild) {
+                          int *__restrict__ nn, int *__restrict__ ns, int *__restrict__ nrl,
+                          int forceRebuild) {
   const int rep = tab.rep[blockIdx.x];
   RepState *S = st + rep;
   if (!rebuilding(S, forceRebuild)) return;
@@ -301,6 +302,7 @@ __global__ void k_scatter(BlockTab tab, const RepConst *__restrict__ rc, RepStat
     tmpIdx[cellStart[P.cellOff + c] + slot[g]] = g;
   } else {
     nn[g] = 0;  // an atom outside the grid has no neighbours (the reference clears NN)
+    ns[g] = 0;
     nrl[g] = 0;
     atomicAdd(&S->cellRange, 1);
   }
@@ -345,13 +347,14 @@ __global__ void k_rank(BlockTab tab, const RepConst *__restrict__ rc, const RepS
 //    self-pair test (subtracting a zero shift changes no bit).
 //  Emit pass: per home atom and word with hits, lane l places candidate l at its rank among
 //    the word's set bits, so consecutive entries of the atom's row nbl[g*rowStride + j] come
-//    from one coalesced store; for a carbon atom the same ranks place its relevant list (every
-//    metal entry and every entry within rCutC + skin, with its position in the full list:
-//    all the carbon-force pass needs; kRelClose marks the entries within rCutC + skin).  The
-//    running lengths are uniform across the warp; stores are predicated, not branched.
+//    from one coalesced store; for a carbon atom the same ranks place its close list (entries
+//    within rCutC + skin, read by the graphene second-neighbour walk of the atoms bonded to
+//    it) and its relevant list (every metal entry and every close entry, with its position in
+//    the full list: all the carbon-force pass needs for the atom itself).  The running lengths
+//    are uniform across the warp; stores are predicated, not branched.
 // A window pass holds kWin candidates; larger stencils take several passes, the lengths
-// carrying over in the lane of each home atom.  The relevant list rests on the skin, as the
-// neighbour list itself does: no pair closes in by more than rNebrShell between rebuilds.
+// carrying over in the lane of each home atom.  Close and relevant lists rest on the skin, as
+// the neighbour list itself does: no pair closes in by more than rNebrShell between rebuilds.
 // ============================================================================================
 __device__ __forceinline__ void stIf(bool p, int *a, int v) {
   asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %0, 0;\n\t@q st.global.u32 [%1], %2;\n\t}" ::"r"((unsigned)p), "l"(a),
@@ -371,6 +374,7 @@ __global__ void __launch_bounds__(kNebrWarps * 32) k_build_nebr(const int *__res
                                                                 const int *__restrict__ cellStart,
                                                                 const float4 *__restrict__ sortPos,
                                                                 int *__restrict__ nn, int *__restrict__ nbl,
+                                                                int *__restrict__ ns, int *__restrict__ sl,
                                                                 int *__restrict__ nrl, int2 *__restrict__ rl,
                                                                 int rowStride, int nebrMax) {
   __shared__ int sK[kNebrWarps][kWin];                 // atom index of each window position
@@ -431,7 +435,7 @@ __global__ void __launch_bounds__(kNebrWarps * 32) k_build_nebr(const int *__res
       if (lane < nh) Ah = sortPos[h0 + lane];
       sHome[w][lane] = Ah;
       const int ga = __float_as_int(Ah.w);
-      int nMy = 0, rMy = 0;  // list and relevant-list lengths of home atom `lane`
+      int nMy = 0, mMy = 0, rMy = 0;  // list, close-list and relevant-list lengths of home atom `lane`
       __syncwarp();
       for (int base = 0; base < total; base += kWin) {
         const int nw = (min(kWin, total - base) + 31) >> 5;
@@ -488,19 +492,26 @@ __global__ void __launch_bounds__(kNebrWarps * 32) k_build_nebr(const int *__res
           int n = __shfl_sync(full, nMy, a);
           int *row = nbl + (size_t)g * rowStride;
           if (g >= metalEnd) {
+            int m = __shfl_sync(full, mMy, a);
             int r = __shfl_sync(full, rMy, a);
+            int *srow = sl + (size_t)g * kShortMax;
             int2 *rrow = rl + (size_t)g * kRelMax;
             for (int i = 0; i < nw; i++) {
               const uint2 hc = sMask[w][i][a];
               const int k = sK[w][32 * i + lane];
               const int j = n + __popc(hc.x & lower);
               stIf((hc.x & laneBit) && j < nebrMax, row + j, k);
+              const unsigned mc = hc.x & hc.y;
+              const int jm = m + __popc(mc & lower);
+              stIf((mc & laneBit) && jm < kShortMax, srow + jm, k);
               const unsigned mr = hc.x & (hc.y | sMetal[w][i]);
               const int jr = r + __popc(mr & lower);
-              stIf2((mr & laneBit) && jr < kRelMax, rrow + jr, k, (hc.y & laneBit) ? (j | kRelClose) : j);
+              stIf2((mr & laneBit) && jr < kRelMax, rrow + jr, k, j);
+              m += __popc(mc);
               r += __popc(mr);
               n += __popc(hc.x);
             }
+            mMy = (lane == a) ? m : mMy;
             rMy = (lane == a) ? r : rMy;
           } else {
             for (int i = 0; i < nw; i++) {
@@ -518,6 +529,7 @@ __global__ void __launch_bounds__(kNebrWarps * 32) k_build_nebr(const int *__res
       if (lane < nh) {
         nn[ga] = min(nMy, nebrMax);
         // -1: the carbon pass walks the full list instead
+        ns[ga] = (ga < metalEnd) ? 0 : (mMy > kShortMax || nMy > nebrMax) ? -1 : mMy;
         nrl[ga] = (ga < metalEnd) ? 0 : (rMy > kRelMax || nMy > nebrMax) ? -1 : rMy;
         want = max(want, nMy);
         over += (nMy > nebrMax) ? 1 : 0;
@@ -720,16 +732,17 @@ __global__ void __launch_bounds__(128) k_force_metal(BlockTab tab, const RepCons
 // The reference reuses its list counter for the bonded loop (cu:989), so after the third close
 // carbon its walk resumes at entry 4: metal entries at positions 4..p2 contribute their LJ term
 // twice, and entry 3 is skipped when p2 == 2.  After the walk, lane q < 3 adds the
-// second-neighbour terms of close carbon q (walking that neighbour's relevant list) and lane 3 the
+// second-neighbour terms of close carbon q (walking that neighbour's close list) and lane 3 the
 // radial, out-of-plane and angle terms; the four partial sums meet in a shuffle tree.
 __device__ __forceinline__ void relEntry(bool full, const int *row, const int2 *rrow, int e, int &k, int &j) {
   if (full) { k = row[e]; j = e; }
-  else { const int2 v = rrow[e]; k = v.x; j = v.y & (kRelClose - 1); }
+  else { const int2 v = rrow[e]; k = v.x; j = v.y; }
 }
 
 __global__ void __launch_bounds__(128) k_force_carbon(BlockTab tab, const RepConst *__restrict__ rc,
                                                       float4 *__restrict__ pos, float4 *__restrict__ acc,
                                                       const int *__restrict__ nn, const int *__restrict__ nbl,
+                                                      const int *__restrict__ ns, const int *__restrict__ sl,
                                                       const int *__restrict__ nrl, const int2 *__restrict__ rl,
                                                       int rowStride) {
   __shared__ float sD[128 / kCT][3][4];  // dx, dy, dz, |d| of close carbon q
@@ -824,16 +837,13 @@ __global__ void __launch_bounds__(128) k_force_carbon(BlockTab tab, const RepCon
     const int k = sK[a][q];
     const float rnx = sD[a][q][0], rny = sD[a][q][1], rnz = sD[a][q][2], absR = sD[a][q][3];
     const float4 B = pos[k];
-    // the entries of the neighbour's relevant list marked kRelClose are, in list order, every
-    // entry that can pass the rCutC test below
-    const int nk = nrl[k];
+    // the neighbour's close list holds, in list order, every entry that can pass the rCutC test
+    // below; four entries per load (a close-list row is 32 bytes, aligned)
+    const int nk = ns[k];
     const bool fullk = nk < 0;
     const int lim = fullk ? nn[k] : nk;
-    const int *krow = nbl + (size_t)k * rowStride;
-    const int2 *krel = rl + (size_t)k * kRelMax;
+    const int *src = fullk ? nbl + (size_t)k * rowStride : sl + (size_t)k * kShortMax;
     int countk = 0;
-    // four entries per load (a relevant-list row holds kRelMax entries, 32-byte aligned, so the
-    // group of the last entry stays inside it); positions are loaded for close entries only
     for (int l0 = 0; l0 < lim && countk < 2; l0 += 4) {
       int mm[4];
       bool use[4];
@@ -841,16 +851,13 @@ __global__ void __launch_bounds__(128) k_force_carbon(BlockTab tab, const RepCon
 #pragma unroll
         for (int t = 0; t < 4; t++) {
           use[t] = l0 + t < lim;
-          mm[t] = use[t] ? krow[l0 + t] : 0;
+          mm[t] = use[t] ? src[l0 + t] : 0;
         }
       } else {
-        const int4 u = *reinterpret_cast<const int4 *>(krel + l0);
-        const int4 v = *reinterpret_cast<const int4 *>(krel + l0 + 2);
-        mm[0] = u.x; mm[1] = u.z; mm[2] = v.x; mm[3] = v.z;
-        use[0] = (u.y & kRelClose) != 0;
-        use[1] = l0 + 1 < lim && (u.w & kRelClose) != 0;
-        use[2] = l0 + 2 < lim && (v.y & kRelClose) != 0;
-        use[3] = l0 + 3 < lim && (v.w & kRelClose) != 0;
+        const int4 u = *reinterpret_cast<const int4 *>(src + l0);
+        mm[0] = u.x; mm[1] = u.y; mm[2] = u.z; mm[3] = u.w;
+#pragma unroll
+        for (int t = 0; t < 4; t++) use[t] = l0 + t < lim;
       }
       for (int t = 0; t < 4; t++) {
         if (!use[t]) continue;

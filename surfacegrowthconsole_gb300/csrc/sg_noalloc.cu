@@ -40,7 +40,7 @@ static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 // Carving of the scratch array (offsets in bytes, each 256-byte aligned).
 struct Carve {
   size_t rc, st, tabRep, tabStart, tileRep, tileStart, tileFirst, tileSum, cellCount, cellStart;
-  size_t cellOf, slot, tmpIdx, sortIdx, nn, sortPos, rho, dF, Fv, fric, nbl, nrl, rl, active, heavy, work, total;
+  size_t cellOf, slot, tmpIdx, sortIdx, nn, ns, sl, sortPos, rho, dF, Fv, fric, nbl, nrl, rl, active, heavy, work, total;
 };
 constexpr size_t up(size_t x) { return (x + 255) & ~size_t(255); }
 constexpr Carve carve() {
@@ -62,6 +62,8 @@ constexpr Carve carve() {
   c.tmpIdx = o; o += up(N * sizeof(int));
   c.sortIdx = o; o += up(N * sizeof(int));
   c.nn = o; o += up(N * sizeof(int));
+  c.ns = o; o += up(N * sizeof(int));
+  c.sl = o; o += up(N * kShortMax * sizeof(int));
   c.sortPos = o; o += up(N * sizeof(float4));
   c.rho = o; o += up(N * sizeof(float));
   c.dF = o; o += up(N * sizeof(float));
@@ -172,7 +174,8 @@ extern "C" int sg_compute_forces_noalloc(const sg_simparams *p, sg_float4 *d_pos
   int *tileFirst = (int *)(base + K.tileFirst), *tileSum = (int *)(base + K.tileSum);
   int *cellCount = (int *)(base + K.cellCount), *cellStart = (int *)(base + K.cellStart);
   int *cellOf = (int *)(base + K.cellOf), *slot = (int *)(base + K.slot), *tmpIdx = (int *)(base + K.tmpIdx);
-  int *sortIdx = (int *)(base + K.sortIdx), *nn = (int *)(base + K.nn);
+  int *sortIdx = (int *)(base + K.sortIdx), *nn = (int *)(base + K.nn), *ns = (int *)(base + K.ns);
+  int *sl = (int *)(base + K.sl);
   float4 *sortPos = (float4 *)(base + K.sortPos);
   float *rho = (float *)(base + K.rho), *dF = (float *)(base + K.dF), *Fv = (float *)(base + K.Fv);
   float *fric = (float *)(base + K.fric);
@@ -200,16 +203,16 @@ extern "C" int sg_compute_forces_noalloc(const sg_simparams *p, sg_float4 *d_pos
   k_scan_tile_prefix<<<1, 1024, 0, s>>>(rc, st, tileFirst, tileSum, 1);
   k_scan_final<<<nTiles, 256, 0, s>>>(tileTab, rc, st, cellCount, tileSum, cellStart, (int)p->blockSize, 1, active,
                                       heavy, work);
-  k_scatter<<<nAtomBlk, kBs, 0, s>>>(atomTab, rc, st, cellOf, slot, cellStart, tmpIdx, nn, nrl, 1);
+  k_scatter<<<nAtomBlk, kBs, 0, s>>>(atomTab, rc, st, cellOf, slot, cellStart, tmpIdx, nn, ns, nrl, 1);
   k_rank<<<nAtomBlk, kBs, 0, s>>>(atomTab, rc, st, cellOf, cellStart, tmpIdx, pos, sortIdx, sortPos, 1);
   const int rowStride = (p->iNebrMax + 3) & ~3;
-  k_build_nebr<<<256, kNebrWarps * 32, 0, s>>>(tileRep, active, heavy, work, rc, st, cellStart, sortPos, nn, nbl, nrl,
-                                               rl, rowStride, p->iNebrMax);
+  k_build_nebr<<<256, kNebrWarps * 32, 0, s>>>(tileRep, active, heavy, work, rc, st, cellStart, sortPos, nn, nbl, ns,
+                                               sl, nrl, rl, rowStride, p->iNebrMax);
   if (nMetalBlk) {
     k_rho<<<nMetalBlk, kBs, 0, s>>>(metalTab, rc, pos, nn, nbl, rho, dF, Fv, rowStride);
     k_force_metal<<<nMetalBlk, kBs, 0, s>>>(metalTab, rc, pos, acc, nn, nbl, dF, Fv, fric, rowStride);
   }
-  if (nCarbBlk) k_force_carbon<<<nCarbBlk, kBs, 0, s>>>(carbTab, rc, pos, acc, nn, nbl, nrl, rl, rowStride);
+  if (nCarbBlk) k_force_carbon<<<nCarbBlk, kBs, 0, s>>>(carbTab, rc, pos, acc, nn, nbl, ns, sl, nrl, rl, rowStride);
   e = cudaGetLastError();
   if (e != cudaSuccess) return sg_fail(SG_ERR_CUDA, "sg_compute_forces_noalloc launch: %s", cudaGetErrorString(e));
   int flags = 0;
