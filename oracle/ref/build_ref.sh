@@ -10,7 +10,8 @@
 # sm_11/sm_12_atomic_functions.h.  cudaThreadExit (removed from CUDA 13) maps to
 # cudaDeviceReset.  SurfaceGrowth.cpp's calls into the CUDA wrappers are renamed to
 # sgref_* stubs (the harness) so that parameter derivation, RNG and the result-file header
-# run without a GPU.  Usage: oracle/ref/build_ref.sh [REFERENCE_ROOT]
+# run without a GPU.  It also builds the reference kernels as cubins (end of file).
+# Usage: oracle/ref/build_ref.sh [REFERENCE_ROOT]
 set -euo pipefail
 REF=${1:-/root/reference}
 SRC="$REF/SurfaceGrowthConsole"
@@ -37,3 +38,10 @@ g++ -O1 -ffp-contract=off -fPIC -w $INC -c "$HERE/ref_host_harness.cpp" -o "$OUT
 g++ -shared -o "$OUT/libsgref_host.so" "$OUT/ref_cpp.o" "$OUT/ref_cu.o" "$OUT/ref_harness.o" \
   -L"$CUDA/lib64" -lcudart -Wl,-rpath,"$CUDA/lib64"
 echo "built $OUT/libsgref_host.so"
+# The reference's device code alone, unmodified, as sm_103a cubins for oracle/ref/refkern.cpp:
+# one without FMA contraction (the operation order the oracle and the PLAIN kernels follow,
+# for parity) and one with nvcc's default flags (the reference as shipped, for timing).
+NVFLAGS="-cubin -gencode arch=compute_103a,code=sm_103a -w $INC -DcudaThreadExit=cudaDeviceReset"
+"$CUDA/bin/nvcc" $NVFLAGS -fmad=false "$SRC/SurfaceGrowth.cu" -o "$OUT/sgref_kernels_nofma.cubin"
+"$CUDA/bin/nvcc" $NVFLAGS "$SRC/SurfaceGrowth.cu" -o "$OUT/sgref_kernels.cubin"
+echo "built $OUT/sgref_kernels_nofma.cubin $OUT/sgref_kernels.cubin"

@@ -1,5 +1,6 @@
 """In-tree build of the native parts: libsgmd.so (CUDA kernels + C ABI, sm_103a), the sgmd
-command-line driver, and the CPU oracle used by the tests (oracle/liboracle.so).
+command-line driver, and the test infrastructure: the CPU oracle (oracle/liboracle.so) and the
+loader of the reference kernels' cubin (oracle/librefkern.so).
 
 Each translation unit compiles in its own process, all in parallel; a unit is rebuilt only
 when a source or header it may include is newer than its object.  No CMake, one -gencode.
@@ -27,6 +28,7 @@ HOSTFLAGS = "-fPIC,-ffp-contract=off,-O2"
 
 LIBSGMD = LIBDIR / "libsgmd.so"
 LIBORACLE = ORACLE / "liboracle.so"
+LIBREFKERN = ORACLE / "librefkern.so"  # loads the reference kernels' cubin (tests only)
 SGMD_BIN = BINDIR / "sgmd"
 
 # (source, extra flags): the PLAIN kernels are compiled without FMA contraction so their
@@ -83,6 +85,12 @@ def build(verbose: bool = False, force: bool = False) -> None:
     if force or _stale(LIBORACLE, [oracle_src, ORACLE / "sg_oracle.h", INC / "sg_api.h", INC / "sg_simparams.h"]):
         jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fopenmp",
                      "-Wall", "-Wno-unused-function", str(oracle_src), "-o", str(LIBORACLE)])
+    refkern_src = ORACLE / "ref" / "refkern.cpp"
+    if refkern_src.exists() and (force or _stale(LIBREFKERN, [refkern_src, INC / "sg_simparams.h"])):
+        # linked against the driver stub; the real libcuda.so.1 resolves at load time
+        jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-Wall", "-I", str(INC),
+                     "-I", str(CUDA_HOME / "include"), str(refkern_src), "-o", str(LIBREFKERN),
+                     "-L" + str(CUDA_HOME / "lib64" / "stubs"), "-lcuda"])
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for cmd, fut in [(j, ex.submit(_run, j)) for j in jobs]:
             if verbose:
@@ -103,8 +111,9 @@ def build(verbose: bool = False, force: bool = False) -> None:
 def clean() -> None:
     shutil.rmtree(LIBDIR, ignore_errors=True)
     shutil.rmtree(BINDIR, ignore_errors=True)
-    if LIBORACLE.exists():
-        LIBORACLE.unlink()
+    for f in (LIBORACLE, LIBREFKERN):
+        if f.exists():
+            f.unlink()
 
 
 if __name__ == "__main__":
