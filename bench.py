@@ -11,8 +11,14 @@ LJ, graphene, reductions, thermostat, RDF/diffusion when due).
           whole state fits in the 129 MB L2.
   e2e   : the same metric through the public C ABI with host buffers: every step uploads the
           state (r, v, a) from pinned host memory, steps, and reads the step's thermo record.
-  roofline : the carbon-force kernel (the largest share of the step), algorithmic bytes per
-          launch / its mean duration in the timed region, against the measured HBM copy peak.
+  roofline : the neighbour-list build (the largest share of the step): its compulsory bytes per
+          launch / its mean duration in the timed region (CUDA events around it on the library's
+          stream), against the measured HBM copy peak.
+  step_roofline : the whole step's lower bound, sum over its parts of max(bytes / HBM peak,
+          FP32 flops / FP32 peak) with bytes and flops per atom and per interaction fixed in
+          advance (integrator 80 B + 20 flop per atom, sort 64 B per atom, density 20 B per
+          metal atom, forces 36 B per atom; 20 flop per EAM density pair, 60 per EAM force pair,
+          20 per LJ pair, 300 per carbon atom), interactions counted from the neighbour lists.
   cpu_baseline : the FP32 CPU restatement of the same step on all host cores (the reference has
           no CPU implementation of this path).
 --impl reference times that CPU restatement on the same workload and prints its own line.
@@ -112,15 +118,47 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def carbon_force_bytes(p, nn: np.ndarray, ns: np.ndarray) -> float:
-    """Compulsory bytes of one carbon-force launch: per carbon atom its position (16), list
-    length (4), list entries (4 each), own short-list length + entries, the acceleration and
-    energy it writes (16 + 4); plus one read of every metal position gathered (16)."""
-    c = slice(p.nMolMe, p.nMol)
-    nc = p.nMol - p.nMolMe
-    entries = float(nn[c].sum())
-    short = float(np.clip(ns[c], 0, 8).sum())
-    return nc * (16 + 4 + 4 + 16 + 4) + 4 * entries + 4 * short + 16 * p.nMolMe
+FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12  # 152 SMs x 128 FP32 lanes x FMA at 2.07 GHz
+
+
+def pair_distances(p, r, nn, nbl):
+    """Ordered pairs (i, k) of the neighbour list with their current squared distances."""
+    i = np.repeat(np.arange(p.nMol), nn)
+    k = np.concatenate([nbl[:nn[a], a] for a in range(p.nMol)]) if p.nMol else np.zeros(0, int)
+    L = np.array([p.region.x, p.region.y, p.region.z], np.float64)
+    d = r[i, :3].astype(np.float64) - r[k, :3].astype(np.float64)
+    d -= L * np.round(d / L)
+    return i, k, (d * d).sum(1)
+
+
+def nebr_build_bytes(p, nn, i, k, rr) -> float:
+    """Compulsory bytes of one list-build launch: every position read once (16 per atom, sorted
+    copy), the cell starts (4 per cell), the list lengths written (nn, close and relevant list:
+    12 per atom), the entries written (4 per list entry, 4 per close entry, 8 per relevant
+    entry of a carbon atom)."""
+    ncells = p.cells.x * p.cells.y * p.cells.z
+    rs = (p.rCutC + p.rNebrShell) ** 2
+    carbon = i >= p.nMolMe
+    close = carbon & (rr < rs)
+    rel = carbon & ((k < p.nMolMe) | (rr < rs))
+    return 16.0 * p.nMol + 4.0 * ncells + 12.0 * p.nMol + 4.0 * nn.sum() + 4.0 * close.sum() + 8.0 * rel.sum()
+
+
+def step_lower_bound_ms(p, i, k, rr, hbm_gbs):
+    """The step's roofline time (see the module docstring)."""
+    bw = hbm_gbs * 1e9
+    fl = FP32_NOMINAL_TFLOPS * 1e12
+    m = p.nMolMe
+    mm = (i < m) & (k < m)
+    eam = int((mm & (rr < p.rrCutEam)).sum())
+    lj = int((((i < m) ^ (k < m)) & (rr < p.rrCutLJ)).sum())  # metal-carbon, either order
+    parts = [(80.0 * p.nMol, 20.0 * p.nMol),                     # integrator
+             (64.0 * p.nMol, 0.0),                               # counting sort
+             (20.0 * m, 20.0 * eam),                             # density
+             (36.0 * p.nMol, 60.0 * eam + 20.0 * lj + 300.0 * (p.nMol - m))]  # forces
+    t = sum(max(b / bw, f / fl) for b, f in parts)
+    return 1e3 * t, {"eam_pairs": eam, "lj_pairs": lj, "carbon_atoms": p.nMol - m,
+                     "bytes": sum(b for b, _ in parts), "flops": sum(f for _, f in parts)}
 
 
 def cpu_baseline(p, r, v, sample_steps: int):
@@ -227,24 +265,30 @@ def main():
     else:
         atoms_all = float(p.nMol)
     value = atoms_all * args.steps / total_s
-    ph = np.mean(np.array(phases), axis=0)  # integrate, rebuild, metal chain, carbon, forces, reduce, extra
+    # integrate, rebuild, metal chain, carbon, forces, reduce, extra, list build
+    ph = np.mean(np.array(phases), axis=0)
 
-    # roofline of the carbon-force kernel
-    nn, _ = sim.nebr()
-    ns = np.zeros(p.nMol, np.int32)  # short-list lengths are not read back; bound by 3 per atom
-    ns[p.nMolMe:] = 3
-    bytes_launch = carbon_force_bytes(p, nn, ns)
+    # roofline of the neighbour-list build (the largest kernel of the step)
+    nn, nbl = sim.nebr()
+    rnow, _, _ = sim.get_state()
+    pi, pk, prr = pair_distances(p, rnow, nn, nbl)
+    bytes_launch = nebr_build_bytes(p, nn, pi, pk, prr)
     peak, peak_kind = measured_peaks()
-    achieved = bytes_launch / (ph[3] * 1e-3) / 1e9
-    roof = {"bound": "hbm", "kernel": "k_force_carbon", "achieved": achieved, "peak": peak, "unit": "GB/s",
+    achieved = bytes_launch / (ph[7] * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": "k_build_nebr", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
-            "algorithmic_bytes_per_launch": bytes_launch, "mean_launch_ms": float(ph[3]),
-            "phase_ms": {"integrate": float(ph[0]), "rebuild": float(ph[1]), "metal_chain_side_stream": float(ph[2]),
-                         "carbon_forces": float(ph[3]), "forces_fork_to_join": float(ph[4]), "reduce": float(ph[5]),
-                         "rdf_shear": float(ph[6])}}
-    prof = ROOT / "profiles" / "bench_carbon_force_traffic.json"
+            "algorithmic_bytes_per_launch": bytes_launch, "mean_launch_ms": float(ph[7]),
+            "phase_ms": {"integrate": float(ph[0]), "rebuild": float(ph[1]), "list_build": float(ph[7]),
+                         "metal_chain_side_stream": float(ph[2]), "carbon_forces": float(ph[3]),
+                         "forces_fork_to_join": float(ph[4]), "reduce": float(ph[5]), "rdf_shear": float(ph[6])}}
+    prof = ROOT / "profiles" / "k_build_nebr_traffic.json"
     if prof.exists():
         roof["traffic"] = json.loads(prof.read_text()).get("dram_bytes_per_launch")
+    t_lb, counts = step_lower_bound_ms(p, pi, pk, prr, peak)
+    step_ms = 1e3 * total_s / args.steps
+    step_roof = {"lower_bound_ms": t_lb, "measured_ms": step_ms, "frac": t_lb / step_ms,
+                 "hbm_peak_gbs": peak, "fp32_peak_tflops": FP32_NOMINAL_TFLOPS, "fp32_peak_kind": "nominal",
+                 **counts}
 
     # end to end through the C ABI with pinned host buffers
     hr = torch.empty((p.nMol, 4), dtype=torch.float32, pin_memory=True).numpy()
@@ -278,7 +322,8 @@ def main():
                                        "GPU, 700 K, dt 1 fs, lists rebuilt every step, RDF + diffusion on",
                            "atoms_per_gpu": p.nMol, "mode": args.mode, "l2": "flushed between timed steps",
                            "parallelism": f"replicas x{world}"},
-                "clocks": clk.summary(), "gpu_launches": launches, "roofline": roof, "e2e": e2e,
+                "clocks": clk.summary(), "gpu_launches": launches, "roofline": roof,
+                "step_roofline": step_roof, "e2e": e2e,
                 "cpu_baseline": cpu}
         print(json.dumps(line, default=float))
     sim.close()

@@ -119,10 +119,11 @@ int sg_step(sg_ctx *ctx, int nsteps);
 int sg_step_async(sg_ctx *ctx, int nsteps);
 /* Kernel launches one step issues (for the step variant that ran last). */
 int sg_kernels_per_step(sg_ctx *ctx);
-/* With phase_timing on: durations in ms of the phases of the last step: integrate, rebuild,
- * metal chain (density, metal forces, metal centre-of-mass velocity; runs beside the carbon
- * pass), carbon pass, forces (fork to join), reduce, extra (shear/RDF).  Returns the number
- * of phases (7), or minus a status code. */
+/* With phase_timing on: durations in ms of the phases of the last step: integrate, rebuild
+ * (counting sort + neighbour-list build), metal chain (density, metal forces, metal
+ * centre-of-mass velocity; runs beside the carbon pass), carbon pass, forces (fork to join),
+ * reduce, extra (shear/RDF), neighbour-list build alone.  Returns the number of phases (8), or
+ * minus a status code. */
 int sg_get_phase_times(sg_ctx *ctx, float *ms, int n);
 
 typedef struct sg_thermo {

@@ -466,6 +466,7 @@ static int enqueueRebuild(sg_ctx *c, int force) {
                                                  c->tmpIdx, c->nn, c->ns, c->nrl, fr);
   k_rank<<<c->atomTab.n, 128, 0, c->stream>>>(c->atomTab.view(), c->rc, c->st, c->cellOf, c->cellStart, c->tmpIdx,
                                               c->pos, c->sortIdx, c->sortPos, fr);
+  if (c->opt.phase_timing) cudaEventRecordWithFlags(c->phaseEv[8], c->stream, cudaEventRecordExternal);
   k_build_nebr<<<c->nebrGrid, kNebrWarps * 32, 0, c->stream>>>(c->tileTab.rep, c->activeCells, c->heavyItems,
                                                                 c->nebrWork, c->rc, c->st, c->cellStart, c->sortPos,
                                                                 c->nn, c->nbl, c->ns, c->sl, c->nrl, c->rl,
@@ -675,10 +676,10 @@ extern "C" int sg_get_phase_times(sg_ctx *c, float *ms, int n) {
   if (!c || !c->opt.phase_timing) return -sg_fail(SG_ERR_UNSUPPORTED, "phase_timing is off");
   cudaError_t e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return -sg_fail(SG_ERR_CUDA, "%s", cudaGetErrorString(e));
-  // integrate, rebuild, metal chain (side stream), carbon pass, forces (fork to join),
-  // reduce, extra
-  const int from[7] = {0, 1, 2, 2, 2, 4, 5}, to[7] = {1, 2, 7, 3, 4, 5, 6};
-  const int np = 7;
+  // integrate, rebuild (sort + list build), metal chain (side stream), carbon pass, forces
+  // (fork to join), reduce, extra, list build alone
+  const int from[8] = {0, 1, 2, 2, 2, 4, 5, 8}, to[8] = {1, 2, 7, 3, 4, 5, 6, 2};
+  const int np = 8;
   for (int k = 0; k < np && k < n; k++) {
     float t = 0.f;
     e = cudaEventElapsedTime(&t, c->phaseEv[from[k]], c->phaseEv[to[k]]);

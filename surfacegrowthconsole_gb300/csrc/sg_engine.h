@@ -61,7 +61,7 @@ struct sg_ctx {
   std::vector<sg_prop> oneStep;  // per replica, host-accumulated step times
   void *mixed = nullptr;         // MIXED-mode buffers (sg_kernels_mixed.cu)
   float *stage = nullptr;        // 3 floats per atom: host float3 arrays in transit
-  cudaEvent_t phaseEv[8] = {};   // phase boundaries of a step (phase_timing)
+  cudaEvent_t phaseEv[9] = {};   // phase boundaries of a step (phase_timing)
   cudaStream_t side = nullptr;   // second stream: the metal force chain runs beside the carbon pass
   cudaEvent_t evFork = nullptr, evJoin = nullptr;
   int launchCount = 0;           // kernel launches counted while enqueueing a step

@@ -169,7 +169,8 @@ class Simulation:
         return lib().sg_kernels_per_step(self._h)
 
     def phase_times(self) -> np.ndarray:
-        """ms of the phases of the last step: integrate, rebuild, forces, reduce, extra."""
+        """ms of the phases of the last step: integrate, rebuild (sort + list build), metal chain,
+        carbon pass, forces (fork to join), reduce, extra (shear/RDF), list build alone."""
         out = np.zeros(8, np.float32)
         n = lib().sg_get_phase_times(self._h, _ptr(out), 8)
         if n < 0:
