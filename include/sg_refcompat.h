@@ -46,5 +46,10 @@ char *DoComputationsW(sg_float4 *hr, sg_float3 *hv, sg_float3 *ha, sg_simparams 
 
 #ifdef __cplusplus
 }
+/* The reference's host program also calls AccumProps (C++ linkage; SurfaceGrowth.cu:2659-2731,
+ * called from SurfaceGrowth.cpp:417): averages of the step properties, icode 0 zero / 1 add /
+ * 2 average.  Exported with the reference's signature; SimParams is its name for sg_simparams. */
+struct SimParams;
+void AccumProps(int icode, SimParams *hparams);
 #endif
 #endif /* SG_REFCOMPAT_H */

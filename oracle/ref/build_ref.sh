@@ -45,3 +45,12 @@ NVFLAGS="-cubin -gencode arch=compute_103a,code=sm_103a -w $INC -DcudaThreadExit
 "$CUDA/bin/nvcc" $NVFLAGS -fmad=false "$SRC/SurfaceGrowth.cu" -o "$OUT/sgref_kernels_nofma.cubin"
 "$CUDA/bin/nvcc" $NVFLAGS "$SRC/SurfaceGrowth.cu" -o "$OUT/sgref_kernels.cubin"
 echo "built $OUT/sgref_kernels_nofma.cubin $OUT/sgref_kernels.cubin"
+# The reference's host program itself (SurfaceGrowth.cpp, unchanged) linked against libsgmd.so
+# instead of its own SurfaceGrowth.cu: the drop-in check of the C ABI (tests/test_abi.py).
+SGLIB="$HERE/../../surfacegrowthconsole_gb300/lib"
+if [ -f "$SGLIB/libsgmd.so" ]; then
+  g++ -O1 -ffp-contract=off -w $INC -D_tmain=main -c "$SRC/SurfaceGrowth.cpp" -o "$OUT/sugr_main.o"
+  g++ "$OUT/sugr_main.o" -o "$OUT/sugr_on_sgmd" -L"$SGLIB" -lsgmd -Wl,-rpath,"$SGLIB" \
+    -L"$CUDA/lib64" -lcudart -Wl,-rpath,"$CUDA/lib64"
+  echo "built $OUT/sugr_on_sgmd"
+fi

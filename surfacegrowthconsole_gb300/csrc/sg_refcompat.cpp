@@ -76,3 +76,12 @@ extern "C" char *DoComputationsW(sg_float4 *hr, sg_float3 *hv, sg_float3 *ha, sg
   sg_destroy(ctx);
   return nullptr;
 }
+
+// SurfaceGrowth.cpp also calls one host function of SurfaceGrowth.cu besides the wrappers:
+// AccumProps (C++ linkage, SurfaceGrowth.cu:2659-2731; called from SetupJob,
+// SurfaceGrowth.cpp:417).  Exported here under the reference's name and signature so that the
+// reference's host program links against this library unchanged.
+struct SimParams;
+void AccumProps(int icode, SimParams *hparams) {
+  sg_accum_props(reinterpret_cast<sg_simparams *>(hparams), icode);
+}
