@@ -1428,38 +1428,85 @@ __global__ void k_rdf(BlockTab tab, const RepConst *__restrict__ rc, RepState *s
   }
 }
 
-// All-pairs metal-metal histogram with minimum image (an extension beyond the stencil-limited
-// reference RDF): tiles of 128 atoms staged in shared memory.
-__global__ void k_rdf_ext(const RepConst *__restrict__ rc, const float4 *__restrict__ pos,
-                          const int *__restrict__ tileRep, const int *__restrict__ tileStart,
-                          unsigned long long *__restrict__ hist, int nbins, float range) {
+__device__ __forceinline__ void blockBox(float4 p, bool valid, float *out6, float (*red)[6]) {
+  // min x, y, z and max x, y, z of the valid points of a 128-thread block
+  float v[6] = {valid ? p.x : 3.4e38f, valid ? p.y : 3.4e38f, valid ? p.z : 3.4e38f,
+                valid ? p.x : -3.4e38f, valid ? p.y : -3.4e38f, valid ? p.z : -3.4e38f};
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int c = 0; c < 6; c++) {
+      const float w = __shfl_xor_sync(0xffffffffu, v[c], o);
+      v[c] = (c < 3) ? fminf(v[c], w) : fmaxf(v[c], w);
+    }
+  const int wid = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0)
+    for (int c = 0; c < 6; c++) red[wid][c] = v[c];
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    float m = red[0][threadIdx.x];
+    for (int w = 1; w < 4; w++) m = (threadIdx.x < 3) ? fminf(m, red[w][threadIdx.x]) : fmaxf(m, red[w][threadIdx.x]);
+    out6[threadIdx.x] = m;
+  }
+}
+
+// RDF extension: all metal pairs of a replica within `range` into nbins (0-15 A / 300 bins in
+// the production configuration), checked against the FP64 all-pairs oracle.  Unordered pairs,
+// each counted twice (the FP32 distance of (i, k) and (k, i) is the same number).  Blocks of
+// 128 atoms against tiles of 128 atoms; a tile whose minimum-image bounding-box gap to the
+// block exceeds the range (with a margin far above rounding) is skipped whole: metal atoms are
+// numbered cluster by cluster, so most tiles of a multi-cluster system drop out.
+__global__ void __launch_bounds__(128) k_rdf_ext(const RepConst *__restrict__ rc, const float4 *__restrict__ pos,
+                                                 const int *__restrict__ tileRep,
+                                                 const int *__restrict__ tileStart,
+                                                 unsigned long long *__restrict__ hist, int nbins, float range) {
   extern __shared__ unsigned eh[];
   __shared__ float4 tileB[128];
+  __shared__ float boxA[6], boxB[6];
+  __shared__ float red[4][6];
   const int rep = tileRep[blockIdx.x];
   const RepConst &P = rc[rep];
   for (int b = threadIdx.x; b < nbins; b += blockDim.x) eh[b] = 0u;
-  const int i = tileStart[blockIdx.x] + threadIdx.x;
-  const int mb = P.atomOff, me = P.atomOff + P.nMolMe;
-  const float4 A = (i < me) ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const int a0 = tileStart[blockIdx.x];
+  const int i = a0 + threadIdx.x;
+  const int me = P.atomOff + P.nMolMe;
+  const bool haveA = i < me;
+  const float4 A = haveA ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float L[3] = {P.region[0], P.region[1], P.region[2]};
+  const float invL[3] = {1.f / L[0], 1.f / L[1], 1.f / L[2]};
   const float scale = nbins / range;
   const float r2max = range * range;
-  for (int j0 = mb; j0 < me; j0 += 128) {
+  blockBox(A, haveA, boxA, red);
+  for (int j0 = a0; j0 < me; j0 += 128) {
     __syncthreads();
-    if (j0 + threadIdx.x < me) tileB[threadIdx.x] = pos[j0 + threadIdx.x];
+    const bool haveB = j0 + threadIdx.x < me;
+    const float4 Bt = haveB ? pos[j0 + threadIdx.x] : make_float4(0.f, 0.f, 0.f, 0.f);
+    tileB[threadIdx.x] = Bt;
+    blockBox(Bt, haveB, boxB, red);
     __syncthreads();
-    if (i < me) {
+    // skip the tile when its boxes are farther apart than the range: per axis, no pair can be
+    // closer in the minimum image than the folded centre distance minus both half extents
+    float gap2 = 0.f;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const float hA = 0.5f * (boxA[3 + c] - boxA[c]), hB = 0.5f * (boxB[3 + c] - boxB[c]);
+      float d = 0.5f * (boxA[3 + c] + boxA[c]) - 0.5f * (boxB[3 + c] + boxB[c]);
+      d -= L[c] * rintf(d * invL[c]);
+      const float g = fmaxf(fabsf(d) - hA - hB - 0.01f, 0.f);
+      gap2 += g * g;
+    }
+    if (gap2 <= r2max && haveA) {
       const int nj = min(128, me - j0);
-      for (int jj = 0; jj < nj; jj++) {
-        if (j0 + jj == i) continue;
+      for (int jj = (j0 == a0) ? threadIdx.x + 1 : 0; jj < nj; jj++) {
         const float4 B = tileB[jj];
         float dx = A.x - B.x, dy = A.y - B.y, dz = A.z - B.z;
-        dx -= P.region[0] * rintf(dx / P.region[0]);
-        dy -= P.region[1] * rintf(dy / P.region[1]);
-        dz -= P.region[2] * rintf(dz / P.region[2]);
+        dx -= L[0] * rintf(dx * invL[0]);
+        dy -= L[1] * rintf(dy * invL[1]);
+        dz -= L[2] * rintf(dz * invL[2]);
         const float rr = dx * dx + dy * dy + dz * dz;
         if (rr < r2max) {
           const int bin = (int)(sqrtf(rr) * scale);
-          if (bin < nbins) atomicAdd(&eh[bin], 1u);
+          if (bin < nbins) atomicAdd(&eh[bin], 2u);
         }
       }
     }
