@@ -22,6 +22,10 @@ LJ, graphene, reductions, thermostat, RDF/diffusion when due).
   cpu_baseline : the FP32 CPU restatement of the same step on all host cores (the reference has
           no CPU implementation of this path).
 --impl reference times that CPU restatement on the same workload and prints its own line.
+--workload batched: the batched form instead (256 independent replicas, graphene U[1,000, 20,000]
+C, one Ni cluster of U{50..2,000} atoms, T U[300, 1,500] K, lists rebuilt by the reference's
+rule) stepped together in one context; the line adds the same replicas run one by one, each in
+its own context, for comparison.
 Multi-GPU (torchrun): replicas only -- each rank runs its own seeded system, no collective on
 the data path; value is the sum over ranks over the slowest rank's time.
 """
@@ -57,6 +61,8 @@ def parse():
     ap.add_argument("--cpu-sample-steps", type=int, default=300)
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="production", choices=["production", "batched"])
+    ap.add_argument("--replicas", type=int, default=256)
     return ap.parse_args()
 
 
@@ -205,6 +211,71 @@ def run_reference(args, rank: int, world: int):
     print(json.dumps(line, default=float))
 
 
+def run_batched(args, rank: int, world: int, local: int):
+    """The batched form: all replicas in one context, against the same replicas one by one."""
+    import torch
+    from surfacegrowthconsole_gb300 import workloads
+    from surfacegrowthconsole_gb300.engine import Simulation
+    reps = workloads.batched(args.replicas, seed=4 + rank)
+    plist = [w[0] for w in reps]
+    r = np.concatenate([w[1] for w in reps])
+    v = np.concatenate([w[2] for w in reps])
+    natoms = int(sum(q.nMol for q in plist))
+    stream = torch.cuda.Stream(device=local)
+    sim = Simulation(plist, device=local, stream=stream.cuda_stream)
+    sim.set_state(r, v, np.zeros((natoms, 3), np.float32))
+    sim.step(args.warmup)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    launches = 0
+    with Clocks(local) as clk:
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+            for _ in range(args.steps):
+                sim.step_async(1)
+                launches += sim.kernels_per_step()
+            ev1.record(stream)
+        torch.cuda.synchronize()
+    sim.step(0)
+    t_batched = ev0.elapsed_time(ev1) * 1e-3
+    rebuilds = int(sum(sim.thermo(k).rebuilds for k in range(len(plist))))
+    sim.close()
+    # the same replicas one by one, each in its own context (fewer steps: 256 contexts)
+    k1 = max(1, min(args.steps, 20))
+    t_one = 0.0
+    atoms_one = 0
+    for w in reps:
+        q, rq, vq = w
+        s1 = Simulation(q, device=local, stream=stream.cuda_stream)
+        s1.set_state(rq, vq, np.zeros((q.nMol, 3), np.float32))
+        s1.step(3)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+            s1.step_async(k1)
+            ev1.record(stream)
+        torch.cuda.synchronize()
+        s1.step(0)
+        t_one += ev0.elapsed_time(ev1) * 1e-3
+        atoms_one += q.nMol
+        s1.close()
+    value = natoms * args.steps / t_batched
+    one = atoms_one * k1 / t_one
+    if rank == 0:
+        line = {"metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_batched / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded replicas: graphene + one fcc Ni cluster each, Maxwell velocities)",
+                "config": {"workload": f"{len(plist)} replicas, {natoms} atoms in all, graphene 1,000-20,000 C + "
+                                       "one Ni cluster of 50-2,000 atoms each, 300-1,500 K, lists rebuilt by the "
+                                       "reference's rule", "replicas": len(plist), "atoms": natoms,
+                           "l2": "state larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
+                "clocks": clk.summary(), "gpu_launches": launches, "rebuilds_all_replicas": rebuilds,
+                "one_by_one": {"value": one, "unit": "atom-steps/s", "steps": k1,
+                               "ms_all_replicas_per_step": 1e3 * t_one / k1}}
+        print(json.dumps(line, default=float))
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -220,6 +291,11 @@ def main():
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
+    if args.workload == "batched":
+        run_batched(args, rank, world, local)
+        if dist:
+            dist.destroy_process_group()
+        return
     from surfacegrowthconsole_gb300 import MODE_MIXED, MODE_PLAIN
     from surfacegrowthconsole_gb300.engine import Simulation
 

@@ -41,7 +41,8 @@ enum {
     SG_ERR_NO_DEVICE = 4,      /* no CUDA device, or not an sm_103 device */
     SG_ERR_NEBR_OVERFLOW = 5,  /* an atom had more than iNebrMax neighbours (list truncated) */
     SG_ERR_CELL_RANGE = 6,     /* an atom mapped outside the cell grid (left out of the lists) */
-    SG_ERR_RDF_RANGE = 7,      /* an RDF bin index reached sizeHistRdf (sample dropped) */
+    SG_ERR_RDF_RANGE = 7,      /* reserved: an RDF bin index that rounds to sizeHistRdf is dropped and
+                                  counted in sg_diag.rdf_range, not reported */
     SG_ERR_TIMEOUT = 8,        /* a bounded device-side wait gave up */
     SG_ERR_IO = 9,             /* output file could not be written */
     SG_ERR_UNSUPPORTED = 10,   /* feature not available in this mode */
@@ -178,7 +179,8 @@ typedef struct sg_diag {
     int nebr_overflow;       /* atoms whose list was truncated */
     int cell_range;          /* atoms left out of the grid */
     int cell_overflow;       /* cells above blockSize atoms */
-    int rdf_range;           /* RDF samples dropped at the top bin */
+    int rdf_range;           /* RDF samples dropped at the top bin (the reference writes them one
+                                element past its histogram) */
     int timeouts;            /* bounded waits that gave up */
     int reserved[9];
 } sg_diag;

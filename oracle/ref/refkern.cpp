@@ -152,8 +152,10 @@ int rk_setup(const sg_simparams *p) {
   CU(cuMemAlloc(&mic, ncells * 4));
   if (p->iRegime != 0 && p->nMolMe != 0) CU(cuMemAlloc(&fric, (size_t)p->nMolMe * 4));
   if (p->bRdf) {
-    CU(cuMemAlloc(&hist, (size_t)p->sizeHistRdf * 4));
-    CU(cuMemsetD32(hist, 0, p->sizeHistRdf));
+    // one spare element: EvalRdfK adds a pair whose bin index rounds up to sizeHistRdf one
+    // element past the histogram (SurfaceGrowth.cu:1988-1989)
+    CU(cuMemAlloc(&hist, ((size_t)p->sizeHistRdf + 1) * 4));
+    CU(cuMemsetD32(hist, 0, p->sizeHistRdf + 1));
   }
   return 0;
 }

@@ -1422,10 +1422,10 @@ __global__ void k_rdf(BlockTab tab, const RepConst *__restrict__ rc, RepState *s
   unsigned *h = hist + (size_t)rep * histStride;
   for (int b = threadIdx.x; b < nb; b += blockDim.x)
     if (shist[b]) atomicAdd(&h[b], shist[b]);
-  if (dropped) {
-    atomicAdd(&S->rdfRange, dropped);
-    setFlag(S, 7 /*SG_ERR_RDF_RANGE*/);
-  }
+  // a pair just inside rangeRdf whose bin index rounds up to sizeHistRdf: the reference adds it
+  // one element past its histogram (SurfaceGrowth.cu:1988-1989), outside every printed bin; it
+  // is dropped here and only counted (sg_diag.rdf_range), not reported as an error
+  if (dropped) atomicAdd(&S->rdfRange, dropped);
 }
 
 __device__ __forceinline__ void blockBox(float4 p, bool valid, float *out6, float (*red)[6]) {
