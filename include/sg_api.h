@@ -71,7 +71,7 @@ typedef struct sg_options {
     void *stream;          /* cudaStream_t to run on; NULL: the context creates its own */
     int rdf_ext_bins;      /* >0: also accumulate an all-pairs metal-metal RDF */
     float rdf_ext_range;   /* its range, dimensionless length */
-    int eam_table_knots;   /* MIXED: knots per tabulated EAM function (0: 2048) */
+    int eam_table_knots;   /* MIXED: knots of the tabulated EAM pair functions (0: 4096; -1: analytic) */
     int tune_force_tpa;    /* threads per atom in the carbon force pass (0: auto) */
     int tune_block;        /* block size of the per-atom passes (0: auto) */
     int phase_timing;      /* 1: record CUDA events between the phases of every step */

@@ -78,10 +78,13 @@ struct RepConst {
   // diffusion
   int nValDiffuse, nBuffDiffuse, stepDiffuse, limitDiffuseAv;
   int stepAvg;
-  // MIXED mode: tabulated EAM (offset of this replica's tables in the table buffer)
+  // MIXED mode: tabulated EAM pair functions, knots r_k = rTabMin + k * rTabH, k < nTab,
+  // at tabOff in the table buffer (nTab == 0: analytic)
   int tabOff;
-  float rTabMin, rTabInv, rhoTabInv;
+  float rTabMin, rTabInv, rTabH;
   int nTab;
+  // MIXED mode: FP64 reciprocals for the step control (no FP64 division on the device)
+  double invNMol, invNMolMe, invRegion[3];
 };
 
 struct RepState {
@@ -173,6 +176,24 @@ __device__ __forceinline__ float minImg(float d, float L) {
   if (d >= 0.5f * L) d -= L;
   else if (d < -0.5f * L) d += L;
   return d;
+}
+
+// The step control of a replica runs in the last block of its reduction: it copies the replica's
+// RepState into shared memory with all threads, works on that copy (its single-thread scalar
+// code then sees shared-memory latency instead of L2 latency) and writes it back.  No other
+// kernel touches the state meanwhile: the reduction is the only kernel of the step running.
+static_assert(sizeof(RepState) % 4 == 0, "RepState is copied as 32-bit words");
+__device__ __forceinline__ void stateToShared(const RepState *g, RepState *s) {
+  const int *src = reinterpret_cast<const int *>(g);
+  int *dst = reinterpret_cast<int *>(s);
+  for (int i = threadIdx.x; i < (int)(sizeof(RepState) / 4); i += blockDim.x) dst[i] = __ldcg(src + i);
+  __syncthreads();
+}
+__device__ __forceinline__ void stateFromShared(const RepState *s, RepState *g) {
+  __syncthreads();
+  const int *src = reinterpret_cast<const int *>(s);
+  int *dst = reinterpret_cast<int *>(g);
+  for (int i = threadIdx.x; i < (int)(sizeof(RepState) / 4); i += blockDim.x) dst[i] = src[i];
 }
 
 __device__ __forceinline__ void setFlag(RepState *st, int code) {

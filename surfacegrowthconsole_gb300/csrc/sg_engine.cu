@@ -135,6 +135,9 @@ static RepConst makeConst(const sg_simparams &p) {
   P.stepDiffuse = p.stepDiffuse > 0 ? p.stepDiffuse : 1;
   P.limitDiffuseAv = p.limitDiffuseAv;
   P.stepAvg = p.stepAvg > 0 ? p.stepAvg : 1;
+  P.invNMol = 1.0 / p.nMol;
+  P.invNMolMe = p.nMolMe ? 1.0 / p.nMolMe : 0.0;
+  P.invRegion[0] = 1.0 / p.region.x; P.invRegion[1] = 1.0 / p.region.y; P.invRegion[2] = 1.0 / p.region.z;
   return P;
 }
 

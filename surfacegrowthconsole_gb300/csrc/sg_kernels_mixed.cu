@@ -1,8 +1,645 @@
-// sg_kernels_mixed.cu - MIXED-mode kernels (placeholder until the mixed path lands).
-#include "sg_engine.h"
+// sg_kernels_mixed.cu - the MIXED ("chosen") form of the step: the same model as PLAIN (same
+// potentials, same neighbour-list semantics, the same force passes from sg_forces.cuh), with the
+// numerics changed where they decide long-run accuracy and speed:
+//  - positions are a hi/lo pair of floats: the drift r += dt v and the periodic wrap are done
+//    with error-free transformations (TwoSum), so the position keeps ~48 significant bits
+//    instead of rounding every step's tiny displacement to 24; forces and lists read the hi
+//    word, which is the position rounded to float;
+//  - FMA contraction is on (this unit is compiled without -fmad=false);
+//  - the step's reductions (kinetic and potential energy, impulse, centre of mass, friction,
+//    virial sum r.F) sum 64 atoms per warp in FP32 (the centre of mass as a double-float of
+//    the hi/lo positions) and everything above in FP64, in a fixed order (warp totals, block
+//    partials, one block over the partials): about 1e-9 relative on the totals; the thermostat
+//    factor is computed in FP64, the diffusion MSD accumulators are FP64; the centre-of-mass velocity that the regime-2 kinetic energy subtracts comes out
+//    of the same pass (sum m (vx - c)^2 = m (sum vx^2 - 2 c sum vx + n c^2)), so the separate
+//    centre-of-mass-velocity launch of PLAIN is gone;
+//  - the EAM pair functions phi(r), f(r) and their derivatives come from cubic Hermite tables
+//    (cubic pieces on 1,024 intervals from 0.6 r_e to the cutoff, coefficients built in FP64
+//    from the analytic forms) instead of
+//    two expf and four powf per pair; the embedding function stays analytic (once per atom);
+//  - particle size is the true extent of the metal (PLAIN keeps the reference's zero padding,
+//    which puts 0 inside every min/max).
+#include <cuda_runtime.h>
 
-int sg_mixed_init(sg_ctx *) { return sg_fail(SG_ERR_UNSUPPORTED, "MIXED mode is not built yet"); }
-void sg_mixed_free(sg_ctx *) {}
-int sg_mixed_enqueue_integrate(sg_ctx *, int) { return SG_ERR_UNSUPPORTED; }
-int sg_mixed_enqueue_forces(sg_ctx *) { return SG_ERR_UNSUPPORTED; }
-int sg_mixed_enqueue_reduce(sg_ctx *, int) { return SG_ERR_UNSUPPORTED; }
+#include <vector>
+
+#include "sg_device.cuh"
+#include "sg_engine.h"
+#include "sg_kernels.h"
+
+#include <cmath>
+
+#define SG_KN(name) name##_mixed
+#define SG_EAM_TABLE
+#include "sg_forces.cuh"
+
+namespace sg {
+
+// Values the MIXED step reduction accumulates in FP64 per block.
+enum MixAcc {
+  MA_VSUM_X = 0, MA_VSUM_Y, MA_VSUM_Z,  // impulse (metal x mass-scaled, as the reference)
+  MA_VV_C,                              // carbon sum v^2
+  MA_VVYZ_M,                            // metal sum vy^2 + vz^2
+  MA_VX2_M, MA_VX_M,                    // metal sum vx^2, sum vx
+  MA_VY_M, MA_VZ_M,                     // metal sum vy, vz (centre-of-mass velocity)
+  MA_USUM,                              // sum U
+  MA_CM_X, MA_CM_Y, MA_CM_Z,            // metal sum r (hi + lo)
+  MA_FRICT,                             // friction sum
+  MA_VIRIAL,                            // sum r . F
+  kMixAcc
+};
+enum MixMax { MM_VVMAX = 0, MM_MIN_X, MM_MIN_Y, MM_MIN_Z, MM_MAX_X, MM_MAX_Y, MM_MAX_Z, kMixMax };
+
+struct MixedBufs {
+  double *part64 = nullptr;  // [reduction blocks][kMixAcc]
+  float *partF = nullptr;    // [reduction blocks][kMixMax]
+  double *diff64 = nullptr;  // per replica: nB x 6 (orgR, rTrue), nB x nV (rr), nV (av)
+  size_t *dDiffOff64 = nullptr;
+  std::vector<size_t> diffOff64;
+  unsigned *counter = nullptr;  // per replica: blocks done
+  float4 *eamTab = nullptr;     // per replica nTab intervals x 2: cubic coefficients of phi, of f
+};
+
+__device__ __forceinline__ void twoSum(float a, float b, float &s, float &e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+// hi += d exactly into (hi, lo), then renormalise so that hi is the pair rounded to float
+__device__ __forceinline__ void addHiLo(float &hi, float &lo, float d) {
+  float s, e;
+  twoSum(hi, d, s, e);
+  lo += e;
+  const float t = s + lo;
+  lo = lo - (t - s);
+  hi = t;
+}
+
+// ============================================================================================
+// Integrator part 1 with hi/lo positions (same schedule as k_integrate_first: pending
+// thermostat, deposition, kick + drift, wrap, freeze mask, cell histogram on rebuild steps).
+// ============================================================================================
+__global__ void k_integrate_mixed(BlockTab tab, const RepConst *__restrict__ rc, RepState *st,
+                                  float4 *__restrict__ pos, float4 *__restrict__ posLo,
+                                  float4 *__restrict__ vel, const float4 *__restrict__ acc,
+                                  int *__restrict__ cellOf, int *__restrict__ slot,
+                                  int *__restrict__ cellCount, int forceRebuild) {
+  const int rep = tab.rep[blockIdx.x];
+  const RepConst &P = rc[rep];
+  RepState *S = st + rep;
+  const int g = tab.start[blockIdx.x] + threadIdx.x;
+  if (g >= P.atomOff + P.nMol) return;
+  const int local = g - P.atomOff;
+  const int sc = S->stepCount + 1;
+  float4 r = pos[g], lo = posLo[g], v = vel[g];
+  const float4 a = acc[g];
+  if (S->thermoPending) {
+    if (local >= P.nMolMe) {
+      const float b = S->betaC;
+      v.x *= b; v.y *= b; v.z *= b;
+    } else if (S->thermoMetal) {
+      const float b = S->betaM;
+      v.x *= b; v.y *= b; v.z *= b;
+    }
+  }
+  if (local < P.nMolMe && P.iRegime == 1) {
+    int nDep = S->nMolDeposited, nTo = 0;
+    bool act = false;
+    if (sc <= P.stepEquil) act = true;
+    else if (nDep < P.nMolMe) {
+      act = true;
+      if ((sc - P.stepEquil) % P.stepDeposit == 0) nTo = P.nMolToDeposit;
+    }
+    if (act) {
+      if (local >= nDep && local < nDep + nTo) {
+        r.z = 0.49f * P.region[2]; lo.z = 0.f;
+        v.z = -P.velMagDepos;
+      }
+      if (local >= nDep + nTo) {
+        r.z = 1.5f * P.region[2] + 0.5f * (float)(local + 1) * P.region[2]; lo.z = 0.f;
+        v.x = 0.f; v.y = 0.f; v.z = 0.f;
+      }
+    }
+  }
+  const bool frozen = (local >= P.nMolMe) &&
+                      !((r.x != P.xLeft) && (r.x < P.xRight) && (r.y != P.yTop) && (r.y != P.yBottom));
+  if (!frozen) {
+    const float h = 0.5f * P.deltaT;
+    v.x += h * a.x; v.y += h * a.y; v.z += h * a.z;
+    addHiLo(r.x, lo.x, P.deltaT * v.x);
+    addHiLo(r.y, lo.y, P.deltaT * v.y);
+    addHiLo(r.z, lo.z, P.deltaT * v.z);
+  }
+  if (r.x >= 0.5f * P.region[0]) addHiLo(r.x, lo.x, -P.region[0]);
+  else if (r.x < -0.5f * P.region[0]) addHiLo(r.x, lo.x, P.region[0]);
+  if (r.y >= 0.5f * P.region[1]) addHiLo(r.y, lo.y, -P.region[1]);
+  else if (r.y < -0.5f * P.region[1]) addHiLo(r.y, lo.y, P.region[1]);
+  if (r.z >= 0.5f * P.region[2]) addHiLo(r.z, lo.z, -P.region[2]);
+  else if (r.z < -0.5f * P.region[2]) addHiLo(r.z, lo.z, P.region[2]);
+  pos[g] = r;
+  posLo[g] = lo;
+  vel[g] = v;
+  if (forceRebuild || S->nebrNow) {
+    const int c = cellIndex(P, r.x, r.y, r.z);
+    cellOf[g] = c;
+    if (c >= 0) slot[g] = atomicAdd(&cellCount[P.cellOff + c], 1);
+  }
+}
+
+// ============================================================================================
+// Verlet part 2 fused with the FP64 step reductions; the last block of each replica sums the
+// block partials in block order (deterministic) and runs the step control.
+// ============================================================================================
+// The centre of mass sums hi/lo positions as double-floats (an unevaluated float pair added
+// with error-free transformations): FP64-class accuracy on the FP32 pipes, FP64 running at a
+// small fraction of the FP32 rate on this GPU.
+struct DF {
+  float hi, lo;
+};
+#define ADDF(k, x) acc[k] = dfAdd(acc[k], DF{(x), 0.f})
+__device__ __forceinline__ DF dfAdd(DF a, DF b) {
+  float s, e;
+  twoSum(a.hi, b.hi, s, e);
+  e += a.lo + b.lo;
+  const float t = s + e;
+  return DF{t, e - (t - s)};
+}
+__device__ __forceinline__ DF dfWarpSum(DF x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    DF y{__shfl_xor_sync(0xffffffffu, x.hi, o), __shfl_xor_sync(0xffffffffu, x.lo, o)};
+    x = dfAdd(x, y);
+  }
+  return x;
+}
+
+__device__ void stepControlMixed(const RepConst &P, RepState *S, const double (&A)[kMixAcc],
+                                 const float (&M)[kMixMax], double *diff, float *diffF,
+                                 int forceRebuild);
+
+__global__ void __launch_bounds__(kRedThreads, 1) k_step_reduce_mixed(
+    BlockTab tab, const RepConst *__restrict__ rc, RepState *st, const float4 *__restrict__ pos,
+    const float4 *__restrict__ posLo, float4 *__restrict__ vel, const float4 *__restrict__ acc4,
+    const float *__restrict__ fric, double *__restrict__ part64, float *__restrict__ partF,
+    const int *__restrict__ redFirst, unsigned *counter, double *__restrict__ diff64,
+    const size_t *__restrict__ diffOff64, float *__restrict__ diffF, const size_t *__restrict__ diffOffF,
+    int forceRebuild) {
+  const int rep = tab.rep[blockIdx.x];
+  const RepConst &P = rc[rep];
+  RepState *S = st + rep;
+  const int b = tab.start[blockIdx.x];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const float h = 0.5f * P.deltaT;
+  // per thread and per warp (64 atoms) in FP32, except the centre of mass (double-float over
+  // the hi/lo positions); warp totals and everything above in FP64
+  float acc[kMixAcc];
+#pragma unroll
+  for (int k = 0; k < kMixAcc; k++) acc[k] = 0.f;
+  DF cm[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+  float mm[kMixMax] = {0.f, 3.4e38f, 3.4e38f, 3.4e38f, -3.4e38f, -3.4e38f, -3.4e38f};
+#pragma unroll
+  for (int half = 0; half < 2; half++) {
+    const int local = kRedElems * b + half * kRedThreads + t;
+    if (local >= P.nMol) continue;
+    const int g = P.atomOff + local;
+    const float4 r = pos[g];
+    float4 v = vel[g];
+    const float4 a = acc4[g];
+    const bool metal = local < P.nMolMe;
+    const bool frozen = !metal && !((r.x != P.xLeft) && (r.x < P.xRight) && (r.y != P.yTop) && (r.y != P.yBottom));
+    if (!frozen) {
+      v.x += h * a.x; v.y += h * a.y; v.z += h * a.z;
+      vel[g] = v;
+    }
+    acc[MA_VSUM_X] += metal ? P.massMe * v.x : v.x;
+    acc[MA_VSUM_Y] += v.y;
+    acc[MA_VSUM_Z] += v.z;
+    const float vv = v.x * v.x + v.y * v.y + v.z * v.z;
+    mm[MM_VVMAX] = fmaxf(mm[MM_VVMAX], vv);
+    acc[MA_USUM] += r.w;
+    acc[MA_VIRIAL] += (metal ? P.massMe : 1.f) * (r.x * a.x + r.y * a.y + r.z * a.z);
+    if (metal) {
+      const float4 l = posLo[g];
+      acc[MA_VVYZ_M] += v.y * v.y + v.z * v.z;
+      acc[MA_VX2_M] += v.x * v.x;
+      acc[MA_VX_M] += v.x;
+      acc[MA_VY_M] += v.y;
+      acc[MA_VZ_M] += v.z;
+      cm[0] = dfAdd(cm[0], DF{r.x, l.x});
+      cm[1] = dfAdd(cm[1], DF{r.y, l.y});
+      cm[2] = dfAdd(cm[2], DF{r.z, l.z});
+      if (P.hasFric) acc[MA_FRICT] += fric[g];
+      mm[MM_MIN_X] = fminf(mm[MM_MIN_X], r.x); mm[MM_MAX_X] = fmaxf(mm[MM_MAX_X], r.x);
+      mm[MM_MIN_Y] = fminf(mm[MM_MIN_Y], r.y); mm[MM_MAX_Y] = fmaxf(mm[MM_MAX_Y], r.y);
+      mm[MM_MIN_Z] = fminf(mm[MM_MIN_Z], r.z); mm[MM_MAX_Z] = fmaxf(mm[MM_MAX_Z], r.z);
+    } else {
+      acc[MA_VV_C] += vv;
+    }
+  }
+  __shared__ double sh64[kRedThreads / 32][kMixAcc];
+  __shared__ float shF[kRedThreads / 32][kMixMax];
+#pragma unroll
+  for (int k = 0; k < kMixAcc; k++) {
+    if (k >= MA_CM_X && k <= MA_CM_Z) continue;
+    float x = acc[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) sh64[w][k] = (double)x;
+  }
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const DF x = dfWarpSum(cm[c]);
+    if (lane == 0) sh64[w][MA_CM_X + c] = (double)x.hi + (double)x.lo;
+  }
+#pragma unroll
+  for (int k = 0; k < kMixMax; k++) {
+    float x = mm[k];
+    for (int o = 16; o > 0; o >>= 1) {
+      const float y = __shfl_xor_sync(0xffffffffu, x, o);
+      x = (k == MM_VVMAX || k >= MM_MAX_X) ? fmaxf(x, y) : fminf(x, y);
+    }
+    if (lane == 0) shF[w][k] = x;
+  }
+  __syncthreads();
+  const int pb = redFirst[rep] + b;
+  if (t < kMixAcc) {
+    double x = 0.0;
+    for (int k = 0; k < kRedThreads / 32; k++) x += sh64[k][t];
+    part64[(size_t)pb * kMixAcc + t] = x;
+  } else if (t >= 32 && t < 32 + kMixMax) {
+    const int k = t - 32;
+    float x = shF[0][k];
+    for (int j = 1; j < kRedThreads / 32; j++)
+      x = (k == MM_VVMAX || k >= MM_MAX_X) ? fmaxf(x, shF[j][k]) : fminf(x, shF[j][k]);
+    partF[(size_t)pb * kMixMax + k] = x;
+  }
+  if (t < kMixAcc || (t >= 32 && t < 32 + kMixMax)) __threadfence();  // partials visible first
+  __syncthreads();
+  __shared__ bool last;
+  if (t == 0) last = (atomicAdd(&counter[rep], 1u) == (unsigned)P.nRedBlocks - 1);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  // block partials: thread (g, k) with k = t % 16, g = t / 16 sums value k over blocks g, g + 32,
+  // ...; the 32 group sums of a value then add up in group order (a fixed order: the result
+  // does not depend on which block finished last)
+  __shared__ double grp64[32][16];
+  __shared__ float grpF[32][8];
+  __shared__ double tot[kMixAcc];
+  __shared__ float totF[kMixMax];
+  const int p0 = redFirst[rep];
+  {
+    const int k = t & 15, gi = t >> 4;
+    double x = 0.0;
+    float y = (k == MM_VVMAX || k >= MM_MAX_X) ? -3.4e38f : 3.4e38f;
+    for (int j = gi; j < P.nRedBlocks; j += 32) {
+      if (k < kMixAcc) x += __ldcg(part64 + (size_t)(p0 + j) * kMixAcc + k);
+      if (k < kMixMax) {
+        const float z = __ldcg(partF + (size_t)(p0 + j) * kMixMax + k);
+        y = (k == MM_VVMAX || k >= MM_MAX_X) ? fmaxf(y, z) : fminf(y, z);
+      }
+    }
+    grp64[gi][k] = x;
+    if (k < 8) grpF[gi][k] = y;
+  }
+  __syncthreads();
+  if (t < kMixAcc) {
+    double x = 0.0;
+    for (int gi = 0; gi < 32; gi++) x += grp64[gi][t];
+    tot[t] = x;
+  } else if (t >= 32 && t < 32 + kMixMax) {
+    const int k = t - 32;
+    float y = grpF[0][k];
+    for (int gi = 1; gi < 32; gi++)
+      y = (k == MM_VVMAX || k >= MM_MAX_X) ? fmaxf(y, grpF[gi][k]) : fminf(y, grpF[gi][k]);
+    totF[k] = y;
+  }
+  __syncthreads();
+  if (t == 0) counter[rep] = 0;
+  double A[kMixAcc];
+  float M[kMixMax];
+#pragma unroll
+  for (int k = 0; k < kMixAcc; k++) A[k] = tot[k];
+#pragma unroll
+  for (int k = 0; k < kMixMax; k++) M[k] = totF[k];
+  __shared__ RepState sS;
+  stateToShared(S, &sS);
+  stepControlMixed(P, &sS, A, M, diff64 ? diff64 + diffOff64[rep] : nullptr,
+                   diffF ? diffF + diffOffF[rep] : nullptr, forceRebuild);
+  stateFromShared(&sS, S);
+}
+
+// Step control in FP64 (same schedule as the PLAIN stepControl: properties, thermostat
+// decision, rebuild criterion, shear, deposition bookkeeping, averages, diffusion).
+__device__ void stepControlMixed(const RepConst &P, RepState *S, const double (&A)[kMixAcc],
+                                 const float (&M)[kMixMax], double *diff, float *diffF,
+                                 int forceRebuild) {
+  const int t = threadIdx.x;
+  const int sc = S->stepCount + 1;
+  __shared__ int diffDue, accumNow, printNow;
+  __shared__ double cmc[3];
+  if (t == 0) {
+    const double nMe = P.nMolMe, invMe = P.invNMolMe;
+    // regime 2 subtracts the metal centre-of-mass velocity from vx in the kinetic energy
+    double vvMetal = A[MA_VX2_M] + A[MA_VVYZ_M];
+    double cmvx = 0.0;
+    if (P.nMolMe != 0) {
+      cmvx = A[MA_VX_M] * invMe;
+      if (P.iRegime == 2) vvMetal = A[MA_VX2_M] - 2.0 * cmvx * A[MA_VX_M] + nMe * cmvx * cmvx + A[MA_VVYZ_M];
+    }
+    const double vvSum = A[MA_VV_C] + (double)P.massMe * vvMetal;
+    S->red[RS_VSUM_X] = (float)A[MA_VSUM_X]; S->red[RS_VSUM_Y] = (float)A[MA_VSUM_Y];
+    S->red[RS_VSUM_Z] = (float)A[MA_VSUM_Z];
+    S->red[RS_VVMAX] = M[MM_VVMAX];
+    S->red[RS_VVSUM] = (float)vvSum;
+    S->red[RS_USUM] = (float)A[MA_USUM];
+    S->red[RS_CM_X] = (float)A[MA_CM_X]; S->red[RS_CM_Y] = (float)A[MA_CM_Y]; S->red[RS_CM_Z] = (float)A[MA_CM_Z];
+    const bool metal = P.nMolMe != 0;
+    S->red[RS_MIN_X] = metal ? M[MM_MIN_X] : 0.f; S->red[RS_MIN_Y] = metal ? M[MM_MIN_Y] : 0.f;
+    S->red[RS_MIN_Z] = metal ? M[MM_MIN_Z] : 0.f;
+    S->red[RS_MAX_X] = metal ? M[MM_MAX_X] : 0.f; S->red[RS_MAX_Y] = metal ? M[MM_MAX_Y] : 0.f;
+    S->red[RS_MAX_Z] = metal ? M[MM_MAX_Z] : 0.f;
+    S->red[RS_FRICT] = (float)A[MA_FRICT];
+    S->cmVel[0] = (float)A[MA_VX_M]; S->cmVel[1] = (float)A[MA_VY_M]; S->cmVel[2] = (float)A[MA_VZ_M];
+    diffDue = 0;
+    if (metal) {
+      S->cmVal = (float)(A[MA_CM_X] * invMe);
+      S->cmVelVal = (float)cmvx;
+      S->frictVal = P.hasFric ? (float)A[MA_FRICT] : 0.f;
+      if (P.iRegime == 2 && sc > P.stepEquil && ((sc - P.stepEquil) % P.stepDiffuse == 0) && diff && diffF) {
+        diffDue = 1;
+        cmc[0] = A[MA_CM_X] * invMe; cmc[1] = A[MA_CM_Y] * invMe; cmc[2] = A[MA_CM_Z] * invMe;
+      }
+    } else {
+      S->cmVal = 0.f; S->cmVelVal = 0.f; S->frictVal = 0.f;
+    }
+    const double kin = 0.5 * vvSum * P.invNMol;
+    const bool thermo = ((P.iRegime == 2) && (sc > P.stepEquil) && (sc % P.stepThermostat == 0)) ||
+                        ((P.iRegime == 1) && (sc % P.stepThermostat == 0));
+    if (thermo) {
+      S->betaC = (float)sqrt(1.0 + (double)P.gammaBerendsen * ((double)P.temperature * 1.5 * P.kB / kin - 1.0));
+      S->betaM = (float)sqrt(1.0 + (double)P.gammaBerendsen * ((double)P.temperature * P.kB / kin - 1.0));
+      S->thermoMetal = (P.iRegime == 2) && (sc > P.stepEquil) && (sc < P.stepEquil + P.stepCool);
+      S->thermoPending = 1;
+    } else {
+      S->thermoPending = 0;
+    }
+    if (forceRebuild || S->nebrNow) {
+      S->nebrNow = 0;
+      S->dispHi = 0.f;
+      S->rebuilds++;
+    }
+    S->dispHi += sqrtf(M[MM_VVMAX]) * P.deltaT;
+    if (S->dispHi > 0.5f * P.rNebrShell) S->nebrNow = 1;
+    S->ke64 = kin;
+    S->pe64 = A[MA_USUM] * P.invNMol;
+    S->virial64 = A[MA_VIRIAL];
+    S->ke = (float)S->ke64;
+    S->pe = (float)S->pe64;
+    S->te = (float)(S->ke64 + S->pe64);
+    if (P.iRegime == 2 && metal && sc > P.stepEquil + P.stepCool) {
+      if (S->cmVelVal < 0.005f) S->shear += P.deltaF;
+      S->shearCount = 0;
+    }
+    if (P.iRegime == 1) {
+      const int nDep = S->nMolDeposited;
+      if (sc > P.stepEquil && nDep < P.nMolMe && (sc - P.stepEquil) % P.stepDeposit == 0)
+        S->nMolDeposited = nDep + P.nMolToDeposit;
+    }
+    const float vals[7] = {S->te, S->pe, S->ke, 0.f, S->cmVal, S->cmVelVal, S->frictVal};
+    for (int p = 0; p < 7; p++) {
+      if (p == 3) continue;
+      S->props[p][0] = vals[p];
+      S->props[p][1] += vals[p];
+      S->props[p][2] += vals[p] * vals[p];
+    }
+    if (sc % P.stepAvg == 0) {
+      for (int p = 0; p < 7; p++) {
+        S->propsSnap[p][0] = S->props[p][0];
+        S->propsSnap[p][1] = S->props[p][1];
+        S->propsSnap[p][2] = S->props[p][2];
+        S->props[p][1] = 0.f;
+        S->props[p][2] = 0.f;
+      }
+      S->snapStep = sc;
+    }
+    S->stepCount = sc;
+  }
+  __syncthreads();
+  if (!diffDue) return;
+  // ---- diffusion sample with FP64 accumulators (EvalDiffusion / AccumDiffusion,
+  // SurfaceGrowth.cu:2898-2952); float mirrors of the counts, the running average and the
+  // finished table keep the host readers' layout (DiffLayout)
+  const int nB = P.nBuffDiffuse, nV = P.nValDiffuse;
+  double *org = diff;                      // nB x 6: orgR, rTrue
+  double *rr = diff + (size_t)nB * 6;      // nB x nV
+  double *av = rr + (size_t)nB * nV;       // nV
+  float *tbF = diffF;                      // nB x 7, element 0 = count (int bits)
+  float *avF = diffF + (size_t)nB * 7 + (size_t)nB * nV;
+  float *prF = avF + nV;
+  if (t == 0) {
+    for (int nb = 0; nb < nB; nb++) {
+      double *o = org + 6 * nb;
+      const int count = __float_as_int(tbF[7 * nb]);
+      if (count == 0) {
+        o[0] = cmc[0]; o[1] = cmc[1]; o[2] = cmc[2];
+        o[3] = cmc[0]; o[4] = cmc[1]; o[5] = cmc[2];
+      }
+      if (count >= 0) {
+        double *rrb = rr + (size_t)nb * nV;
+        double d[3];
+        for (int k = 0; k < 3; k++) {
+          // unwrap the centre of mass by whole boxes (Nint of the jump, ComputeDefs.h:70-71)
+          const double L = P.region[k];
+          const double j = (o[3 + k] - cmc[k]) * P.invRegion[k];
+          o[3 + k] = cmc[k] + L * (double)((j < 0.) ? -(long long)(0.5 - j) : (long long)(0.5 + j));
+          d[k] = o[3 + k] - o[k];
+        }
+        rrb[count] = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+      }
+      tbF[7 * nb] = __int_as_float(count + 1);
+    }
+  }
+  __syncthreads();
+  for (int nb = 0; nb < nB; nb++) {
+    if (t == 0) {
+      accumNow = (__float_as_int(tbF[7 * nb]) == nV);
+      printNow = 0;
+    }
+    __syncthreads();
+    if (accumNow) {
+      const double *rrb = rr + (size_t)nb * nV;
+      for (int j = t; j < nV; j += blockDim.x) {
+        av[j] += rrb[j];
+        avF[j] = (float)av[j];
+      }
+      __syncthreads();
+      if (t == 0) {
+        tbF[7 * nb] = __int_as_float(0);
+        S->countDiffuseAv++;
+        printNow = (S->countDiffuseAv == P.limitDiffuseAv);
+      }
+      __syncthreads();
+      if (printNow) {
+        const double fac = 1.0 / (3.0 * 2.0 * P.stepDiffuse * (double)P.deltaT * P.limitDiffuseAv);
+        for (int j = t; j < nV; j += blockDim.x) {
+          double vj = av[j];
+          if (j >= 1) vj *= fac / j;
+          prF[j] = (float)vj;
+          av[j] = 0.0;
+          avF[j] = 0.f;
+        }
+        __syncthreads();
+        if (t == 0) {
+          S->countDiffuseAv = 0;
+          S->diffPrints++;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace sg
+
+using namespace sg;
+
+#define MCK(call)                                                                              \
+  do {                                                                                         \
+    cudaError_t e_ = (call);                                                                   \
+    if (e_ != cudaSuccess) return sg_fail(SG_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+// phi(r), phi'(r), f(r), f'(r) of the Zhou-Wadley-Johnson forms (SurfaceGrowth.cu:46-69) in FP64
+static void eamPairExact(const RepConst &P, double r, double out[4]) {
+  const double rei = P.rei, x = r * rei;
+  const double eA = std::exp(-(double)P.alpha * (x - 1.0)), eB = std::exp(-(double)P.beta * (x - 1.0));
+  const double uk = x - P.kappa, ul = x - P.lambda;
+  const double dA = 1.0 + std::pow(uk, 20.0), dB = 1.0 + std::pow(ul, 20.0);
+  const double tA = P.alpha + 20.0 * std::pow(uk, 19.0) / dA, tB = P.beta + 20.0 * std::pow(ul, 19.0) / dB;
+  out[0] = P.A * eA / dA - P.B * eB / dB;
+  out[1] = (-(double)P.A * eA * tA / dA + (double)P.B * eB * tB / dB) * rei;
+  out[2] = P.fe * eB / dB;
+  out[3] = -(double)P.fe * rei * eB * tB / dB;
+}
+
+int sg_mixed_init(sg_ctx *c) {
+  MixedBufs *m = new MixedBufs;
+  c->mixed = m;
+  // EAM tables
+  const int knots = (c->opt.eam_table_knots == 0) ? 1024 : c->opt.eam_table_knots;
+  std::vector<float4> tab;
+  for (int r = 0; r < c->nrep; r++) {
+    RepConst &P = c->hrc[r];
+    P.nTab = 0;
+    if (knots < 2 || P.nMolMe == 0 || P.rei <= 0.f) continue;
+    const double rmin = 0.6 / P.rei, rmax = std::sqrt((double)P.rrCutEam);
+    const double h = (rmax - rmin) / (knots - 1);
+    P.tabOff = (int)(tab.size() / 2);  // in intervals (two float4 each)
+    P.nTab = knots;
+    P.rTabMin = (float)rmin;
+    P.rTabH = (float)h;
+    P.rTabInv = (float)(1.0 / h);
+    // interval k: g(r_k + s) = c0 + c1 s + c2 s^2 + c3 s^3, the cubic Hermite interpolant of
+    // the values and slopes at r_k and r_k+1, expanded around r_k in FP64 (its derivative
+    // c1 + 2 c2 s + 3 c3 s^2 then carries no cancellation of neighbouring table values)
+    for (int k = 0; k < knots; k++) {
+      double a[4], b[4];
+      eamPairExact(P, rmin + k * h, a);
+      eamPairExact(P, rmin + (k + 1) * h, b);
+      for (int fn = 0; fn < 2; fn++) {
+        const double g0 = a[2 * fn], d0 = a[2 * fn + 1], g1 = b[2 * fn], d1 = b[2 * fn + 1];
+        const double c2 = (3.0 * (g1 - g0) / h - 2.0 * d0 - d1) / h;
+        const double c3 = (d0 + d1 - 2.0 * (g1 - g0) / h) / (h * h);
+        tab.push_back(make_float4((float)g0, (float)d0, (float)c2, (float)c3));
+      }
+    }
+  }
+  MCK(cudaMalloc(&m->eamTab, sizeof(float4) * std::max<size_t>(tab.size(), 1)));
+  if (!tab.empty())
+    MCK(cudaMemcpyAsync(m->eamTab, tab.data(), sizeof(float4) * tab.size(), cudaMemcpyHostToDevice, c->stream));
+  MCK(cudaMemcpyAsync(c->rc, c->hrc.data(), sizeof(RepConst) * c->nrep, cudaMemcpyHostToDevice, c->stream));
+  MCK(cudaStreamSynchronize(c->stream));
+  const int nRed = std::max(c->redTab.n, 1);
+  MCK(cudaMalloc(&m->part64, sizeof(double) * nRed * kMixAcc));
+  MCK(cudaMalloc(&m->partF, sizeof(float) * nRed * kMixMax));
+  MCK(cudaMalloc(&m->counter, sizeof(unsigned) * c->nrep));
+  MCK(cudaMemsetAsync(m->counter, 0, sizeof(unsigned) * c->nrep, c->stream));
+  size_t total = 0;
+  m->diffOff64.resize(c->nrep);
+  for (int r = 0; r < c->nrep; r++) {
+    m->diffOff64[r] = total;
+    const sg_simparams &p = c->hp[r];
+    if (p.iRegime == 2) total += (size_t)p.nBuffDiffuse * 6 + (size_t)p.nBuffDiffuse * p.nValDiffuse + p.nValDiffuse;
+  }
+  MCK(cudaMalloc(&m->diff64, sizeof(double) * std::max<size_t>(total, 1)));
+  MCK(cudaMemsetAsync(m->diff64, 0, sizeof(double) * std::max<size_t>(total, 1), c->stream));
+  MCK(cudaMalloc(&m->dDiffOff64, sizeof(size_t) * c->nrep));
+  MCK(cudaMemcpyAsync(m->dDiffOff64, m->diffOff64.data(), sizeof(size_t) * c->nrep, cudaMemcpyHostToDevice,
+                      c->stream));
+  MCK(cudaStreamSynchronize(c->stream));
+  return SG_OK;
+}
+
+void sg_mixed_free(sg_ctx *c) {
+  MixedBufs *m = static_cast<MixedBufs *>(c->mixed);
+  if (!m) return;
+  cudaFree(m->part64);
+  cudaFree(m->partF);
+  cudaFree(m->counter);
+  cudaFree(m->diff64);
+  cudaFree(m->dDiffOff64);
+  cudaFree(m->eamTab);
+  delete m;
+  c->mixed = nullptr;
+}
+
+int sg_mixed_enqueue_integrate(sg_ctx *c, int forceRebuild) {
+  if (!c->atomTab.n) return SG_OK;
+  k_integrate_mixed<<<c->atomTab.n, 128, 0, c->stream>>>(c->atomTab.view(), c->rc, c->st, c->pos, c->posLo, c->vel,
+                                                         c->acc, c->cellOf, c->slot, c->cellCount, forceRebuild);
+  MCK(cudaGetLastError());
+  return SG_OK;
+}
+
+// The metal chain (density, metal forces) on the side stream beside the carbon pass, joined
+// before the reduction, as in PLAIN; no centre-of-mass-velocity pass.
+int sg_mixed_enqueue_forces(sg_ctx *c) {
+  MixedBufs *m = static_cast<MixedBufs *>(c->mixed);
+  const bool fork = c->metalTabT.n > 0;
+  if (fork) {
+    MCK(cudaEventRecord(c->evFork, c->stream));
+    MCK(cudaStreamWaitEvent(c->side, c->evFork, 0));
+    k_rho_mixed<<<c->metalTabT.n, 128, 0, c->side>>>(c->metalTabT.view(), c->rc, c->pos, c->nn, c->nbl, c->rho,
+                                                     c->dF, c->Fv, c->rowStride, m->eamTab);
+    k_force_metal_mixed<<<c->metalTabT.n, 128, 0, c->side>>>(c->metalTabT.view(), c->rc, c->pos, c->acc, c->nn,
+                                                             c->nbl, c->dF, c->Fv, c->fric, c->rowStride,
+                                                             m->eamTab);
+    if (c->opt.phase_timing) cudaEventRecordWithFlags(c->phaseEv[7], c->side, cudaEventRecordExternal);
+    MCK(cudaGetLastError());
+  }
+  if (c->carbonTabT.n) {
+    k_force_carbon_mixed<<<c->carbonTabT.n, 128, 0, c->stream>>>(c->carbonTabT.view(), c->rc, c->pos, c->acc,
+                                                                 c->nn, c->nbl, c->ns, c->sl, c->nrl, c->rl,
+                                                                 c->rowStride);
+    }
+  if (c->opt.phase_timing) cudaEventRecordWithFlags(c->phaseEv[3], c->stream, cudaEventRecordExternal);
+  MCK(cudaGetLastError());
+  if (fork) {
+    MCK(cudaEventRecord(c->evJoin, c->side));
+    MCK(cudaStreamWaitEvent(c->stream, c->evJoin, 0));
+  } else if (c->opt.phase_timing) {
+    cudaEventRecordWithFlags(c->phaseEv[7], c->stream, cudaEventRecordExternal);
+  }
+  return SG_OK;
+}
+
+int sg_mixed_enqueue_reduce(sg_ctx *c, int forceRebuild) {
+  MixedBufs *m = static_cast<MixedBufs *>(c->mixed);
+  if (!c->redTab.n) return SG_OK;
+  k_step_reduce_mixed<<<c->redTab.n, kRedThreads, 0, c->stream>>>(
+      c->redTab.view(), c->rc, c->st, c->pos, c->posLo, c->vel, c->acc, c->fric, m->part64, m->partF,
+      c->dRedFirst, m->counter, m->diff64, m->dDiffOff64, c->diffBuf, c->dDiffOff, forceRebuild);
+  MCK(cudaGetLastError());
+  return SG_OK;
+}

@@ -1,0 +1,117 @@
+"""MIXED ("chosen") form: the same model as PLAIN with hi/lo positions, FMA contraction,
+tabulated EAM pair functions and FP64 reductions.  Checked against the FP64 oracle (forces on
+thermalised states, NVE energy drift) and against PLAIN (same model: energies of one step)."""
+import numpy as np
+import pytest
+
+import oracle
+from surfacegrowthconsole_gb300 import MODE_MIXED, MODE_PLAIN, workloads
+from surfacegrowthconsole_gb300.engine import Simulation, default_input, init_coords, init_vels, set_params
+
+pytestmark = pytest.mark.gpu
+
+EV = 0.06275049  # energy unit, eV
+
+
+def thermalised(p, r, v, steps=40):
+    """A state some steps into the run: forces no longer cancel to round-off as in the perfect
+    lattices the generators build."""
+    sim = Simulation(p)
+    sim.set_state(r, v, np.zeros((p.nMol, 3), np.float32))
+    sim.step(steps)
+    r2, v2, _ = sim.get_state()
+    sim.close()
+    return r2, v2
+
+
+def forces(p, r, v, mode):
+    sim = Simulation(p, mode=mode)
+    sim.set_state(r, v, np.zeros((p.nMol, 3), np.float32))
+    sim.build_lists()
+    sim.compute_forces()
+    a = sim.get_state()[2].astype(np.float64)
+    sim.close()
+    return a
+
+
+def bulk_ni(n=10, T=300, seed=5):
+    inp = default_input(); inp.iRegime = 0; inp.iMaterial = 3; inp.ucx = inp.ucy = inp.ucz = n
+    inp.temperatureK = T; inp.deltaT = 0.005; inp.randSeed = seed; inp.stepEquil = 10 ** 9
+    inp.stepLimit = 10 ** 9
+    p = set_params(inp)
+    return p, init_coords(p), init_vels(p)
+
+
+@pytest.mark.parametrize("which", ["small", "production", "bulk"])
+def test_forces_against_the_fp64_oracle(which):
+    """RMS force error relative to the RMS force, MIXED and PLAIN against the FP64 oracle on the
+    same FP32 positions: MIXED (FMA, tables) is no less accurate than PLAIN."""
+    p, r, v = {"small": lambda: workloads.small(seed=81), "production": lambda: workloads.production(seed=2),
+               "bulk": bulk_ni}[which]()
+    r, v = thermalised(p, r, v)
+    o = oracle.OracleSim(p, 64)
+    o.set_state(r, v, np.zeros((p.nMol, 3), np.float32))
+    o.build_lists()
+    o.compute_forces()
+    a64 = o.get_state64()[2]
+    scale = np.sqrt((a64 ** 2).mean())
+    err = {m: float(np.sqrt(((forces(p, r, v, m) - a64) ** 2).mean()) / scale) for m in (MODE_PLAIN, MODE_MIXED)}
+    print(which, "rms force error vs FP64: plain", err[MODE_PLAIN], "mixed", err[MODE_MIXED])
+    assert err[MODE_MIXED] <= 1e-4
+    assert err[MODE_MIXED] <= 2.0 * err[MODE_PLAIN] + 1e-7
+
+
+def test_replicas_together_equal_each_alone():
+    reps = [workloads.small(seed=s) for s in (82, 83, 84)]
+    plist = [w[0] for w in reps]
+    sim = Simulation(plist, mode=MODE_MIXED)
+    sim.set_state(np.concatenate([w[1] for w in reps]), np.concatenate([w[2] for w in reps]),
+                  np.zeros((sum(q.nMol for q in plist), 3), np.float32))
+    sim.step(30)
+    for k, (q, r, v) in enumerate(reps):
+        one = Simulation(q, mode=MODE_MIXED)
+        one.set_state(r, v, np.zeros((q.nMol, 3), np.float32))
+        one.step(30)
+        rb, vb, _ = sim.get_state(k)
+        ro, vo, _ = one.get_state()
+        assert np.array_equal(rb, ro) and np.array_equal(vb, vo), f"replica {k}"
+        assert sim.thermo(k).kinEnergy64 == one.thermo().kinEnergy64
+        one.close()
+    sim.close()
+
+
+def test_one_step_energies_match_plain():
+    p, r, v = workloads.production(seed=2)
+    th = {}
+    for m in (MODE_PLAIN, MODE_MIXED):
+        sim = Simulation(p, mode=m)
+        sim.set_state(r, v, np.zeros((p.nMol, 3), np.float32))
+        sim.step(1)
+        th[m] = sim.thermo()
+        sim.close()
+    for k in ("kinEnergy", "potEnergy"):
+        a, b = getattr(th[MODE_MIXED], k + "64"), getattr(th[MODE_PLAIN], k)
+        assert abs(a - b) <= 2e-5 * abs(b), (k, a, b)
+
+
+def test_nve_drift_no_worse_than_plain():
+    """Bulk Ni (a conservative EAM system), 10,000 NVE steps (10 ps): the linear drift of the
+    total energy.  The reference's graphene model does not conserve energy (it applies the
+    second-neighbour angle force but leaves its energy out), so drift is measured on the metal."""
+    p, r, v = bulk_ni()
+    steps, every = 10000, 100
+    drift = {}
+    for m in (MODE_PLAIN, MODE_MIXED):
+        sim = Simulation(p, mode=m)
+        sim.set_state(r, v, np.zeros((p.nMol, 3), np.float32))
+        es = []
+        for _ in range(steps // every):
+            sim.step(every)
+            t = sim.thermo()
+            es.append(t.kinEnergy64 + t.potEnergy64 if m == MODE_MIXED else float(t.totEnergy))
+        sim.close()
+        x = np.arange(len(es)) * every
+        drift[m] = abs(np.polyfit(x, np.array(es), 1)[0]) * 1e6 * EV  # eV / atom / ns (1 step = 1 fs)
+    print("NVE drift eV/atom/ns: plain", drift[MODE_PLAIN], "mixed", drift[MODE_MIXED])
+    assert drift[MODE_MIXED] <= drift[MODE_PLAIN] + 2e-5
+    assert drift[MODE_MIXED] < 1e-3
