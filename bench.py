@@ -26,6 +26,9 @@ LJ, graphene, reductions, thermostat, RDF/diffusion when due).
 C, one Ni cluster of U{50..2,000} atoms, T U[300, 1,500] K, lists rebuilt by the reference's
 rule) stepped together in one context; the line adds the same replicas run one by one, each in
 its own context, for comparison.
+--workload diff: the differentiation form: gradients of the force-matching loss with respect to
+the 66 fit parameters (LJ epsilon, sigma, 64 EAM spline coefficients) over 64 jittered frames of
+the ~20,000-atom graphene + Ni system, forward + adjoint per gradient; metric grads/s.
 Multi-GPU (torchrun): replicas only -- each rank runs its own seeded system, no collective on
 the data path; value is the sum over ranks over the slowest rank's time.
 """
@@ -61,7 +64,7 @@ def parse():
     ap.add_argument("--cpu-sample-steps", type=int, default=300)
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="production", choices=["production", "batched"])
+    ap.add_argument("--workload", default="production", choices=["production", "batched", "diff"])
     ap.add_argument("--replicas", type=int, default=256)
     return ap.parse_args()
 
@@ -276,6 +279,45 @@ def run_batched(args, rank: int, world: int, local: int):
         print(json.dumps(line, default=float))
 
 
+def run_diff(args, rank: int, world: int, local: int):
+    """Gradient evaluations per second of the force-matching loss over 64 frames."""
+    import torch
+    from surfacegrowthconsole_gb300 import workloads
+    from surfacegrowthconsole_gb300.engine import DiffModel, diff_init_theta
+    frames, r = workloads.differentiation_frames(n_frames=64, seed=5 + rank)
+    theta = diff_init_theta(frames[0])
+    model = DiffModel(frames, r, device=local)
+    pert = theta.copy()
+    pert[0] *= 1.2
+    pert[1] *= 0.97
+    ref = model.forces(pert)
+    for _ in range(args.warmup):
+        model.force_matching(theta, ref)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        ev0.record()
+        for _ in range(args.steps):
+            loss, grad = model.force_matching(theta, ref)
+        ev1.record()
+        torch.cuda.synchronize()
+    t = ev0.elapsed_time(ev1) * 1e-3
+    natoms = model.n
+    model.close()
+    if rank == 0:
+        line = {"metric": "grads/s", "value": world * args.steps / t, "unit": "grads/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32 pair math, f64 sums",
+                "data": "synthetic (64 snapshots of a seeded graphene + Ni trajectory, +-0.05 A jitter)",
+                "config": {"workload": f"64 frames x {natoms // 64} atoms (graphene 18,432 C + 2,000 Ni), "
+                                       "force-matching loss, gradient w.r.t. 66 parameters (forward + adjoint)",
+                           "frames": 64, "atoms_all_frames": natoms, "parallelism": f"replicas x{world}"},
+                "atom_frames_per_s": natoms * args.steps / t, "loss": loss, "clocks": clk.summary(),
+                "host_copies_per_step": "theta (66 doubles) and reference forces up, loss and gradient down"}
+        print(json.dumps(line, default=float))
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -291,8 +333,8 @@ def main():
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
-    if args.workload == "batched":
-        run_batched(args, rank, world, local)
+    if args.workload in ("batched", "diff"):
+        (run_batched if args.workload == "batched" else run_diff)(args, rank, world, local)
         if dist:
             dist.destroy_process_group()
         return

@@ -57,9 +57,9 @@ enum {
      * assignment, neighbour lists, RDF counts) are bit-exact with the reference; forces
      * agree to within the accuracy of the CUDA/libm transcendental functions. */
     SG_MODE_PLAIN = 0,
-    /* FP32 pair arithmetic with FMA, tabulated EAM in shared memory, FP64 accumulation of
-     * energy/virial/momentum sums, FP64 thermostat factor and MSD accumulators, and
-     * positions carried as a float hi/lo pair. */
+    /* The same model: FP32 pair arithmetic with FMA, EAM pair functions from cubic tables (read
+     * through L1), FP64 accumulation of energy/virial/momentum sums, FP64 thermostat factor and
+     * MSD accumulators, and positions carried as a float hi/lo pair. */
     SG_MODE_MIXED = 1
 };
 
@@ -71,7 +71,7 @@ typedef struct sg_options {
     void *stream;          /* cudaStream_t to run on; NULL: the context creates its own */
     int rdf_ext_bins;      /* >0: also accumulate an all-pairs metal-metal RDF */
     float rdf_ext_range;   /* its range, dimensionless length */
-    int eam_table_knots;   /* MIXED: knots of the tabulated EAM pair functions (0: 4096; -1: analytic) */
+    int eam_table_knots;   /* MIXED: intervals of the tabulated EAM pair functions (0: 1024; -1: analytic) */
     int tune_force_tpa;    /* threads per atom in the carbon force pass (0: auto) */
     int tune_block;        /* block size of the per-atom passes (0: auto) */
     int phase_timing;      /* 1: record CUDA events between the phases of every step */
@@ -287,6 +287,52 @@ int sg_read_backup(const char *path, sg_simparams *p, sg_float4 *r, sg_float3 *v
 #define SG_NOALLOC_MAX_NEBR 128      /* iNebrMax */
 #define SG_NOALLOC_SCRATCH_BYTES (20u << 20)
 int sg_compute_forces_noalloc(const sg_simparams *p, sg_float4 *d_pos, sg_float4 *d_acc, void *stream);
+
+/* ---- differentiation ---------------------------------------------------------------------
+ * The metal part of the model as a function of fit parameters, with its gradient from a
+ * hand-written adjoint (no counterpart in the reference, which has fixed analytic potentials).
+ * theta[SG_DIFF_NPARAM]:
+ *   theta[0]      epsilon of the metal-carbon 12-6 Lennard-Jones term,
+ *   theta[1]      its sigma (the cutoff stays the parameter block's rrCutLJ),
+ *   theta[2..33]  the 32 uniform cubic B-spline coefficients of the EAM pair potential phi(r),
+ *   theta[34..65] those of the EAM density function f(r),
+ * both splines on SG_DIFF_SPLINE_INTERVALS equal intervals from 0.6 r_e to the EAM cutoff
+ * (below 0.6 r_e the first cubic piece continues); the embedding function F(rho) is the
+ * reference's analytic form.  Energy of a frame:
+ *   E = sum over metal pairs (r < rCutEam) phi(r) + sum over metal atoms F(rho_i),
+ *       rho_i = sum over metal neighbours (r < rCutEam) f(r),
+ *     + sum over metal-carbon pairs (r < rCutLJ) 4 eps ((sigma/r)^12 - (sigma/r)^6);
+ * the graphene bonded terms have no fit parameter and are left out; forces F = -grad_r E.
+ * Frames are independent configurations of systems of the same kind (one parameter block per
+ * frame; the frames' iNebrMax must agree).  Pair arithmetic in FP32, sums of energies, losses
+ * and gradients in FP64 (through atomics: repeated calls agree to about 1e-7 relative).  The force-matching loss over all frames is
+ *   L = (1 / (3 N)) sum_i |F_i(theta) - F_ref,i|^2      (N: atoms of all frames),
+ * its gradient comes from the adjoint pass, which recomputes the densities instead of storing
+ * them. */
+#define SG_DIFF_NPARAM 66
+#define SG_DIFF_SPLINE_COEFFS 32
+#define SG_DIFF_SPLINE_INTERVALS 29
+typedef struct sg_diff sg_diff;
+/* The parameter block a frame is evaluated with: the list radius raised to cover the LJ
+ * cutoff (the cell grid and iNebrMax follow), everything else as given.  Host only. */
+int sg_diff_frame_params(const sg_simparams *in, sg_simparams *out);
+int sg_diff_create(const sg_simparams *frame_params, int n_frames, int device, sg_diff **out);
+int sg_diff_destroy(sg_diff *d);
+int sg_diff_num_atoms(const sg_diff *d);
+/* Positions of all frames, concatenated (float4, w ignored); builds the pair lists. */
+int sg_diff_set_positions(sg_diff *d, const sg_float4 *r);
+/* theta at the reference model of a parameter block: its epsilon and sigma, splines fitted by
+ * least squares (FP64) to its analytic phi and f.  Host only. */
+int sg_diff_init_theta(const sg_simparams *p, double *theta);
+/* Energy of every frame (n_frames values) and, if grad is not NULL, dE/dtheta summed over the
+ * frames. */
+int sg_diff_energy(sg_diff *d, const double *theta, double *energy, double *grad);
+/* Forces of all atoms of all frames (3 floats per atom). */
+int sg_diff_forces(sg_diff *d, const double *theta, float *forces);
+/* Force-matching loss against ref_forces (3 floats per atom, all frames) and, if grad is not
+ * NULL, dL/dtheta. */
+int sg_diff_force_matching(sg_diff *d, const double *theta, const float *ref_forces, double *loss,
+                           double *grad);
 
 /* ---- tuning ------------------------------------------------------------------------------- */
 /* Times the candidate launch shapes of the tunable passes on the context's own state for

@@ -52,6 +52,7 @@ def lib():
             "orc_diffusion_replay": (C.c_int, [C.POINTER(SimParams), C.c_int, V, V, C.c_int]),
             "orc_eam_eval": (C.c_double, [C.POINTER(SimParams), C.c_int, C.c_double, C.c_int]),
             "orc_rdf_allpairs": (None, [C.POINTER(SimParams), V, C.c_int, C.c_double, V]),
+            "orc_diff_eval": (C.c_int, [V, C.c_int, V, V, V, V, V, V, V, V]),
         }
         for n, (r, a) in sigs.items():
             f = getattr(L, n)
@@ -203,3 +204,22 @@ def diffusion_replay(params, cm):
     out = np.zeros((maxt, params.nValDiffuse), np.float32)
     k = lib().orc_diffusion_replay(C.byref(params), len(cm), _p(cm), _p(out), maxt)
     return [out[i] for i in range(k)]
+
+
+def diff_eval(frames, r, theta, ref=None):
+    """The differentiation form in FP64: (energy per frame, forces (N, 3), dE/dtheta,
+    loss, dL/dtheta); frames are parameter blocks from sg_diff_frame_params."""
+    from surfacegrowthconsole_gb300._lib import SimParams
+    arr = (SimParams * len(frames))(*frames)
+    n = sum(q.nMol for q in frames)
+    r = np.ascontiguousarray(r, np.float32).reshape(n, 4)
+    theta = np.ascontiguousarray(theta, np.float64)
+    rf = None if ref is None else np.ascontiguousarray(ref, np.float32).reshape(n, 3)
+    e = np.zeros(len(frames))
+    f = np.zeros((n, 3))
+    gE = np.zeros(66)
+    loss = np.zeros(1)
+    gL = np.zeros(66)
+    lib().orc_diff_eval(C.cast(arr, C.c_void_p), len(frames), _p(r), _p(theta), _p(rf), _p(e), _p(f), _p(gE),
+                        _p(loss), _p(gL))
+    return e, f, gE, float(loss[0]), gL

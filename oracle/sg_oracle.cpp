@@ -908,6 +908,66 @@ struct orc_sim { Handle h; };
 
 #define DISPATCH(s, call) ((s)->h.prec == 32 ? (s)->h.f->call : (s)->h.d->call)
 
+// ---- differentiation form in FP64 ----------------------------------------------------------
+// TEST INFRASTRUCTURE: the model of surfacegrowthconsole_gb300/csrc/sg_adjoint.cu restated in
+// FP64 (energies, forces, force-matching loss, and the gradients of both by the same adjoint
+// formulas), for the GPU checks and for checking the formulas against central finite
+// differences.  Pair lists come from the FP32 list code on the same frame parameters, so they
+// are the lists the GPU builds; every pair term is then evaluated in FP64.
+namespace diff {
+constexpr int NP = 66, SC = 32, SI = 29, PHI = 2, DEN = 34;
+
+struct Frame {
+  sg_simparams p;
+  Model<double> M;
+  int n, nMe;
+  std::vector<int> NN, NBL;
+  std::vector<V4<double>> r;
+  double r0, h;
+};
+
+static int bsp(const Frame &f, double r, double b[4], double db[4]) {
+  const double x = (r - f.r0) / f.h;
+  const int k = std::max(0, std::min((int)std::floor(x), SI - 1));
+  const double t = x - k, u = 1.0 - t;
+  b[0] = u * u * u / 6; b[1] = (3 * t * t * t - 6 * t * t + 4) / 6;
+  b[2] = (-3 * t * t * t + 3 * t * t + 3 * t + 1) / 6; b[3] = t * t * t / 6;
+  db[0] = -0.5 * u * u / f.h; db[1] = (1.5 * t * t - 2 * t) / f.h;
+  db[2] = (-1.5 * t * t + t + 0.5) / f.h; db[3] = 0.5 * t * t / f.h;
+  return k;
+}
+
+static void embed(const sg_simparams &P, double rho, double &F, double &Fp, double &Fpp) {
+  const double rhoe = P.rhoe, rhoei = P.rhoei;
+  if (rho < 0.85f * P.rhoe) {
+    const double s = rhoei * (double)1.176471f, x = rho * s - 1.0;
+    F = P.Fn[0] + x * (P.Fn[1] + x * (P.Fn[2] + x * P.Fn[3]));
+    Fp = s * (P.Fn[1] + x * (2.0 * P.Fn[2] + 3.0 * x * P.Fn[3]));
+    Fpp = s * s * (2.0 * P.Fn[2] + 6.0 * x * P.Fn[3]);
+  } else if (rho < 1.15f * P.rhoe) {
+    const double s = rhoei, x = rho * s - 1.0;
+    F = P.F[0] + x * (P.F[1] + x * (P.F[2] + x * P.F[3]));
+    Fp = s * (P.F[1] + x * (2.0 * P.F[2] + 3.0 * x * P.F[3]));
+    Fpp = s * s * (2.0 * P.F[2] + 6.0 * x * P.F[3]);
+  } else {
+    const double eta = P.eta, y = rho * rhoei, ly = std::log(y), ye = std::pow(y, eta);
+    F = P.Fe * (1.0 - eta * ly) * ye;
+    Fp = -P.Fe * eta * eta * rhoei * ye / y * ly;
+    Fpp = -P.Fe * eta * eta * rhoei * rhoei * ye / (y * y) * ((eta - 1.0) * ly + 1.0);
+  }
+  (void)rhoe;
+}
+
+static double mi(double d, double L) { return d - L * std::nearbyint(d / L); }
+
+// pair geometry of (i, k): d = r_i - r_k (minimum image), rr
+static void geom(const Frame &f, int i, int k, double d[3], double &rr) {
+  const double L[3] = {f.p.region.x, f.p.region.y, f.p.region.z};
+  d[0] = mi(f.r[i].x - f.r[k].x, L[0]); d[1] = mi(f.r[i].y - f.r[k].y, L[1]); d[2] = mi(f.r[i].z - f.r[k].z, L[2]);
+  rr = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+}
+}  // namespace diff
+
 extern "C" {
 
 orc_sim *orc_create(const sg_simparams *p, int precision, int force_rebuild) {
@@ -1064,6 +1124,150 @@ void orc_rdf_allpairs(const sg_simparams *p, const sg_float4 *r, int nbins, doub
         if (b >= 0 && b < nbins) hist[b]++;
       }
     }
+}
+
+// Frames (their parameter blocks from sg_diff_frame_params), positions of all frames
+// concatenated; ref may be NULL (no loss).  Outputs may be NULL.
+int orc_diff_eval(const sg_simparams *frames, int nFrames, const sg_float4 *r, const double *theta,
+                  const float *ref, double *energy, double *forces, double *gradE, double *loss, double *gradL) {
+  using namespace diff;
+  std::vector<Frame> F(nFrames);
+  int off = 0, ntot = 0;
+  for (int q = 0; q < nFrames; q++) ntot += frames[q].nMol;
+  std::vector<double> force((size_t)3 * ntot, 0.0), gE(NP, 0.0), gD(NP, 0.0), en(nFrames, 0.0);
+  std::vector<double> Fp((size_t)ntot, 0.0), Fpp((size_t)ntot, 0.0), rhoA((size_t)ntot, 0.0);
+  const double eps = theta[0], sig = theta[1];
+  for (int q = 0; q < nFrames; q++) {
+    Frame &f = F[q];
+    f.p = frames[q];
+    f.M.load(f.p);
+    f.n = f.p.nMol;
+    f.nMe = f.p.nMolMe;
+    f.r0 = 0.6 / (double)f.p.rei;
+    f.h = (std::sqrt((double)f.p.rrCutEam) - f.r0) / SI;
+    Sim<float> S(f.p, 1);
+    for (int i = 0; i < f.n; i++) S.r[i] = V4<float>{r[off + i].x, r[off + i].y, r[off + i].z, 0.f};
+    S.binAtoms();
+    S.buildNebr();
+    f.NN = S.NN;
+    f.NBL = S.NBL;
+    f.r.resize(f.n);
+    for (int i = 0; i < f.n; i++) f.r[i] = V4<double>{r[off + i].x, r[off + i].y, r[off + i].z, 0.0};
+    // densities and embedding
+    for (int i = 0; i < f.nMe; i++) {
+      double rho = 0;
+      for (int j = 0; j < f.NN[i]; j++) {
+        const int k = f.NBL[(size_t)j * f.n + i];
+        if (k >= f.nMe) continue;
+        double d[3], rr;
+        geom(f, i, k, d, rr);
+        if (rr >= (double)f.p.rrCutEam) continue;
+        double b[4], db[4];
+        const int kk = bsp(f, std::sqrt(rr), b, db);
+        for (int m = 0; m < 4; m++) rho += theta[DEN + kk + m] * b[m];
+      }
+      double Fv, Fd, Fdd;
+      embed(f.p, rho, Fv, Fd, Fdd);
+      rhoA[off + i] = rho; Fp[off + i] = Fd; Fpp[off + i] = Fdd;
+      en[q] += Fv;
+    }
+    // forces, pair energies, energy gradient
+    for (int i = 0; i < f.nMe; i++) {
+      for (int j = 0; j < f.NN[i]; j++) {
+        const int k = f.NBL[(size_t)j * f.n + i];
+        double d[3], rr;
+        geom(f, i, k, d, rr);
+        if (k < f.nMe) {
+          if (rr >= (double)f.p.rrCutEam) continue;
+          const double rl = std::sqrt(rr);
+          double b[4], db[4];
+          const int kk = bsp(f, rl, b, db);
+          double phi = 0, dphi = 0, df = 0;
+          for (int m = 0; m < 4; m++) {
+            phi += theta[PHI + kk + m] * b[m]; dphi += theta[PHI + kk + m] * db[m]; df += theta[DEN + kk + m] * db[m];
+            gE[PHI + kk + m] += 0.5 * b[m];
+            gE[DEN + kk + m] += Fp[off + i] * b[m];
+          }
+          const double fc = -(dphi + df * (Fp[off + i] + Fp[off + k])) / rl;
+          for (int c = 0; c < 3; c++) force[3 * (off + i) + c] += fc * d[c];
+          en[q] += 0.5 * phi;
+        } else {
+          if (rr >= (double)f.p.rrCutLJ) continue;
+          const double s2 = sig * sig / rr, s6 = s2 * s2 * s2, s12 = s6 * s6;
+          const double fc = 24.0 * eps * (2.0 * s12 - s6) / rr;
+          for (int c = 0; c < 3; c++) {
+            force[3 * (off + i) + c] += fc * d[c];
+            force[3 * (off + k) + c] -= fc * d[c];
+          }
+          en[q] += 4.0 * eps * (s12 - s6);
+          gE[0] += 4.0 * (s12 - s6);
+          gE[1] += 24.0 * eps * (2.0 * s12 - s6) / sig;
+        }
+      }
+    }
+    off += f.n;
+  }
+  double L = 0;
+  if (ref) {
+    const double inv3N = 1.0 / (3.0 * ntot);
+    std::vector<double> e((size_t)3 * ntot);
+    for (size_t t = 0; t < e.size(); t++) {
+      const double x = force[t] - (double)ref[t];
+      L += x * x * inv3N;
+      e[t] = 2.0 * inv3N * x;
+    }
+    off = 0;
+    for (int q = 0; q < nFrames; q++) {
+      Frame &f = F[q];
+      for (int i = 0; i < f.nMe; i++) {
+        const double *ei = &e[3 * (off + i)];
+        // g_i
+        double g = 0;
+        for (int j = 0; j < f.NN[i]; j++) {
+          const int k = f.NBL[(size_t)j * f.n + i];
+          if (k >= f.nMe) continue;
+          double d[3], rr;
+          geom(f, i, k, d, rr);
+          if (rr >= (double)f.p.rrCutEam) continue;
+          const double rl = std::sqrt(rr);
+          const double *ek = &e[3 * (off + k)];
+          const double w = (d[0] * (ei[0] - ek[0]) + d[1] * (ei[1] - ek[1]) + d[2] * (ei[2] - ek[2])) / rl;
+          double b[4], db[4];
+          const int kk = bsp(f, rl, b, db);
+          for (int m = 0; m < 4; m++) g += theta[DEN + kk + m] * db[m] * w;
+        }
+        for (int j = 0; j < f.NN[i]; j++) {
+          const int k = f.NBL[(size_t)j * f.n + i];
+          double d[3], rr;
+          geom(f, i, k, d, rr);
+          const double rl = std::sqrt(rr);
+          const double *ek = &e[3 * (off + k)];
+          const double w = (d[0] * (ei[0] - ek[0]) + d[1] * (ei[1] - ek[1]) + d[2] * (ei[2] - ek[2])) / rl;
+          if (k < f.nMe) {
+            if (rr >= (double)f.p.rrCutEam) continue;
+            double b[4], db[4];
+            const int kk = bsp(f, rl, b, db);
+            for (int m = 0; m < 4; m++) {
+              gD[PHI + kk + m] += 0.5 * db[m] * w;
+              gD[DEN + kk + m] += Fpp[off + i] * g * b[m] + Fp[off + i] * db[m] * w;
+            }
+          } else {
+            if (rr >= (double)f.p.rrCutLJ) continue;
+            const double s2 = sig * sig / rr, s6 = s2 * s2 * s2, s12 = s6 * s6;
+            gD[0] += 24.0 * (s6 - 2.0 * s12) / rl * w;
+            gD[1] += 144.0 * eps * (s6 - 4.0 * s12) / (rl * sig) * w;
+          }
+        }
+      }
+      off += f.n;
+    }
+  }
+  if (energy) std::copy(en.begin(), en.end(), energy);
+  if (forces) std::copy(force.begin(), force.end(), forces);
+  if (gradE) std::copy(gE.begin(), gE.end(), gradE);
+  if (loss) *loss = L;
+  if (gradL) for (int t = 0; t < NP; t++) gradL[t] = -gD[t];
+  return 0;
 }
 
 }  // extern "C"

@@ -204,6 +204,15 @@ _SIGS = {
     "sg_read_backup": (C.c_int, [C.c_char_p, C.POINTER(SimParams), C.c_void_p, C.c_void_p, C.c_void_p]),
     "sg_compute_forces_noalloc": (C.c_int, [C.POINTER(SimParams), C.c_void_p, C.c_void_p, C.c_void_p]),
     "sg_autotune": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p, C.c_int]),
+    "sg_diff_frame_params": (C.c_int, [C.POINTER(SimParams), C.POINTER(SimParams)]),
+    "sg_diff_create": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "sg_diff_destroy": (C.c_int, [C.c_void_p]),
+    "sg_diff_num_atoms": (C.c_int, [C.c_void_p]),
+    "sg_diff_set_positions": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "sg_diff_init_theta": (C.c_int, [C.POINTER(SimParams), C.c_void_p]),
+    "sg_diff_energy": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "sg_diff_forces": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "sg_diff_force_matching": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "CudaInitW": (None, [C.c_int, C.c_void_p]),
     "SetParametersW": (None, [C.POINTER(SimParams)]),
     "InitCoordsW": (C.c_char_p, [C.c_void_p, C.c_void_p, C.POINTER(SimParams)]),

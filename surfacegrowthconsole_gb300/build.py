@@ -39,6 +39,7 @@ CUDA_UNITS = [
     ("sg_engine.cu", []),
     ("sg_run.cu", []),
     ("sg_noalloc.cu", []),
+    ("sg_adjoint.cu", []),
 ]
 CXX_UNITS = ["sg_host.cpp", "sg_refcompat.cpp"]
 

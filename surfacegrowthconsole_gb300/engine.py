@@ -258,3 +258,71 @@ class Simulation:
         buf = C.create_string_buffer(4096)
         check(lib().sg_autotune(self._h, steps, buf, len(buf)))
         return buf.value.decode()
+
+
+DIFF_NPARAM = 66  # SG_DIFF_NPARAM
+
+
+def diff_frame_params(p: SimParams) -> SimParams:
+    """The parameter block a differentiation frame is evaluated with (list radius covering the
+    LJ cutoff); host only."""
+    q = SimParams()
+    check(lib().sg_diff_frame_params(C.byref(p), C.byref(q)))
+    return q
+
+
+def diff_init_theta(p: SimParams) -> np.ndarray:
+    """theta at the reference model of a parameter block (splines fitted to the analytic EAM)."""
+    t = np.zeros(DIFF_NPARAM)
+    check(lib().sg_diff_init_theta(C.byref(p), _ptr(t)))
+    return t
+
+
+class DiffModel:
+    """The differentiation form over a set of frames: energies, forces, force-matching loss and
+    their gradients with respect to the 66 fit parameters (see include/sg_api.h)."""
+
+    def __init__(self, frames: Sequence[SimParams], positions: np.ndarray, device: int = 0):
+        arr = (SimParams * len(frames))(*frames)
+        h = C.c_void_p()
+        check(lib().sg_diff_create(arr, len(frames), device, C.byref(h)))
+        self._h = h
+        self.nframes = len(frames)
+        self.n = lib().sg_diff_num_atoms(h)
+        self.set_positions(positions)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().sg_diff_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_positions(self, r: np.ndarray) -> None:
+        r = np.ascontiguousarray(r, np.float32).reshape(self.n, 4)
+        check(lib().sg_diff_set_positions(self._h, _ptr(r)))
+
+    def energy(self, theta: np.ndarray, grad: bool = True):
+        theta = np.ascontiguousarray(theta, np.float64)
+        e = np.zeros(self.nframes)
+        g = np.zeros(DIFF_NPARAM) if grad else None
+        check(lib().sg_diff_energy(self._h, _ptr(theta), _ptr(e), _ptr(g)))
+        return (e, g) if grad else e
+
+    def forces(self, theta: np.ndarray) -> np.ndarray:
+        theta = np.ascontiguousarray(theta, np.float64)
+        f = np.zeros((self.n, 3), np.float32)
+        check(lib().sg_diff_forces(self._h, _ptr(theta), _ptr(f)))
+        return f
+
+    def force_matching(self, theta: np.ndarray, ref_forces: np.ndarray, grad: bool = True):
+        theta = np.ascontiguousarray(theta, np.float64)
+        ref = np.ascontiguousarray(ref_forces, np.float32).reshape(self.n, 3)
+        loss = np.zeros(1)
+        g = np.zeros(DIFF_NPARAM) if grad else None
+        check(lib().sg_diff_force_matching(self._h, _ptr(theta), _ptr(ref), _ptr(loss), _ptr(g)))
+        return (float(loss[0]), g) if grad else float(loss[0])

@@ -61,3 +61,27 @@ def differentiation_system(seed: int = 5):
     """~20,000 atoms: 18,432 C (24 x 24 units) + 2,000 Ni in one cluster, c2 settings (700 K)."""
     return build_workload(24, 24, [2000], 700.0, seed, step_limit=1000, step_avg=100, step_equil=0,
                           step_rdf=100, limit_rdf=10, delta_t=DT_1FS)
+
+
+def differentiation_frames(n_frames: int = 64, seed: int = 5, every: int = 10, warm: int = 50,
+                           jitter_A: float = 0.05, small_system: bool = False):
+    """Frames of the differentiation form: snapshots every `every` steps of a trajectory of the
+    ~20,000-atom system (or of the 2,217-atom system with small_system=True), each with Gaussian jitter
+    of jitter_A angstrom per coordinate.  Runs the trajectory on the GPU.  Returns (frame
+    parameter blocks, positions of all frames concatenated as (n_frames * nMol, 4) float32)."""
+    from .engine import Simulation, diff_frame_params
+    p, r, v = small(seed=seed) if small_system else differentiation_system(seed=seed)
+    sim = Simulation(p)
+    sim.set_state(r, v, np.zeros((p.nMol, 3), np.float32))
+    sim.step(warm)
+    rng = np.random.RandomState(seed)
+    out = []
+    for _ in range(n_frames):
+        sim.step(every)
+        x = sim.get_state()[0].copy()
+        x[:, :3] += rng.normal(0, jitter_A / 1.42, size=(p.nMol, 3)).astype(np.float32)
+        x[:, 3] = 0.0
+        out.append(x)
+    sim.close()
+    q = diff_frame_params(p)
+    return [q] * n_frames, np.concatenate(out)
