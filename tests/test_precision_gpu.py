@@ -1,0 +1,173 @@
+"""Precision form: 1,000,000 C + 100,000 Ni in 64 clusters of 1,562-1,563 atoms, equilibrated
+at 1,000 K with the thermostat on, then NVE.  PLAIN (the reference's FP32 arithmetic) and MIXED
+(hi/lo positions, FP64 sums) against FP64:
+
+  * force error: RMS over all atoms of |a - a_FP64| / RMS |a_FP64| on the equilibrated state
+    (FP64 oracle forces from the same FP32 positions);
+  * short window: the FP64 oracle, PLAIN and MIXED advance the same state; RMS position deviation
+    from FP64 and total-energy difference after the window;
+  * NVE energy drift (eV/atom/ns) and fluctuation of PLAIN and MIXED;
+  * RDF: the 0-15 A / 300-bin metal histogram of the GPU against FP64 pair counts (periodic
+    k-d tree) on the same positions, L1 distance.
+
+The lengths are sized for a test run; SG_PRECISION=full selects the long ones (1,000
+equilibration steps, 20,000 NVE steps, a 200-step FP64 window), and SG_PRECISION_REPORT=<path>
+writes the numbers as JSON.  The reference's graphene model gains about 1.8 eV/atom/ns in NVE at
+1,000 K (it applies the second-neighbour angle forces without their energy); within 100,000 NVE
+steps the heated system crowds a cell past the reference's 64-atom cap, which the library
+reports as SG_ERR_CELL_OVERFLOW, so the NVE leg stops at 20 ps.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from surfacegrowthconsole_gb300 import MODE_MIXED, MODE_PLAIN, workloads
+from surfacegrowthconsole_gb300.engine import Simulation
+
+pytestmark = pytest.mark.gpu
+
+FULL = os.environ.get("SG_PRECISION") == "full"
+EQUIL = 1000 if FULL else 200
+NVE_STEPS = 20000 if FULL else 2000
+WINDOW = 200 if FULL else 20
+EV = 0.06275049
+A = 1.42  # length unit, angstrom
+RDF_BINS, RDF_RANGE = 300, 15.0 / A
+REPORT = {"equilibration_steps": EQUIL, "nve_steps": NVE_STEPS, "fp64_window_steps": WINDOW}
+
+
+def _write_report():
+    path = os.environ.get("SG_PRECISION_REPORT")
+    if path:
+        with open(path, "w") as f:
+            json.dump(REPORT, f, indent=1, default=float)
+
+
+@pytest.fixture(scope="module")
+def state():
+    p, r, v = workloads.precision(seed=3)
+    REPORT["atoms"] = p.nMol
+    REPORT["metal_atoms"] = p.nMolMe
+    sim = Simulation(p)
+    sim.set_state(r, v, np.zeros((p.nMol, 3), np.float32))
+    sim.step(EQUIL)
+    r, v, a = sim.get_state()
+    REPORT["kinetic_energy_after_equilibration_eV_per_atom"] = float(sim.thermo().kinEnergy) * EV
+    sim.close()
+    q = p.copy()
+    q.stepEquil = 10 ** 9   # thermostat, shear and diffusion start after stepEquil: NVE
+    q.stepCool = 10 ** 9
+    yield q, r, v, a
+    _write_report()
+
+
+def _forces(p, r, v, mode):
+    sim = Simulation(p, mode=mode)
+    sim.set_state(r, v, np.zeros((p.nMol, 3), np.float32))
+    sim.build_lists()
+    sim.compute_forces()
+    acc = sim.get_state()[2].astype(np.float64)
+    sim.close()
+    return acc
+
+
+def test_force_error_against_fp64(state):
+    p, r, v, _ = state
+    o = oracle.OracleSim(p, 64)
+    o.set_state(r, v, np.zeros((p.nMol, 3), np.float32))
+    o.build_lists()
+    o.compute_forces()
+    a64 = o.get_state64()[2]
+    scale = np.sqrt((a64 ** 2).mean())
+    err = {name: float(np.sqrt(((_forces(p, r, v, m) - a64) ** 2).mean()) / scale)
+           for name, m in (("plain", MODE_PLAIN), ("mixed", MODE_MIXED))}
+    REPORT["force_rms_error_vs_fp64"] = err
+    assert err["mixed"] <= 1e-4 and err["mixed"] <= 2.0 * err["plain"] + 1e-7, err
+
+
+def _min_image(d, p):
+    L = np.array([p.region.x, p.region.y, p.region.z])
+    return d - L * np.round(d / L)
+
+
+def test_short_window_against_fp64(state):
+    p, r, v, a = state
+    o = oracle.OracleSim(p, 64)
+    o.set_state(r, v, a)
+    o.step(WINDOW)
+    r64 = o.get_state64()[0]
+    t64 = o.thermo()
+    e64 = t64.kinEnergy64 + t64.potEnergy64
+    out = {}
+    for name, m in (("plain", MODE_PLAIN), ("mixed", MODE_MIXED)):
+        sim = Simulation(p, mode=m)
+        sim.set_state(r, v, a)
+        sim.step(WINDOW)
+        rg = sim.get_state()[0].astype(np.float64)
+        t = sim.thermo()
+        e = t.kinEnergy64 + t.potEnergy64 if m == MODE_MIXED else float(t.totEnergy)
+        sim.close()
+        dev = _min_image(rg[:, :3] - r64[:, :3], p)
+        out[name] = {"rms_position_deviation_A": float(np.sqrt((dev ** 2).sum(1).mean())) * A,
+                     "max_position_deviation_A": float(np.sqrt((dev ** 2).sum(1)).max()) * A,
+                     "energy_minus_fp64_eV_per_atom": (e - e64) * EV}
+    REPORT["fp64_window"] = out
+    for name in out:
+        assert out[name]["rms_position_deviation_A"] < 1e-2, out
+
+
+def test_nve_drift(state):
+    p, r, v, a = state
+    every = 100
+    out = {}
+    for name, m in (("plain", MODE_PLAIN), ("mixed", MODE_MIXED)):
+        sim = Simulation(p, mode=m)
+        sim.set_state(r, v, a)
+        es = []
+        for _ in range(NVE_STEPS // every):
+            sim.step(every)
+            t = sim.thermo()
+            es.append(t.kinEnergy64 + t.potEnergy64 if m == MODE_MIXED else float(t.totEnergy))
+        sim.close()
+        x = np.arange(len(es)) * every
+        c = np.polyfit(x, es, 1)
+        out[name] = {"drift_eV_per_atom_per_ns": float(c[0]) * 1e6 * EV,  # 1 step = 1 fs
+                     "fluctuation_eV_per_atom": float(np.std(np.array(es) - np.polyval(c, x))) * EV,
+                     "first_eV": es[0] * EV, "last_eV": es[-1] * EV}
+    REPORT["nve"] = out
+    d_plain = abs(out["plain"]["drift_eV_per_atom_per_ns"])
+    d_mixed = abs(out["mixed"]["drift_eV_per_atom_per_ns"])
+    assert d_mixed <= 1.1 * d_plain + 1e-3, out
+
+
+def _fp64_rdf(p, r):
+    """Metal pair counts per bin in FP64 (periodic k-d tree; ordered pairs, as the GPU counts)."""
+    from scipy.spatial import cKDTree
+    L = np.array([p.region.x, p.region.y, p.region.z], np.float64)
+    x = np.mod(r[:p.nMolMe, :3].astype(np.float64) + 0.5 * L, L)
+    tree = cKDTree(x, boxsize=L)
+    edges = np.arange(1, RDF_BINS + 1) * (RDF_RANGE / RDF_BINS)
+    cum = tree.count_neighbors(tree, edges).astype(np.int64) - p.nMolMe  # drop the self pairs
+    return np.diff(np.concatenate([[0], cum]))
+
+
+def test_rdf_against_fp64(state):
+    p, r, v, _ = state
+    h64 = _fp64_rdf(p, r)
+    out = {}
+    for name, m in (("plain", MODE_PLAIN), ("mixed", MODE_MIXED)):
+        sim = Simulation(p, mode=m, rdf_ext_bins=RDF_BINS, rdf_ext_range=RDF_RANGE)
+        sim.set_state(r, v, np.zeros((p.nMol, 3), np.float32))
+        sim.build_lists()
+        sim.reset_rdf()
+        sim.eval_rdf()
+        h = sim.rdf_ext(0, RDF_BINS).astype(np.int64)
+        sim.close()
+        out[name] = {"l1_distance": float(np.abs(h - h64).sum() / h64.sum()), "pairs": int(h.sum()),
+                     "pairs_fp64": int(h64.sum())}
+    REPORT["rdf_0_15A"] = out
+    for name in out:
+        assert out[name]["l1_distance"] < 1e-3, out
