@@ -29,6 +29,10 @@ its own context, for comparison.
 --workload diff: the differentiation form: gradients of the force-matching loss with respect to
 the 66 fit parameters (LJ epsilon, sigma, 64 EAM spline coefficients) over 64 jittered frames of
 the ~20,000-atom graphene + Ni system, forward + adjoint per gradient; metric grads/s.
+Launch shape: before the warm-up, sg_autotune times the lanes per metal atom (4, 8, 16, 32) and
+the list build's blocks per SM (2, 4, 8, 16) on the workload's own state, keeps the fastest and
+restores the state (--no-tune keeps the defaults, 16 lanes and 8 blocks per SM); the line's
+config carries the choice and the trial timings.
 Multi-GPU (torchrun): replicas only -- each rank runs its own seeded system, no collective on
 the data path; value is the sum over ranks over the slowest rank's time.
 """
@@ -64,6 +68,7 @@ def parse():
     ap.add_argument("--cpu-sample-steps", type=int, default=300)
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--workload", default="production", choices=["production", "batched", "diff"])
     ap.add_argument("--replicas", type=int, default=256)
     return ap.parse_args()
@@ -227,6 +232,7 @@ def run_batched(args, rank: int, world: int, local: int):
     stream = torch.cuda.Stream(device=local)
     sim = Simulation(plist, device=local, stream=stream.cuda_stream)
     sim.set_state(r, v, np.zeros((natoms, 3), np.float32))
+    tune = None if args.no_tune else sim.autotune(steps=10)
     sim.step(args.warmup)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
@@ -272,7 +278,8 @@ def run_batched(args, rank: int, world: int, local: int):
                 "config": {"workload": f"{len(plist)} replicas, {natoms} atoms in all, graphene 1,000-20,000 C + "
                                        "one Ni cluster of 50-2,000 atoms each, 300-1,500 K, lists rebuilt by the "
                                        "reference's rule", "replicas": len(plist), "atoms": natoms,
-                           "l2": "state larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
+                           "l2": "state larger than L2 (no flush)", "parallelism": f"replicas x{world}",
+                           "launch_shape": tune},
                 "clocks": clk.summary(), "gpu_launches": launches, "rebuilds_all_replicas": rebuilds,
                 "one_by_one": {"value": one, "unit": "atom-steps/s", "steps": k1,
                                "ms_all_replicas_per_step": 1e3 * t_one / k1}}
@@ -348,6 +355,7 @@ def main():
     sim = Simulation(p, mode=mode, force_rebuild=True, device=local, stream=stream.cuda_stream, phase_timing=True,
                      rdf_ext_bins=RDF_EXT_BINS, rdf_ext_range=RDF_EXT_RANGE)
     sim.set_state(r, v, a)
+    tune = None if args.no_tune else sim.autotune(steps=20)
     sim.step(args.warmup)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
@@ -439,7 +447,7 @@ def main():
                 "config": {"workload": f"graphene 40000 C + 8 Ni clusters ({p.nMolMe} Ni), {p.nMol} atoms per "
                                        "GPU, 700 K, dt 1 fs, lists rebuilt every step, RDF + diffusion on",
                            "atoms_per_gpu": p.nMol, "mode": args.mode, "l2": "flushed between timed steps",
-                           "parallelism": f"replicas x{world}"},
+                           "parallelism": f"replicas x{world}", "launch_shape": tune},
                 "clocks": clk.summary(), "gpu_launches": launches, "roofline": roof,
                 "step_roofline": step_roof, "e2e": e2e,
                 "cpu_baseline": cpu}

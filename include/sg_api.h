@@ -72,8 +72,10 @@ typedef struct sg_options {
     int rdf_ext_bins;      /* >0: also accumulate an all-pairs metal-metal RDF */
     float rdf_ext_range;   /* its range, dimensionless length */
     int eam_table_knots;   /* MIXED: intervals of the tabulated EAM pair functions (0: 1024; -1: analytic) */
-    int tune_force_tpa;    /* threads per atom in the carbon force pass (0: auto) */
-    int tune_block;        /* block size of the per-atom passes (0: auto) */
+    int metal_lanes;       /* lanes per metal atom in the density and metal force passes:
+                            * 4, 8, 16 or 32 (0: 16) */
+    int nebr_blocks_per_sm;/* resident 128-thread blocks per SM of the list build's work queue,
+                            * 1..32 (0: 8) */
     int phase_timing;      /* 1: record CUDA events between the phases of every step */
     int reserved[7];
 } sg_options;
@@ -335,9 +337,19 @@ int sg_diff_force_matching(sg_diff *d, const double *theta, const float *ref_for
                            double *grad);
 
 /* ---- tuning ------------------------------------------------------------------------------- */
-/* Times the candidate launch shapes of the tunable passes on the context's own state for
- * `steps` steps each, keeps the fastest; state is restored afterwards. */
+/* Times the launch shapes of the tunable passes on the context's own state and keeps the
+ * fastest: the metal lanes per atom (4, 8, 16, 32; `steps` steps each, the context's own
+ * rebuild schedule), then the list build's blocks per SM (2, 4, 8, 16; `steps` steps each with
+ * a rebuild in every step).  Every device buffer and the host step counters are copied first
+ * and put back after each trial, so the context continues from the state it had; the trials
+ * change no results but the summation order of the metal passes.  `report` (if not NULL)
+ * receives a JSON object with the milliseconds per step of every trial and the choice.
+ * steps <= 0 selects 20. */
 int sg_autotune(sg_ctx *ctx, int steps, char *report, int report_len);
+/* The launch shape in use (from the options, or as sg_autotune chose it). */
+int sg_get_launch_shape(sg_ctx *ctx, int *metal_lanes, int *nebr_blocks_per_sm);
+/* Sets the launch shape (a shape an earlier sg_autotune reported, for instance). */
+int sg_set_launch_shape(sg_ctx *ctx, int metal_lanes, int nebr_blocks_per_sm);
 
 #ifdef __cplusplus
 }

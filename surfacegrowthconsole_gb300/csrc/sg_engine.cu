@@ -62,6 +62,7 @@ static int devAlloc(sg_ctx *c, void **p, size_t bytes) {
   cudaError_t e = cudaMalloc(p, bytes);
   if (e != cudaSuccess) return sg_fail(SG_ERR_NOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
   c->allocs.push_back(*p);
+  c->regions.emplace_back(*p, bytes);
   e = cudaMemsetAsync(*p, 0, bytes, c->stream);
   if (e != cudaSuccess) return sg_fail(SG_ERR_CUDA, "cudaMemset: %s", cudaGetErrorString(e));
   return SG_OK;
@@ -168,6 +169,32 @@ static void destroyGraphs(sg_ctx *c) {
   c->graphs.clear();
 }
 
+// Launch shape of the metal chain: lanes per metal atom and the matching block table.
+static int setMetalLanes(sg_ctx *c, int lanes) {
+  const int slot = lanes == 4 ? 0 : lanes == 8 ? 1 : lanes == 16 ? 2 : lanes == 32 ? 3 : -1;
+  if (slot < 0) return sg_fail(SG_ERR_INVALID, "metal_lanes %d: 4, 8, 16 or 32", lanes);
+  DevTab &t = c->metalLaneTab[slot];
+  if (!t.rep) {
+    const int rc = makeRangeTab(c, t, 128 / lanes, 1);
+    if (rc) return rc;
+  }
+  if (lanes != c->metalLanes) destroyGraphs(c);
+  c->metalLanes = lanes;
+  c->metalRun = t;
+  return SG_OK;
+}
+
+// Grid of the list build's work queue: blocksPerSM resident blocks per SM, no more blocks
+// than there are cells for their warps.
+static void setNebrBlocks(sg_ctx *c, int blocksPerSM) {
+  const int g = std::max(1, std::min((c->ctot + kNebrWarps - 1) / kNebrWarps, c->numSMs * blocksPerSM));
+  if (g != c->nebrGrid) destroyGraphs(c);
+  c->nebrGrid = g;
+  c->nebrBlocksPerSM = blocksPerSM;
+}
+
+void sg_register_region(sg_ctx *c, void *p, size_t bytes) { c->regions.emplace_back(p, bytes); }
+
 extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_options *opt, sg_ctx **out) {
   if (!params || n_replicas < 1 || !out) return sg_fail(SG_ERR_INVALID, "sg_create: bad arguments");
   *out = nullptr;
@@ -234,7 +261,12 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
   c->ntot = atomOff;
   c->ctot = cellOff;
   // list build: one warp per home cell, a grid of a few resident blocks per SM walking the cells
-  c->nebrGrid = std::max(1, std::min((c->ctot + kNebrWarps - 1) / kNebrWarps, numSMs * 8));
+  c->numSMs = numSMs;
+  if (c->opt.nebr_blocks_per_sm < 0 || c->opt.nebr_blocks_per_sm > 32) {
+    sg_destroy(c);
+    return sg_fail(SG_ERR_INVALID, "nebr_blocks_per_sm %d: 0 (default) or 1..32", c->opt.nebr_blocks_per_sm);
+  }
+  setNebrBlocks(c, c->opt.nebr_blocks_per_sm ? c->opt.nebr_blocks_per_sm : 8);
   const size_t N = c->ntot;
 #define AL(ptr, n)                          \
   if ((rc = devAllocT(c, &ptr, (n)))) {     \
@@ -273,6 +305,11 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
   if ((rc = makeRangeTab(c, c->atomTab, 128, 0)) || (rc = makeRangeTab(c, c->metalTab, 128, 1)) ||
       (rc = makeRangeTab(c, c->carbonTab, 128, 2)) || (rc = makeRangeTab(c, c->metalTabT, kMetalPerBlock, 1)) ||
       (rc = makeRangeTab(c, c->carbonTabT, kCarbonPerBlock, 2))) {
+    sg_destroy(c);
+    return rc;
+  }
+  c->metalLaneTab[2] = c->metalTabT;
+  if ((rc = setMetalLanes(c, c->opt.metal_lanes ? c->opt.metal_lanes : kMT))) {
     sg_destroy(c);
     return rc;
   }
@@ -483,14 +520,12 @@ static int enqueueRebuild(sg_ctx *c, int force) {
 // reduction.  Inside a capture the fork and join become graph edges.
 static int enqueueForces(sg_ctx *c, bool withCmVel) {
   if (c->opt.mode == SG_MODE_MIXED) return sg_mixed_enqueue_forces(c);
-  const bool fork = c->metalTabT.n > 0;
+  const bool fork = c->metalRun.n > 0;
   if (fork) {
     CK(cudaEventRecord(c->evFork, c->stream));
     CK(cudaStreamWaitEvent(c->side, c->evFork, 0));
-    k_rho<<<c->metalTabT.n, 128, 0, c->side>>>(c->metalTabT.view(), c->rc, c->pos, c->nn, c->nbl, c->rho, c->dF,
-                                               c->Fv, c->rowStride);
-    k_force_metal<<<c->metalTabT.n, 128, 0, c->side>>>(c->metalTabT.view(), c->rc, c->pos, c->acc, c->nn, c->nbl,
-                                                       c->dF, c->Fv, c->fric, c->rowStride);
+    launchMetalChain(c->metalLanes, c->metalRun.n, c->side, c->metalRun.view(), c->rc, c->pos, c->acc, c->nn,
+                     c->nbl, c->rho, c->dF, c->Fv, c->fric, c->rowStride);
     if (withCmVel && c->cmvTab.n)
       k_cmvel<<<c->cmvTab.n, kRedThreads, 0, c->side>>>(c->cmvTab.view(), c->rc, c->st, c->vel, c->acc,
                                                         c->partialCmv, c->dCmvFirst);
@@ -927,9 +962,151 @@ sg_prop &sg_one_step_prop(sg_ctx *c, int rep) { return c->oneStep[rep]; }
 int sg_check_flags(sg_ctx *c) { return checkFlags(c); }
 
 // ---- autotuner ----------------------------------------------------------------------------
-// Placeholder: PLAIN mode has no tunable launch shape yet.
-extern "C" int sg_autotune(sg_ctx *c, int, char *report, int report_len) {
+// A copy of every device buffer of the context and of the host's step counters.  The trials
+// run real steps on the context's own state; the copy is put back after each.
+namespace {
+struct Snapshot {
+  void *dev = nullptr;           // one device block holding all buffers, or
+  std::vector<char> host;        // a host copy when the device has no room
+  std::vector<std::pair<void *, size_t>> regions;  // the buffers copied
+  int stepCount = 0, countRdf = 0, lastVariant = 0;
+};
+
+int takeSnapshot(sg_ctx *c, Snapshot &s) {
+  s.regions = c->regions;
+  size_t total = 0;
+  for (auto &r : s.regions) total += (r.second + 255) & ~size_t(255);
+  CK(cudaStreamSynchronize(c->stream));
+  if (cudaMalloc(&s.dev, std::max<size_t>(total, 256)) != cudaSuccess) {
+    cudaGetLastError();
+    s.dev = nullptr;
+    s.host.resize(total);
+  }
+  size_t off = 0;
+  for (auto &r : s.regions) {
+    char *dst = s.dev ? static_cast<char *>(s.dev) + off : s.host.data() + off;
+    CK(cudaMemcpyAsync(dst, r.first, r.second, s.dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                       c->stream));
+    off += (r.second + 255) & ~size_t(255);
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  s.stepCount = c->stepCount;
+  s.countRdf = c->countRdf;
+  s.lastVariant = c->lastVariant;
+  return SG_OK;
+}
+
+int restoreSnapshot(sg_ctx *c, const Snapshot &s) {
+  CK(cudaStreamSynchronize(c->stream));
+  size_t off = 0;
+  for (auto &r : s.regions) {
+    const char *src = s.dev ? static_cast<const char *>(s.dev) + off : s.host.data() + off;
+    CK(cudaMemcpyAsync(r.first, src, r.second, s.dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                       c->stream));
+    off += (r.second + 255) & ~size_t(255);
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  c->stepCount = s.stepCount;
+  c->countRdf = s.countRdf;
+  c->lastVariant = s.lastVariant;
+  return SG_OK;
+}
+
+// Milliseconds per step of `steps` steps after three warm-up steps (which capture the graphs).
+int timeSteps(sg_ctx *c, int steps, float *msPerStep) {
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  int rc = sg_step_async(c, 3);
+  if (!rc) rc = checkFlags(c);
+  if (!rc) {
+    CK(cudaEventRecord(e0, c->stream));
+    rc = sg_step_async(c, steps);
+    CK(cudaEventRecord(e1, c->stream));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    *msPerStep = ms / steps;
+    if (!rc) rc = checkFlags(c);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+}  // namespace
+
+extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
   if (!c) return sg_fail(SG_ERR_INVALID, "null context");
-  if (report && report_len > 0) snprintf(report, report_len, "{}");
+  if (steps <= 0) steps = 20;
+  Snapshot snap;
+  int rc = takeSnapshot(c, snap);
+  if (rc) return rc;
+  const int lanes0 = c->metalLanes, bps0 = c->nebrBlocksPerSM, fr0 = c->opt.force_rebuild;
+  const int laneChoice[4] = {4, 8, 16, 32}, bpsChoice[4] = {2, 4, 8, 16};
+  float laneMs[4] = {}, bpsMs[4] = {};
+  int bestLanes = lanes0, bestBps = bps0;
+  // 1. lanes per metal atom, on the context's own schedule
+  if (c->metalRun.n > 0) {
+    float best = 0.f;
+    for (int k = 0; k < 4 && !rc; k++) {
+      if ((rc = restoreSnapshot(c, snap)) || (rc = setMetalLanes(c, laneChoice[k]))) break;
+      rc = timeSteps(c, steps, &laneMs[k]);
+      if (!rc && (k == 0 || laneMs[k] < best)) { best = laneMs[k]; bestLanes = laneChoice[k]; }
+    }
+  }
+  // 2. blocks per SM of the list build, with a rebuild in every step
+  if (!rc) {
+    c->opt.force_rebuild = 1;
+    destroyGraphs(c);
+    if (!(rc = setMetalLanes(c, bestLanes))) {
+      float best = 0.f;
+      for (int k = 0; k < 4 && !rc; k++) {
+        if ((rc = restoreSnapshot(c, snap))) break;
+        setNebrBlocks(c, bpsChoice[k]);
+        rc = timeSteps(c, steps, &bpsMs[k]);
+        if (!rc && (k == 0 || bpsMs[k] < best)) { best = bpsMs[k]; bestBps = bpsChoice[k]; }
+      }
+    }
+    c->opt.force_rebuild = fr0;
+    destroyGraphs(c);
+  }
+  // the state as it was, with the chosen shape (the starting shape if a trial failed)
+  const int rc2 = restoreSnapshot(c, snap);
+  if (snap.dev) cudaFree(snap.dev);
+  if (rc) {
+    setMetalLanes(c, lanes0);
+    setNebrBlocks(c, bps0);
+    return rc;
+  }
+  if (rc2) return rc2;
+  if ((rc = setMetalLanes(c, bestLanes))) return rc;
+  setNebrBlocks(c, bestBps);
+  if (report && report_len > 0) {
+    snprintf(report, report_len,
+             "{\"steps\": %d, \"metal_lanes_ms_per_step\": {\"4\": %.6g, \"8\": %.6g, \"16\": %.6g, "
+             "\"32\": %.6g}, \"nebr_blocks_per_sm_ms_per_step_rebuilding\": {\"2\": %.6g, \"4\": %.6g, "
+             "\"8\": %.6g, \"16\": %.6g}, \"metal_lanes\": %d, \"nebr_blocks_per_sm\": %d, "
+             "\"nebr_grid\": %d}",
+             steps, laneMs[0], laneMs[1], laneMs[2], laneMs[3], bpsMs[0], bpsMs[1], bpsMs[2], bpsMs[3],
+             c->metalLanes, c->nebrBlocksPerSM, c->nebrGrid);
+  }
+  return SG_OK;
+}
+
+extern "C" int sg_set_launch_shape(sg_ctx *c, int metal_lanes, int nebr_blocks_per_sm) {
+  if (!c) return sg_fail(SG_ERR_INVALID, "null context");
+  if (nebr_blocks_per_sm < 1 || nebr_blocks_per_sm > 32)
+    return sg_fail(SG_ERR_INVALID, "nebr_blocks_per_sm %d: 1..32", nebr_blocks_per_sm);
+  CK(cudaStreamSynchronize(c->stream));
+  const int rc = setMetalLanes(c, metal_lanes);
+  if (rc) return rc;
+  setNebrBlocks(c, nebr_blocks_per_sm);
+  return SG_OK;
+}
+
+extern "C" int sg_get_launch_shape(sg_ctx *c, int *metal_lanes, int *nebr_blocks_per_sm) {
+  if (!c) return sg_fail(SG_ERR_INVALID, "null context");
+  if (metal_lanes) *metal_lanes = c->metalLanes;
+  if (nebr_blocks_per_sm) *nebr_blocks_per_sm = c->nebrBlocksPerSM;
   return SG_OK;
 }

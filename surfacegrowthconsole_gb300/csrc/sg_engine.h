@@ -52,6 +52,13 @@ struct sg_ctx {
   size_t *dDiffOff = nullptr;
   DevTab atomTab, metalTab, carbonTab, redTab, cmvTab, tileTab;
   DevTab metalTabT, carbonTabT;  // blocks of kMetalPerBlock / kCarbonPerBlock atoms
+  // launch shape of the metal chain: lanes per atom and its block table (128 / lanes atoms per
+  // block; lanes 4, 8, 16, 32 -> slot 0..3, made on first use, slot 2 is metalTabT)
+  int metalLanes = sg::kMT;
+  DevTab metalLaneTab[4];
+  DevTab metalRun;
+  int numSMs = 0, nebrBlocksPerSM = 8;
+  std::vector<std::pair<void *, size_t>> regions;  // every device buffer with its size
   int anyMetal = 0, anyCarbon = 0, maxHist = 0;
   // graphs keyed by variant bits
   std::map<int, cudaGraphExec_t> graphs;
@@ -83,4 +90,6 @@ int sg_mixed_init(sg_ctx *c);
 void sg_mixed_free(sg_ctx *c);
 int sg_mixed_enqueue_integrate(sg_ctx *c, int forceRebuild);
 int sg_mixed_enqueue_forces(sg_ctx *c);
+// registers a buffer the library allocated outside devAlloc (autotuner snapshots)
+void sg_register_region(sg_ctx *c, void *p, size_t bytes);
 int sg_mixed_enqueue_reduce(sg_ctx *c, int forceRebuild);

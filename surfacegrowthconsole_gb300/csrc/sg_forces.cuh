@@ -14,10 +14,12 @@
 // analytic forms; the table buffer is one more kernel parameter.
 #ifdef SG_EAM_TABLE
 #define SG_EAM_PARAM , const float4 *__restrict__ eamTab
+#define SG_EAM_ARG , eamTab
 #define SG_EAM_PAIR(P, r) eamPairTab(P, eamTab, r)
 #define SG_EAM_DENS(P, r) eamDensTab(P, eamTab, r)
 #else
 #define SG_EAM_PARAM
+#define SG_EAM_ARG
 #define SG_EAM_PAIR(P, r) eamPair(P, r)
 #define SG_EAM_DENS(P, r) eamDensity(P, r)
 #endif
@@ -122,18 +124,24 @@ __device__ __forceinline__ float eamDensTab(const RepConst &P, const float4 *tab
 #endif
 
 // Electron density of each metal atom (EamComputeRhoK, cu:716-773), plus F(rho) and F'(rho),
-// which the reference re-evaluates per pair in the force kernel.  kMT lanes share one metal
-// atom: lane l takes list entries l, l + kMT, ...; the partial sums meet in a shuffle tree.
-__global__ void __launch_bounds__(128) SG_KN(k_rho)(BlockTab tab, const RepConst *__restrict__ rc,
-                                             const float4 *__restrict__ pos, const int *__restrict__ nn,
-                                             const int *__restrict__ nbl, float *__restrict__ rho,
-                                             float *__restrict__ dF, float *__restrict__ Fv,
-                                             int rowStride SG_EAM_PARAM) {
+// which the reference re-evaluates per pair in the force kernel.  MT lanes share one metal
+// atom (128 / MT atoms per block): lane l takes list entries l, l + MT, ...; the partial sums
+// meet in a shuffle tree.  k_rho runs MT = kMT; k_rho_tpa<MT> the choices of the autotuner.
+template <int MT> __device__ __forceinline__ unsigned laneGroupMask() {
+  return MT == 32 ? 0xffffffffu : ((1u << MT) - 1) << (threadIdx.x & 31 & ~(MT - 1));
+}
+
+template <int MT>
+__device__ __forceinline__ void SG_KN(rhoBody)(BlockTab tab, const RepConst *__restrict__ rc,
+                                               const float4 *__restrict__ pos, const int *__restrict__ nn,
+                                               const int *__restrict__ nbl, float *__restrict__ rho,
+                                               float *__restrict__ dF, float *__restrict__ Fv,
+                                               int rowStride SG_EAM_PARAM) {
   const int rep = tab.rep[blockIdx.x];
   const RepConst &P = rc[rep];
-  const int sub = threadIdx.x & (kMT - 1);
-  const unsigned gmask = ((1u << kMT) - 1) << (threadIdx.x & 31 & ~(kMT - 1));
-  const int i = tab.start[blockIdx.x] + threadIdx.x / kMT;
+  const int sub = threadIdx.x & (MT - 1);
+  const unsigned gmask = laneGroupMask<MT>();
+  const int i = tab.start[blockIdx.x] + threadIdx.x / MT;
   const int metalEnd = P.atomOff + P.nMolMe;
   const bool valid = i < metalEnd;
   float sum = 0.f;
@@ -141,7 +149,7 @@ __global__ void __launch_bounds__(128) SG_KN(k_rho)(BlockTab tab, const RepConst
     const float4 A = pos[i];
     const int n = nn[i];
     const int *row = nbl + (size_t)i * rowStride;
-    for (int j = sub; j < n; j += kMT) {
+    for (int j = sub; j < n; j += MT) {
       const int k = row[j];
       const float4 B = pos[k];
       const float dx = minImg(A.x - B.x, P.region[0]);
@@ -152,12 +160,28 @@ __global__ void __launch_bounds__(128) SG_KN(k_rho)(BlockTab tab, const RepConst
     }
   }
 #pragma unroll
-  for (int o = kMT / 2; o > 0; o >>= 1) sum += __shfl_xor_sync(gmask, sum, o);
+  for (int o = MT / 2; o > 0; o >>= 1) sum += __shfl_xor_sync(gmask, sum, o);
   if (valid && sub == 0) {
     rho[i] = sum;
     dF[i] = eamEmbedDeriv(P, sum);
     Fv[i] = eamEmbed(P, sum);
   }
+}
+
+__global__ void __launch_bounds__(128) SG_KN(k_rho)(BlockTab tab, const RepConst *__restrict__ rc,
+                                             const float4 *__restrict__ pos, const int *__restrict__ nn,
+                                             const int *__restrict__ nbl, float *__restrict__ rho,
+                                             float *__restrict__ dF, float *__restrict__ Fv,
+                                             int rowStride SG_EAM_PARAM) {
+  SG_KN(rhoBody)<kMT>(tab, rc, pos, nn, nbl, rho, dF, Fv, rowStride SG_EAM_ARG);
+}
+template <int MT>
+__global__ void __launch_bounds__(128) SG_KN(k_rho_tpa)(BlockTab tab, const RepConst *__restrict__ rc,
+                                                 const float4 *__restrict__ pos, const int *__restrict__ nn,
+                                                 const int *__restrict__ nbl, float *__restrict__ rho,
+                                                 float *__restrict__ dF, float *__restrict__ Fv,
+                                                 int rowStride SG_EAM_PARAM) {
+  SG_KN(rhoBody)<MT>(tab, rc, pos, nn, nbl, rho, dF, Fv, rowStride SG_EAM_ARG);
 }
 
 // Lennard-Jones metal-carbon term (cu:880-884).
@@ -169,17 +193,20 @@ __device__ __forceinline__ void ljTerms(const RepConst &P, float rr, float &fc, 
 }
 
 // Forces on metal atoms: EAM pair + embedding with metal neighbours, LJ with carbon neighbours
-// (ComputeForcesK case 0, cu:856-897, epilogue cu:1069-1082); kMT lanes per atom.
-__global__ void __launch_bounds__(128) SG_KN(k_force_metal)(BlockTab tab, const RepConst *__restrict__ rc,
-                                                     float4 *__restrict__ pos, float4 *__restrict__ acc,
-                                                     const int *__restrict__ nn, const int *__restrict__ nbl,
-                                                     const float *__restrict__ dF, const float *__restrict__ Fv,
-                                                     float *__restrict__ fric, int rowStride SG_EAM_PARAM) {
+// (ComputeForcesK case 0, cu:856-897, epilogue cu:1069-1082); MT lanes per atom as in the
+// density pass (k_force_metal: MT = kMT; k_force_metal_tpa<MT>: the autotuner's choices).
+template <int MT>
+__device__ __forceinline__ void SG_KN(forceMetalBody)(BlockTab tab, const RepConst *__restrict__ rc,
+                                                      float4 *__restrict__ pos, float4 *__restrict__ acc,
+                                                      const int *__restrict__ nn, const int *__restrict__ nbl,
+                                                      const float *__restrict__ dF,
+                                                      const float *__restrict__ Fv, float *__restrict__ fric,
+                                                      int rowStride SG_EAM_PARAM) {
   const int rep = tab.rep[blockIdx.x];
   const RepConst &P = rc[rep];
-  const int sub = threadIdx.x & (kMT - 1);
-  const unsigned gmask = ((1u << kMT) - 1) << (threadIdx.x & 31 & ~(kMT - 1));
-  const int i = tab.start[blockIdx.x] + threadIdx.x / kMT;
+  const int sub = threadIdx.x & (MT - 1);
+  const unsigned gmask = laneGroupMask<MT>();
+  const int i = tab.start[blockIdx.x] + threadIdx.x / MT;
   const int metalEnd = P.atomOff + P.nMolMe;
   const bool valid = i < metalEnd;
   float fx = 0.f, fy = 0.f, fz = 0.f, rx = 0.f, u = 0.f;
@@ -188,7 +215,7 @@ __global__ void __launch_bounds__(128) SG_KN(k_force_metal)(BlockTab tab, const 
     const int n = nn[i];
     const float dFi = dF[i];
     const int *row = nbl + (size_t)i * rowStride;
-    for (int j = sub; j < n; j += kMT) {
+    for (int j = sub; j < n; j += MT) {
       const int k = row[j];
       const float4 B = pos[k];
       const float dx = minImg(A.x - B.x, P.region[0]);
@@ -215,7 +242,7 @@ __global__ void __launch_bounds__(128) SG_KN(k_force_metal)(BlockTab tab, const 
     }
   }
 #pragma unroll
-  for (int o = kMT / 2; o > 0; o >>= 1) {
+  for (int o = MT / 2; o > 0; o >>= 1) {
     fx += __shfl_xor_sync(gmask, fx, o);
     fy += __shfl_xor_sync(gmask, fy, o);
     fz += __shfl_xor_sync(gmask, fz, o);
@@ -226,6 +253,47 @@ __global__ void __launch_bounds__(128) SG_KN(k_force_metal)(BlockTab tab, const 
     acc[i] = make_float4(fx / P.massMe, fy / P.massMe, fz / P.massMe, 0.f);
     pos[i].w = 0.5f * u + Fv[i];
     if (P.hasFric) fric[i] = rx;
+  }
+}
+
+__global__ void __launch_bounds__(128) SG_KN(k_force_metal)(BlockTab tab, const RepConst *__restrict__ rc,
+                                                     float4 *__restrict__ pos, float4 *__restrict__ acc,
+                                                     const int *__restrict__ nn, const int *__restrict__ nbl,
+                                                     const float *__restrict__ dF, const float *__restrict__ Fv,
+                                                     float *__restrict__ fric, int rowStride SG_EAM_PARAM) {
+  SG_KN(forceMetalBody)<kMT>(tab, rc, pos, acc, nn, nbl, dF, Fv, fric, rowStride SG_EAM_ARG);
+}
+template <int MT>
+__global__ void __launch_bounds__(128) SG_KN(k_force_metal_tpa)(BlockTab tab, const RepConst *__restrict__ rc,
+                                                         float4 *__restrict__ pos, float4 *__restrict__ acc,
+                                                         const int *__restrict__ nn, const int *__restrict__ nbl,
+                                                         const float *__restrict__ dF,
+                                                         const float *__restrict__ Fv, float *__restrict__ fric,
+                                                         int rowStride SG_EAM_PARAM) {
+  SG_KN(forceMetalBody)<MT>(tab, rc, pos, acc, nn, nbl, dF, Fv, fric, rowStride SG_EAM_ARG);
+}
+
+// The metal chain with MT lanes per metal atom (4, 8, 16 or 32; grid = the block table for
+// 128 / MT atoms per block), from the host of the including unit.
+void SG_KN(launchMetalChain)(int mt, int grid, cudaStream_t s, BlockTab tab, const RepConst *rc,
+                                    float4 *pos, float4 *acc, const int *nn, const int *nbl, float *rho,
+                                    float *dF, float *Fv, float *fric, int rowStride SG_EAM_PARAM) {
+  switch (mt) {
+    case 4:
+      SG_KN(k_rho_tpa)<4><<<grid, 128, 0, s>>>(tab, rc, pos, nn, nbl, rho, dF, Fv, rowStride SG_EAM_ARG);
+      SG_KN(k_force_metal_tpa)<4><<<grid, 128, 0, s>>>(tab, rc, pos, acc, nn, nbl, dF, Fv, fric, rowStride SG_EAM_ARG);
+      break;
+    case 8:
+      SG_KN(k_rho_tpa)<8><<<grid, 128, 0, s>>>(tab, rc, pos, nn, nbl, rho, dF, Fv, rowStride SG_EAM_ARG);
+      SG_KN(k_force_metal_tpa)<8><<<grid, 128, 0, s>>>(tab, rc, pos, acc, nn, nbl, dF, Fv, fric, rowStride SG_EAM_ARG);
+      break;
+    case 32:
+      SG_KN(k_rho_tpa)<32><<<grid, 128, 0, s>>>(tab, rc, pos, nn, nbl, rho, dF, Fv, rowStride SG_EAM_ARG);
+      SG_KN(k_force_metal_tpa)<32><<<grid, 128, 0, s>>>(tab, rc, pos, acc, nn, nbl, dF, Fv, fric, rowStride SG_EAM_ARG);
+      break;
+    default:
+      SG_KN(k_rho)<<<grid, 128, 0, s>>>(tab, rc, pos, nn, nbl, rho, dF, Fv, rowStride SG_EAM_ARG);
+      SG_KN(k_force_metal)<<<grid, 128, 0, s>>>(tab, rc, pos, acc, nn, nbl, dF, Fv, fric, rowStride SG_EAM_ARG);
   }
 }
 

@@ -36,6 +36,11 @@ __global__ void k_rho(BlockTab tab, const RepConst *rc, const float4 *pos, const
 __global__ void k_force_metal(BlockTab tab, const RepConst *rc, float4 *pos, float4 *acc,
                               const int *nn, const int *nbl, const float *dF, const float *Fv,
                               float *fric, int rowStride);
+// the metal chain (k_rho, k_force_metal) with mt lanes per atom (4, 8, 16, 32) on the table of
+// 128 / mt atoms per block
+void launchMetalChain(int mt, int grid, cudaStream_t s, BlockTab tab, const RepConst *rc, float4 *pos,
+                      float4 *acc, const int *nn, const int *nbl, float *rho, float *dF, float *Fv,
+                      float *fric, int rowStride);
 __global__ void k_force_carbon(BlockTab tab, const RepConst *rc, float4 *pos, float4 *acc,
                                const int *nn, const int *nbl, const int *ns, const int *sl,
                                const int *nrl, const int2 *rl, int rowStride);

@@ -556,14 +556,18 @@ int sg_mixed_init(sg_ctx *c) {
     }
   }
   MCK(cudaMalloc(&m->eamTab, sizeof(float4) * std::max<size_t>(tab.size(), 1)));
+  sg_register_region(c, m->eamTab, sizeof(float4) * std::max<size_t>(tab.size(), 1));
   if (!tab.empty())
     MCK(cudaMemcpyAsync(m->eamTab, tab.data(), sizeof(float4) * tab.size(), cudaMemcpyHostToDevice, c->stream));
   MCK(cudaMemcpyAsync(c->rc, c->hrc.data(), sizeof(RepConst) * c->nrep, cudaMemcpyHostToDevice, c->stream));
   MCK(cudaStreamSynchronize(c->stream));
   const int nRed = std::max(c->redTab.n, 1);
   MCK(cudaMalloc(&m->part64, sizeof(double) * nRed * kMixAcc));
+  sg_register_region(c, m->part64, sizeof(double) * nRed * kMixAcc);
   MCK(cudaMalloc(&m->partF, sizeof(float) * nRed * kMixMax));
+  sg_register_region(c, m->partF, sizeof(float) * nRed * kMixMax);
   MCK(cudaMalloc(&m->counter, sizeof(unsigned) * c->nrep));
+  sg_register_region(c, m->counter, sizeof(unsigned) * c->nrep);
   MCK(cudaMemsetAsync(m->counter, 0, sizeof(unsigned) * c->nrep, c->stream));
   size_t total = 0;
   m->diffOff64.resize(c->nrep);
@@ -573,8 +577,10 @@ int sg_mixed_init(sg_ctx *c) {
     if (p.iRegime == 2) total += (size_t)p.nBuffDiffuse * 6 + (size_t)p.nBuffDiffuse * p.nValDiffuse + p.nValDiffuse;
   }
   MCK(cudaMalloc(&m->diff64, sizeof(double) * std::max<size_t>(total, 1)));
+  sg_register_region(c, m->diff64, sizeof(double) * std::max<size_t>(total, 1));
   MCK(cudaMemsetAsync(m->diff64, 0, sizeof(double) * std::max<size_t>(total, 1), c->stream));
   MCK(cudaMalloc(&m->dDiffOff64, sizeof(size_t) * c->nrep));
+  sg_register_region(c, m->dDiffOff64, sizeof(size_t) * c->nrep);
   MCK(cudaMemcpyAsync(m->dDiffOff64, m->diffOff64.data(), sizeof(size_t) * c->nrep, cudaMemcpyHostToDevice,
                       c->stream));
   MCK(cudaStreamSynchronize(c->stream));
@@ -606,15 +612,12 @@ int sg_mixed_enqueue_integrate(sg_ctx *c, int forceRebuild) {
 // before the reduction, as in PLAIN; no centre-of-mass-velocity pass.
 int sg_mixed_enqueue_forces(sg_ctx *c) {
   MixedBufs *m = static_cast<MixedBufs *>(c->mixed);
-  const bool fork = c->metalTabT.n > 0;
+  const bool fork = c->metalRun.n > 0;
   if (fork) {
     MCK(cudaEventRecord(c->evFork, c->stream));
     MCK(cudaStreamWaitEvent(c->side, c->evFork, 0));
-    k_rho_mixed<<<c->metalTabT.n, 128, 0, c->side>>>(c->metalTabT.view(), c->rc, c->pos, c->nn, c->nbl, c->rho,
-                                                     c->dF, c->Fv, c->rowStride, m->eamTab);
-    k_force_metal_mixed<<<c->metalTabT.n, 128, 0, c->side>>>(c->metalTabT.view(), c->rc, c->pos, c->acc, c->nn,
-                                                             c->nbl, c->dF, c->Fv, c->fric, c->rowStride,
-                                                             m->eamTab);
+    launchMetalChain_mixed(c->metalLanes, c->metalRun.n, c->side, c->metalRun.view(), c->rc, c->pos, c->acc,
+                           c->nn, c->nbl, c->rho, c->dF, c->Fv, c->fric, c->rowStride, m->eamTab);
     if (c->opt.phase_timing) cudaEventRecordWithFlags(c->phaseEv[7], c->side, cudaEventRecordExternal);
     MCK(cudaGetLastError());
   }

@@ -12,6 +12,7 @@ velocities and accelerations (N, 3) float32, metal atoms first.
 from __future__ import annotations
 
 import ctypes as C
+import json
 from typing import Sequence
 
 import numpy as np
@@ -85,7 +86,8 @@ class Simulation:
 
     def __init__(self, params: SimParams | Sequence[SimParams], mode: int = MODE_PLAIN, force_rebuild: bool = False,
                  use_graphs: bool = True, device: int = 0, rdf_ext_bins: int = 0, rdf_ext_range: float = 0.0,
-                 eam_table_knots: int = 0, stream: int = 0, phase_timing: bool = False):
+                 eam_table_knots: int = 0, stream: int = 0, phase_timing: bool = False, metal_lanes: int = 0,
+                 nebr_blocks_per_sm: int = 0):
         plist = [params] if isinstance(params, SimParams) else list(params)
         arr = (SimParams * len(plist))(*plist)
         opt = Options()
@@ -99,6 +101,8 @@ class Simulation:
         opt.eam_table_knots = eam_table_knots
         opt.stream = stream or None
         opt.phase_timing = int(phase_timing)
+        opt.metal_lanes = metal_lanes
+        opt.nebr_blocks_per_sm = nebr_blocks_per_sm
         h = C.c_void_p()
         check(lib().sg_create(arr, len(plist), C.byref(opt), C.byref(h)))
         self._h = h
@@ -254,10 +258,21 @@ class Simulation:
             if f:
                 L.fclose(f)
 
-    def autotune(self, steps: int = 20) -> str:
+    def autotune(self, steps: int = 20) -> dict:
+        """Times the launch shapes (lanes per metal atom, list-build blocks per SM) on this
+        context's state, keeps the fastest and restores the state; returns the timings."""
         buf = C.create_string_buffer(4096)
         check(lib().sg_autotune(self._h, steps, buf, len(buf)))
-        return buf.value.decode()
+        return json.loads(buf.value.decode())
+
+    def launch_shape(self) -> tuple[int, int]:
+        """(lanes per metal atom, list-build blocks per SM) in use."""
+        a, b = C.c_int(), C.c_int()
+        check(lib().sg_get_launch_shape(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def set_launch_shape(self, metal_lanes: int, nebr_blocks_per_sm: int) -> None:
+        check(lib().sg_set_launch_shape(self._h, metal_lanes, nebr_blocks_per_sm))
 
 
 DIFF_NPARAM = 66  # SG_DIFF_NPARAM

@@ -1,0 +1,85 @@
+"""Launch-shape tuning: the lanes per metal atom of the density and metal force passes (4, 8,
+16, 32) change only the summation order of the metal sums; the list build's blocks per SM change
+nothing (every list row is written by the one warp that owns its atom's cell); sg_autotune
+restores the context's state, so a tuned run continues exactly as an untuned one switched to
+the chosen shape at the same step."""
+import numpy as np
+import pytest
+
+from surfacegrowthconsole_gb300 import MODE_MIXED, MODE_PLAIN, workloads
+from surfacegrowthconsole_gb300.engine import Simulation
+
+pytestmark = pytest.mark.gpu
+
+SUM_ORDER_RTOL = 2e-6
+
+
+def _forces(p, r, v, **shape):
+    sim = Simulation(p, **shape)
+    sim.set_state(r, v, np.zeros((p.nMol, 3), np.float32))
+    sim.build_lists()
+    sim.compute_forces()
+    rg, _, a = sim.get_state()
+    out = (a.astype(np.float64), rg[:, 3].astype(np.float64), sim.rho().astype(np.float64), sim.nebr())
+    sim.close()
+    return out
+
+
+@pytest.mark.parametrize("lanes", [4, 8, 32])
+def test_metal_lanes_change_only_the_summation_order(lanes):
+    p, r, v = workloads.production(seed=2, steps=10)
+    a16, e16, rho16, _ = _forces(p, r, v)
+    a, e, rho, _ = _forces(p, r, v, metal_lanes=lanes)
+    m = p.nMolMe
+    assert np.array_equal(a[m:], a16[m:]), "carbon forces do not depend on the metal lanes"
+    for name, x, y in (("metal acc", a[:m], a16[:m]), ("energy", e, e16), ("rho", rho, rho16)):
+        err = np.abs(x - y).max() / np.abs(y).max()
+        assert err <= SUM_ORDER_RTOL, (name, err)
+
+
+def test_list_build_grid_changes_nothing():
+    p, r, v = workloads.production(seed=2, steps=10)
+    lists = [_forces(p, r, v, nebr_blocks_per_sm=b)[3] for b in (1, 4, 16, 32)]
+    for nn, nbl in lists[1:]:
+        assert np.array_equal(nn, lists[0][0]) and np.array_equal(nbl, lists[0][1])
+
+
+def test_bad_shapes_are_refused():
+    p, r, v = workloads.small(seed=3)
+    for kw in ({"metal_lanes": 6}, {"nebr_blocks_per_sm": 33}):
+        with pytest.raises(Exception):
+            Simulation(p, **kw)
+    sim = Simulation(p)
+    with pytest.raises(Exception):
+        sim.set_launch_shape(64, 8)
+    assert sim.launch_shape() == (16, 8)
+    sim.close()
+
+
+@pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_MIXED])
+def test_autotune_restores_the_state(mode):
+    p, r, v = workloads.production(seed=2, steps=10)
+    a0 = np.zeros((p.nMol, 3), np.float32)
+    tuned = Simulation(p, mode=mode)
+    tuned.set_state(r, v, a0)
+    tuned.step(30)
+    rep = tuned.autotune(steps=10)
+    shape = tuned.launch_shape()
+    assert shape == (rep["metal_lanes"], rep["nebr_blocks_per_sm"])
+    assert shape[0] in (4, 8, 16, 32) and shape[1] in (2, 4, 8, 16)
+    for k in ("4", "8", "16", "32"):
+        assert rep["metal_lanes_ms_per_step"][k] > 0
+    plain = Simulation(p, mode=mode)
+    plain.set_state(r, v, a0)
+    plain.step(30)
+    for x, y in zip(tuned.get_state(), plain.get_state()):
+        assert np.array_equal(x, y), "state after sg_autotune"
+    plain.set_launch_shape(*shape)
+    tuned.step(40)
+    plain.step(40)
+    for x, y in zip(tuned.get_state(), plain.get_state()):
+        assert np.array_equal(x, y), "40 steps after sg_autotune"
+    t1, t2 = tuned.thermo(), plain.thermo()
+    assert t1.kinEnergy64 == t2.kinEnergy64 and float(t1.potEnergy) == float(t2.potEnergy)
+    tuned.close()
+    plain.close()
