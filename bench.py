@@ -6,14 +6,20 @@ Workload (the production-size configuration): a 40,000-atom graphene sheet with 
 centre-of-mass diffusion on.  One step = one full timestep of every atom (Verlet, lists, EAM,
 LJ, graphene, reductions, thermostat, RDF/diffusion when due).
 
-  value : atom-steps/s with the state resident in HBM, each step timed with CUDA events on the
-          library's stream; the L2 is flushed (a 512 MB write) between timed steps because the
-          whole state fits in the 129 MB L2.
+  value : atom-steps/s of the chosen form (MIXED: hi/lo positions, FP64 sums; --mode plain
+          makes the PLAIN FP32 drop-in the headline) with the state resident in HBM, each step
+          timed with CUDA events on the library's stream; the L2 is flushed (a 512 MB write)
+          between timed steps because the whole state fits in the 129 MB L2.  The other form is
+          timed the same way and reported beside it (`plain` / `mixed`, `mixed_over_plain`).
+  nve_drift : the total-energy drift of both forms on bulk Ni (4,000 atoms, 300 K, 10 ps NVE),
+          the "stated drift" the two forms are compared at.
   e2e   : the same metric through the public C ABI with host buffers: every step uploads the
           state (r, v, a) from pinned host memory, steps, and reads the step's thermo record.
   roofline : the neighbour-list build (the largest share of the step): its compulsory bytes per
-          launch / its mean duration in the timed region (CUDA events around it on the library's
-          stream), against the measured HBM copy peak.
+          launch / its mean duration (CUDA events around it on the library's stream), against
+          the measured HBM copy peak.  The phase durations come from a second pass of the same
+          steps with event-record nodes between the phases of every step; those nodes cost a few
+          microseconds each, so the headline pass carries none.
   step_roofline : the whole step's lower bound, sum over its parts of max(bytes / HBM peak,
           FP32 flops / FP32 peak) with bytes and flops per atom and per interaction fixed in
           advance (integrator 80 B + 20 flop per atom, sort 64 B per atom, density 20 B per
@@ -56,6 +62,7 @@ sys.path.insert(0, str(ROOT))
 L2_FLUSH_BYTES = 512 << 20
 RDF_EXT_BINS = 300
 RDF_EXT_RANGE = 15.0 / 1.42  # 0-15 A
+EV = 0.06275049  # energy unit of the reference, eV
 
 
 def parse():
@@ -64,7 +71,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="sgmd", choices=["sgmd", "reference"])
-    ap.add_argument("--mode", default="plain", choices=["plain", "mixed"])
+    ap.add_argument("--mode", default="mixed", choices=["plain", "mixed"])
+    ap.add_argument("--drift-steps", type=int, default=10000)
     ap.add_argument("--cpu-sample-steps", type=int, default=300)
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--no-cpu", action="store_true")
@@ -220,9 +228,10 @@ def run_reference(args, rank: int, world: int):
 
 
 def run_batched(args, rank: int, world: int, local: int):
-    """The batched form: all replicas in one context, against the same replicas one by one."""
+    """The batched form: all replicas in one context, in both forms (the headline --mode and the
+    other), against the same replicas one by one in the headline form."""
     import torch
-    from surfacegrowthconsole_gb300 import workloads
+    from surfacegrowthconsole_gb300 import MODE_MIXED, MODE_PLAIN, workloads
     from surfacegrowthconsole_gb300.engine import Simulation
     reps = workloads.batched(args.replicas, seed=4 + rank)
     plist = [w[0] for w in reps]
@@ -230,32 +239,38 @@ def run_batched(args, rank: int, world: int, local: int):
     v = np.concatenate([w[2] for w in reps])
     natoms = int(sum(q.nMol for q in plist))
     stream = torch.cuda.Stream(device=local)
-    sim = Simulation(plist, device=local, stream=stream.cuda_stream)
-    sim.set_state(r, v, np.zeros((natoms, 3), np.float32))
-    tune = None if args.no_tune else sim.autotune(steps=10)
-    sim.step(args.warmup)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    launches = 0
-    with Clocks(local) as clk:
-        with torch.cuda.stream(stream):
-            ev0.record(stream)
-            for _ in range(args.steps):
-                sim.step_async(1)
-                launches += sim.kernels_per_step()
-            ev1.record(stream)
+    head = args.mode
+    modes = {"plain": MODE_PLAIN, "mixed": MODE_MIXED}
+    forms = {}
+    for name in (head, "plain" if head == "mixed" else "mixed"):
+        sim = Simulation(plist, mode=modes[name], device=local, stream=stream.cuda_stream)
+        sim.set_state(r, v, np.zeros((natoms, 3), np.float32))
+        tune = None if args.no_tune else sim.autotune(steps=10)
+        sim.step(args.warmup)
         torch.cuda.synchronize()
-    sim.step(0)
-    t_batched = ev0.elapsed_time(ev1) * 1e-3
-    rebuilds = int(sum(sim.thermo(k).rebuilds for k in range(len(plist))))
-    sim.close()
+        launches = 0
+        with Clocks(local) as clk:
+            with torch.cuda.stream(stream):
+                ev0.record(stream)
+                for _ in range(args.steps):
+                    sim.step_async(1)
+                    launches += sim.kernels_per_step()
+                ev1.record(stream)
+            torch.cuda.synchronize()
+        sim.step(0)
+        t = ev0.elapsed_time(ev1) * 1e-3
+        forms[name] = {"value": natoms * args.steps / t, "ms_per_step": 1e3 * t / args.steps,
+                       "gpu_launches": launches, "clocks": clk.summary(), "launch_shape": tune,
+                       "rebuilds_all_replicas": int(sum(sim.thermo(k).rebuilds for k in range(len(plist))))}
+        sim.close()
     # the same replicas one by one, each in its own context (fewer steps: 256 contexts)
     k1 = max(1, min(args.steps, 20))
     t_one = 0.0
     atoms_one = 0
     for w in reps:
         q, rq, vq = w
-        s1 = Simulation(q, device=local, stream=stream.cuda_stream)
+        s1 = Simulation(q, mode=modes[head], device=local, stream=stream.cuda_stream)
         s1.set_state(rq, vq, np.zeros((q.nMol, 3), np.float32))
         s1.step(3)
         torch.cuda.synchronize()
@@ -268,20 +283,24 @@ def run_batched(args, rank: int, world: int, local: int):
         t_one += ev0.elapsed_time(ev1) * 1e-3
         atoms_one += q.nMol
         s1.close()
-    value = natoms * args.steps / t_batched
     one = atoms_one * k1 / t_one
     if rank == 0:
-        line = {"metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": world,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_batched / args.steps,
+        f = forms[head]
+        other = "plain" if head == "mixed" else "mixed"
+        line = {"metric": "atom-steps/s", "value": f["value"], "unit": "atom-steps/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": f["ms_per_step"],
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded replicas: graphene + one fcc Ni cluster each, Maxwell velocities)",
                 "config": {"workload": f"{len(plist)} replicas, {natoms} atoms in all, graphene 1,000-20,000 C + "
                                        "one Ni cluster of 50-2,000 atoms each, 300-1,500 K, lists rebuilt by the "
-                                       "reference's rule", "replicas": len(plist), "atoms": natoms,
+                                       "reference's rule", "replicas": len(plist), "atoms": natoms, "mode": head,
                            "l2": "state larger than L2 (no flush)", "parallelism": f"replicas x{world}",
-                           "launch_shape": tune},
-                "clocks": clk.summary(), "gpu_launches": launches, "rebuilds_all_replicas": rebuilds,
-                "one_by_one": {"value": one, "unit": "atom-steps/s", "steps": k1,
+                           "launch_shape": f["launch_shape"]},
+                "clocks": f["clocks"], "gpu_launches": f["gpu_launches"],
+                "rebuilds_all_replicas": f["rebuilds_all_replicas"],
+                other: forms[other],
+                "mixed_over_plain": forms["mixed"]["value"] / forms["plain"]["value"],
+                "one_by_one": {"value": one, "unit": "atom-steps/s", "steps": k1, "mode": head,
                                "ms_all_replicas_per_step": 1e3 * t_one / k1}}
         print(json.dumps(line, default=float))
 
@@ -345,52 +364,115 @@ def main():
         if dist:
             dist.destroy_process_group()
         return
+    run_production(args, rank, world, local, dist)
+    if dist:
+        dist.destroy_process_group()
+
+
+def nve_drift(mode: int, local: int, steps: int) -> dict:
+    """Linear drift of the total energy of bulk Ni (4,000 atoms, 300 K) over `steps` NVE steps."""
+    from surfacegrowthconsole_gb300 import MODE_MIXED, workloads
+    from surfacegrowthconsole_gb300.engine import Simulation
+    p, r, v = workloads.bulk_metal()
+    sim = Simulation(p, mode=mode, device=local)
+    sim.set_state(r, v, np.zeros((p.nMol, 3), np.float32))
+    every = 100
+    es = []
+    for _ in range(max(steps // every, 2)):
+        sim.step(every)
+        t = sim.thermo()
+        es.append(t.kinEnergy64 + t.potEnergy64 if mode == MODE_MIXED else float(t.totEnergy))
+    sim.close()
+    x = np.arange(len(es)) * every
+    return {"eV_per_atom_per_ns": float(np.polyfit(x, np.array(es), 1)[0]) * 1e6 * EV, "steps": len(es) * every}
+
+
+def run_production(args, rank: int, world: int, local: int, dist):
+    """The production workload in both forms: PLAIN (the reference's FP32 arithmetic) and MIXED
+    (the chosen form).  The headline arm (--mode, default mixed) gives value, e2e and the
+    roofline; each form is timed the same way (steps with CUDA events, L2 flushed between)."""
+    import torch
     from surfacegrowthconsole_gb300 import MODE_MIXED, MODE_PLAIN
     from surfacegrowthconsole_gb300.engine import Simulation
 
     p, r, v = workload(rank)
     a = np.zeros((p.nMol, 3), np.float32)
     stream = torch.cuda.Stream(device=local)
-    mode = MODE_MIXED if args.mode == "mixed" else MODE_PLAIN
-    sim = Simulation(p, mode=mode, force_rebuild=True, device=local, stream=stream.cuda_stream, phase_timing=True,
-                     rdf_ext_bins=RDF_EXT_BINS, rdf_ext_range=RDF_EXT_RANGE)
-    sim.set_state(r, v, a)
-    tune = None if args.no_tune else sim.autotune(steps=20)
-    sim.step(args.warmup)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    phases = []
-    launches = 0
 
     def barrier():
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
 
-    barrier()
-    with Clocks(local) as clk:
+    def max_over_ranks(x: float) -> float:
+        if not dist:
+            return x
+        t = torch.tensor([x], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def make(mode, phase_timing=False):
+        return Simulation(p, mode=mode, force_rebuild=True, device=local, stream=stream.cuda_stream,
+                          phase_timing=phase_timing, rdf_ext_bins=RDF_EXT_BINS, rdf_ext_range=RDF_EXT_RANGE)
+
+    def timed(sim, phases=None):
+        """args.steps steps, each bracketed by CUDA events on the library's stream, the L2 flushed
+        before each; returns (seconds, kernel launches)."""
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+        launches = 0
+        barrier()
         with torch.cuda.stream(stream):
             for k in range(args.steps):
                 flush.zero_()
                 ev[k][0].record(stream)
                 sim.step_async(1)
                 ev[k][1].record(stream)
-                phases.append(sim.phase_times())  # waits for this step
+                if phases is not None:
+                    phases.append(sim.phase_times())  # waits for this step
                 launches += sim.kernels_per_step()
         barrier()
-    sim.step(0)  # collects device status (overflow flags)
-    step_ms = [e0.elapsed_time(e1) for e0, e1 in ev]
-    total_s = sum(step_ms) * 1e-3
+        sim.step(0)  # collects device status (overflow flags)
+        return max_over_ranks(sum(e0.elapsed_time(e1) for e0, e1 in ev) * 1e-3), launches
+
+    head = args.mode
+    forms = {}
+    sims = {}
+    clk_head = None
+    for name, mode in (("plain", MODE_PLAIN), ("mixed", MODE_MIXED)):
+        sim = make(mode)
+        sim.set_state(r, v, a)
+        tune = None if args.no_tune else sim.autotune(steps=20)
+        sim.step(args.warmup)
+        with Clocks(local) as clk:
+            total_s, launches = timed(sim)
+        forms[name] = {"total_s": total_s, "launches": launches, "launch_shape": tune,
+                       "shape": sim.launch_shape(), "clocks": clk.summary()}
+        sims[name] = sim
     if dist:
-        t = torch.tensor([total_s], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t.item())
         n_all = torch.tensor([float(p.nMol)], device=f"cuda:{local}")
         dist.all_reduce(n_all)
         atoms_all = float(n_all.item())
     else:
         atoms_all = float(p.nMol)
-    value = atoms_all * args.steps / total_s
+    for f in forms.values():
+        f["value"] = atoms_all * args.steps / f["total_s"]
+        f["ms_per_step"] = 1e3 * f["total_s"] / args.steps
+    sim = sims[head]
+    sims["plain" if head == "mixed" else "mixed"].close()
+    total_s = forms[head]["total_s"]
+    value = forms[head]["value"]
+
+    # phase boundaries: a second pass of the same steps with event-record nodes between the
+    # phases of each step (they cost a few microseconds each, so the headline pass has none)
+    psim = make(MODE_MIXED if head == "mixed" else MODE_PLAIN, phase_timing=True)
+    psim.set_state(r, v, a)
+    psim.set_launch_shape(*forms[head]["shape"])
+    psim.step(args.warmup)
+    phases = []
+    phase_total_s, _ = timed(psim, phases)
+    psim.close()
     # integrate, rebuild, metal chain, carbon, forces, reduce, extra, list build
     ph = np.mean(np.array(phases), axis=0)
 
@@ -404,6 +486,7 @@ def main():
     roof = {"bound": "hbm", "kernel": "k_build_nebr", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
             "algorithmic_bytes_per_launch": bytes_launch, "mean_launch_ms": float(ph[7]),
+            "phase_pass_ms_per_step": 1e3 * phase_total_s / args.steps,
             "phase_ms": {"integrate": float(ph[0]), "rebuild": float(ph[1]), "list_build": float(ph[7]),
                          "metal_chain_side_stream": float(ph[2]), "carbon_forces": float(ph[3]),
                          "forces_fork_to_join": float(ph[4]), "reduce": float(ph[5]), "rdf_shear": float(ph[6])}}
@@ -429,33 +512,41 @@ def main():
         sim.step(1)
         th = sim.thermo()
     barrier()
-    e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
     import ctypes
     e2e = {"value": atoms_all * e2e_steps / e2e_s, "unit": "atom-steps/s",
            "h2d_bytes_per_step": p.nMol * (16 + 12 + 12), "d2h_bytes_per_step": ctypes.sizeof(th), "steps": e2e_steps}
+    sim.close()
+
+    drift = None
+    if args.drift_steps > 0:
+        drift = {"system": "bulk fcc Ni, 4,000 atoms, 300 K, NVE, dt 1 fs (the EAM alone: the reference's "
+                           "graphene energy omits the angle term its forces apply)"}
+        for name, mode in (("plain", MODE_PLAIN), ("mixed", MODE_MIXED)):
+            drift[name] = nve_drift(mode, local, args.drift_steps)
 
     if rank == 0:
         cpu = None if args.no_cpu or world > 1 else cpu_baseline(p, r, v, args.cpu_sample_steps)
+        other = "plain" if head == "mixed" else "mixed"
         line = {"metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": world,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded graphene + fcc Ni clusters, Maxwell velocities)",
                 "config": {"workload": f"graphene 40000 C + 8 Ni clusters ({p.nMolMe} Ni), {p.nMol} atoms per "
                                        "GPU, 700 K, dt 1 fs, lists rebuilt every step, RDF + diffusion on",
-                           "atoms_per_gpu": p.nMol, "mode": args.mode, "l2": "flushed between timed steps",
-                           "parallelism": f"replicas x{world}", "launch_shape": tune},
-                "clocks": clk.summary(), "gpu_launches": launches, "roofline": roof,
+                           "atoms_per_gpu": p.nMol, "mode": head,
+                           "form": "chosen (MIXED)" if head == "mixed" else "plain FP32 drop-in",
+                           "l2": "flushed between timed steps", "parallelism": f"replicas x{world}",
+                           "launch_shape": forms[head]["launch_shape"]},
+                "clocks": forms[head]["clocks"], "gpu_launches": forms[head]["launches"], "roofline": roof,
                 "step_roofline": step_roof, "e2e": e2e,
+                other: {"value": forms[other]["value"], "ms_per_step": forms[other]["ms_per_step"],
+                        "gpu_launches": forms[other]["launches"], "clocks": forms[other]["clocks"],
+                        "launch_shape": forms[other]["launch_shape"]},
+                "mixed_over_plain": forms["mixed"]["value"] / forms["plain"]["value"],
+                "nve_drift": drift,
                 "cpu_baseline": cpu}
         print(json.dumps(line, default=float))
-    sim.close()
-    if dist:
-        dist.destroy_process_group()
-
 
 if __name__ == "__main__":
     main()

@@ -77,7 +77,13 @@ typedef struct sg_options {
     int nebr_blocks_per_sm;/* resident 128-thread blocks per SM of the list build's work queue,
                             * 1..32 (0: 8) */
     int phase_timing;      /* 1: record CUDA events between the phases of every step */
-    int reserved[7];
+    int programmatic_launch; /* 1: launch the kernels of a step with programmatic dependent launch
+                            * (a kernel is scheduled while its predecessor drains); 0: off */
+    int nebr_descending;   /* 1: the list build takes the non-crowded cells in descending cell
+                            * order (0: ascending) */
+    int nebr_item_atoms;   /* list build: most home atoms of one work item (a warp's share); a
+                            * cell of more atoms is split into near-equal items, 4..64 (0: 8) */
+    int reserved[4];
 } sg_options;
 
 /* Initialise *opt with the defaults (PLAIN mode, graphs on, device 0). */
@@ -339,17 +345,27 @@ int sg_diff_force_matching(sg_diff *d, const double *theta, const float *ref_for
 /* ---- tuning ------------------------------------------------------------------------------- */
 /* Times the launch shapes of the tunable passes on the context's own state and keeps the
  * fastest: the metal lanes per atom (4, 8, 16, 32; `steps` steps each, the context's own
- * rebuild schedule), then the list build's blocks per SM (2, 4, 8, 16; `steps` steps each with
- * a rebuild in every step).  Every device buffer and the host step counters are copied first
+ * rebuild schedule), then the list build's home atoms per work item (4, 6, 8, 16), blocks
+ * per SM (2, 4, 8, 16) and cell order (ascending, descending), `steps` steps each with a
+ * rebuild in every step, then programmatic dependent launch off and on.  Every device buffer and the host step counters are copied first
  * and put back after each trial, so the context continues from the state it had; the trials
  * change no results but the summation order of the metal passes.  `report` (if not NULL)
  * receives a JSON object with the milliseconds per step of every trial and the choice.
  * steps <= 0 selects 20. */
 int sg_autotune(sg_ctx *ctx, int steps, char *report, int report_len);
+/* The tunable launch shape: the options of the same names. */
+typedef struct sg_launch_shape {
+    int metal_lanes;        /* 4, 8, 16 or 32 */
+    int nebr_blocks_per_sm; /* 1..32 */
+    int nebr_descending;    /* 0 or 1 */
+    int nebr_item_atoms;    /* 4..64 */
+    int programmatic_launch; /* 0 or 1 */
+    int reserved[3];
+} sg_launch_shape;
 /* The launch shape in use (from the options, or as sg_autotune chose it). */
-int sg_get_launch_shape(sg_ctx *ctx, int *metal_lanes, int *nebr_blocks_per_sm);
+int sg_get_launch_shape(sg_ctx *ctx, sg_launch_shape *shape);
 /* Sets the launch shape (a shape an earlier sg_autotune reported, for instance). */
-int sg_set_launch_shape(sg_ctx *ctx, int metal_lanes, int nebr_blocks_per_sm);
+int sg_set_launch_shape(sg_ctx *ctx, const sg_launch_shape *shape);
 
 #ifdef __cplusplus
 }

@@ -88,8 +88,15 @@ class Options(C.Structure):
         ("mode", C.c_int), ("force_rebuild", C.c_int), ("use_graphs", C.c_int), ("device", C.c_int),
         ("stream", C.c_void_p), ("rdf_ext_bins", C.c_int), ("rdf_ext_range", C.c_float),
         ("eam_table_knots", C.c_int), ("metal_lanes", C.c_int), ("nebr_blocks_per_sm", C.c_int),
-        ("phase_timing", C.c_int), ("reserved", C.c_int * 7),
+        ("phase_timing", C.c_int),
+        ("programmatic_launch", C.c_int), ("nebr_descending", C.c_int), ("nebr_item_atoms", C.c_int),
+        ("reserved", C.c_int * 4),
     ]
+
+
+class LaunchShape(C.Structure):
+    _fields_ = [("metal_lanes", C.c_int), ("nebr_blocks_per_sm", C.c_int), ("nebr_descending", C.c_int),
+                ("nebr_item_atoms", C.c_int), ("programmatic_launch", C.c_int), ("reserved", C.c_int * 3)]
 
 
 class Thermo(C.Structure):
@@ -204,8 +211,8 @@ _SIGS = {
     "sg_read_backup": (C.c_int, [C.c_char_p, C.POINTER(SimParams), C.c_void_p, C.c_void_p, C.c_void_p]),
     "sg_compute_forces_noalloc": (C.c_int, [C.POINTER(SimParams), C.c_void_p, C.c_void_p, C.c_void_p]),
     "sg_autotune": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p, C.c_int]),
-    "sg_get_launch_shape": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
-    "sg_set_launch_shape": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "sg_get_launch_shape": (C.c_int, [C.c_void_p, C.POINTER(LaunchShape)]),
+    "sg_set_launch_shape": (C.c_int, [C.c_void_p, C.POINTER(LaunchShape)]),
     "sg_diff_frame_params": (C.c_int, [C.POINTER(SimParams), C.POINTER(SimParams)]),
     "sg_diff_create": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
     "sg_diff_destroy": (C.c_int, [C.c_void_p]),

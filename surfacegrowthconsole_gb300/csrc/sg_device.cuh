@@ -37,8 +37,12 @@ constexpr int kNebrWarps = 4;     // warps per block in the neighbour-list build
 constexpr int kWin = 512;         // candidates per shared-memory window of the list build
 constexpr int kRelMax = 48;       // relevant-list capacity per carbon atom
 constexpr int kShortMax = 8;      // close-list capacity per carbon atom (a multiple of 4)
-constexpr int kHeavyCell = 16;    // list build: cells above this many atoms are split into items
-constexpr int kHeavyChunk = 8;    // of this many home atoms
+constexpr int kHeavyCell = 16;    // list build: default home atoms per work item (larger cells split)
+constexpr int kHeavyChunk = 8;    // sizes the item list of the fixed-size scratch (>= kHeavyCell / 2)
+constexpr int kScanCells = 512;   // cells per block of the single-pass cell scan (kCellTile / 4)
+constexpr int kScanThreads = 128;
+constexpr int kMinItemAtoms = 4;  // smallest home atoms per work item the engine allows
+constexpr int kItemAtoms = 8;     // the engine's default home atoms per work item
 constexpr int kMetalPerBlock = 128 / kMT;   // atoms per 128-thread block
 constexpr int kCarbonPerBlock = 128 / kCT;
 
@@ -172,6 +176,29 @@ __device__ __forceinline__ int cellIndex(const RepConst &P, float x, float y, fl
 }
 
 // Minimum image of one component as the force kernels do it (SurfaceGrowth.cu:750-759).
+// Cell of atom g and its arrival slot in the cell; with a bucket (cap slots per cell, the
+// reference's blockSize) the atom is also filed there, and counted in blockCount per block of
+// kScanCells cells (one atomic per block among the warp's atoms), for k_scan_cells and
+// k_rank_cells.
+__device__ __forceinline__ void binAtom(const RepConst &P, int g, const float4 &r, int *cellOf, int *slot,
+                                        int *cellCount, int *bucket, int cap, int *blockCount) {
+  const int c = cellIndex(P, r.x, r.y, r.z);
+  cellOf[g] = c;
+  int key = -1;
+  if (c >= 0) {
+    const int s = atomicAdd(&cellCount[P.cellOff + c], 1);
+    slot[g] = s;
+    if (bucket && s < cap) {
+      bucket[(size_t)(P.cellOff + c) * cap + s] = g;
+      key = (P.cellOff + c) / kScanCells;
+    }
+  }
+  if (blockCount) {
+    const unsigned same = __match_any_sync(__activemask(), key);
+    if (key >= 0 && __ffs(same) - 1 == (int)(threadIdx.x & 31)) atomicAdd(&blockCount[key], __popc(same));
+  }
+}
+
 __device__ __forceinline__ float minImg(float d, float L) {
   if (d >= 0.5f * L) d -= L;
   else if (d < -0.5f * L) d += L;
@@ -200,4 +227,37 @@ __device__ __forceinline__ void setFlag(RepState *st, int code) {
   atomicOr(&st->flags, 1 << code);
 }
 
+// Programmatic dependent launch.  A kernel of the step chain, launched with the
+// programmatic-serialization attribute, may be scheduled while its predecessor in the stream
+// still runs; it waits here, before its first global memory access, for the predecessor grid to
+// complete with its memory visible, then allows its own successor to be scheduled.  Every kernel
+// of the chain waits, so completion is transitive.  Launched without the attribute, both
+// instructions return at once.
+__device__ __forceinline__ void pdlEnter() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 }  // namespace sg
+
+#ifdef __CUDACC__
+namespace sg {
+// Launches kernel k on stream s, with the programmatic-serialization attribute when pdl is set
+// (the kernel must begin with pdlEnter()).
+template <typename... KArgs, typename... Args>
+inline cudaError_t launchK(bool pdl, void (*k)(KArgs...), int grid, int block, size_t smem, cudaStream_t s,
+                           Args... args) {
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, k, static_cast<KArgs>(args)...);
+}
+}  // namespace sg
+#endif

@@ -150,6 +150,8 @@ static int validate(const sg_simparams *p, int n) {
     if (q.cells.x < 1 || q.cells.y < 1 || q.cells.z < 1)
       return sg_fail(SG_ERR_INVALID, "replica %d: bad cell grid", r);
     if (q.iNebrMax < 1) return sg_fail(SG_ERR_INVALID, "replica %d: iNebrMax < 1", r);
+    if (q.blockSize < 1 || q.blockSize > 1024)
+      return sg_fail(SG_ERR_INVALID, "replica %d: blockSize %u (atoms per cell) outside 1..1024", r, q.blockSize);
     if (q.bRdf && (q.sizeHistRdf < 1 || q.stepRdf < 1 || q.limitRdf < 1))
       return sg_fail(SG_ERR_INVALID, "replica %d: bad RDF settings", r);
     if (q.iRegime == 2 && (q.nBuffDiffuse < 1 || q.nValDiffuse < 1 || q.limitDiffuseAv < 1 || q.nBuffDiffuse > 4096))
@@ -260,13 +262,23 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
   }
   c->ntot = atomOff;
   c->ctot = cellOff;
+  c->bucketCap = 1;
+  for (int r = 0; r < n_replicas; r++) c->bucketCap = std::max(c->bucketCap, (int)params[r].blockSize);
   // list build: one warp per home cell, a grid of a few resident blocks per SM walking the cells
   c->numSMs = numSMs;
+  c->pdl = c->opt.programmatic_launch != 0;
   if (c->opt.nebr_blocks_per_sm < 0 || c->opt.nebr_blocks_per_sm > 32) {
     sg_destroy(c);
     return sg_fail(SG_ERR_INVALID, "nebr_blocks_per_sm %d: 0 (default) or 1..32", c->opt.nebr_blocks_per_sm);
   }
   setNebrBlocks(c, c->opt.nebr_blocks_per_sm ? c->opt.nebr_blocks_per_sm : 8);
+  c->nebrDescending = c->opt.nebr_descending ? 1 : 0;
+  c->nebrItemAtoms = c->opt.nebr_item_atoms ? c->opt.nebr_item_atoms : kItemAtoms;
+  if (c->nebrItemAtoms < kMinItemAtoms || c->nebrItemAtoms > 64) {
+    sg_destroy(c);
+    return sg_fail(SG_ERR_INVALID, "nebr_item_atoms %d: 0 (default) or %d..64", c->opt.nebr_item_atoms,
+                   kMinItemAtoms);
+  }
   const size_t N = c->ntot;
 #define AL(ptr, n)                          \
   if ((rc = devAllocT(c, &ptr, (n)))) {     \
@@ -285,9 +297,11 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
   AL(c->nrl, N);
   AL(c->rl, N * kRelMax);
   AL(c->activeCells, (size_t)c->ctot);
-  // every crowded cell (> kHeavyCell atoms) adds at most one partial chunk
-  AL(c->heavyItems, (size_t)N / kHeavyChunk + (size_t)N / (kHeavyCell + 1) + 16);
+  // a cell of n > t atoms (t = home atoms per item >= kMinItemAtoms) gives ceil(n / t) < n / t + 1
+  // items: at most N / t + N / (t + 1) in all
+  AL(c->heavyItems, (size_t)N / kMinItemAtoms + (size_t)N / (kMinItemAtoms + 1) + 16);
   AL(c->nebrWork, 3);
+  AL(c->bucket, (size_t)c->ctot * c->bucketCap);
   AL(c->rho, N); AL(c->dF, N); AL(c->Fv, N); AL(c->fric, N);
   AL(c->partial, (size_t)std::max(redOff, 1) * kNumRed);
   AL(c->partialCmv, (size_t)std::max(cmvOff, 1) * 3);
@@ -323,13 +337,15 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
       for (int t = 0; t < P.ncellsPad; t += kCellTile) { tr.push_back(r); ts.push_back(t); }
     }
     c->ntiles = (int)tr.size();
+    c->nScanBlocks = c->ntiles * (kCellTile / kScanCells);
     if ((rc = uploadTab(c, c->redTab, rr, ss)) || (rc = uploadTab(c, c->cmvTab, cr, cs)) ||
         (rc = uploadTab(c, c->tileTab, tr, ts))) {
       sg_destroy(c);
       return rc;
     }
     if ((rc = devAllocT(c, &c->tileSum, std::max<size_t>(tr.size(), 1))) ||
-        (rc = devAllocT(c, &c->dTileFirst, n_replicas))) {
+        (rc = devAllocT(c, &c->dTileFirst, n_replicas)) ||
+        (rc = devAllocT(c, &c->blockCount, std::max<size_t>(tr.size() * (kCellTile / kScanCells), 1)))) {
       sg_destroy(c);
       return rc;
     }
@@ -493,25 +509,16 @@ enum { V_SHEAR = 1, V_RDF = 2, V_RDF_ZERO = 4 };
 
 static int enqueueRebuild(sg_ctx *c, int force) {
   const int fr = force;
-  CK(cudaMemsetAsync(c->nebrWork, 0, 3 * sizeof(int), c->stream));
-  if (c->ntiles) {
-    k_scan_tiles<<<c->tileTab.n, 256, 0, c->stream>>>(c->tileTab.view(), c->rc, c->st, c->cellCount, c->tileSum, fr);
-    k_scan_tile_prefix<<<c->nrep, 1024, 0, c->stream>>>(c->rc, c->st, c->dTileFirst, c->tileSum, fr);
-    k_scan_final<<<c->tileTab.n, 256, 0, c->stream>>>(c->tileTab.view(), c->rc, c->st, c->cellCount, c->tileSum,
-                                                       c->cellStart, (int)c->hp[0].blockSize, fr, c->activeCells,
-                                                       c->heavyItems, c->nebrWork);
-    LAUNCH_OK();
-  }
-  k_scatter<<<c->atomTab.n, 128, 0, c->stream>>>(c->atomTab.view(), c->rc, c->st, c->cellOf, c->slot, c->cellStart,
-                                                 c->tmpIdx, c->nn, c->ns, c->nrl, fr);
-  k_rank<<<c->atomTab.n, 128, 0, c->stream>>>(c->atomTab.view(), c->rc, c->st, c->cellOf, c->cellStart, c->tmpIdx,
-                                              c->pos, c->sortIdx, c->sortPos, fr);
+  CK(launchK(c->pdl, k_scan_cells, c->nScanBlocks, kScanThreads, 0, c->stream, c->tileTab.rep, c->tileTab.start,
+             c->dTileFirst, c->rc, c->st, c->cellCount, c->cellStart, c->bucketCap, fr, c->activeCells,
+             c->heavyItems, c->nebrWork, c->nebrItemAtoms, c->blockCount));
+  CK(launchK(c->pdl, k_rank_cells, c->atomTab.n, 128, 0, c->stream, c->atomTab.view(), c->rc, c->st, c->cellOf,
+             c->slot, c->cellStart, c->bucket, c->bucketCap, c->pos, c->sortIdx, c->sortPos, c->nn, c->ns, c->nrl,
+             fr, c->blockCount, c->nScanBlocks));
   if (c->opt.phase_timing) cudaEventRecordWithFlags(c->phaseEv[8], c->stream, cudaEventRecordExternal);
-  k_build_nebr<<<c->nebrGrid, kNebrWarps * 32, 0, c->stream>>>(c->tileTab.rep, c->activeCells, c->heavyItems,
-                                                                c->nebrWork, c->rc, c->st, c->cellStart, c->sortPos,
-                                                                c->nn, c->nbl, c->ns, c->sl, c->nrl, c->rl,
-                                                                c->rowStride, c->nebrMax);
-  LAUNCH_OK();
+  CK(launchK(c->pdl, k_build_nebr, c->nebrGrid, kNebrWarps * 32, 0, c->stream, c->tileTab.rep, c->activeCells,
+             c->heavyItems, c->nebrWork, c->rc, c->st, c->cellStart, c->sortPos, c->nn, c->nbl, c->ns, c->sl, c->nrl,
+             c->rl, c->rowStride, c->nebrMax, c->nebrDescending));
   return SG_OK;
 }
 
@@ -524,17 +531,17 @@ static int enqueueForces(sg_ctx *c, bool withCmVel) {
   if (fork) {
     CK(cudaEventRecord(c->evFork, c->stream));
     CK(cudaStreamWaitEvent(c->side, c->evFork, 0));
-    launchMetalChain(c->metalLanes, c->metalRun.n, c->side, c->metalRun.view(), c->rc, c->pos, c->acc, c->nn,
+    launchMetalChain(c->pdl, c->metalLanes, c->metalRun.n, c->side, c->metalRun.view(), c->rc, c->pos, c->acc, c->nn,
                      c->nbl, c->rho, c->dF, c->Fv, c->fric, c->rowStride);
     if (withCmVel && c->cmvTab.n)
-      k_cmvel<<<c->cmvTab.n, kRedThreads, 0, c->side>>>(c->cmvTab.view(), c->rc, c->st, c->vel, c->acc,
-                                                        c->partialCmv, c->dCmvFirst);
+      CK(launchK(c->pdl, k_cmvel, c->cmvTab.n, kRedThreads, 0, c->side, c->cmvTab.view(), c->rc, c->st, c->vel, c->acc,
+                                                        c->partialCmv, c->dCmvFirst));
     if (c->opt.phase_timing) cudaEventRecordWithFlags(c->phaseEv[7], c->side, cudaEventRecordExternal);
     LAUNCH_OK();
   }
   if (c->carbonTabT.n)
-    k_force_carbon<<<c->carbonTabT.n, 128, 0, c->stream>>>(c->carbonTabT.view(), c->rc, c->pos, c->acc, c->nn,
-                                                           c->nbl, c->ns, c->sl, c->nrl, c->rl, c->rowStride);
+    CK(launchK(c->pdl, k_force_carbon, c->carbonTabT.n, 128, 0, c->stream, c->carbonTabT.view(), c->rc, c->pos, c->acc, c->nn,
+                                                           c->nbl, c->ns, c->sl, c->nrl, c->rl, c->rowStride));
   if (c->opt.phase_timing) cudaEventRecordWithFlags(c->phaseEv[3], c->stream, cudaEventRecordExternal);
   LAUNCH_OK();
   if (fork) {
@@ -553,13 +560,13 @@ static int enqueueRdf(sg_ctx *c, bool zero) {
       CK(cudaMemsetAsync(c->histExt, 0, sizeof(unsigned long long) * c->nrep * c->opt.rdf_ext_bins, c->stream));
   }
   if (c->metalTab.n && c->maxHist > 0) {
-    k_rdf<<<c->metalTab.n, 128, c->maxHist * sizeof(unsigned), c->stream>>>(
-        c->metalTab.view(), c->rc, c->st, c->pos, c->cellOf, c->cellStart, c->sortIdx, c->hist, c->histStride);
+    CK(launchK(c->pdl, k_rdf, c->metalTab.n, 128, c->maxHist * sizeof(unsigned), c->stream, 
+        c->metalTab.view(), c->rc, c->st, c->pos, c->cellOf, c->cellStart, c->sortIdx, c->hist, c->histStride));
     LAUNCH_OK();
   }
   if (c->histExt && c->metalTab.n) {
-    k_rdf_ext<<<c->metalTab.n, 128, c->opt.rdf_ext_bins * sizeof(unsigned), c->stream>>>(
-        c->rc, c->pos, c->metalTab.rep, c->metalTab.start, c->histExt, c->opt.rdf_ext_bins, c->opt.rdf_ext_range);
+    CK(launchK(c->pdl, k_rdf_ext, c->metalTab.n, 128, c->opt.rdf_ext_bins * sizeof(unsigned), c->stream, 
+        c->rc, c->pos, c->metalTab.rep, c->metalTab.start, c->histExt, c->opt.rdf_ext_bins, c->opt.rdf_ext_range));
     LAUNCH_OK();
   }
   return SG_OK;
@@ -578,8 +585,9 @@ static int enqueueStep(sg_ctx *c, int variant) {
   if (c->opt.mode == SG_MODE_MIXED) {
     if ((rc = sg_mixed_enqueue_integrate(c, fr))) return rc;
   } else {
-    k_integrate_first<<<c->atomTab.n, 128, 0, c->stream>>>(c->atomTab.view(), c->rc, c->st, c->pos, c->vel, c->acc,
-                                                           c->cellOf, c->slot, c->cellCount, fr);
+    CK(launchK(c->pdl, k_integrate_first, c->atomTab.n, 128, 0, c->stream, c->atomTab.view(), c->rc, c->st, c->pos,
+               c->vel, c->acc, c->cellOf, c->slot, c->cellCount, fr, c->bucket, c->bucketCap,
+               c->blockCount));
     LAUNCH_OK();
   }
   phaseMark(c, 1);
@@ -590,14 +598,14 @@ static int enqueueStep(sg_ctx *c, int variant) {
   if (c->opt.mode == SG_MODE_MIXED) {
     if ((rc = sg_mixed_enqueue_reduce(c, fr))) return rc;
   } else {
-    k_step_reduce<<<c->redTab.n, kRedThreads, 0, c->stream>>>(c->redTab.view(), c->rc, c->st, c->pos, c->vel, c->acc,
+    CK(launchK(c->pdl, k_step_reduce, c->redTab.n, kRedThreads, 0, c->stream, c->redTab.view(), c->rc, c->st, c->pos, c->vel, c->acc,
                                                               c->fric, c->partial, c->dRedFirst, c->diffBuf,
-                                                              c->dDiffOff, fr);
+                                                              c->dDiffOff, fr));
     LAUNCH_OK();
   }
   phaseMark(c, 5);
   if ((variant & V_SHEAR) && c->metalTab.n) {
-    k_shear<<<c->metalTab.n, 128, 0, c->stream>>>(c->metalTab.view(), c->rc, c->st, c->pos, c->acc);
+    CK(launchK(c->pdl, k_shear, c->metalTab.n, 128, 0, c->stream, c->metalTab.view(), c->rc, c->st, c->pos, c->acc));
     LAUNCH_OK();
   }
   if (variant & V_RDF) {
@@ -741,7 +749,8 @@ extern "C" int sg_step_async(sg_ctx *c, int nsteps) {
 
 extern "C" int sg_build_lists(sg_ctx *c) {
   if (!c) return sg_fail(SG_ERR_INVALID, "null context");
-  k_cell_count<<<c->atomTab.n, 128, 0, c->stream>>>(c->atomTab.view(), c->rc, c->pos, c->cellOf, c->slot, c->cellCount);
+  k_cell_bucket<<<c->atomTab.n, 128, 0, c->stream>>>(c->atomTab.view(), c->rc, c->pos, c->cellOf, c->slot,
+                                                     c->cellCount, c->bucket, c->bucketCap, c->blockCount);
   LAUNCH_OK();
   int rc = enqueueRebuild(c, 1);
   if (rc) return rc;
@@ -1041,10 +1050,13 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
   Snapshot snap;
   int rc = takeSnapshot(c, snap);
   if (rc) return rc;
-  const int lanes0 = c->metalLanes, bps0 = c->nebrBlocksPerSM, fr0 = c->opt.force_rebuild;
-  const int laneChoice[4] = {4, 8, 16, 32}, bpsChoice[4] = {2, 4, 8, 16};
-  float laneMs[4] = {}, bpsMs[4] = {};
-  int bestLanes = lanes0, bestBps = bps0;
+  const int lanes0 = c->metalLanes, bps0 = c->nebrBlocksPerSM, desc0 = c->nebrDescending;
+  const int item0 = c->nebrItemAtoms, fr0 = c->opt.force_rebuild;
+  const bool pdl0 = c->pdl;
+  const int laneChoice[4] = {4, 8, 16, 32}, bpsChoice[4] = {2, 4, 8, 16}, itemChoice[4] = {4, 6, 8, 16};
+  float laneMs[4] = {}, bpsMs[4] = {}, orderMs[2] = {}, itemMs[4] = {}, pdlMs[2] = {};
+  int bestLanes = lanes0, bestBps = bps0, bestDesc = desc0, bestItem = item0;
+  bool bestPdl = pdl0;
   // 1. lanes per metal atom, on the context's own schedule
   if (c->metalRun.n > 0) {
     float best = 0.f;
@@ -1054,7 +1066,8 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
       if (!rc && (k == 0 || laneMs[k] < best)) { best = laneMs[k]; bestLanes = laneChoice[k]; }
     }
   }
-  // 2. blocks per SM of the list build, with a rebuild in every step
+  // 2. the list build (home atoms per item, blocks per SM, cell order), with a rebuild in
+  //    every step
   if (!rc) {
     c->opt.force_rebuild = 1;
     destroyGraphs(c);
@@ -1062,13 +1075,42 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
       float best = 0.f;
       for (int k = 0; k < 4 && !rc; k++) {
         if ((rc = restoreSnapshot(c, snap))) break;
+        c->nebrItemAtoms = itemChoice[k];
+        destroyGraphs(c);
+        rc = timeSteps(c, steps, &itemMs[k]);
+        if (!rc && (k == 0 || itemMs[k] < best)) { best = itemMs[k]; bestItem = itemChoice[k]; }
+      }
+      c->nebrItemAtoms = bestItem;
+      destroyGraphs(c);
+      best = 0.f;
+      for (int k = 0; k < 4 && !rc; k++) {
+        if ((rc = restoreSnapshot(c, snap))) break;
         setNebrBlocks(c, bpsChoice[k]);
         rc = timeSteps(c, steps, &bpsMs[k]);
         if (!rc && (k == 0 || bpsMs[k] < best)) { best = bpsMs[k]; bestBps = bpsChoice[k]; }
       }
+      if (!rc) setNebrBlocks(c, bestBps);
+      for (int d = 0; d < 2 && !rc; d++) {
+        if ((rc = restoreSnapshot(c, snap))) break;
+        c->nebrDescending = d;
+        destroyGraphs(c);
+        rc = timeSteps(c, steps, &orderMs[d]);
+      }
+      if (!rc) bestDesc = orderMs[1] < orderMs[0] ? 1 : 0;
     }
     c->opt.force_rebuild = fr0;
     destroyGraphs(c);
+  }
+  // 3. programmatic dependent launch, on the context's own schedule
+  if (!rc) {
+    c->nebrDescending = bestDesc;
+    for (int k = 0; k < 2 && !rc; k++) {
+      if ((rc = restoreSnapshot(c, snap))) break;
+      c->pdl = k == 1;
+      destroyGraphs(c);
+      rc = timeSteps(c, steps, &pdlMs[k]);
+    }
+    if (!rc) bestPdl = pdlMs[1] < pdlMs[0];
   }
   // the state as it was, with the chosen shape (the starting shape if a trial failed)
   const int rc2 = restoreSnapshot(c, snap);
@@ -1076,37 +1118,66 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
   if (rc) {
     setMetalLanes(c, lanes0);
     setNebrBlocks(c, bps0);
+    c->nebrDescending = desc0;
+    c->nebrItemAtoms = item0;
+    c->pdl = pdl0;
+    destroyGraphs(c);
     return rc;
   }
   if (rc2) return rc2;
   if ((rc = setMetalLanes(c, bestLanes))) return rc;
   setNebrBlocks(c, bestBps);
+  c->nebrDescending = bestDesc;
+  c->nebrItemAtoms = bestItem;
+  c->pdl = bestPdl;
+  destroyGraphs(c);
   if (report && report_len > 0) {
     snprintf(report, report_len,
              "{\"steps\": %d, \"metal_lanes_ms_per_step\": {\"4\": %.6g, \"8\": %.6g, \"16\": %.6g, "
              "\"32\": %.6g}, \"nebr_blocks_per_sm_ms_per_step_rebuilding\": {\"2\": %.6g, \"4\": %.6g, "
-             "\"8\": %.6g, \"16\": %.6g}, \"metal_lanes\": %d, \"nebr_blocks_per_sm\": %d, "
-             "\"nebr_grid\": %d}",
+             "\"8\": %.6g, \"16\": %.6g}, \"nebr_order_ms_per_step_rebuilding\": {\"ascending\": %.6g, "
+             "\"descending\": %.6g}, \"nebr_item_atoms_ms_per_step_rebuilding\": {\"4\": %.6g, "
+             "\"6\": %.6g, \"8\": %.6g, \"16\": %.6g}, \"programmatic_launch_ms_per_step\": {\"0\": %.6g, "
+             "\"1\": %.6g}, \"metal_lanes\": %d, \"nebr_blocks_per_sm\": %d, \"nebr_descending\": %d, "
+             "\"nebr_item_atoms\": %d, \"programmatic_launch\": %d, \"nebr_grid\": %d}",
              steps, laneMs[0], laneMs[1], laneMs[2], laneMs[3], bpsMs[0], bpsMs[1], bpsMs[2], bpsMs[3],
-             c->metalLanes, c->nebrBlocksPerSM, c->nebrGrid);
+             orderMs[0], orderMs[1], itemMs[0], itemMs[1], itemMs[2], itemMs[3], pdlMs[0], pdlMs[1],
+             c->metalLanes, c->nebrBlocksPerSM, c->nebrDescending, c->nebrItemAtoms, c->pdl ? 1 : 0,
+             c->nebrGrid);
   }
   return SG_OK;
 }
 
-extern "C" int sg_set_launch_shape(sg_ctx *c, int metal_lanes, int nebr_blocks_per_sm) {
-  if (!c) return sg_fail(SG_ERR_INVALID, "null context");
-  if (nebr_blocks_per_sm < 1 || nebr_blocks_per_sm > 32)
-    return sg_fail(SG_ERR_INVALID, "nebr_blocks_per_sm %d: 1..32", nebr_blocks_per_sm);
+extern "C" int sg_set_launch_shape(sg_ctx *c, const sg_launch_shape *shape) {
+  if (!c || !shape) return sg_fail(SG_ERR_INVALID, "null argument");
+  if (shape->nebr_blocks_per_sm < 1 || shape->nebr_blocks_per_sm > 32)
+    return sg_fail(SG_ERR_INVALID, "nebr_blocks_per_sm %d: 1..32", shape->nebr_blocks_per_sm);
+  if (shape->nebr_descending != 0 && shape->nebr_descending != 1)
+    return sg_fail(SG_ERR_INVALID, "nebr_descending %d: 0 or 1", shape->nebr_descending);
+  if (shape->nebr_item_atoms < kMinItemAtoms || shape->nebr_item_atoms > 64)
+    return sg_fail(SG_ERR_INVALID, "nebr_item_atoms %d: %d..64", shape->nebr_item_atoms, kMinItemAtoms);
+  if (shape->programmatic_launch != 0 && shape->programmatic_launch != 1)
+    return sg_fail(SG_ERR_INVALID, "programmatic_launch %d: 0 or 1", shape->programmatic_launch);
   CK(cudaStreamSynchronize(c->stream));
-  const int rc = setMetalLanes(c, metal_lanes);
+  const int rc = setMetalLanes(c, shape->metal_lanes);
   if (rc) return rc;
-  setNebrBlocks(c, nebr_blocks_per_sm);
+  setNebrBlocks(c, shape->nebr_blocks_per_sm);
+  if (shape->nebr_descending != c->nebrDescending || shape->nebr_item_atoms != c->nebrItemAtoms ||
+      (shape->programmatic_launch != 0) != c->pdl)
+    destroyGraphs(c);
+  c->nebrDescending = shape->nebr_descending;
+  c->nebrItemAtoms = shape->nebr_item_atoms;
+  c->pdl = shape->programmatic_launch != 0;
   return SG_OK;
 }
 
-extern "C" int sg_get_launch_shape(sg_ctx *c, int *metal_lanes, int *nebr_blocks_per_sm) {
-  if (!c) return sg_fail(SG_ERR_INVALID, "null context");
-  if (metal_lanes) *metal_lanes = c->metalLanes;
-  if (nebr_blocks_per_sm) *nebr_blocks_per_sm = c->nebrBlocksPerSM;
+extern "C" int sg_get_launch_shape(sg_ctx *c, sg_launch_shape *shape) {
+  if (!c || !shape) return sg_fail(SG_ERR_INVALID, "null argument");
+  memset(shape, 0, sizeof(*shape));
+  shape->metal_lanes = c->metalLanes;
+  shape->nebr_blocks_per_sm = c->nebrBlocksPerSM;
+  shape->nebr_descending = c->nebrDescending;
+  shape->nebr_item_atoms = c->nebrItemAtoms;
+  shape->programmatic_launch = c->pdl ? 1 : 0;
   return SG_OK;
 }

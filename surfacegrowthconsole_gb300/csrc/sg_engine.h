@@ -41,6 +41,9 @@ struct sg_ctx {
   int2 *rl = nullptr;
   int nebrGrid = 0;
   int *activeCells = nullptr, *nebrWork = nullptr;
+  int *bucket = nullptr, bucketCap = 64;  // atoms of each cell in arrival order, bucketCap slots per cell
+  int *blockCount = nullptr;  // filed atoms per block of kScanCells cells (zero between rebuilds)
+  int nScanBlocks = 0;
   int2 *heavyItems = nullptr;
   float *rho = nullptr, *dF = nullptr, *Fv = nullptr, *fric = nullptr;
   float *partial = nullptr, *partialCmv = nullptr;
@@ -57,7 +60,8 @@ struct sg_ctx {
   int metalLanes = sg::kMT;
   DevTab metalLaneTab[4];
   DevTab metalRun;
-  int numSMs = 0, nebrBlocksPerSM = 8;
+  int numSMs = 0, nebrBlocksPerSM = 8, nebrDescending = 0, nebrItemAtoms = sg::kItemAtoms;
+  bool pdl = false;  // programmatic dependent launch between the kernels of a step
   std::vector<std::pair<void *, size_t>> regions;  // every device buffer with its size
   int anyMetal = 0, anyCarbon = 0, maxHist = 0;
   // graphs keyed by variant bits

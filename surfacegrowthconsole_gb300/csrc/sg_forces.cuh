@@ -137,6 +137,7 @@ __device__ __forceinline__ void SG_KN(rhoBody)(BlockTab tab, const RepConst *__r
                                                const int *__restrict__ nbl, float *__restrict__ rho,
                                                float *__restrict__ dF, float *__restrict__ Fv,
                                                int rowStride SG_EAM_PARAM) {
+  pdlEnter();
   const int rep = tab.rep[blockIdx.x];
   const RepConst &P = rc[rep];
   const int sub = threadIdx.x & (MT - 1);
@@ -202,6 +203,7 @@ __device__ __forceinline__ void SG_KN(forceMetalBody)(BlockTab tab, const RepCon
                                                       const float *__restrict__ dF,
                                                       const float *__restrict__ Fv, float *__restrict__ fric,
                                                       int rowStride SG_EAM_PARAM) {
+  pdlEnter();
   const int rep = tab.rep[blockIdx.x];
   const RepConst &P = rc[rep];
   const int sub = threadIdx.x & (MT - 1);
@@ -274,26 +276,31 @@ __global__ void __launch_bounds__(128) SG_KN(k_force_metal_tpa)(BlockTab tab, co
 }
 
 // The metal chain with MT lanes per metal atom (4, 8, 16 or 32; grid = the block table for
-// 128 / MT atoms per block), from the host of the including unit.
-void SG_KN(launchMetalChain)(int mt, int grid, cudaStream_t s, BlockTab tab, const RepConst *rc,
-                                    float4 *pos, float4 *acc, const int *nn, const int *nbl, float *rho,
-                                    float *dF, float *Fv, float *fric, int rowStride SG_EAM_PARAM) {
+// 128 / MT atoms per block), from the host of the including unit; pdl: programmatic
+// dependent launch (launch errors are left for cudaGetLastError).
+void SG_KN(launchMetalChain)(bool pdl, int mt, int grid, cudaStream_t s, BlockTab tab, const RepConst *rc,
+                             float4 *pos, float4 *acc, const int *nn, const int *nbl, float *rho, float *dF,
+                             float *Fv, float *fric, int rowStride SG_EAM_PARAM) {
   switch (mt) {
     case 4:
-      SG_KN(k_rho_tpa)<4><<<grid, 128, 0, s>>>(tab, rc, pos, nn, nbl, rho, dF, Fv, rowStride SG_EAM_ARG);
-      SG_KN(k_force_metal_tpa)<4><<<grid, 128, 0, s>>>(tab, rc, pos, acc, nn, nbl, dF, Fv, fric, rowStride SG_EAM_ARG);
+      launchK(pdl, SG_KN(k_rho_tpa)<4>, grid, 128, 0, s, tab, rc, pos, nn, nbl, rho, dF, Fv, rowStride SG_EAM_ARG);
+      launchK(pdl, SG_KN(k_force_metal_tpa)<4>, grid, 128, 0, s, tab, rc, pos, acc, nn, nbl, dF, Fv, fric,
+              rowStride SG_EAM_ARG);
       break;
     case 8:
-      SG_KN(k_rho_tpa)<8><<<grid, 128, 0, s>>>(tab, rc, pos, nn, nbl, rho, dF, Fv, rowStride SG_EAM_ARG);
-      SG_KN(k_force_metal_tpa)<8><<<grid, 128, 0, s>>>(tab, rc, pos, acc, nn, nbl, dF, Fv, fric, rowStride SG_EAM_ARG);
+      launchK(pdl, SG_KN(k_rho_tpa)<8>, grid, 128, 0, s, tab, rc, pos, nn, nbl, rho, dF, Fv, rowStride SG_EAM_ARG);
+      launchK(pdl, SG_KN(k_force_metal_tpa)<8>, grid, 128, 0, s, tab, rc, pos, acc, nn, nbl, dF, Fv, fric,
+              rowStride SG_EAM_ARG);
       break;
     case 32:
-      SG_KN(k_rho_tpa)<32><<<grid, 128, 0, s>>>(tab, rc, pos, nn, nbl, rho, dF, Fv, rowStride SG_EAM_ARG);
-      SG_KN(k_force_metal_tpa)<32><<<grid, 128, 0, s>>>(tab, rc, pos, acc, nn, nbl, dF, Fv, fric, rowStride SG_EAM_ARG);
+      launchK(pdl, SG_KN(k_rho_tpa)<32>, grid, 128, 0, s, tab, rc, pos, nn, nbl, rho, dF, Fv, rowStride SG_EAM_ARG);
+      launchK(pdl, SG_KN(k_force_metal_tpa)<32>, grid, 128, 0, s, tab, rc, pos, acc, nn, nbl, dF, Fv, fric,
+              rowStride SG_EAM_ARG);
       break;
     default:
-      SG_KN(k_rho)<<<grid, 128, 0, s>>>(tab, rc, pos, nn, nbl, rho, dF, Fv, rowStride SG_EAM_ARG);
-      SG_KN(k_force_metal)<<<grid, 128, 0, s>>>(tab, rc, pos, acc, nn, nbl, dF, Fv, fric, rowStride SG_EAM_ARG);
+      launchK(pdl, SG_KN(k_rho), grid, 128, 0, s, tab, rc, pos, nn, nbl, rho, dF, Fv, rowStride SG_EAM_ARG);
+      launchK(pdl, SG_KN(k_force_metal), grid, 128, 0, s, tab, rc, pos, acc, nn, nbl, dF, Fv, fric,
+              rowStride SG_EAM_ARG);
   }
 }
 
@@ -320,6 +327,7 @@ __global__ void __launch_bounds__(128, 8) SG_KN(k_force_carbon)(BlockTab tab, co
                                                       const int *__restrict__ ns, const int *__restrict__ sl,
                                                       const int *__restrict__ nrl, const int2 *__restrict__ rl,
                                                       int rowStride) {
+  pdlEnter();
   __shared__ float sD[128 / kCT][3][4];  // dx, dy, dz, |d| of close carbon q
   __shared__ float sZ[128 / kCT][3];     // its z - z_0
   __shared__ int sK[128 / kCT][3];       // its index

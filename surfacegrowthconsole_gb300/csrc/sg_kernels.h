@@ -8,16 +8,26 @@ namespace sg {
 // ---- shared list building (PLAIN TU, also used by MIXED) ----
 __global__ void k_integrate_first(BlockTab tab, const RepConst *rc, RepState *st, float4 *pos,
                                   float4 *vel, const float4 *acc, int *cellOf, int *slot,
-                                  int *cellCount, int forceRebuild);
+                                  int *cellCount, int forceRebuild, int *bucket, int cap, int *blockCount);
 __global__ void k_cell_count(BlockTab tab, const RepConst *rc, const float4 *pos, int *cellOf,
                              int *slot, int *cellCount);
+__global__ void k_cell_bucket(BlockTab tab, const RepConst *rc, const float4 *pos, int *cellOf, int *slot,
+                              int *cellCount, int *bucket, int cap, int *blockCount);
+// one block of kScanThreads threads per kScanCells cells
+__global__ void k_scan_cells(const int *tileRep, const int *tileStart, const int *tileFirst, const RepConst *rc,
+                             RepState *st, int *cellCount, int *cellStart, int cap, int forceRebuild, int *active,
+                             int2 *heavy, int *work, int itemAtoms, const int *blockCount);
+__global__ void k_rank_cells(BlockTab tab, const RepConst *rc, RepState *st, const int *cellOf, const int *slot,
+                             const int *cellStart, const int *bucket, int cap, const float4 *pos, int *sortIdx,
+                             float4 *sortPos, int *nn, int *ns, int *nrl, int forceRebuild, int *blockCount,
+                             int nBlockCount);
 __global__ void k_scan_tiles(BlockTab tab, const RepConst *rc, const RepState *st,
                              const int *cellCount, int *tileSum, int forceRebuild);
 __global__ void k_scan_tile_prefix(const RepConst *rc, const RepState *st, const int *tileFirst,
-                                   int *tileSum, int forceRebuild);
+                                   int *tileSum, int forceRebuild, int *work);
 __global__ void k_scan_final(BlockTab tab, const RepConst *rc, RepState *st, int *cellCount,
                              const int *tileSum, int *cellStart, int blockSizeCap, int forceRebuild,
-                             int *active, int2 *heavy, int *work);
+                             int *active, int2 *heavy, int *work, int itemAtoms);
 __global__ void k_scatter(BlockTab tab, const RepConst *rc, RepState *st, const int *cellOf,
                           const int *slot, const int *cellStart, int *tmpIdx, int *nn, int *ns, int *nrl,
                           int forceRebuild);
@@ -28,7 +38,7 @@ __global__ void k_rank(BlockTab tab, const RepConst *rc, const RepState *st, con
 // of the home-chunk list `heavy` (all reset before the scan of every rebuild).
 __global__ void k_build_nebr(const int *tileRep, const int *active, const int2 *heavy, int *work, const RepConst *rc, RepState *st,
                              const int *cellStart, const float4 *sortPos, int *nn, int *nbl, int *ns, int *sl,
-                             int *nrl, int2 *rl, int rowStride, int nebrMax);
+                             int *nrl, int2 *rl, int rowStride, int nebrMax, int descending);
 
 // ---- PLAIN force and step kernels ----
 __global__ void k_rho(BlockTab tab, const RepConst *rc, const float4 *pos, const int *nn,
@@ -38,7 +48,7 @@ __global__ void k_force_metal(BlockTab tab, const RepConst *rc, float4 *pos, flo
                               float *fric, int rowStride);
 // the metal chain (k_rho, k_force_metal) with mt lanes per atom (4, 8, 16, 32) on the table of
 // 128 / mt atoms per block
-void launchMetalChain(int mt, int grid, cudaStream_t s, BlockTab tab, const RepConst *rc, float4 *pos,
+void launchMetalChain(bool pdl, int mt, int grid, cudaStream_t s, BlockTab tab, const RepConst *rc, float4 *pos,
                       float4 *acc, const int *nn, const int *nbl, float *rho, float *dF, float *Fv,
                       float *fric, int rowStride);
 __global__ void k_force_carbon(BlockTab tab, const RepConst *rc, float4 *pos, float4 *acc,

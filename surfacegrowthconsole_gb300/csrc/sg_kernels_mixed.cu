@@ -83,7 +83,9 @@ __global__ void k_integrate_mixed(BlockTab tab, const RepConst *__restrict__ rc,
                                   float4 *__restrict__ pos, float4 *__restrict__ posLo,
                                   float4 *__restrict__ vel, const float4 *__restrict__ acc,
                                   int *__restrict__ cellOf, int *__restrict__ slot,
-                                  int *__restrict__ cellCount, int forceRebuild) {
+                                  int *__restrict__ cellCount, int forceRebuild, int *__restrict__ bucket,
+                                  int cap, int *__restrict__ blockCount) {
+  pdlEnter();
   const int rep = tab.rep[blockIdx.x];
   const RepConst &P = rc[rep];
   RepState *S = st + rep;
@@ -139,11 +141,7 @@ __global__ void k_integrate_mixed(BlockTab tab, const RepConst *__restrict__ rc,
   pos[g] = r;
   posLo[g] = lo;
   vel[g] = v;
-  if (forceRebuild || S->nebrNow) {
-    const int c = cellIndex(P, r.x, r.y, r.z);
-    cellOf[g] = c;
-    if (c >= 0) slot[g] = atomicAdd(&cellCount[P.cellOff + c], 1);
-  }
+  if (forceRebuild || S->nebrNow) binAtom(P, g, r, cellOf, slot, cellCount, bucket, cap, blockCount);
 }
 
 // ============================================================================================
@@ -184,6 +182,7 @@ __global__ void __launch_bounds__(kRedThreads, 1) k_step_reduce_mixed(
     const int *__restrict__ redFirst, unsigned *counter, double *__restrict__ diff64,
     const size_t *__restrict__ diffOff64, float *__restrict__ diffF, const size_t *__restrict__ diffOffF,
     int forceRebuild) {
+  pdlEnter();
   const int rep = tab.rep[blockIdx.x];
   const RepConst &P = rc[rep];
   RepState *S = st + rep;
@@ -602,8 +601,9 @@ void sg_mixed_free(sg_ctx *c) {
 
 int sg_mixed_enqueue_integrate(sg_ctx *c, int forceRebuild) {
   if (!c->atomTab.n) return SG_OK;
-  k_integrate_mixed<<<c->atomTab.n, 128, 0, c->stream>>>(c->atomTab.view(), c->rc, c->st, c->pos, c->posLo, c->vel,
-                                                         c->acc, c->cellOf, c->slot, c->cellCount, forceRebuild);
+  MCK(launchK(c->pdl, k_integrate_mixed, c->atomTab.n, 128, 0, c->stream, c->atomTab.view(), c->rc, c->st, c->pos, c->posLo, c->vel,
+                                                         c->acc, c->cellOf, c->slot, c->cellCount, forceRebuild,
+                c->bucket, c->bucketCap, c->blockCount));
   MCK(cudaGetLastError());
   return SG_OK;
 }
@@ -616,15 +616,15 @@ int sg_mixed_enqueue_forces(sg_ctx *c) {
   if (fork) {
     MCK(cudaEventRecord(c->evFork, c->stream));
     MCK(cudaStreamWaitEvent(c->side, c->evFork, 0));
-    launchMetalChain_mixed(c->metalLanes, c->metalRun.n, c->side, c->metalRun.view(), c->rc, c->pos, c->acc,
+    launchMetalChain_mixed(c->pdl, c->metalLanes, c->metalRun.n, c->side, c->metalRun.view(), c->rc, c->pos, c->acc,
                            c->nn, c->nbl, c->rho, c->dF, c->Fv, c->fric, c->rowStride, m->eamTab);
     if (c->opt.phase_timing) cudaEventRecordWithFlags(c->phaseEv[7], c->side, cudaEventRecordExternal);
     MCK(cudaGetLastError());
   }
   if (c->carbonTabT.n) {
-    k_force_carbon_mixed<<<c->carbonTabT.n, 128, 0, c->stream>>>(c->carbonTabT.view(), c->rc, c->pos, c->acc,
+    MCK(launchK(c->pdl, k_force_carbon_mixed, c->carbonTabT.n, 128, 0, c->stream, c->carbonTabT.view(), c->rc, c->pos, c->acc,
                                                                  c->nn, c->nbl, c->ns, c->sl, c->nrl, c->rl,
-                                                                 c->rowStride);
+                                                                 c->rowStride));
     }
   if (c->opt.phase_timing) cudaEventRecordWithFlags(c->phaseEv[3], c->stream, cudaEventRecordExternal);
   MCK(cudaGetLastError());
@@ -640,9 +640,9 @@ int sg_mixed_enqueue_forces(sg_ctx *c) {
 int sg_mixed_enqueue_reduce(sg_ctx *c, int forceRebuild) {
   MixedBufs *m = static_cast<MixedBufs *>(c->mixed);
   if (!c->redTab.n) return SG_OK;
-  k_step_reduce_mixed<<<c->redTab.n, kRedThreads, 0, c->stream>>>(
+  MCK(launchK(c->pdl, k_step_reduce_mixed, c->redTab.n, kRedThreads, 0, c->stream, 
       c->redTab.view(), c->rc, c->st, c->pos, c->posLo, c->vel, c->acc, c->fric, m->part64, m->partF,
-      c->dRedFirst, m->counter, m->diff64, m->dDiffOff64, c->diffBuf, c->dDiffOff, forceRebuild);
+      c->dRedFirst, m->counter, m->diff64, m->dDiffOff64, c->diffBuf, c->dDiffOff, forceRebuild));
   MCK(cudaGetLastError());
   return SG_OK;
 }

@@ -42,7 +42,9 @@ __global__ void k_integrate_first(BlockTab tab, const RepConst *__restrict__ rc,
                                   float4 *__restrict__ pos, float4 *__restrict__ vel,
                                   const float4 *__restrict__ acc, int *__restrict__ cellOf,
                                   int *__restrict__ slot, int *__restrict__ cellCount,
-                                  int forceRebuild) {
+                                  int forceRebuild, int *__restrict__ bucket, int cap,
+                                  int *__restrict__ blockCount) {
+  pdlEnter();
   const int rep = tab.rep[blockIdx.x];
   const RepConst &P = rc[rep];
   RepState *S = st + rep;
@@ -99,11 +101,7 @@ __global__ void k_integrate_first(BlockTab tab, const RepConst *__restrict__ rc,
   else if (r.z < -0.5f * P.region[2]) r.z += P.region[2];
   pos[g] = r;
   vel[g] = v;
-  if (forceRebuild || S->nebrNow) {
-    const int c = cellIndex(P, r.x, r.y, r.z);
-    cellOf[g] = c;
-    if (c >= 0) slot[g] = atomicAdd(&cellCount[P.cellOff + c], 1);
-  }
+  if (forceRebuild || S->nebrNow) binAtom(P, g, r, cellOf, slot, cellCount, bucket, cap, blockCount);
 }
 
 // Histogram pass alone (used when lists are rebuilt outside a step).
@@ -120,6 +118,18 @@ __global__ void k_cell_count(BlockTab tab, const RepConst *__restrict__ rc,
   if (c >= 0) slot[g] = atomicAdd(&cellCount[P.cellOff + c], 1);
 }
 
+// Histogram and bucket pass alone (lists rebuilt outside a step).
+__global__ void k_cell_bucket(BlockTab tab, const RepConst *__restrict__ rc, const float4 *__restrict__ pos,
+                              int *__restrict__ cellOf, int *__restrict__ slot, int *__restrict__ cellCount,
+                              int *__restrict__ bucket, int cap, int *__restrict__ blockCount) {
+  pdlEnter();
+  const int rep = tab.rep[blockIdx.x];
+  const RepConst &P = rc[rep];
+  const int g = tab.start[blockIdx.x] + threadIdx.x;
+  if (g >= P.atomOff + P.nMol) return;
+  binAtom(P, g, pos[g], cellOf, slot, cellCount, bucket, cap, blockCount);
+}
+
 __device__ __forceinline__ bool rebuilding(const RepState *S, int forceRebuild) {
   return forceRebuild || S->nebrNow;
 }
@@ -131,6 +141,7 @@ __device__ __forceinline__ bool rebuilding(const RepState *S, int forceRebuild) 
 __global__ void k_scan_tiles(BlockTab tab, const RepConst *__restrict__ rc, const RepState *st,
                              const int *__restrict__ cellCount, int *__restrict__ tileSum,
                              int forceRebuild) {
+  pdlEnter();
   const int rep = tab.rep[blockIdx.x];
   if (!rebuilding(st + rep, forceRebuild)) return;
   const RepConst &P = rc[rep];
@@ -149,10 +160,13 @@ __global__ void k_scan_tiles(BlockTab tab, const RepConst *__restrict__ rc, cons
 }
 
 // One block per replica: exclusive prefix over the replica's tiles (tiles of a replica are
-// consecutive blocks of the tile table starting at tileFirst[rep]).
+// consecutive blocks of the tile table starting at tileFirst[rep]).  Block 0 also clears the
+// list build's work counters (work, if not NULL) for k_scan_final and k_build_nebr.
 __global__ void k_scan_tile_prefix(const RepConst *__restrict__ rc, const RepState *st,
                                    const int *__restrict__ tileFirst, int *__restrict__ tileSum,
-                                   int forceRebuild) {
+                                   int forceRebuild, int *__restrict__ work) {
+  pdlEnter();
+  if (work && blockIdx.x == 0 && threadIdx.x < 3) work[threadIdx.x] = 0;
   const int rep = blockIdx.x;
   if (!rebuilding(st + rep, forceRebuild)) return;
   const RepConst &P = rc[rep];
@@ -196,7 +210,9 @@ __global__ void k_scan_tile_prefix(const RepConst *__restrict__ rc, const RepSta
 __global__ void k_scan_final(BlockTab tab, const RepConst *__restrict__ rc, RepState *st,
                              int *__restrict__ cellCount, const int *__restrict__ tileSum,
                              int *__restrict__ cellStart, int blockSizeCap, int forceRebuild,
-                             int *__restrict__ active, int2 *__restrict__ heavy, int *__restrict__ work) {
+                             int *__restrict__ active, int2 *__restrict__ heavy, int *__restrict__ work,
+                             int itemAtoms) {
+  pdlEnter();
   const int rep = tab.rep[blockIdx.x];
   RepState *S = st + rep;
   if (!rebuilding(S, forceRebuild)) return;
@@ -237,14 +253,15 @@ __global__ void k_scan_final(BlockTab tab, const RepConst *__restrict__ rc, RepS
     run += v[i];
     cellCount[cb + i] = 0;
   }
-  // work items of the list build (any order): a cell of up to kHeavyCell atoms is one item;
-  // a larger one is split into items of kHeavyChunk home atoms, queued apart so that the list
-  // build takes them first
+  // work items of the list build (any order): a cell of up to itemAtoms atoms is one item; a
+  // cell of n > itemAtoms atoms is split into k = ceil(n / itemAtoms) items of n / k home atoms
+  // (rounded), queued apart so that the list build takes them first.  A split item is
+  // {cell, first home atom << 16 | home atoms}.
   int nLight = 0, nHeavy = 0;
 #pragma unroll
   for (int i = 0; i < kPer; i++) {
     if (v[i] > 0 && c0 + threadIdx.x * kPer + i < P.ncells) {
-      if (v[i] > kHeavyCell) nHeavy += (v[i] + kHeavyChunk - 1) / kHeavyChunk;
+      if (v[i] > itemAtoms) nHeavy += (v[i] + itemAtoms - 1) / itemAtoms;
       else nLight++;
     }
   }
@@ -265,8 +282,12 @@ __global__ void k_scan_final(BlockTab tab, const RepConst *__restrict__ rc, RepS
 #pragma unroll
   for (int i = 0; i < kPer; i++) {
     if (v[i] > 0 && c0 + threadIdx.x * kPer + i < P.ncells) {
-      if (v[i] > kHeavyCell) {
-        for (int h = 0; h < v[i]; h += kHeavyChunk) heavy[outH++] = make_int2(cb + i, h);
+      if (v[i] > itemAtoms) {
+        const int k = (v[i] + itemAtoms - 1) / itemAtoms;
+        for (int j = 0; j < k; j++) {
+          const int h0 = j * v[i] / k, h1 = (j + 1) * v[i] / k;
+          heavy[outH++] = make_int2(cb + i, (h0 << 16) | (h1 - h0));
+        }
       } else {
         active[outL++] = cb + i;
       }
@@ -291,6 +312,7 @@ __global__ void k_scatter(BlockTab tab, const RepConst *__restrict__ rc, RepStat
                           const int *__restrict__ cellStart, int *__restrict__ tmpIdx,
                           int *__restrict__ nn, int *__restrict__ ns, int *__restrict__ nrl,
                           int forceRebuild) {
+  pdlEnter();
   const int rep = tab.rep[blockIdx.x];
   RepState *S = st + rep;
   if (!rebuilding(S, forceRebuild)) return;
@@ -315,6 +337,7 @@ __global__ void k_rank(BlockTab tab, const RepConst *__restrict__ rc, const RepS
                        const int *__restrict__ cellOf, const int *__restrict__ cellStart,
                        const int *__restrict__ tmpIdx, const float4 *__restrict__ pos,
                        int *__restrict__ sortIdx, float4 *__restrict__ sortPos, int forceRebuild) {
+  pdlEnter();
   const int rep = tab.rep[blockIdx.x];
   if (!rebuilding(st + rep, forceRebuild)) return;
   const RepConst &P = rc[rep];
@@ -332,9 +355,195 @@ __global__ void k_rank(BlockTab tab, const RepConst *__restrict__ rc, const RepS
 }
 
 // ============================================================================================
+// Counting sort in two passes (the engine's path).  The histogram pass (binAtom) files each
+// atom in its cell's bucket and counts the filed atoms per block of kScanCells cells
+// (blockCount).  k_scan_cells: one block per kScanCells cells takes its exclusive offset from
+// the counts of the replica's earlier blocks (no wait on another block), scans its cells and
+// writes cellStart and the list build's work items.  k_rank_cells orders each cell from its
+// bucket and clears blockCount for the next rebuild.
+// ============================================================================================
+__global__ void __launch_bounds__(kScanThreads) k_scan_cells(const int *__restrict__ tileRep,
+                                                             const int *__restrict__ tileStart,
+                                                             const int *__restrict__ tileFirst,
+                                                             const RepConst *__restrict__ rc, RepState *st,
+                                                             int *__restrict__ cellCount, int *__restrict__ cellStart,
+                                                             int cap, int forceRebuild, int *__restrict__ active,
+                                                             int2 *__restrict__ heavy, int *__restrict__ work,
+                                                             int itemAtoms, const int *__restrict__ blockCount) {
+  pdlEnter();
+  constexpr int kSub = kCellTile / kScanCells;  // scan blocks per tile of the tile table
+  constexpr int kPer = kScanCells / kScanThreads;
+  constexpr int kWarps = kScanThreads / 32;
+  __shared__ int ws[kWarps], wp[kWarps];
+  __shared__ int wl[kWarps], wh[kWarps], wOcc[kWarps], wOver[kWarps], sBaseL, sBaseH;
+  const int t = blockIdx.x;
+  const int rep = tileRep[t / kSub];
+  RepState *S = st + rep;
+  if (!rebuilding(S, forceRebuild)) return;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const RepConst &P = rc[rep];
+  const int first = tileFirst[rep] * kSub;  // the replica's first scan block
+  const int c0 = tileStart[t / kSub] + (t % kSub) * kScanCells;
+  int v[kPer];
+  int sum = 0, occ = 0, over = 0;
+  const int cb = P.cellOff + c0 + threadIdx.x * kPer;
+#pragma unroll
+  for (int i = 0; i < kPer; i++) {
+    const int n = cellCount[cb + i];
+    occ = max(occ, n);
+    over += (n > cap) ? 1 : 0;
+    v[i] = min(n, cap);  // atoms past the cap are not in the bucket (SG_ERR_CELL_OVERFLOW)
+    sum += v[i];
+  }
+  int pre = 0;  // atoms filed in the replica's earlier blocks
+  for (int q = first + threadIdx.x; q < t; q += kScanThreads) pre += blockCount[q];
+  int x = sum;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  for (int o = 16; o > 0; o >>= 1) pre += __shfl_xor_sync(0xffffffffu, pre, o);
+  if (lane == 31) ws[wid] = x;
+  if (lane == 0) wp[wid] = pre;
+  __syncthreads();
+  int warpOff = 0, excl = 0;
+#pragma unroll
+  for (int k = 0; k < kWarps; k++) {
+    warpOff += (k < wid) ? ws[k] : 0;
+    excl += wp[k];
+  }
+  int run = P.atomOff + excl + warpOff + x - sum;
+#pragma unroll
+  for (int i = 0; i < kPer; i++) {
+    cellStart[cb + i] = run;
+    run += v[i];
+    cellCount[cb + i] = 0;
+  }
+  // work items of the list build, as in k_scan_final; one atomic per list for the block
+  int nLight = 0, nHeavy = 0;
+#pragma unroll
+  for (int i = 0; i < kPer; i++) {
+    if (v[i] > 0 && c0 + threadIdx.x * kPer + i < P.ncells) {
+      if (v[i] > itemAtoms) nHeavy += (v[i] + itemAtoms - 1) / itemAtoms;
+      else nLight++;
+    }
+  }
+  int preL = nLight, preH = nHeavy;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int yl = __shfl_up_sync(0xffffffffu, preL, o);
+    const int yh = __shfl_up_sync(0xffffffffu, preH, o);
+    if (lane >= o) { preL += yl; preH += yh; }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    occ = max(occ, __shfl_xor_sync(0xffffffffu, occ, o));
+    over += __shfl_xor_sync(0xffffffffu, over, o);
+  }
+  if (lane == 31) {
+    wl[wid] = preL;
+    wh[wid] = preH;
+    wOcc[wid] = occ;
+    wOver[wid] = over;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int tl = 0, th = 0, to = 0, tv = 0;
+    for (int k = 0; k < kWarps; k++) {
+      const int l = wl[k], h = wh[k];
+      wl[k] = tl; wh[k] = th;  // exclusive warp offsets
+      tl += l; th += h;
+      to = max(to, wOcc[k]);
+      tv += wOver[k];
+    }
+    sBaseL = tl > 0 ? atomicAdd(&work[1], tl) : 0;
+    sBaseH = th > 0 ? atomicAdd(&work[2], th) : 0;
+    if (to > 0) atomicMax(&S->maxCellOcc, to);
+    if (tv > 0) {
+      atomicAdd(&S->cellOverflow, tv);
+      setFlag(S, 11 /*SG_ERR_CELL_OVERFLOW*/);
+    }
+  }
+  __syncthreads();
+  int outL = sBaseL + wl[wid] + preL - nLight;
+  int outH = sBaseH + wh[wid] + preH - nHeavy;
+#pragma unroll
+  for (int i = 0; i < kPer; i++) {
+    if (v[i] > 0 && c0 + threadIdx.x * kPer + i < P.ncells) {
+      if (v[i] > itemAtoms) {
+        const int k = (v[i] + itemAtoms - 1) / itemAtoms;
+        for (int j = 0; j < k; j++) {
+          const int h0 = j * v[i] / k, h1 = (j + 1) * v[i] / k;
+          heavy[outH++] = make_int2(cb + i, (h0 << 16) | (h1 - h0));
+        }
+      } else {
+        active[outL++] = cb + i;
+      }
+    }
+  }
+}
+
+// Orders each cell by ascending atom index, from the cell's bucket: the rank of an atom is the
+// number of atoms of its bucket with a smaller index.  Also clears blockCount.  Writes the sorted index and a sorted
+// position copy whose w holds the atom index (as int bits); an atom outside the grid gets
+// empty lists (the reference clears its NN) and is counted in cellRange.
+__global__ void k_rank_cells(BlockTab tab, const RepConst *__restrict__ rc, RepState *st,
+                             const int *__restrict__ cellOf, const int *__restrict__ slot,
+                             const int *__restrict__ cellStart, const int *__restrict__ bucket, int cap,
+                             const float4 *__restrict__ pos, int *__restrict__ sortIdx,
+                             float4 *__restrict__ sortPos, int *__restrict__ nn, int *__restrict__ ns,
+                             int *__restrict__ nrl, int forceRebuild, int *__restrict__ blockCount,
+                             int nBlockCount) {
+  pdlEnter();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nBlockCount; i += gridDim.x * blockDim.x)
+    blockCount[i] = 0;  // k_scan_cells has read them
+  const int rep = tab.rep[blockIdx.x];
+  RepState *S = st + rep;
+  const RepConst &P = rc[rep];
+  const int g = tab.start[blockIdx.x] + threadIdx.x;
+  if (g >= P.atomOff + P.nMol) return;
+  // independent loads first: one round trip for all of them
+  const int c = cellOf[g];
+  const int sg = slot[g];
+  float4 r = pos[g];
+  if (!rebuilding(S, forceRebuild)) return;
+  if (c < 0) {
+    nn[g] = 0;
+    ns[g] = 0;
+    nrl[g] = 0;
+    atomicAdd(&S->cellRange, 1);
+    return;
+  }
+  if (sg >= cap) return;  // not filed: the cell overflowed
+  const int gc = P.cellOff + c;
+  const int b = cellStart[gc], n = cellStart[gc + 1] - b;
+  const int *bk = bucket + (size_t)gc * cap;
+  int rank = 0;
+  if ((cap & 3) == 0) {  // rows of a multiple of 4 slots: 16-byte loads, four at a time
+    for (int q = 0; q < n; q += 16) {
+      int4 u[4];
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+        u[k] = (q + 4 * k < n) ? *reinterpret_cast<const int4 *>(bk + q + 4 * k) : make_int4(g, g, g, g);
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const int q0 = q + 4 * k;
+        rank += (q0 < n && u[k].x < g) + (q0 + 1 < n && u[k].y < g) + (q0 + 2 < n && u[k].z < g) +
+                (q0 + 3 < n && u[k].w < g);
+      }
+    }
+  } else {
+    for (int q = 0; q < n; q++) rank += (bk[q] < g) ? 1 : 0;
+  }
+  sortIdx[b + rank] = g;
+  r.w = __int_as_float(g);
+  sortPos[b + rank] = r;
+}
+
+// ============================================================================================
 // Neighbour list (BuildNebrListK, SurfaceGrowth.cu:612-711), cell-centric.  Warps take work
-// items from the lists k_scan_final wrote, through an atomic work counter: first the chunks of
-// kHeavyChunk home atoms of the crowded cells, then the other non-empty cells whole.  Lanes
+// items from the lists k_scan_final wrote, through an atomic work counter: first the parts of
+// the cells split into several items, then the other non-empty cells whole, in
+// ascending cell order or (descending != 0) descending: the queue should end on cheap items,
+// and in a surface system the dense metal cells sit at the high cell indices (z-major).  Lanes
 // 0..26 look up the 27 stencil cells (reference visiting order); their segments, in that order
 // and ascending atom index inside each, form the cell's window of candidates: exactly the
 // order in which the reference's one-thread walk meets them.  A lane finds the segment of its
@@ -376,7 +585,8 @@ __global__ void __launch_bounds__(kNebrWarps * 32) k_build_nebr(const int *__res
                                                                 int *__restrict__ nn, int *__restrict__ nbl,
                                                                 int *__restrict__ ns, int *__restrict__ sl,
                                                                 int *__restrict__ nrl, int2 *__restrict__ rl,
-                                                                int rowStride, int nebrMax) {
+                                                                int rowStride, int nebrMax, int descending) {
+  pdlEnter();
   __shared__ int sK[kNebrWarps][kWin];                 // atom index of each window position
   __shared__ uint2 sMask[kNebrWarps][kWin / 32][32];   // [word][home atom]: {hit, close}
   __shared__ unsigned sMetal[kNebrWarps][kWin / 32];   // [word]: candidate is a metal atom
@@ -391,15 +601,24 @@ __global__ void __launch_bounds__(kNebrWarps * 32) k_build_nebr(const int *__res
     int idx = 0;
     if (lane == 0) idx = atomicAdd(&work[0], 1);
     idx = __shfl_sync(full, idx, 0);
-    if (idx >= nHeavy + nLight) break;
+    if (idx >= nHeavy + nLight) {
+      // every warp takes one ticket past the end; the last one clears the counters for the
+      // next rebuild (all warps have read them by then)
+      if (lane == 0 && idx == nHeavy + nLight + (int)gridDim.x * kNebrWarps - 1) {
+        work[0] = 0;
+        work[1] = 0;
+        work[2] = 0;
+      }
+      break;
+    }
     int gc, hOff = 0, hCnt = 1 << 30;
     if (idx < nHeavy) {
       const int2 it = heavy[idx];
       gc = it.x;
-      hOff = it.y;
-      hCnt = kHeavyChunk;
+      hOff = it.y >> 16;
+      hCnt = it.y & 0xffff;
     } else {
-      gc = active[idx - nHeavy];
+      gc = active[descending ? nHeavy + nLight - 1 - idx : idx - nHeavy];
     }
     const int rep = tileRep[gc / kCellTile];
     RepState *S = st + rep;
@@ -615,6 +834,7 @@ __global__ void __launch_bounds__(kRedThreads) k_cmvel(BlockTab tab, const RepCo
                                                        const float4 *__restrict__ acc,
                                                        float *__restrict__ partial,
                                                        const int *__restrict__ redFirst) {
+  pdlEnter();
   const int rep = tab.rep[blockIdx.x];
   const RepConst &P = rc[rep];
   RepState *S = st + rep;
@@ -715,6 +935,7 @@ __global__ void __launch_bounds__(kRedThreads) k_step_reduce(
     float4 *__restrict__ vel, const float4 *__restrict__ acc, const float *__restrict__ fric,
     float *__restrict__ partial, const int *__restrict__ redFirst, float *__restrict__ diffBuf,
     const size_t *__restrict__ diffOff, int forceRebuild) {
+  pdlEnter();
   const int rep = tab.rep[blockIdx.x];
   const RepConst &P = rc[rep];
   RepState *S = st + rep;
@@ -958,6 +1179,7 @@ __device__ void stepControl(const RepConst &P, RepState *S, const float (&red)[k
 // updated the shear value, add it to a.x of metal atoms left of the centre of mass.
 __global__ void k_shear(BlockTab tab, const RepConst *__restrict__ rc, RepState *st,
                         const float4 *__restrict__ pos, float4 *__restrict__ acc) {
+  pdlEnter();
   const int rep = tab.rep[blockIdx.x];
   const RepConst &P = rc[rep];
   RepState *S = st + rep;
@@ -1001,6 +1223,7 @@ __global__ void k_rdf(BlockTab tab, const RepConst *__restrict__ rc, RepState *s
                       const float4 *__restrict__ pos, const int *__restrict__ cellOf,
                       const int *__restrict__ cellStart, const int *__restrict__ sortIdx,
                       unsigned *__restrict__ hist, int histStride) {
+  pdlEnter();
   extern __shared__ unsigned shist[];
   const int rep = tab.rep[blockIdx.x];
   const RepConst &P = rc[rep];
@@ -1090,6 +1313,7 @@ __global__ void __launch_bounds__(128) k_rdf_ext(const RepConst *__restrict__ rc
                                                  const int *__restrict__ tileRep,
                                                  const int *__restrict__ tileStart,
                                                  unsigned long long *__restrict__ hist, int nbins, float range) {
+  pdlEnter();
   extern __shared__ unsigned eh[];
   __shared__ float4 tileB[128];
   __shared__ float boxA[6], boxB[6];
@@ -1149,6 +1373,7 @@ __global__ void __launch_bounds__(128) k_rdf_ext(const RepConst *__restrict__ rc
 // Apply a pending thermostat rescale now (before the state is read back).
 __global__ void k_apply_pending(BlockTab tab, const RepConst *__restrict__ rc, RepState *st,
                                 float4 *__restrict__ vel) {
+  pdlEnter();
   const int rep = tab.rep[blockIdx.x];
   const RepConst &P = rc[rep];
   const RepState *S = st + rep;
@@ -1182,6 +1407,7 @@ __global__ void k_pack3(const float4 *src, float *dst, int n) {
 }
 
 __global__ void k_clear_pending(RepState *st, int nrep) {
+  pdlEnter();
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r < nrep) st[r].thermoPending = 0;
 }

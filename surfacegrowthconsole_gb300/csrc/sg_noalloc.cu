@@ -200,14 +200,14 @@ extern "C" int sg_compute_forces_noalloc(const sg_simparams *p, sg_float4 *d_pos
   k_noalloc_setup<<<64, 256, 0, s>>>(P, st, rc, tabRep, tabStart, tileRep, tileStart, tileFirst, cellCount, work);
   k_cell_count<<<nAtomBlk, kBs, 0, s>>>(atomTab, rc, pos, cellOf, slot, cellCount);
   k_scan_tiles<<<nTiles, 256, 0, s>>>(tileTab, rc, st, cellCount, tileSum, 1);
-  k_scan_tile_prefix<<<1, 1024, 0, s>>>(rc, st, tileFirst, tileSum, 1);
+  k_scan_tile_prefix<<<1, 1024, 0, s>>>(rc, st, tileFirst, tileSum, 1, nullptr);
   k_scan_final<<<nTiles, 256, 0, s>>>(tileTab, rc, st, cellCount, tileSum, cellStart, (int)p->blockSize, 1, active,
-                                      heavy, work);
+                                      heavy, work, kHeavyCell);
   k_scatter<<<nAtomBlk, kBs, 0, s>>>(atomTab, rc, st, cellOf, slot, cellStart, tmpIdx, nn, ns, nrl, 1);
   k_rank<<<nAtomBlk, kBs, 0, s>>>(atomTab, rc, st, cellOf, cellStart, tmpIdx, pos, sortIdx, sortPos, 1);
   const int rowStride = (p->iNebrMax + 3) & ~3;
   k_build_nebr<<<256, kNebrWarps * 32, 0, s>>>(tileRep, active, heavy, work, rc, st, cellStart, sortPos, nn, nbl, ns,
-                                               sl, nrl, rl, rowStride, p->iNebrMax);
+                                               sl, nrl, rl, rowStride, p->iNebrMax, 0);
   if (nMetalBlk) {
     k_rho<<<nMetalBlk, kBs, 0, s>>>(metalTab, rc, pos, nn, nbl, rho, dF, Fv, rowStride);
     k_force_metal<<<nMetalBlk, kBs, 0, s>>>(metalTab, rc, pos, acc, nn, nbl, dF, Fv, fric, rowStride);

@@ -17,7 +17,7 @@ from typing import Sequence
 
 import numpy as np
 
-from ._lib import (MODE_MIXED, MODE_PLAIN, Diag, Input, Options, SimParams, Thermo, Workload,
+from ._lib import (MODE_MIXED, MODE_PLAIN, Diag, Input, LaunchShape, Options, SimParams, Thermo, Workload,
                    check, lib, libc)
 
 __all__ = ["Simulation", "read_input_file", "default_input", "set_params", "init_coords", "init_vels",
@@ -87,7 +87,8 @@ class Simulation:
     def __init__(self, params: SimParams | Sequence[SimParams], mode: int = MODE_PLAIN, force_rebuild: bool = False,
                  use_graphs: bool = True, device: int = 0, rdf_ext_bins: int = 0, rdf_ext_range: float = 0.0,
                  eam_table_knots: int = 0, stream: int = 0, phase_timing: bool = False, metal_lanes: int = 0,
-                 nebr_blocks_per_sm: int = 0):
+                 nebr_blocks_per_sm: int = 0, programmatic_launch: bool = False, nebr_descending: int = 0,
+                 nebr_item_atoms: int = 0):
         plist = [params] if isinstance(params, SimParams) else list(params)
         arr = (SimParams * len(plist))(*plist)
         opt = Options()
@@ -103,6 +104,9 @@ class Simulation:
         opt.phase_timing = int(phase_timing)
         opt.metal_lanes = metal_lanes
         opt.nebr_blocks_per_sm = nebr_blocks_per_sm
+        opt.programmatic_launch = int(programmatic_launch)
+        opt.nebr_descending = nebr_descending
+        opt.nebr_item_atoms = nebr_item_atoms
         h = C.c_void_p()
         check(lib().sg_create(arr, len(plist), C.byref(opt), C.byref(h)))
         self._h = h
@@ -265,14 +269,17 @@ class Simulation:
         check(lib().sg_autotune(self._h, steps, buf, len(buf)))
         return json.loads(buf.value.decode())
 
-    def launch_shape(self) -> tuple[int, int]:
-        """(lanes per metal atom, list-build blocks per SM) in use."""
-        a, b = C.c_int(), C.c_int()
-        check(lib().sg_get_launch_shape(self._h, C.byref(a), C.byref(b)))
-        return a.value, b.value
+    def launch_shape(self) -> tuple[int, int, int, int, int]:
+        """(lanes per metal atom, list-build blocks per SM, list-build descending order, list-build
+        home atoms per work item, programmatic dependent launch) in use."""
+        s = LaunchShape()
+        check(lib().sg_get_launch_shape(self._h, C.byref(s)))
+        return s.metal_lanes, s.nebr_blocks_per_sm, s.nebr_descending, s.nebr_item_atoms, s.programmatic_launch
 
-    def set_launch_shape(self, metal_lanes: int, nebr_blocks_per_sm: int) -> None:
-        check(lib().sg_set_launch_shape(self._h, metal_lanes, nebr_blocks_per_sm))
+    def set_launch_shape(self, metal_lanes: int, nebr_blocks_per_sm: int, nebr_descending: int = 0,
+                         nebr_item_atoms: int = 8, programmatic_launch: int = 0) -> None:
+        s = LaunchShape(metal_lanes, nebr_blocks_per_sm, nebr_descending, nebr_item_atoms, programmatic_launch)
+        check(lib().sg_set_launch_shape(self._h, C.byref(s)))
 
 
 DIFF_NPARAM = 66  # SG_DIFF_NPARAM

@@ -1,0 +1,66 @@
+"""Steps a benchmark workload under a CUDA profiler range, for kernel profilers.
+
+    python -m surfacegrowthconsole_gb300.profile_step [--workload production|batched|precision]
+        [--mode plain|mixed] [--warmup 3] [--steps 1] [--replicas 16]
+
+Builds the workload, steps it `warmup` times (graph capture, caches), then runs `steps` steps
+between cudaProfilerStart and cudaProfilerStop, so that a profiler started with its
+from-start profiling off (ncu --profile-from-start off) sees exactly those steps' kernels.
+Lists are rebuilt every step, as in the production benchmark.  Prints the kernel launches per
+step.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+
+import numpy as np
+
+from . import MODE_MIXED, MODE_PLAIN, workloads
+from .engine import Simulation
+
+
+def _cudart():
+    """The CUDA runtime libsgmd.so is linked against (already loaded with the library)."""
+    for name in ("libcudart.so.13", "libcudart.so"):
+        try:
+            return ctypes.CDLL(name)
+        except OSError:
+            continue
+    raise RuntimeError("the CUDA runtime library was not found")
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="production", choices=["production", "batched", "precision"])
+    ap.add_argument("--mode", default="plain", choices=["plain", "mixed"])
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=1)
+    ap.add_argument("--replicas", type=int, default=16)
+    a = ap.parse_args()
+    if a.workload == "production":
+        p, r, v = workloads.production(seed=2)
+        plist = [p]
+    elif a.workload == "precision":
+        p, r, v = workloads.precision(seed=3)
+        plist = [p]
+    else:
+        reps = workloads.batched(a.replicas, seed=4)
+        plist = [w[0] for w in reps]
+        r = np.concatenate([w[1] for w in reps])
+        v = np.concatenate([w[2] for w in reps])
+    n = int(sum(q.nMol for q in plist))
+    sim = Simulation(plist, mode=MODE_MIXED if a.mode == "mixed" else MODE_PLAIN, force_rebuild=True)
+    sim.set_state(r, v, np.zeros((n, 3), np.float32))
+    sim.step(a.warmup)
+    rt = _cudart()
+    rt.cudaProfilerStart()
+    sim.step(a.steps)
+    rt.cudaProfilerStop()
+    print(f"{a.workload} {a.mode}: {n} atoms, {sim.kernels_per_step()} kernel launches per step, "
+          f"{a.steps} profiled step(s)")
+    sim.close()
+
+
+if __name__ == "__main__":
+    main()

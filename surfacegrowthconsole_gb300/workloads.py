@@ -57,6 +57,24 @@ def batched(n: int = 256, seed: int = 4, steps: int = 5000):
     return out
 
 
+def bulk_metal(n: int = 10, temperature_K: float = 300.0, seed: int = 5):
+    """Bulk fcc Ni (regime 0), n x n x n unit cells (4 n^3 atoms), no thermostat: an NVE system
+    of the EAM alone, the conservative part of the model (the reference's graphene energy omits
+    the second-neighbour angle term its forces apply)."""
+    from .engine import default_input, init_coords, init_vels, set_params
+    inp = default_input()
+    inp.iRegime = 0
+    inp.iMaterial = 3
+    inp.ucx = inp.ucy = inp.ucz = n
+    inp.temperatureK = temperature_K
+    inp.deltaT = DT_1FS
+    inp.randSeed = seed
+    inp.stepEquil = 10 ** 9
+    inp.stepLimit = 10 ** 9
+    p = set_params(inp)
+    return p, init_coords(p), init_vels(p)
+
+
 def differentiation_system(seed: int = 5):
     """~20,000 atoms: 18,432 C (24 x 24 units) + 2,000 Ni in one cluster, c2 settings (700 K)."""
     return build_workload(24, 24, [2000], 700.0, seed, step_limit=1000, step_avg=100, step_equil=0,

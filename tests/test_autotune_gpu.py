@@ -1,6 +1,7 @@
-"""Launch-shape tuning: the lanes per metal atom of the density and metal force passes (4, 8,
+"""Launch-shape tuning and launch modes: the lanes per metal atom of the density and metal force passes (4, 8,
 16, 32) change only the summation order of the metal sums; the list build's blocks per SM change
-nothing (every list row is written by the one warp that owns its atom's cell); sg_autotune
+nothing, nor does the order in which it takes the cells (every list row is written by the
+one warp that owns its atom's cell); sg_autotune
 restores the context's state, so a tuned run continues exactly as an untuned one switched to
 the chosen shape at the same step."""
 import numpy as np
@@ -37,22 +38,23 @@ def test_metal_lanes_change_only_the_summation_order(lanes):
         assert err <= SUM_ORDER_RTOL, (name, err)
 
 
-def test_list_build_grid_changes_nothing():
+def test_list_build_grid_and_order_change_nothing():
     p, r, v = workloads.production(seed=2, steps=10)
-    lists = [_forces(p, r, v, nebr_blocks_per_sm=b)[3] for b in (1, 4, 16, 32)]
+    lists = [_forces(p, r, v, nebr_blocks_per_sm=b, nebr_descending=d, nebr_item_atoms=t)[3]
+             for b, d, t in ((1, 0, 16), (4, 1, 4), (16, 0, 6), (32, 1, 64))]
     for nn, nbl in lists[1:]:
         assert np.array_equal(nn, lists[0][0]) and np.array_equal(nbl, lists[0][1])
 
 
 def test_bad_shapes_are_refused():
     p, r, v = workloads.small(seed=3)
-    for kw in ({"metal_lanes": 6}, {"nebr_blocks_per_sm": 33}):
+    for kw in ({"metal_lanes": 6}, {"nebr_blocks_per_sm": 33}, {"nebr_item_atoms": 3}):
         with pytest.raises(Exception):
             Simulation(p, **kw)
     sim = Simulation(p)
     with pytest.raises(Exception):
         sim.set_launch_shape(64, 8)
-    assert sim.launch_shape() == (16, 8)
+    assert sim.launch_shape() == (16, 8, 0, 8, 0)
     sim.close()
 
 
@@ -65,8 +67,10 @@ def test_autotune_restores_the_state(mode):
     tuned.step(30)
     rep = tuned.autotune(steps=10)
     shape = tuned.launch_shape()
-    assert shape == (rep["metal_lanes"], rep["nebr_blocks_per_sm"])
-    assert shape[0] in (4, 8, 16, 32) and shape[1] in (2, 4, 8, 16)
+    assert shape == (rep["metal_lanes"], rep["nebr_blocks_per_sm"], rep["nebr_descending"],
+                     rep["nebr_item_atoms"], rep["programmatic_launch"])
+    assert shape[0] in (4, 8, 16, 32) and shape[1] in (2, 4, 8, 16) and shape[2] in (0, 1)
+    assert shape[3] in (4, 6, 8, 16)
     for k in ("4", "8", "16", "32"):
         assert rep["metal_lanes_ms_per_step"][k] > 0
     plain = Simulation(p, mode=mode)
@@ -83,3 +87,19 @@ def test_autotune_restores_the_state(mode):
     assert t1.kinEnergy64 == t2.kinEnergy64 and float(t1.potEnergy) == float(t2.potEnergy)
     tuned.close()
     plain.close()
+
+
+@pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_MIXED])
+def test_programmatic_launch_changes_nothing(mode):
+    """With programmatic dependent launch every kernel of a step still waits for its predecessor
+    before touching memory: the trajectory is bit-identical."""
+    p, r, v = workloads.production(seed=2, steps=10)
+    out = []
+    for pdl in (False, True):
+        sim = Simulation(p, mode=mode, programmatic_launch=pdl, force_rebuild=True)
+        sim.set_state(r, v, np.zeros((p.nMol, 3), np.float32))
+        sim.step(25)
+        out.append(sim.get_state())
+        sim.close()
+    for x, y in zip(*out):
+        assert np.array_equal(x, y)

@@ -6,7 +6,7 @@ import pytest
 
 import oracle
 from surfacegrowthconsole_gb300 import MODE_MIXED, MODE_PLAIN, workloads
-from surfacegrowthconsole_gb300.engine import Simulation, default_input, init_coords, init_vels, set_params
+from surfacegrowthconsole_gb300.engine import Simulation
 
 pytestmark = pytest.mark.gpu
 
@@ -35,11 +35,7 @@ def forces(p, r, v, mode):
 
 
 def bulk_ni(n=10, T=300, seed=5):
-    inp = default_input(); inp.iRegime = 0; inp.iMaterial = 3; inp.ucx = inp.ucy = inp.ucz = n
-    inp.temperatureK = T; inp.deltaT = 0.005; inp.randSeed = seed; inp.stepEquil = 10 ** 9
-    inp.stepLimit = 10 ** 9
-    p = set_params(inp)
-    return p, init_coords(p), init_vels(p)
+    return workloads.bulk_metal(n, T, seed)
 
 
 @pytest.mark.parametrize("which", ["small", "production", "bulk"])
