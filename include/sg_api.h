@@ -83,7 +83,9 @@ typedef struct sg_options {
                             * order (0: ascending) */
     int nebr_item_atoms;   /* list build: most home atoms of one work item (a warp's share); a
                             * cell of more atoms is split into near-equal items, 4..64 (0: 8) */
-    int reserved[4];
+    int nebr_atom_threads; /* list build: 0 a warp per cell (windows of candidates), 1 a thread
+                            * per atom; the same lists */
+    int reserved[3];
 } sg_options;
 
 /* Initialise *opt with the defaults (PLAIN mode, graphs on, device 0). */
@@ -173,6 +175,12 @@ int sg_num_cells(const sg_ctx *ctx, int rep);
 /* Neighbour list in the reference layout: nn[nMol], nbl[iNebrMax * nMol] column-major
  * (entry j of atom i at nbl[j*nMol + i]), local indices, unused entries -1. */
 int sg_get_nebr(sg_ctx *ctx, int rep, int *nn, int *nbl);
+/* The carbon pass's lists of each atom, local indices: ns[nMol] close-list lengths (-1: the
+ * pass walks the full list), sl[nMol * 8] close entries (within rCutC + rNebrShell, list
+ * order); nrl[nMol] relevant-list lengths (-1 as ns), rl[nMol * 48 * 2] relevant entries
+ * {atom, position in the full list} (metal entries and close entries, list order).  Entries
+ * past a length are -1.  Metal atoms have length 0. */
+int sg_get_carbon_lists(sg_ctx *ctx, int rep, int *ns, int *sl, int *nrl, int *rl);
 int sg_get_rho(sg_ctx *ctx, int rep, float *rho);          /* nMolMe values */
 int sg_get_friction(sg_ctx *ctx, int rep, float *fric);    /* nMolMe values */
 int sg_get_rdf(sg_ctx *ctx, int rep, unsigned int *hist);  /* sizeHistRdf counts */
@@ -345,9 +353,10 @@ int sg_diff_force_matching(sg_diff *d, const double *theta, const float *ref_for
 /* ---- tuning ------------------------------------------------------------------------------- */
 /* Times the launch shapes of the tunable passes on the context's own state and keeps the
  * fastest: the metal lanes per atom (4, 8, 16, 32; `steps` steps each, the context's own
- * rebuild schedule), then the list build's home atoms per work item (4, 6, 8, 16), blocks
- * per SM (2, 4, 8, 16) and cell order (ascending, descending), `steps` steps each with a
- * rebuild in every step, then programmatic dependent launch off and on.  Every device buffer and the host step counters are copied first
+ * rebuild schedule), then the list build (a thread per atom, or a warp per cell with its home
+ * atoms per work item 4, 6, 8, 16, blocks per SM 2, 4, 8, 16 and cell order ascending or
+ * descending), `steps` steps each with a rebuild in every step, then programmatic dependent
+ * launch off and on.  Every device buffer and the host step counters are copied first
  * and put back after each trial, so the context continues from the state it had; the trials
  * change no results but the summation order of the metal passes.  `report` (if not NULL)
  * receives a JSON object with the milliseconds per step of every trial and the choice.
@@ -360,7 +369,8 @@ typedef struct sg_launch_shape {
     int nebr_descending;    /* 0 or 1 */
     int nebr_item_atoms;    /* 4..64 */
     int programmatic_launch; /* 0 or 1 */
-    int reserved[3];
+    int nebr_atom_threads;  /* 0 or 1 */
+    int reserved[2];
 } sg_launch_shape;
 /* The launch shape in use (from the options, or as sg_autotune chose it). */
 int sg_get_launch_shape(sg_ctx *ctx, sg_launch_shape *shape);

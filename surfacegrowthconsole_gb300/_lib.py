@@ -90,13 +90,14 @@ class Options(C.Structure):
         ("eam_table_knots", C.c_int), ("metal_lanes", C.c_int), ("nebr_blocks_per_sm", C.c_int),
         ("phase_timing", C.c_int),
         ("programmatic_launch", C.c_int), ("nebr_descending", C.c_int), ("nebr_item_atoms", C.c_int),
-        ("reserved", C.c_int * 4),
+        ("nebr_atom_threads", C.c_int), ("reserved", C.c_int * 3),
     ]
 
 
 class LaunchShape(C.Structure):
     _fields_ = [("metal_lanes", C.c_int), ("nebr_blocks_per_sm", C.c_int), ("nebr_descending", C.c_int),
-                ("nebr_item_atoms", C.c_int), ("programmatic_launch", C.c_int), ("reserved", C.c_int * 3)]
+                ("nebr_item_atoms", C.c_int), ("programmatic_launch", C.c_int), ("nebr_atom_threads", C.c_int),
+                ("reserved", C.c_int * 2)]
 
 
 class Thermo(C.Structure):
@@ -187,6 +188,7 @@ _SIGS = {
     "sg_reset_rdf": (C.c_int, [C.c_void_p]),
     "sg_get_cells": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "sg_get_nebr": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "sg_get_carbon_lists": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "sg_get_rho": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "sg_get_friction": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "sg_get_rdf": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),

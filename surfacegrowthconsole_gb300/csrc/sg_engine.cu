@@ -274,6 +274,7 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
   setNebrBlocks(c, c->opt.nebr_blocks_per_sm ? c->opt.nebr_blocks_per_sm : 8);
   c->nebrDescending = c->opt.nebr_descending ? 1 : 0;
   c->nebrItemAtoms = c->opt.nebr_item_atoms ? c->opt.nebr_item_atoms : kItemAtoms;
+  c->nebrAlgo = c->opt.nebr_atom_threads ? 1 : 0;
   if (c->nebrItemAtoms < kMinItemAtoms || c->nebrItemAtoms > 64) {
     sg_destroy(c);
     return sg_fail(SG_ERR_INVALID, "nebr_item_atoms %d: 0 (default) or %d..64", c->opt.nebr_item_atoms,
@@ -516,9 +517,14 @@ static int enqueueRebuild(sg_ctx *c, int force) {
              c->slot, c->cellStart, c->bucket, c->bucketCap, c->pos, c->sortIdx, c->sortPos, c->nn, c->ns, c->nrl,
              fr, c->blockCount, c->nScanBlocks));
   if (c->opt.phase_timing) cudaEventRecordWithFlags(c->phaseEv[8], c->stream, cudaEventRecordExternal);
-  CK(launchK(c->pdl, k_build_nebr, c->nebrGrid, kNebrWarps * 32, 0, c->stream, c->tileTab.rep, c->activeCells,
-             c->heavyItems, c->nebrWork, c->rc, c->st, c->cellStart, c->sortPos, c->nn, c->nbl, c->ns, c->sl, c->nrl,
-             c->rl, c->rowStride, c->nebrMax, c->nebrDescending));
+  if (c->nebrAlgo == 1)
+    CK(launchK(c->pdl, k_build_nebr_atoms, c->atomTab.n, 128, 0, c->stream, c->atomTab.view(), c->rc, c->st,
+               c->cellOf, c->cellStart, c->sortPos, c->nn, c->nbl, c->ns, c->sl, c->nrl, c->rl, c->rowStride,
+               c->nebrMax, c->nebrWork, fr));
+  else
+    CK(launchK(c->pdl, k_build_nebr, c->nebrGrid, kNebrWarps * 32, 0, c->stream, c->tileTab.rep, c->activeCells,
+               c->heavyItems, c->nebrWork, c->rc, c->st, c->cellStart, c->sortPos, c->nn, c->nbl, c->ns, c->sl,
+               c->nrl, c->rl, c->rowStride, c->nebrMax, c->nebrDescending));
   return SG_OK;
 }
 
@@ -869,6 +875,35 @@ extern "C" int sg_get_cells(sg_ctx *c, int rep, int *cellOfOut, int *cellStartOu
   return SG_OK;
 }
 
+extern "C" int sg_get_carbon_lists(sg_ctx *c, int rep, int *nsOut, int *slOut, int *nrlOut, int *rlOut) {
+  if (!c || rep < 0 || rep >= c->nrep) return sg_fail(SG_ERR_INVALID, "sg_get_carbon_lists: bad arguments");
+  const RepConst &P = c->hrc[rep];
+  std::vector<int> ns(P.nMol), nrl(P.nMol);
+  std::vector<int> sl((size_t)P.nMol * kShortMax), rl((size_t)P.nMol * kRelMax * 2);
+  int rc;
+  if ((rc = readArr(c, ns.data(), c->ns + P.atomOff, P.nMol)) ||
+      (rc = readArr(c, nrl.data(), c->nrl + P.atomOff, P.nMol)) ||
+      (rc = readArr(c, sl.data(), c->sl + (size_t)P.atomOff * kShortMax, sl.size())) ||
+      (rc = readArr(c, rl.data(), reinterpret_cast<int *>(c->rl) + (size_t)P.atomOff * kRelMax * 2, rl.size())))
+    return rc;
+  for (int i = 0; i < P.nMol; i++) {
+    for (int e = 0; e < kShortMax; e++) {
+      int &x = sl[(size_t)i * kShortMax + e];
+      x = (e < ns[i]) ? x - P.atomOff : -1;
+    }
+    for (int e = 0; e < kRelMax; e++) {
+      int *x = &rl[((size_t)i * kRelMax + e) * 2];
+      if (e < nrl[i]) x[0] -= P.atomOff;
+      else x[0] = x[1] = -1;
+    }
+  }
+  if (nsOut) memcpy(nsOut, ns.data(), sizeof(int) * P.nMol);
+  if (nrlOut) memcpy(nrlOut, nrl.data(), sizeof(int) * P.nMol);
+  if (slOut) memcpy(slOut, sl.data(), sizeof(int) * sl.size());
+  if (rlOut) memcpy(rlOut, rl.data(), sizeof(int) * rl.size());
+  return SG_OK;
+}
+
 extern "C" int sg_get_nebr(sg_ctx *c, int rep, int *nnOut, int *nblOut) {
   if (!c || rep < 0 || rep >= c->nrep) return sg_fail(SG_ERR_INVALID, "sg_get_nebr: bad arguments");
   const RepConst &P = c->hrc[rep];
@@ -1053,9 +1088,10 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
   const int lanes0 = c->metalLanes, bps0 = c->nebrBlocksPerSM, desc0 = c->nebrDescending;
   const int item0 = c->nebrItemAtoms, fr0 = c->opt.force_rebuild;
   const bool pdl0 = c->pdl;
+  const int algo0 = c->nebrAlgo;
   const int laneChoice[4] = {4, 8, 16, 32}, bpsChoice[4] = {2, 4, 8, 16}, itemChoice[4] = {4, 6, 8, 16};
-  float laneMs[4] = {}, bpsMs[4] = {}, orderMs[2] = {}, itemMs[4] = {}, pdlMs[2] = {};
-  int bestLanes = lanes0, bestBps = bps0, bestDesc = desc0, bestItem = item0;
+  float laneMs[4] = {}, bpsMs[4] = {}, orderMs[2] = {}, itemMs[4] = {}, pdlMs[2] = {}, algoMs[2] = {};
+  int bestLanes = lanes0, bestBps = bps0, bestDesc = desc0, bestItem = item0, bestAlgo = algo0;
   bool bestPdl = pdl0;
   // 1. lanes per metal atom, on the context's own schedule
   if (c->metalRun.n > 0) {
@@ -1066,12 +1102,20 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
       if (!rc && (k == 0 || laneMs[k] < best)) { best = laneMs[k]; bestLanes = laneChoice[k]; }
     }
   }
-  // 2. the list build (home atoms per item, blocks per SM, cell order), with a rebuild in
-  //    every step
-  if (!rc) {
+  // 2. the list build (atom threads or cell windows; for cell windows the home atoms per item,
+  //    blocks per SM and cell order), with a rebuild in every step
+  if (!rc && !(rc = setMetalLanes(c, bestLanes))) {
     c->opt.force_rebuild = 1;
     destroyGraphs(c);
-    if (!(rc = setMetalLanes(c, bestLanes))) {
+    for (int a = 0; a < 2 && !rc; a++) {
+      if ((rc = restoreSnapshot(c, snap))) break;
+      c->nebrAlgo = a;
+      destroyGraphs(c);
+      rc = timeSteps(c, steps, &algoMs[a]);
+    }
+    if (!rc) bestAlgo = algoMs[1] < algoMs[0] ? 1 : 0;
+    c->nebrAlgo = 0;
+    if (!rc && bestAlgo == 0) {
       float best = 0.f;
       for (int k = 0; k < 4 && !rc; k++) {
         if ((rc = restoreSnapshot(c, snap))) break;
@@ -1104,6 +1148,9 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
   // 3. programmatic dependent launch, on the context's own schedule
   if (!rc) {
     c->nebrDescending = bestDesc;
+    c->nebrItemAtoms = bestItem;
+    c->nebrAlgo = bestAlgo;
+    setNebrBlocks(c, bestBps);
     for (int k = 0; k < 2 && !rc; k++) {
       if ((rc = restoreSnapshot(c, snap))) break;
       c->pdl = k == 1;
@@ -1121,6 +1168,7 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
     c->nebrDescending = desc0;
     c->nebrItemAtoms = item0;
     c->pdl = pdl0;
+    c->nebrAlgo = algo0;
     destroyGraphs(c);
     return rc;
   }
@@ -1130,6 +1178,7 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
   c->nebrDescending = bestDesc;
   c->nebrItemAtoms = bestItem;
   c->pdl = bestPdl;
+  c->nebrAlgo = bestAlgo;
   destroyGraphs(c);
   if (report && report_len > 0) {
     snprintf(report, report_len,
@@ -1138,12 +1187,14 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
              "\"8\": %.6g, \"16\": %.6g}, \"nebr_order_ms_per_step_rebuilding\": {\"ascending\": %.6g, "
              "\"descending\": %.6g}, \"nebr_item_atoms_ms_per_step_rebuilding\": {\"4\": %.6g, "
              "\"6\": %.6g, \"8\": %.6g, \"16\": %.6g}, \"programmatic_launch_ms_per_step\": {\"0\": %.6g, "
-             "\"1\": %.6g}, \"metal_lanes\": %d, \"nebr_blocks_per_sm\": %d, \"nebr_descending\": %d, "
-             "\"nebr_item_atoms\": %d, \"programmatic_launch\": %d, \"nebr_grid\": %d}",
+             "\"1\": %.6g}, \"nebr_atom_threads_ms_per_step_rebuilding\": {\"0\": %.6g, \"1\": %.6g}, "
+             "\"metal_lanes\": %d, \"nebr_blocks_per_sm\": %d, \"nebr_descending\": %d, "
+             "\"nebr_item_atoms\": %d, \"programmatic_launch\": %d, \"nebr_atom_threads\": %d, "
+             "\"nebr_grid\": %d}",
              steps, laneMs[0], laneMs[1], laneMs[2], laneMs[3], bpsMs[0], bpsMs[1], bpsMs[2], bpsMs[3],
              orderMs[0], orderMs[1], itemMs[0], itemMs[1], itemMs[2], itemMs[3], pdlMs[0], pdlMs[1],
-             c->metalLanes, c->nebrBlocksPerSM, c->nebrDescending, c->nebrItemAtoms, c->pdl ? 1 : 0,
-             c->nebrGrid);
+             algoMs[0], algoMs[1], c->metalLanes, c->nebrBlocksPerSM, c->nebrDescending, c->nebrItemAtoms,
+             c->pdl ? 1 : 0, c->nebrAlgo, c->nebrGrid);
   }
   return SG_OK;
 }
@@ -1158,13 +1209,16 @@ extern "C" int sg_set_launch_shape(sg_ctx *c, const sg_launch_shape *shape) {
     return sg_fail(SG_ERR_INVALID, "nebr_item_atoms %d: %d..64", shape->nebr_item_atoms, kMinItemAtoms);
   if (shape->programmatic_launch != 0 && shape->programmatic_launch != 1)
     return sg_fail(SG_ERR_INVALID, "programmatic_launch %d: 0 or 1", shape->programmatic_launch);
+  if (shape->nebr_atom_threads != 0 && shape->nebr_atom_threads != 1)
+    return sg_fail(SG_ERR_INVALID, "nebr_atom_threads %d: 0 or 1", shape->nebr_atom_threads);
   CK(cudaStreamSynchronize(c->stream));
   const int rc = setMetalLanes(c, shape->metal_lanes);
   if (rc) return rc;
   setNebrBlocks(c, shape->nebr_blocks_per_sm);
   if (shape->nebr_descending != c->nebrDescending || shape->nebr_item_atoms != c->nebrItemAtoms ||
-      (shape->programmatic_launch != 0) != c->pdl)
+      (shape->programmatic_launch != 0) != c->pdl || shape->nebr_atom_threads != c->nebrAlgo)
     destroyGraphs(c);
+  c->nebrAlgo = shape->nebr_atom_threads;
   c->nebrDescending = shape->nebr_descending;
   c->nebrItemAtoms = shape->nebr_item_atoms;
   c->pdl = shape->programmatic_launch != 0;
@@ -1179,5 +1233,6 @@ extern "C" int sg_get_launch_shape(sg_ctx *c, sg_launch_shape *shape) {
   shape->nebr_descending = c->nebrDescending;
   shape->nebr_item_atoms = c->nebrItemAtoms;
   shape->programmatic_launch = c->pdl ? 1 : 0;
+  shape->nebr_atom_threads = c->nebrAlgo;
   return SG_OK;
 }

@@ -61,6 +61,7 @@ struct sg_ctx {
   DevTab metalLaneTab[4];
   DevTab metalRun;
   int numSMs = 0, nebrBlocksPerSM = 8, nebrDescending = 0, nebrItemAtoms = sg::kItemAtoms;
+  int nebrAlgo = 0;  // list build: 0 cell windows (k_build_nebr), 1 atom threads (k_build_nebr_atoms)
   bool pdl = false;  // programmatic dependent launch between the kernels of a step
   std::vector<std::pair<void *, size_t>> regions;  // every device buffer with its size
   int anyMetal = 0, anyCarbon = 0, maxHist = 0;

@@ -13,6 +13,10 @@ __global__ void k_cell_count(BlockTab tab, const RepConst *rc, const float4 *pos
                              int *slot, int *cellCount);
 __global__ void k_cell_bucket(BlockTab tab, const RepConst *rc, const float4 *pos, int *cellOf, int *slot,
                               int *cellCount, int *bucket, int cap, int *blockCount);
+__global__ void k_build_nebr_atoms(BlockTab tab, const RepConst *rc, RepState *st, const int *cellOf,
+                                   const int *cellStart, const float4 *sortPos, int *nn, int *nbl, int *ns,
+                                   int *sl, int *nrl, int2 *rl, int rowStride, int nebrMax, int *work,
+                                   int forceRebuild);
 // one block of kScanThreads threads per kScanCells cells
 __global__ void k_scan_cells(const int *tileRep, const int *tileStart, const int *tileFirst, const RepConst *rc,
                              RepState *st, int *cellCount, int *cellStart, int cap, int forceRebuild, int *active,

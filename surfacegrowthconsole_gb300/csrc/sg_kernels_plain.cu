@@ -776,6 +776,92 @@ __global__ void __launch_bounds__(kNebrWarps * 32) k_build_nebr(const int *__res
 namespace sg {
 
 // ============================================================================================
+// Neighbour list, atom-centric (the same lists as k_build_nebr).  One thread per atom, threads
+// in the cell-sorted order, so that the lanes of a warp mostly share their home cell and read
+// the same candidates.  Each thread walks the 27 stencil cells in the reference's order and
+// each cell in ascending atom index, which is the reference's list order itself, and appends
+// every hit to the atom's full list and, for a carbon atom, to its close list and relevant
+// list, with the same arithmetic and limits as k_build_nebr.  The counters of the cell-window
+// build are not used and are cleared here.
+// ============================================================================================
+__global__ void __launch_bounds__(128) k_build_nebr_atoms(BlockTab tab, const RepConst *__restrict__ rc,
+                                                          RepState *st, const int *__restrict__ cellOf,
+                                                          const int *__restrict__ cellStart,
+                                                          const float4 *__restrict__ sortPos,
+                                                          int *__restrict__ nn, int *__restrict__ nbl,
+                                                          int *__restrict__ ns, int *__restrict__ sl,
+                                                          int *__restrict__ nrl, int2 *__restrict__ rl,
+                                                          int rowStride, int nebrMax, int *__restrict__ work,
+                                                          int forceRebuild) {
+  pdlEnter();
+  if (blockIdx.x == 0 && threadIdx.x < 3) work[threadIdx.x] = 0;
+  const int rep = tab.rep[blockIdx.x];
+  RepState *S = st + rep;
+  if (!rebuilding(S, forceRebuild)) return;
+  const RepConst &P = rc[rep];
+  const int s = tab.start[blockIdx.x] + threadIdx.x;  // sorted position
+  const int sortedEnd = cellStart[P.cellOff + P.ncells];  // atoms outside the grid are not sorted
+  const bool valid = s < sortedEnd;
+  int n = 0;
+  if (valid) {
+    const float4 A = sortPos[s];
+    const int g = __float_as_int(A.w);
+    const int c = cellOf[g];
+    const int metalEnd = P.atomOff + P.nMolMe;
+    const bool carbon = g >= metalEnd;
+    const float rrNebr = P.rrNebr, rrShort = P.rrShort;
+    int *row = nbl + (size_t)g * rowStride;
+    int *srow = sl + (size_t)g * kShortMax;
+    int2 *rrow = rl + (size_t)g * kRelMax;
+    int m = 0, r = 0;
+    for (int o = 0; o < 27; o++) {
+      float sx, sy, sz;
+      const int C = P.cellOff + stencilCell(P, c, o, sx, sy, sz);
+      const int qb = cellStart[C], qe = cellStart[C + 1];
+      for (int q = qb; q < qe; q++) {
+        const float4 B = sortPos[q];
+        const int k = __float_as_int(B.w);
+        // the reference subtracts the cell shift after the difference: both roundings kept
+        float dx = A.x - B.x, dy = A.y - B.y, dz = A.z - B.z;
+        dx = dx - sx; dy = dy - sy; dz = dz - sz;
+        const float rr = dx * dx + dy * dy + dz * dz;
+        if (rr < rrNebr && k != g) {
+          if (n < nebrMax) row[n] = k;
+          if (carbon) {
+            const bool close = rr < rrShort;
+            if (close) {
+              if (m < kShortMax) srow[m] = k;
+              m++;
+            }
+            if (close || k < metalEnd) {
+              if (r < kRelMax) rrow[r] = make_int2(k, n);
+              r++;
+            }
+          }
+          n++;
+        }
+      }
+    }
+    nn[g] = min(n, nebrMax);
+    // -1: the carbon pass walks the full list instead
+    ns[g] = carbon ? ((m > kShortMax || n > nebrMax) ? -1 : m) : 0;
+    nrl[g] = carbon ? ((r > kRelMax || n > nebrMax) ? -1 : r) : 0;
+  }
+  int want = n, over = (n > nebrMax) ? 1 : 0;
+  for (int off = 16; off > 0; off >>= 1) {
+    want = max(want, __shfl_xor_sync(0xffffffffu, want, off));
+    over += __shfl_xor_sync(0xffffffffu, over, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (want > 0) atomicMax(&S->maxNeighbours, want);
+    if (over > 0) {
+      atomicAdd(&S->nebrOverflow, over);
+      setFlag(S, 5 /*SG_ERR_NEBR_OVERFLOW*/);
+    }
+  }
+}
+
+// ============================================================================================
 // Reductions in the reference's tree order (cu:1101-1892): a block of 512 threads reduces the
 // 1024 elements [1024 b, 1024 b + 1024) with the stride-halving tree, the last block of the
 // replica reduces the block partials in a zero-padded 1024-slot tree.

@@ -88,7 +88,7 @@ class Simulation:
                  use_graphs: bool = True, device: int = 0, rdf_ext_bins: int = 0, rdf_ext_range: float = 0.0,
                  eam_table_knots: int = 0, stream: int = 0, phase_timing: bool = False, metal_lanes: int = 0,
                  nebr_blocks_per_sm: int = 0, programmatic_launch: bool = False, nebr_descending: int = 0,
-                 nebr_item_atoms: int = 0):
+                 nebr_item_atoms: int = 0, nebr_atom_threads: int = 0):
         plist = [params] if isinstance(params, SimParams) else list(params)
         arr = (SimParams * len(plist))(*plist)
         opt = Options()
@@ -107,6 +107,7 @@ class Simulation:
         opt.programmatic_launch = int(programmatic_launch)
         opt.nebr_descending = nebr_descending
         opt.nebr_item_atoms = nebr_item_atoms
+        opt.nebr_atom_threads = nebr_atom_threads
         h = C.c_void_p()
         check(lib().sg_create(arr, len(plist), C.byref(opt), C.byref(h)))
         self._h = h
@@ -219,6 +220,15 @@ class Simulation:
         check(lib().sg_get_nebr(self._h, rep, _ptr(nn), _ptr(nbl)))
         return nn, nbl
 
+    def short_lists(self, rep: int = 0):
+        """The carbon pass's lists: (ns, sl[nMol, 8], nrl, rl[nMol, 48, 2]), local indices."""
+        n = self.params0[rep].nMol
+        ns, nrl = np.zeros(n, np.int32), np.zeros(n, np.int32)
+        sl = np.zeros((n, 8), np.int32)
+        rl = np.zeros((n, 48, 2), np.int32)
+        check(lib().sg_get_carbon_lists(self._h, rep, _ptr(ns), _ptr(sl), _ptr(nrl), _ptr(rl)))
+        return ns, sl, nrl, rl
+
     def rho(self, rep: int = 0) -> np.ndarray:
         out = np.zeros(self.params0[rep].nMolMe, np.float32)
         check(lib().sg_get_rho(self._h, rep, _ptr(out)))
@@ -269,16 +279,21 @@ class Simulation:
         check(lib().sg_autotune(self._h, steps, buf, len(buf)))
         return json.loads(buf.value.decode())
 
-    def launch_shape(self) -> tuple[int, int, int, int, int]:
-        """(lanes per metal atom, list-build blocks per SM, list-build descending order, list-build
-        home atoms per work item, programmatic dependent launch) in use."""
+    SHAPE_FIELDS = ("metal_lanes", "nebr_blocks_per_sm", "nebr_descending", "nebr_item_atoms",
+                    "programmatic_launch", "nebr_atom_threads")
+
+    def launch_shape(self) -> dict:
+        """The launch shape in use: the fields of sg_launch_shape."""
         s = LaunchShape()
         check(lib().sg_get_launch_shape(self._h, C.byref(s)))
-        return s.metal_lanes, s.nebr_blocks_per_sm, s.nebr_descending, s.nebr_item_atoms, s.programmatic_launch
+        return {f: getattr(s, f) for f in self.SHAPE_FIELDS}
 
-    def set_launch_shape(self, metal_lanes: int, nebr_blocks_per_sm: int, nebr_descending: int = 0,
-                         nebr_item_atoms: int = 8, programmatic_launch: int = 0) -> None:
-        s = LaunchShape(metal_lanes, nebr_blocks_per_sm, nebr_descending, nebr_item_atoms, programmatic_launch)
+    def set_launch_shape(self, shape: dict) -> None:
+        """Applies a launch shape (a dict as launch_shape() returns; missing fields keep their
+        current values)."""
+        cur = self.launch_shape()
+        cur.update(shape)
+        s = LaunchShape(*[cur[f] for f in self.SHAPE_FIELDS])
         check(lib().sg_set_launch_shape(self._h, C.byref(s)))
 
 

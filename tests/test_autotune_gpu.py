@@ -1,7 +1,6 @@
 """Launch-shape tuning and launch modes: the lanes per metal atom of the density and metal force passes (4, 8,
-16, 32) change only the summation order of the metal sums; the list build's blocks per SM change
-nothing, nor does the order in which it takes the cells (every list row is written by the
-one warp that owns its atom's cell); sg_autotune
+16, 32) change only the summation order of the metal sums; the list build's algorithm (a warp per cell
+or a thread per atom), blocks per SM, item size and cell order change nothing; sg_autotune
 restores the context's state, so a tuned run continues exactly as an untuned one switched to
 the chosen shape at the same step."""
 import numpy as np
@@ -38,12 +37,28 @@ def test_metal_lanes_change_only_the_summation_order(lanes):
         assert err <= SUM_ORDER_RTOL, (name, err)
 
 
-def test_list_build_grid_and_order_change_nothing():
-    p, r, v = workloads.production(seed=2, steps=10)
-    lists = [_forces(p, r, v, nebr_blocks_per_sm=b, nebr_descending=d, nebr_item_atoms=t)[3]
-             for b, d, t in ((1, 0, 16), (4, 1, 4), (16, 0, 6), (32, 1, 64))]
-    for nn, nbl in lists[1:]:
-        assert np.array_equal(nn, lists[0][0]) and np.array_equal(nbl, lists[0][1])
+def _lists(p, r, v, **shape):
+    sim = Simulation(p, **shape)
+    sim.set_state(r, v, np.zeros((p.nMol, 3), np.float32))
+    sim.build_lists()
+    out = (*sim.nebr(), *sim.short_lists())
+    sim.close()
+    return out
+
+
+@pytest.mark.parametrize("which", ["small", "production", "bulk"])
+def test_list_builds_and_shapes_change_nothing(which):
+    """Both list builds (cell windows in any grid, order and item size; atom threads) give the
+    same full, close and relevant lists."""
+    p, r, v = {"small": lambda: workloads.small(seed=3), "production": lambda: workloads.production(seed=2, steps=10),
+               "bulk": lambda: workloads.bulk_metal(8, 600.0, 7)}[which]()
+    ref = _lists(p, r, v)
+    for kw in ({"nebr_atom_threads": 1}, {"nebr_blocks_per_sm": 1, "nebr_item_atoms": 16},
+               {"nebr_blocks_per_sm": 4, "nebr_descending": 1, "nebr_item_atoms": 4},
+               {"nebr_blocks_per_sm": 32, "nebr_descending": 1, "nebr_item_atoms": 64}):
+        got = _lists(p, r, v, **kw)
+        for a, b in zip(got, ref):
+            assert np.array_equal(a, b), kw
 
 
 def test_bad_shapes_are_refused():
@@ -53,8 +68,9 @@ def test_bad_shapes_are_refused():
             Simulation(p, **kw)
     sim = Simulation(p)
     with pytest.raises(Exception):
-        sim.set_launch_shape(64, 8)
-    assert sim.launch_shape() == (16, 8, 0, 8, 0)
+        sim.set_launch_shape({"metal_lanes": 64})
+    assert sim.launch_shape() == {"metal_lanes": 16, "nebr_blocks_per_sm": 8, "nebr_descending": 0,
+                                  "nebr_item_atoms": 8, "programmatic_launch": 0, "nebr_atom_threads": 0}
     sim.close()
 
 
@@ -67,10 +83,9 @@ def test_autotune_restores_the_state(mode):
     tuned.step(30)
     rep = tuned.autotune(steps=10)
     shape = tuned.launch_shape()
-    assert shape == (rep["metal_lanes"], rep["nebr_blocks_per_sm"], rep["nebr_descending"],
-                     rep["nebr_item_atoms"], rep["programmatic_launch"])
-    assert shape[0] in (4, 8, 16, 32) and shape[1] in (2, 4, 8, 16) and shape[2] in (0, 1)
-    assert shape[3] in (4, 6, 8, 16)
+    assert shape == {f: rep[f] for f in Simulation.SHAPE_FIELDS}
+    assert shape["metal_lanes"] in (4, 8, 16, 32) and shape["nebr_blocks_per_sm"] in (2, 4, 8, 16)
+    assert shape["nebr_item_atoms"] in (4, 6, 8, 16) and shape["nebr_atom_threads"] in (0, 1)
     for k in ("4", "8", "16", "32"):
         assert rep["metal_lanes_ms_per_step"][k] > 0
     plain = Simulation(p, mode=mode)
@@ -78,7 +93,7 @@ def test_autotune_restores_the_state(mode):
     plain.step(30)
     for x, y in zip(tuned.get_state(), plain.get_state()):
         assert np.array_equal(x, y), "state after sg_autotune"
-    plain.set_launch_shape(*shape)
+    plain.set_launch_shape(shape)
     tuned.step(40)
     plain.step(40)
     for x, y in zip(tuned.get_state(), plain.get_state()):
