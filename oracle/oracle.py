@@ -32,6 +32,7 @@ def lib():
             "orc_set_state": (None, [V, V, V, V]),
             "orc_get_state": (None, [V, V, V, V]),
             "orc_get_state64": (None, [V, V, V, V]),
+            "orc_metal_cm64": (None, [V, V]),
             "orc_set_state64": (None, [V, V, V, V]),
             "orc_step": (C.c_int, [V, C.c_int]),
             "orc_get_thermo": (None, [V, C.POINTER(Thermo)]),
@@ -98,6 +99,12 @@ class OracleSim:
         a = np.zeros((self.n, 3))
         lib().orc_get_state64(self._h, _p(r), _p(v), _p(a))
         return r, v, a
+
+    def metal_cm64(self):
+        """Mean metal position in FP64."""
+        out = np.zeros(3)
+        lib().orc_metal_cm64(self._h, _p(out))
+        return out
 
     def step(self, n: int = 1):
         lib().orc_step(self._h, n)

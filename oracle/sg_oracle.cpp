@@ -876,6 +876,14 @@ template <class R> void getState64(Sim<R> &s, double *r4, double *v3, double *a3
     if (a3) { a3[3 * i] = s.a[i].x; a3[3 * i + 1] = s.a[i].y; a3[3 * i + 2] = s.a[i].z; }
   }
 }
+// Mean position of the metal atoms in FP64 (wrapped positions, as the reference's
+// centerOfMass; SurfaceGrowth.cu:1706-1760 sums them in its reduction tree).
+template <class R> void metalCm64(const Sim<R> &s, double *cm) {
+  double x = 0, y = 0, z = 0;
+  for (int i = 0; i < s.P.nMolMe; i++) { x += s.r[i].x; y += s.r[i].y; z += s.r[i].z; }
+  const double inv = s.P.nMolMe ? 1.0 / s.P.nMolMe : 0.0;
+  cm[0] = x * inv; cm[1] = y * inv; cm[2] = z * inv;
+}
 template <class R> void setState64(Sim<R> &s, const double *r4, const double *v3, const double *a3) {
   for (int i = 0; i < s.nMol; i++) {
     if (r4) s.r[i] = V4<R>{(R)r4[4 * i], (R)r4[4 * i + 1], (R)r4[4 * i + 2], (R)r4[4 * i + 3]};
@@ -1008,6 +1016,10 @@ void orc_get_state(orc_sim *s, sg_float4 *r, sg_float3 *v, sg_float3 *a) {
 void orc_get_state64(orc_sim *s, double *r4, double *v3, double *a3) {
   if (s->h.prec == 32) getState64(*s->h.f, r4, v3, a3);
   else getState64(*s->h.d, r4, v3, a3);
+}
+void orc_metal_cm64(orc_sim *s, double *cm) {
+  if (s->h.prec == 32) metalCm64(*s->h.f, cm);
+  else metalCm64(*s->h.d, cm);
 }
 void orc_set_state64(orc_sim *s, const double *r4, const double *v3, const double *a3) {
   if (s->h.prec == 32) setState64(*s->h.f, r4, v3, a3);
