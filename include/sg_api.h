@@ -85,7 +85,9 @@ typedef struct sg_options {
                             * cell of more atoms is split into near-equal items, 4..64 (0: 8) */
     int nebr_atom_threads; /* list build: 0 a warp per cell (windows of candidates), 1 a thread
                             * per atom; the same lists */
-    int reserved[3];
+    int eam_table_smem;    /* MIXED: 1 the metal passes stage the EAM table in shared memory
+                            * (a grid of 4 blocks per SM), 0 read it through L1 */
+    int reserved[2];
 } sg_options;
 
 /* Initialise *opt with the defaults (PLAIN mode, graphs on, device 0). */
@@ -356,7 +358,7 @@ int sg_diff_force_matching(sg_diff *d, const double *theta, const float *ref_for
  * rebuild schedule), then the list build (a thread per atom, or a warp per cell with its home
  * atoms per work item 4, 6, 8, 16, blocks per SM 2, 4, 8, 16 and cell order ascending or
  * descending), `steps` steps each with a rebuild in every step, then programmatic dependent
- * launch off and on.  Every device buffer and the host step counters are copied first
+ * launch off and on, and (MIXED) the EAM table read through L1 or staged in shared memory.  Every device buffer and the host step counters are copied first
  * and put back after each trial, so the context continues from the state it had; the trials
  * change no results but the summation order of the metal passes.  `report` (if not NULL)
  * receives a JSON object with the milliseconds per step of every trial and the choice.
@@ -370,7 +372,8 @@ typedef struct sg_launch_shape {
     int nebr_item_atoms;    /* 4..64 */
     int programmatic_launch; /* 0 or 1 */
     int nebr_atom_threads;  /* 0 or 1 */
-    int reserved[2];
+    int eam_table_smem;     /* 0 or 1 (MIXED) */
+    int reserved[1];
 } sg_launch_shape;
 /* The launch shape in use (from the options, or as sg_autotune chose it). */
 int sg_get_launch_shape(sg_ctx *ctx, sg_launch_shape *shape);

@@ -275,6 +275,7 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
   c->nebrDescending = c->opt.nebr_descending ? 1 : 0;
   c->nebrItemAtoms = c->opt.nebr_item_atoms ? c->opt.nebr_item_atoms : kItemAtoms;
   c->nebrAlgo = c->opt.nebr_atom_threads ? 1 : 0;
+  c->eamStaged = c->opt.mode == SG_MODE_MIXED && c->opt.eam_table_smem != 0;  // sg_mixed_init may clear it
   if (c->nebrItemAtoms < kMinItemAtoms || c->nebrItemAtoms > 64) {
     sg_destroy(c);
     return sg_fail(SG_ERR_INVALID, "nebr_item_atoms %d: 0 (default) or %d..64", c->opt.nebr_item_atoms,
@@ -537,7 +538,7 @@ static int enqueueForces(sg_ctx *c, bool withCmVel) {
   if (fork) {
     CK(cudaEventRecord(c->evFork, c->stream));
     CK(cudaStreamWaitEvent(c->side, c->evFork, 0));
-    launchMetalChain(c->pdl, c->metalLanes, c->metalRun.n, c->side, c->metalRun.view(), c->rc, c->pos, c->acc, c->nn,
+    launchMetalChain(c->pdl, c->metalLanes, c->metalRun.n, 0, 0, c->side, c->metalRun.view(), c->rc, c->pos, c->acc, c->nn,
                      c->nbl, c->rho, c->dF, c->Fv, c->fric, c->rowStride);
     if (withCmVel && c->cmvTab.n)
       CK(launchK(c->pdl, k_cmvel, c->cmvTab.n, kRedThreads, 0, c->side, c->cmvTab.view(), c->rc, c->st, c->vel, c->acc,
@@ -1089,8 +1090,11 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
   const int item0 = c->nebrItemAtoms, fr0 = c->opt.force_rebuild;
   const bool pdl0 = c->pdl;
   const int algo0 = c->nebrAlgo;
+  const bool staged0 = c->eamStaged;
   const int laneChoice[4] = {4, 8, 16, 32}, bpsChoice[4] = {2, 4, 8, 16}, itemChoice[4] = {4, 6, 8, 16};
   float laneMs[4] = {}, bpsMs[4] = {}, orderMs[2] = {}, itemMs[4] = {}, pdlMs[2] = {}, algoMs[2] = {};
+  float stagedMs[2] = {};
+  bool bestStaged = staged0;
   int bestLanes = lanes0, bestBps = bps0, bestDesc = desc0, bestItem = item0, bestAlgo = algo0;
   bool bestPdl = pdl0;
   // 1. lanes per metal atom, on the context's own schedule
@@ -1159,6 +1163,17 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
     }
     if (!rc) bestPdl = pdlMs[1] < pdlMs[0];
   }
+  // 4. (MIXED) the EAM table through L1 or staged in shared memory
+  if (!rc && c->opt.mode == SG_MODE_MIXED && sg_mixed_staging_ok(c) && c->metalRun.n > 0) {
+    c->pdl = bestPdl;
+    for (int k = 0; k < 2 && !rc; k++) {
+      if ((rc = restoreSnapshot(c, snap))) break;
+      c->eamStaged = k == 1;
+      destroyGraphs(c);
+      rc = timeSteps(c, steps, &stagedMs[k]);
+    }
+    if (!rc) bestStaged = stagedMs[1] < stagedMs[0];
+  }
   // the state as it was, with the chosen shape (the starting shape if a trial failed)
   const int rc2 = restoreSnapshot(c, snap);
   if (snap.dev) cudaFree(snap.dev);
@@ -1169,6 +1184,7 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
     c->nebrItemAtoms = item0;
     c->pdl = pdl0;
     c->nebrAlgo = algo0;
+    c->eamStaged = staged0;
     destroyGraphs(c);
     return rc;
   }
@@ -1179,6 +1195,7 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
   c->nebrItemAtoms = bestItem;
   c->pdl = bestPdl;
   c->nebrAlgo = bestAlgo;
+  c->eamStaged = bestStaged;
   destroyGraphs(c);
   if (report && report_len > 0) {
     snprintf(report, report_len,
@@ -1188,13 +1205,14 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
              "\"descending\": %.6g}, \"nebr_item_atoms_ms_per_step_rebuilding\": {\"4\": %.6g, "
              "\"6\": %.6g, \"8\": %.6g, \"16\": %.6g}, \"programmatic_launch_ms_per_step\": {\"0\": %.6g, "
              "\"1\": %.6g}, \"nebr_atom_threads_ms_per_step_rebuilding\": {\"0\": %.6g, \"1\": %.6g}, "
+             "\"eam_table_smem_ms_per_step\": {\"0\": %.6g, \"1\": %.6g}, "
              "\"metal_lanes\": %d, \"nebr_blocks_per_sm\": %d, \"nebr_descending\": %d, "
              "\"nebr_item_atoms\": %d, \"programmatic_launch\": %d, \"nebr_atom_threads\": %d, "
-             "\"nebr_grid\": %d}",
+             "\"eam_table_smem\": %d, \"nebr_grid\": %d}",
              steps, laneMs[0], laneMs[1], laneMs[2], laneMs[3], bpsMs[0], bpsMs[1], bpsMs[2], bpsMs[3],
              orderMs[0], orderMs[1], itemMs[0], itemMs[1], itemMs[2], itemMs[3], pdlMs[0], pdlMs[1],
-             algoMs[0], algoMs[1], c->metalLanes, c->nebrBlocksPerSM, c->nebrDescending, c->nebrItemAtoms,
-             c->pdl ? 1 : 0, c->nebrAlgo, c->nebrGrid);
+             algoMs[0], algoMs[1], stagedMs[0], stagedMs[1], c->metalLanes, c->nebrBlocksPerSM,
+             c->nebrDescending, c->nebrItemAtoms, c->pdl ? 1 : 0, c->nebrAlgo, c->eamStaged ? 1 : 0, c->nebrGrid);
   }
   return SG_OK;
 }
@@ -1211,6 +1229,10 @@ extern "C" int sg_set_launch_shape(sg_ctx *c, const sg_launch_shape *shape) {
     return sg_fail(SG_ERR_INVALID, "programmatic_launch %d: 0 or 1", shape->programmatic_launch);
   if (shape->nebr_atom_threads != 0 && shape->nebr_atom_threads != 1)
     return sg_fail(SG_ERR_INVALID, "nebr_atom_threads %d: 0 or 1", shape->nebr_atom_threads);
+  if (shape->eam_table_smem != 0 && shape->eam_table_smem != 1)
+    return sg_fail(SG_ERR_INVALID, "eam_table_smem %d: 0 or 1", shape->eam_table_smem);
+  if (shape->eam_table_smem && !(c->opt.mode == SG_MODE_MIXED && sg_mixed_staging_ok(c)))
+    return sg_fail(SG_ERR_UNSUPPORTED, "eam_table_smem: MIXED mode with tabulated EAM only");
   CK(cudaStreamSynchronize(c->stream));
   const int rc = setMetalLanes(c, shape->metal_lanes);
   if (rc) return rc;
@@ -1219,6 +1241,8 @@ extern "C" int sg_set_launch_shape(sg_ctx *c, const sg_launch_shape *shape) {
       (shape->programmatic_launch != 0) != c->pdl || shape->nebr_atom_threads != c->nebrAlgo)
     destroyGraphs(c);
   c->nebrAlgo = shape->nebr_atom_threads;
+  if ((shape->eam_table_smem != 0) != c->eamStaged) destroyGraphs(c);
+  c->eamStaged = shape->eam_table_smem != 0;
   c->nebrDescending = shape->nebr_descending;
   c->nebrItemAtoms = shape->nebr_item_atoms;
   c->pdl = shape->programmatic_launch != 0;
@@ -1234,5 +1258,6 @@ extern "C" int sg_get_launch_shape(sg_ctx *c, sg_launch_shape *shape) {
   shape->nebr_item_atoms = c->nebrItemAtoms;
   shape->programmatic_launch = c->pdl ? 1 : 0;
   shape->nebr_atom_threads = c->nebrAlgo;
+  shape->eam_table_smem = c->eamStaged ? 1 : 0;
   return SG_OK;
 }

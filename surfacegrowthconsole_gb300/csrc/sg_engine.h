@@ -62,6 +62,7 @@ struct sg_ctx {
   DevTab metalRun;
   int numSMs = 0, nebrBlocksPerSM = 8, nebrDescending = 0, nebrItemAtoms = sg::kItemAtoms;
   int nebrAlgo = 0;  // list build: 0 cell windows (k_build_nebr), 1 atom threads (k_build_nebr_atoms)
+  bool eamStaged = false;  // MIXED: metal passes with the EAM table staged in shared memory
   bool pdl = false;  // programmatic dependent launch between the kernels of a step
   std::vector<std::pair<void *, size_t>> regions;  // every device buffer with its size
   int anyMetal = 0, anyCarbon = 0, maxHist = 0;
@@ -98,3 +99,4 @@ int sg_mixed_enqueue_forces(sg_ctx *c);
 // registers a buffer the library allocated outside devAlloc (autotuner snapshots)
 void sg_register_region(sg_ctx *c, void *p, size_t bytes);
 int sg_mixed_enqueue_reduce(sg_ctx *c, int forceRebuild);
+bool sg_mixed_staging_ok(sg_ctx *c);

@@ -11,15 +11,20 @@
 #endif
 
 // SG_EAM_TABLE (MIXED): the EAM pair functions come from cubic Hermite tables instead of the
-// analytic forms; the table buffer is one more kernel parameter.
+// analytic forms; the table buffer is one more kernel parameter, and the force bodies take the
+// start of the replica's table (in global memory, or staged in shared memory).
 #ifdef SG_EAM_TABLE
 #define SG_EAM_PARAM , const float4 *__restrict__ eamTab
 #define SG_EAM_ARG , eamTab
-#define SG_EAM_PAIR(P, r) eamPairTab(P, eamTab, r)
-#define SG_EAM_DENS(P, r) eamDensTab(P, eamTab, r)
+#define SG_EAM_BODY_PARAM , const float4 *tabBase
+#define SG_EAM_BASE(P) , eamTab + 2 * (P).tabOff
+#define SG_EAM_PAIR(P, r) eamPairTab(P, tabBase, r)
+#define SG_EAM_DENS(P, r) eamDensTab(P, tabBase, r)
 #else
 #define SG_EAM_PARAM
 #define SG_EAM_ARG
+#define SG_EAM_BODY_PARAM
+#define SG_EAM_BASE(P)
 #define SG_EAM_PAIR(P, r) eamPair(P, r)
 #define SG_EAM_DENS(P, r) eamDensity(P, r)
 #endif
@@ -103,11 +108,12 @@ __device__ __forceinline__ bool tabLocate(const RepConst &P, float r, int &k, fl
   sd = r - (P.rTabMin + (float)k * P.rTabH);
   return true;
 }
+// tab: the replica's table (interval k at tab[2k], tab[2k + 1]), in global or shared memory.
 __device__ __forceinline__ EamPair eamPairTab(const RepConst &P, const float4 *tab, float r) {
   int k;
   float x;
   if (!tabLocate(P, r, k, x)) return eamPair(P, r);
-  const float4 cp = __ldg(tab + 2 * (P.tabOff + k)), cf = __ldg(tab + 2 * (P.tabOff + k) + 1);
+  const float4 cp = tab[2 * k], cf = tab[2 * k + 1];
   EamPair e;
   e.phi = cp.x + x * (cp.y + x * (cp.z + x * cp.w));
   e.dphi = cp.y + x * (2.f * cp.z + 3.f * x * cp.w);
@@ -118,7 +124,7 @@ __device__ __forceinline__ float eamDensTab(const RepConst &P, const float4 *tab
   int k;
   float x;
   if (!tabLocate(P, r, k, x)) return eamDensity(P, r);
-  const float4 cf = __ldg(tab + 2 * (P.tabOff + k) + 1);
+  const float4 cf = tab[2 * k + 1];
   return cf.x + x * (cf.y + x * (cf.z + x * cf.w));
 }
 #endif
@@ -131,18 +137,16 @@ template <int MT> __device__ __forceinline__ unsigned laneGroupMask() {
   return MT == 32 ? 0xffffffffu : ((1u << MT) - 1) << (threadIdx.x & 31 & ~(MT - 1));
 }
 
+// Block-table entry e (128 / MT atoms of replica rep) with replica constants P.
 template <int MT>
-__device__ __forceinline__ void SG_KN(rhoBody)(BlockTab tab, const RepConst *__restrict__ rc,
+__device__ __forceinline__ void SG_KN(rhoBody)(int e, const RepConst &P, BlockTab tab,
                                                const float4 *__restrict__ pos, const int *__restrict__ nn,
                                                const int *__restrict__ nbl, float *__restrict__ rho,
                                                float *__restrict__ dF, float *__restrict__ Fv,
-                                               int rowStride SG_EAM_PARAM) {
-  pdlEnter();
-  const int rep = tab.rep[blockIdx.x];
-  const RepConst &P = rc[rep];
+                                               int rowStride SG_EAM_BODY_PARAM) {
   const int sub = threadIdx.x & (MT - 1);
   const unsigned gmask = laneGroupMask<MT>();
-  const int i = tab.start[blockIdx.x] + threadIdx.x / MT;
+  const int i = tab.start[e] + threadIdx.x / MT;
   const int metalEnd = P.atomOff + P.nMolMe;
   const bool valid = i < metalEnd;
   float sum = 0.f;
@@ -174,7 +178,9 @@ __global__ void __launch_bounds__(128) SG_KN(k_rho)(BlockTab tab, const RepConst
                                              const int *__restrict__ nbl, float *__restrict__ rho,
                                              float *__restrict__ dF, float *__restrict__ Fv,
                                              int rowStride SG_EAM_PARAM) {
-  SG_KN(rhoBody)<kMT>(tab, rc, pos, nn, nbl, rho, dF, Fv, rowStride SG_EAM_ARG);
+  pdlEnter();
+  const RepConst &P = rc[tab.rep[blockIdx.x]];
+  SG_KN(rhoBody)<kMT>(blockIdx.x, P, tab, pos, nn, nbl, rho, dF, Fv, rowStride SG_EAM_BASE(P));
 }
 template <int MT>
 __global__ void __launch_bounds__(128) SG_KN(k_rho_tpa)(BlockTab tab, const RepConst *__restrict__ rc,
@@ -182,7 +188,9 @@ __global__ void __launch_bounds__(128) SG_KN(k_rho_tpa)(BlockTab tab, const RepC
                                                  const int *__restrict__ nbl, float *__restrict__ rho,
                                                  float *__restrict__ dF, float *__restrict__ Fv,
                                                  int rowStride SG_EAM_PARAM) {
-  SG_KN(rhoBody)<MT>(tab, rc, pos, nn, nbl, rho, dF, Fv, rowStride SG_EAM_ARG);
+  pdlEnter();
+  const RepConst &P = rc[tab.rep[blockIdx.x]];
+  SG_KN(rhoBody)<MT>(blockIdx.x, P, tab, pos, nn, nbl, rho, dF, Fv, rowStride SG_EAM_BASE(P));
 }
 
 // Lennard-Jones metal-carbon term (cu:880-884).
@@ -197,18 +205,15 @@ __device__ __forceinline__ void ljTerms(const RepConst &P, float rr, float &fc, 
 // (ComputeForcesK case 0, cu:856-897, epilogue cu:1069-1082); MT lanes per atom as in the
 // density pass (k_force_metal: MT = kMT; k_force_metal_tpa<MT>: the autotuner's choices).
 template <int MT>
-__device__ __forceinline__ void SG_KN(forceMetalBody)(BlockTab tab, const RepConst *__restrict__ rc,
+__device__ __forceinline__ void SG_KN(forceMetalBody)(int e, const RepConst &P, BlockTab tab,
                                                       float4 *__restrict__ pos, float4 *__restrict__ acc,
                                                       const int *__restrict__ nn, const int *__restrict__ nbl,
                                                       const float *__restrict__ dF,
                                                       const float *__restrict__ Fv, float *__restrict__ fric,
-                                                      int rowStride SG_EAM_PARAM) {
-  pdlEnter();
-  const int rep = tab.rep[blockIdx.x];
-  const RepConst &P = rc[rep];
+                                                      int rowStride SG_EAM_BODY_PARAM) {
   const int sub = threadIdx.x & (MT - 1);
   const unsigned gmask = laneGroupMask<MT>();
-  const int i = tab.start[blockIdx.x] + threadIdx.x / MT;
+  const int i = tab.start[e] + threadIdx.x / MT;
   const int metalEnd = P.atomOff + P.nMolMe;
   const bool valid = i < metalEnd;
   float fx = 0.f, fy = 0.f, fz = 0.f, rx = 0.f, u = 0.f;
@@ -263,7 +268,9 @@ __global__ void __launch_bounds__(128) SG_KN(k_force_metal)(BlockTab tab, const 
                                                      const int *__restrict__ nn, const int *__restrict__ nbl,
                                                      const float *__restrict__ dF, const float *__restrict__ Fv,
                                                      float *__restrict__ fric, int rowStride SG_EAM_PARAM) {
-  SG_KN(forceMetalBody)<kMT>(tab, rc, pos, acc, nn, nbl, dF, Fv, fric, rowStride SG_EAM_ARG);
+  pdlEnter();
+  const RepConst &P = rc[tab.rep[blockIdx.x]];
+  SG_KN(forceMetalBody)<kMT>(blockIdx.x, P, tab, pos, acc, nn, nbl, dF, Fv, fric, rowStride SG_EAM_BASE(P));
 }
 template <int MT>
 __global__ void __launch_bounds__(128) SG_KN(k_force_metal_tpa)(BlockTab tab, const RepConst *__restrict__ rc,
@@ -272,15 +279,92 @@ __global__ void __launch_bounds__(128) SG_KN(k_force_metal_tpa)(BlockTab tab, co
                                                          const float *__restrict__ dF,
                                                          const float *__restrict__ Fv, float *__restrict__ fric,
                                                          int rowStride SG_EAM_PARAM) {
-  SG_KN(forceMetalBody)<MT>(tab, rc, pos, acc, nn, nbl, dF, Fv, fric, rowStride SG_EAM_ARG);
+  pdlEnter();
+  const RepConst &P = rc[tab.rep[blockIdx.x]];
+  SG_KN(forceMetalBody)<MT>(blockIdx.x, P, tab, pos, acc, nn, nbl, dF, Fv, fric, rowStride SG_EAM_BASE(P));
 }
+
+#ifdef SG_EAM_TABLE
+// Staged variants (MIXED): a grid of at most stagedGrid blocks; each block copies its replica's
+// table into shared memory (again when a later entry belongs to another replica) and walks the
+// block-table entries blockIdx.x, blockIdx.x + gridDim.x, ...
+template <int MT>
+__global__ void __launch_bounds__(128) SG_KN(k_rho_staged)(BlockTab tab, const RepConst *__restrict__ rc,
+                                                    const float4 *__restrict__ pos, const int *__restrict__ nn,
+                                                    const int *__restrict__ nbl, float *__restrict__ rho,
+                                                    float *__restrict__ dF, float *__restrict__ Fv,
+                                                    int rowStride SG_EAM_PARAM) {
+  extern __shared__ float4 sTab[];
+  pdlEnter();
+  int staged = -1;
+  for (int e = blockIdx.x; e < tab.nblocks; e += gridDim.x) {
+    const int rep = tab.rep[e];
+    const RepConst &P = rc[rep];
+    if (rep != staged) {
+      __syncthreads();
+      for (int q = threadIdx.x; q < 2 * P.nTab; q += blockDim.x) sTab[q] = eamTab[2 * P.tabOff + q];
+      __syncthreads();
+      staged = rep;
+    }
+    SG_KN(rhoBody)<MT>(e, P, tab, pos, nn, nbl, rho, dF, Fv, rowStride, sTab);
+  }
+}
+template <int MT>
+__global__ void __launch_bounds__(128) SG_KN(k_force_metal_staged)(BlockTab tab, const RepConst *__restrict__ rc,
+                                                            float4 *__restrict__ pos, float4 *__restrict__ acc,
+                                                            const int *__restrict__ nn, const int *__restrict__ nbl,
+                                                            const float *__restrict__ dF,
+                                                            const float *__restrict__ Fv,
+                                                            float *__restrict__ fric, int rowStride SG_EAM_PARAM) {
+  extern __shared__ float4 sTab[];
+  pdlEnter();
+  int staged = -1;
+  for (int e = blockIdx.x; e < tab.nblocks; e += gridDim.x) {
+    const int rep = tab.rep[e];
+    const RepConst &P = rc[rep];
+    if (rep != staged) {
+      __syncthreads();
+      for (int q = threadIdx.x; q < 2 * P.nTab; q += blockDim.x) sTab[q] = eamTab[2 * P.tabOff + q];
+      __syncthreads();
+      staged = rep;
+    }
+    SG_KN(forceMetalBody)<MT>(e, P, tab, pos, acc, nn, nbl, dF, Fv, fric, rowStride, sTab);
+  }
+}
+
+template <int MT>
+static void SG_KN(launchStaged)(bool pdl, int grid, size_t smem, cudaStream_t s, BlockTab tab, const RepConst *rc,
+                                float4 *pos, float4 *acc, const int *nn, const int *nbl, float *rho, float *dF,
+                                float *Fv, float *fric, int rowStride, const float4 *eamTab) {
+  launchK(pdl, SG_KN(k_rho_staged)<MT>, grid, 128, smem, s, tab, rc, pos, nn, nbl, rho, dF, Fv, rowStride, eamTab);
+  launchK(pdl, SG_KN(k_force_metal_staged)<MT>, grid, 128, smem, s, tab, rc, pos, acc, nn, nbl, dF, Fv, fric,
+          rowStride, eamTab);
+}
+#endif
 
 // The metal chain with MT lanes per metal atom (4, 8, 16 or 32; grid = the block table for
 // 128 / MT atoms per block), from the host of the including unit; pdl: programmatic
-// dependent launch (launch errors are left for cudaGetLastError).
-void SG_KN(launchMetalChain)(bool pdl, int mt, int grid, cudaStream_t s, BlockTab tab, const RepConst *rc,
-                             float4 *pos, float4 *acc, const int *nn, const int *nbl, float *rho, float *dF,
-                             float *Fv, float *fric, int rowStride SG_EAM_PARAM) {
+// dependent launch; stagedGrid > 0 (MIXED): the staged variants on at most that many blocks
+// with stagedSmem bytes of table (launch errors are left for cudaGetLastError).
+void SG_KN(launchMetalChain)(bool pdl, int mt, int grid, int stagedGrid, size_t stagedSmem, cudaStream_t s,
+                             BlockTab tab, const RepConst *rc, float4 *pos, float4 *acc, const int *nn,
+                             const int *nbl, float *rho, float *dF, float *Fv, float *fric,
+                             int rowStride SG_EAM_PARAM) {
+#ifdef SG_EAM_TABLE
+  if (stagedGrid > 0) {
+    const int g = grid < stagedGrid ? grid : stagedGrid;
+    switch (mt) {
+      case 4: SG_KN(launchStaged)<4>(pdl, g, stagedSmem, s, tab, rc, pos, acc, nn, nbl, rho, dF, Fv, fric, rowStride, eamTab); break;
+      case 8: SG_KN(launchStaged)<8>(pdl, g, stagedSmem, s, tab, rc, pos, acc, nn, nbl, rho, dF, Fv, fric, rowStride, eamTab); break;
+      case 32: SG_KN(launchStaged)<32>(pdl, g, stagedSmem, s, tab, rc, pos, acc, nn, nbl, rho, dF, Fv, fric, rowStride, eamTab); break;
+      default: SG_KN(launchStaged)<16>(pdl, g, stagedSmem, s, tab, rc, pos, acc, nn, nbl, rho, dF, Fv, fric, rowStride, eamTab);
+    }
+    return;
+  }
+#else
+  (void)stagedGrid;
+  (void)stagedSmem;
+#endif
   switch (mt) {
     case 4:
       launchK(pdl, SG_KN(k_rho_tpa)<4>, grid, 128, 0, s, tab, rc, pos, nn, nbl, rho, dF, Fv, rowStride SG_EAM_ARG);

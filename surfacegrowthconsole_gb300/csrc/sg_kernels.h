@@ -52,7 +52,7 @@ __global__ void k_force_metal(BlockTab tab, const RepConst *rc, float4 *pos, flo
                               float *fric, int rowStride);
 // the metal chain (k_rho, k_force_metal) with mt lanes per atom (4, 8, 16, 32) on the table of
 // 128 / mt atoms per block
-void launchMetalChain(bool pdl, int mt, int grid, cudaStream_t s, BlockTab tab, const RepConst *rc, float4 *pos,
+void launchMetalChain(bool pdl, int mt, int grid, int stagedGrid, size_t stagedSmem, cudaStream_t s, BlockTab tab, const RepConst *rc, float4 *pos,
                       float4 *acc, const int *nn, const int *nbl, float *rho, float *dF, float *Fv,
                       float *fric, int rowStride);
 __global__ void k_force_carbon(BlockTab tab, const RepConst *rc, float4 *pos, float4 *acc,

@@ -58,7 +58,17 @@ struct MixedBufs {
   std::vector<size_t> diffOff64;
   unsigned *counter = nullptr;  // per replica: blocks done
   float4 *eamTab = nullptr;     // per replica nTab intervals x 2: cubic coefficients of phi, of f
+  size_t stagedSmem = 0;        // shared memory of the staged metal kernels (the largest table)
+  bool stagedOk = false;
 };
+
+template <int MT> static cudaError_t allowStagedSmem(size_t bytes) {
+  cudaError_t e = cudaFuncSetAttribute(k_rho_staged_mixed<MT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_force_metal_staged_mixed<MT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  return e;
+}
+
 
 __device__ __forceinline__ void twoSum(float a, float b, float &s, float &e) {
   s = a + b;
@@ -522,6 +532,11 @@ static void eamPairExact(const RepConst &P, double r, double out[4]) {
   out[3] = -(double)P.fe * rei * eB * tB / dB;
 }
 
+bool sg_mixed_staging_ok(sg_ctx *c) {
+  const MixedBufs *m = static_cast<const MixedBufs *>(c->mixed);
+  return m && m->stagedOk;
+}
+
 int sg_mixed_init(sg_ctx *c) {
   MixedBufs *m = new MixedBufs;
   c->mixed = m;
@@ -554,6 +569,16 @@ int sg_mixed_init(sg_ctx *c) {
       }
     }
   }
+  // the staged metal kernels hold the largest replica table in shared memory
+  int maxTab = 0;
+  for (int r = 0; r < c->nrep; r++) maxTab = std::max(maxTab, c->hrc[r].nTab);
+  m->stagedSmem = (size_t)2 * maxTab * sizeof(float4);
+  m->stagedOk = maxTab > 0 && m->stagedSmem <= 160 * 1024;
+  if (m->stagedOk && m->stagedSmem > 48 * 1024)
+    m->stagedOk = allowStagedSmem<4>(m->stagedSmem) == cudaSuccess && allowStagedSmem<8>(m->stagedSmem) == cudaSuccess &&
+                  allowStagedSmem<16>(m->stagedSmem) == cudaSuccess && allowStagedSmem<32>(m->stagedSmem) == cudaSuccess;
+  cudaGetLastError();
+  if (!m->stagedOk) c->eamStaged = false;
   MCK(cudaMalloc(&m->eamTab, sizeof(float4) * std::max<size_t>(tab.size(), 1)));
   sg_register_region(c, m->eamTab, sizeof(float4) * std::max<size_t>(tab.size(), 1));
   if (!tab.empty())
@@ -616,7 +641,8 @@ int sg_mixed_enqueue_forces(sg_ctx *c) {
   if (fork) {
     MCK(cudaEventRecord(c->evFork, c->stream));
     MCK(cudaStreamWaitEvent(c->side, c->evFork, 0));
-    launchMetalChain_mixed(c->pdl, c->metalLanes, c->metalRun.n, c->side, c->metalRun.view(), c->rc, c->pos, c->acc,
+    launchMetalChain_mixed(c->pdl, c->metalLanes, c->metalRun.n, c->eamStaged ? c->numSMs * 4 : 0,
+                           m->stagedSmem, c->side, c->metalRun.view(), c->rc, c->pos, c->acc,
                            c->nn, c->nbl, c->rho, c->dF, c->Fv, c->fric, c->rowStride, m->eamTab);
     if (c->opt.phase_timing) cudaEventRecordWithFlags(c->phaseEv[7], c->side, cudaEventRecordExternal);
     MCK(cudaGetLastError());

@@ -70,7 +70,8 @@ def test_bad_shapes_are_refused():
     with pytest.raises(Exception):
         sim.set_launch_shape({"metal_lanes": 64})
     assert sim.launch_shape() == {"metal_lanes": 16, "nebr_blocks_per_sm": 8, "nebr_descending": 0,
-                                  "nebr_item_atoms": 8, "programmatic_launch": 0, "nebr_atom_threads": 0}
+                                  "nebr_item_atoms": 8, "programmatic_launch": 0, "nebr_atom_threads": 0,
+                                  "eam_table_smem": 0}
     sim.close()
 
 
@@ -118,3 +119,24 @@ def test_programmatic_launch_changes_nothing(mode):
         sim.close()
     for x, y in zip(*out):
         assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("lanes", [4, 16, 32])
+def test_staged_eam_table_changes_nothing(lanes):
+    """MIXED: the metal passes with the EAM table staged in shared memory read the same table
+    values and do the same arithmetic: bit-identical forces, densities and energies."""
+    reps = [workloads.small(seed=s) for s in (91, 92)]
+    plist = [w[0] for w in reps]
+    r = np.concatenate([w[1] for w in reps])
+    v = np.concatenate([w[2] for w in reps])
+    out = []
+    for staged in (0, 1):
+        sim = Simulation(plist, mode=MODE_MIXED, metal_lanes=lanes, eam_table_smem=staged)
+        assert sim.launch_shape()["eam_table_smem"] == staged
+        sim.set_state(r, v, np.zeros((len(r), 3), np.float32))
+        sim.step(5)
+        out.append([sim.get_state(k) for k in range(2)] + [sim.rho(k) for k in range(2)])
+        sim.close()
+    for a, b in zip(out[0], out[1]):
+        for x, y in zip(a, b) if isinstance(a, tuple) else [(a, b)]:
+            assert np.array_equal(x, y)
