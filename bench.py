@@ -468,7 +468,7 @@ def run_production(args, rank: int, world: int, local: int, dist):
     # phases of each step (they cost a few microseconds each, so the headline pass has none)
     psim = make(MODE_MIXED if head == "mixed" else MODE_PLAIN, phase_timing=True)
     psim.set_state(r, v, a)
-    psim.set_launch_shape(*forms[head]["shape"])
+    psim.set_launch_shape(forms[head]["shape"])
     psim.step(args.warmup)
     phases = []
     phase_total_s, _ = timed(psim, phases)

@@ -1,9 +1,11 @@
 """Steps a benchmark workload under a CUDA profiler range, for kernel profilers.
 
     python -m surfacegrowthconsole_gb300.profile_step [--workload production|batched|precision]
-        [--mode plain|mixed] [--warmup 3] [--steps 1] [--replicas 16]
+        [--mode plain|mixed] [--warmup 3] [--steps 1] [--replicas 16] [--shape JSON]
 
-Builds the workload, steps it `warmup` times (graph capture, caches), then runs `steps` steps
+Builds the workload (--shape: a launch shape as sg_get_launch_shape reports it, a JSON object
+of its fields, e.g. the one the benchmark's autotuning chose; default: the library's
+defaults), steps it `warmup` times (graph capture, caches), then runs `steps` steps
 between cudaProfilerStart and cudaProfilerStop, so that a profiler started with its
 from-start profiling off (ncu --profile-from-start off) sees exactly those steps' kernels.
 Lists are rebuilt every step, as in the production benchmark.  Prints the kernel launches per
@@ -13,6 +15,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes
+import json
 
 import numpy as np
 
@@ -37,6 +40,7 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--replicas", type=int, default=16)
+    ap.add_argument("--shape", default="")
     a = ap.parse_args()
     if a.workload == "production":
         p, r, v = workloads.production(seed=2)
@@ -52,13 +56,15 @@ def main() -> None:
     n = int(sum(q.nMol for q in plist))
     sim = Simulation(plist, mode=MODE_MIXED if a.mode == "mixed" else MODE_PLAIN, force_rebuild=True)
     sim.set_state(r, v, np.zeros((n, 3), np.float32))
+    if a.shape:
+        sim.set_launch_shape(json.loads(a.shape))
     sim.step(a.warmup)
     rt = _cudart()
     rt.cudaProfilerStart()
     sim.step(a.steps)
     rt.cudaProfilerStop()
     print(f"{a.workload} {a.mode}: {n} atoms, {sim.kernels_per_step()} kernel launches per step, "
-          f"{a.steps} profiled step(s)")
+          f"{a.steps} profiled step(s), launch shape {sim.launch_shape()}")
     sim.close()
 
 
