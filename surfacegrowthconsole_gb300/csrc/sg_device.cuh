@@ -41,6 +41,8 @@ constexpr int kHeavyCell = 16;    // list build: default home atoms per work ite
 constexpr int kHeavyChunk = 8;    // sizes the item list of the fixed-size scratch (>= kHeavyCell / 2)
 constexpr int kScanCells = 512;   // cells per block of the single-pass cell scan (kCellTile / 4)
 constexpr int kScanThreads = 128;
+constexpr int kMixThreads = 128;  // MIXED step reduction: threads per block
+constexpr int kMixAtoms = 256;    // and atoms per block (2 per thread)
 constexpr int kMinItemAtoms = 4;  // smallest home atoms per work item the engine allows
 constexpr int kItemAtoms = 8;     // the engine's default home atoms per work item
 constexpr int kMetalPerBlock = 128 / kMT;   // atoms per 128-thread block
@@ -64,6 +66,7 @@ struct RepConst {
   int cells[3], ncells, ncellsPad;
   int atomOff, nMol, nMolMe, cellOff;
   int nRedBlocks;  // ceil(nMol / 1024)
+  int nRedBlocksM, redFirstM;  // MIXED reduction: blocks of kMixAtoms atoms, first partial slot
   // integrator
   float deltaT, rrNebr, rNebrShell, rrShort;
   float xLeft, xRight, yBottom, yTop;

@@ -51,13 +51,15 @@ enum MixAcc {
 enum MixMax { MM_VVMAX = 0, MM_MIN_X, MM_MIN_Y, MM_MIN_Z, MM_MAX_X, MM_MAX_Y, MM_MAX_Z, kMixMax };
 
 struct MixedBufs {
-  double *part64 = nullptr;  // [reduction blocks][kMixAcc]
+  float2 *partDF = nullptr;  // [reduction blocks][kMixAcc]: double-float block sums
   float *partF = nullptr;    // [reduction blocks][kMixMax]
   double *diff64 = nullptr;  // per replica: nB x 6 (orgR, rTrue), nB x nV (rr), nV (av)
   size_t *dDiffOff64 = nullptr;
   std::vector<size_t> diffOff64;
   unsigned *counter = nullptr;  // per replica: blocks done
   float4 *eamTab = nullptr;     // per replica nTab intervals x 2: cubic coefficients of phi, of f
+  int *redRep = nullptr, *redStart = nullptr;  // reduction blocks: replica, block index in it
+  int redN = 0;
   size_t stagedSmem = 0;        // shared memory of the staged metal kernels (the largest table)
   bool stagedOk = false;
 };
@@ -185,10 +187,10 @@ __device__ void stepControlMixed(const RepConst &P, RepState *S, const double (&
                                  const float (&M)[kMixMax], double *diff, float *diffF,
                                  int forceRebuild);
 
-__global__ void __launch_bounds__(kRedThreads, 1) k_step_reduce_mixed(
+__global__ void __launch_bounds__(kMixThreads) k_step_reduce_mixed(
     BlockTab tab, const RepConst *__restrict__ rc, RepState *st, const float4 *__restrict__ pos,
     const float4 *__restrict__ posLo, float4 *__restrict__ vel, const float4 *__restrict__ acc4,
-    const float *__restrict__ fric, double *__restrict__ part64, float *__restrict__ partF,
+    const float *__restrict__ fric, float2 *__restrict__ partDF, float *__restrict__ partF,
     const int *__restrict__ redFirst, unsigned *counter, double *__restrict__ diff64,
     const size_t *__restrict__ diffOff64, float *__restrict__ diffF, const size_t *__restrict__ diffOffF,
     int forceRebuild) {
@@ -208,7 +210,7 @@ __global__ void __launch_bounds__(kRedThreads, 1) k_step_reduce_mixed(
   float mm[kMixMax] = {0.f, 3.4e38f, 3.4e38f, 3.4e38f, -3.4e38f, -3.4e38f, -3.4e38f};
 #pragma unroll
   for (int half = 0; half < 2; half++) {
-    const int local = kRedElems * b + half * kRedThreads + t;
+    const int local = kMixAtoms * b + half * kMixThreads + t;
     if (local >= P.nMol) continue;
     const int g = P.atomOff + local;
     const float4 r = pos[g];
@@ -245,20 +247,20 @@ __global__ void __launch_bounds__(kRedThreads, 1) k_step_reduce_mixed(
       acc[MA_VV_C] += vv;
     }
   }
-  __shared__ double sh64[kRedThreads / 32][kMixAcc];
-  __shared__ float shF[kRedThreads / 32][kMixMax];
+  __shared__ DF shDF[kMixThreads / 32][kMixAcc];
+  __shared__ float shF[kMixThreads / 32][kMixMax];
 #pragma unroll
   for (int k = 0; k < kMixAcc; k++) {
     if (k >= MA_CM_X && k <= MA_CM_Z) continue;
     float x = acc[k];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    if (lane == 0) sh64[w][k] = (double)x;
+    if (lane == 0) shDF[w][k] = DF{x, 0.f};
   }
 #pragma unroll
   for (int c = 0; c < 3; c++) {
     const DF x = dfWarpSum(cm[c]);
-    if (lane == 0) sh64[w][MA_CM_X + c] = (double)x.hi + (double)x.lo;
+    if (lane == 0) shDF[w][MA_CM_X + c] = x;
   }
 #pragma unroll
   for (int k = 0; k < kMixMax; k++) {
@@ -270,58 +272,86 @@ __global__ void __launch_bounds__(kRedThreads, 1) k_step_reduce_mixed(
     if (lane == 0) shF[w][k] = x;
   }
   __syncthreads();
-  const int pb = redFirst[rep] + b;
+  const int pb = P.redFirstM + b;
   if (t < kMixAcc) {
-    double x = 0.0;
-    for (int k = 0; k < kRedThreads / 32; k++) x += sh64[k][t];
-    part64[(size_t)pb * kMixAcc + t] = x;
+    DF x{0.f, 0.f};
+    for (int k = 0; k < kMixThreads / 32; k++) x = dfAdd(x, shDF[k][t]);
+    partDF[(size_t)pb * kMixAcc + t] = make_float2(x.hi, x.lo);
   } else if (t >= 32 && t < 32 + kMixMax) {
     const int k = t - 32;
     float x = shF[0][k];
-    for (int j = 1; j < kRedThreads / 32; j++)
+    for (int j = 1; j < kMixThreads / 32; j++)
       x = (k == MM_VVMAX || k >= MM_MAX_X) ? fmaxf(x, shF[j][k]) : fminf(x, shF[j][k]);
     partF[(size_t)pb * kMixMax + k] = x;
   }
   if (t < kMixAcc || (t >= 32 && t < 32 + kMixMax)) __threadfence();  // partials visible first
   __syncthreads();
   __shared__ bool last;
-  if (t == 0) last = (atomicAdd(&counter[rep], 1u) == (unsigned)P.nRedBlocks - 1);
+  if (t == 0) last = (atomicAdd(&counter[rep], 1u) == (unsigned)P.nRedBlocksM - 1);
   __syncthreads();
   if (!last) return;
   __threadfence();
-  // block partials: thread (g, k) with k = t % 16, g = t / 16 sums value k over blocks g, g + 32,
-  // ...; the 32 group sums of a value then add up in group order (a fixed order: the result
-  // does not depend on which block finished last)
-  __shared__ double grp64[32][16];
-  __shared__ float grpF[32][8];
+  // block partials in a fixed order (whichever block finished last), as double-floats on the
+  // FP32 pipes (FP64 runs at a small fraction of their rate on this GPU; a double-float sum of
+  // a few hundred partials keeps ~1e-14 relative, far below the FP32 warp sums' own rounding):
+  // thread t adds rows t, t + kMixThreads, ... (independent loads, in flight together); then 8
+  // threads per value each add 16 of those sums, and one thread per value the 8 results.
+  constexpr int kParts = kMixThreads / 16;
+  __shared__ DF s1[kMixThreads][kMixAcc];
+  __shared__ float s1F[kMixThreads][kMixMax];
+  __shared__ DF s2[kParts][kMixAcc];
   __shared__ double tot[kMixAcc];
   __shared__ float totF[kMixMax];
-  const int p0 = redFirst[rep];
+  const int p0 = P.redFirstM, nb = P.nRedBlocksM;
   {
-    const int k = t & 15, gi = t >> 4;
-    double x = 0.0;
-    float y = (k == MM_VVMAX || k >= MM_MAX_X) ? -3.4e38f : 3.4e38f;
-    for (int j = gi; j < P.nRedBlocks; j += 32) {
-      if (k < kMixAcc) x += __ldcg(part64 + (size_t)(p0 + j) * kMixAcc + k);
-      if (k < kMixMax) {
-        const float z = __ldcg(partF + (size_t)(p0 + j) * kMixMax + k);
-        y = (k == MM_VVMAX || k >= MM_MAX_X) ? fmaxf(y, z) : fminf(y, z);
+    DF x[kMixAcc];
+    float y[kMixMax];
+#pragma unroll
+    for (int k = 0; k < kMixAcc; k++) x[k] = DF{0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < kMixMax; k++) y[k] = (k == MM_VVMAX || k >= MM_MAX_X) ? -3.4e38f : 3.4e38f;
+    for (int j = t; j < nb; j += kMixThreads) {
+      const float2 *row = partDF + (size_t)(p0 + j) * kMixAcc;
+      const float *rowF = partF + (size_t)(p0 + j) * kMixMax;
+#pragma unroll
+      for (int k = 0; k < kMixAcc; k++) {
+        const float2 v = __ldcg(row + k);
+        x[k] = dfAdd(x[k], DF{v.x, v.y});
+      }
+#pragma unroll
+      for (int k = 0; k < kMixMax; k++) {
+        const float z = __ldcg(rowF + k);
+        y[k] = (k == MM_VVMAX || k >= MM_MAX_X) ? fmaxf(y[k], z) : fminf(y[k], z);
       }
     }
-    grp64[gi][k] = x;
-    if (k < 8) grpF[gi][k] = y;
+#pragma unroll
+    for (int k = 0; k < kMixAcc; k++) s1[t][k] = x[k];
+#pragma unroll
+    for (int k = 0; k < kMixMax; k++) s1F[t][k] = y[k];
+  }
+  __syncthreads();
+  {
+    const int k = t & 15, part = t >> 4;
+    if (k < kMixAcc) {
+      DF x{0.f, 0.f};
+#pragma unroll
+      for (int q = 0; q < 16; q++) x = dfAdd(x, s1[part * 16 + q][k]);
+      s2[part][k] = x;
+    }
+  }
+  if (t >= 96 && t < 96 + kMixMax) {
+    const int k = t - 96;
+    const bool isMax = (k == MM_VVMAX || k >= MM_MAX_X);
+    float y = s1F[0][k];
+    for (int q = 1; q < kMixThreads; q++) y = isMax ? fmaxf(y, s1F[q][k]) : fminf(y, s1F[q][k]);
+    totF[k] = y;
   }
   __syncthreads();
   if (t < kMixAcc) {
-    double x = 0.0;
-    for (int gi = 0; gi < 32; gi++) x += grp64[gi][t];
-    tot[t] = x;
-  } else if (t >= 32 && t < 32 + kMixMax) {
-    const int k = t - 32;
-    float y = grpF[0][k];
-    for (int gi = 1; gi < 32; gi++)
-      y = (k == MM_VVMAX || k >= MM_MAX_X) ? fmaxf(y, grpF[gi][k]) : fminf(y, grpF[gi][k]);
-    totF[k] = y;
+    DF x{0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < kParts; q++) x = dfAdd(x, s2[q][t]);
+    tot[t] = (double)x.hi + (double)x.lo;
   }
   __syncthreads();
   if (t == 0) counter[rep] = 0;
@@ -585,9 +615,28 @@ int sg_mixed_init(sg_ctx *c) {
     MCK(cudaMemcpyAsync(m->eamTab, tab.data(), sizeof(float4) * tab.size(), cudaMemcpyHostToDevice, c->stream));
   MCK(cudaMemcpyAsync(c->rc, c->hrc.data(), sizeof(RepConst) * c->nrep, cudaMemcpyHostToDevice, c->stream));
   MCK(cudaStreamSynchronize(c->stream));
-  const int nRed = std::max(c->redTab.n, 1);
-  MCK(cudaMalloc(&m->part64, sizeof(double) * nRed * kMixAcc));
-  sg_register_region(c, m->part64, sizeof(double) * nRed * kMixAcc);
+  // reduction blocks of kMixAtoms atoms
+  {
+    std::vector<int> rr, ss;
+    for (int r = 0; r < c->nrep; r++) {
+      RepConst &P = c->hrc[r];
+      P.nRedBlocksM = (P.nMol + kMixAtoms - 1) / kMixAtoms;
+      P.redFirstM = (int)rr.size();
+      for (int b = 0; b < P.nRedBlocksM; b++) { rr.push_back(r); ss.push_back(b); }
+    }
+    m->redN = (int)rr.size();
+    MCK(cudaMalloc(&m->redRep, sizeof(int) * std::max<size_t>(rr.size(), 1)));
+    sg_register_region(c, m->redRep, sizeof(int) * std::max<size_t>(rr.size(), 1));
+    MCK(cudaMalloc(&m->redStart, sizeof(int) * std::max<size_t>(ss.size(), 1)));
+    sg_register_region(c, m->redStart, sizeof(int) * std::max<size_t>(ss.size(), 1));
+    MCK(cudaMemcpyAsync(m->redRep, rr.data(), sizeof(int) * rr.size(), cudaMemcpyHostToDevice, c->stream));
+    MCK(cudaMemcpyAsync(m->redStart, ss.data(), sizeof(int) * ss.size(), cudaMemcpyHostToDevice, c->stream));
+    MCK(cudaMemcpyAsync(c->rc, c->hrc.data(), sizeof(RepConst) * c->nrep, cudaMemcpyHostToDevice, c->stream));
+    MCK(cudaStreamSynchronize(c->stream));
+  }
+  const int nRed = std::max(m->redN, 1);
+  MCK(cudaMalloc(&m->partDF, sizeof(float2) * nRed * kMixAcc));
+  sg_register_region(c, m->partDF, sizeof(float2) * nRed * kMixAcc);
   MCK(cudaMalloc(&m->partF, sizeof(float) * nRed * kMixMax));
   sg_register_region(c, m->partF, sizeof(float) * nRed * kMixMax);
   MCK(cudaMalloc(&m->counter, sizeof(unsigned) * c->nrep));
@@ -614,12 +663,14 @@ int sg_mixed_init(sg_ctx *c) {
 void sg_mixed_free(sg_ctx *c) {
   MixedBufs *m = static_cast<MixedBufs *>(c->mixed);
   if (!m) return;
-  cudaFree(m->part64);
+  cudaFree(m->partDF);
   cudaFree(m->partF);
   cudaFree(m->counter);
   cudaFree(m->diff64);
   cudaFree(m->dDiffOff64);
   cudaFree(m->eamTab);
+  cudaFree(m->redRep);
+  cudaFree(m->redStart);
   delete m;
   c->mixed = nullptr;
 }
@@ -666,8 +717,8 @@ int sg_mixed_enqueue_forces(sg_ctx *c) {
 int sg_mixed_enqueue_reduce(sg_ctx *c, int forceRebuild) {
   MixedBufs *m = static_cast<MixedBufs *>(c->mixed);
   if (!c->redTab.n) return SG_OK;
-  MCK(launchK(c->pdl, k_step_reduce_mixed, c->redTab.n, kRedThreads, 0, c->stream, 
-      c->redTab.view(), c->rc, c->st, c->pos, c->posLo, c->vel, c->acc, c->fric, m->part64, m->partF,
+  MCK(launchK(c->pdl, k_step_reduce_mixed, m->redN, kMixThreads, 0, c->stream,
+      BlockTab{m->redRep, m->redStart, m->redN}, c->rc, c->st, c->pos, c->posLo, c->vel, c->acc, c->fric, m->partDF, m->partF,
       c->dRedFirst, m->counter, m->diff64, m->dDiffOff64, c->diffBuf, c->dDiffOff, forceRebuild));
   MCK(cudaGetLastError());
   return SG_OK;
