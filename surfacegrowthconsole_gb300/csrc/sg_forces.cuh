@@ -133,6 +133,7 @@ __device__ __forceinline__ float eamDensTab(const RepConst &P, const float4 *tab
 // which the reference re-evaluates per pair in the force kernel.  MT lanes share one metal
 // atom (128 / MT atoms per block): lane l takes list entries l, l + MT, ...; the partial sums
 // meet in a shuffle tree.  k_rho runs MT = kMT; k_rho_tpa<MT> the choices of the autotuner.
+constexpr int kMetalBatch = 4;  // list entries per lane whose loads are issued together
 template <int MT> __device__ __forceinline__ unsigned laneGroupMask() {
   return MT == 32 ? 0xffffffffu : ((1u << MT) - 1) << (threadIdx.x & 31 & ~(MT - 1));
 }
@@ -154,14 +155,24 @@ __device__ __forceinline__ void SG_KN(rhoBody)(int e, const RepConst &P, BlockTa
     const float4 A = pos[i];
     const int n = nn[i];
     const int *row = nbl + (size_t)i * rowStride;
-    for (int j = sub; j < n; j += MT) {
-      const int k = row[j];
-      const float4 B = pos[k];
-      const float dx = minImg(A.x - B.x, P.region[0]);
-      const float dy = minImg(A.y - B.y, P.region[1]);
-      const float dz = minImg(A.z - B.z, P.region[2]);
-      const float rr = dx * dx + dy * dy + dz * dz;
-      if ((rr < P.rrCutEam) && (k < metalEnd)) sum += SG_EAM_DENS(P, sqrtf(rr));
+    // kMetalBatch entries per lane per round: their indices, then their positions, load
+    // together (the sum still takes the entries in the same order)
+    for (int j0 = sub; j0 < n; j0 += kMetalBatch * MT) {
+      int k[kMetalBatch];
+      float4 B[kMetalBatch];
+#pragma unroll
+      for (int q = 0; q < kMetalBatch; q++) k[q] = (j0 + q * MT < n) ? row[j0 + q * MT] : -1;
+#pragma unroll
+      for (int q = 0; q < kMetalBatch; q++) B[q] = (k[q] >= 0) ? pos[k[q]] : A;
+#pragma unroll
+      for (int q = 0; q < kMetalBatch; q++) {
+        if (k[q] < 0) continue;
+        const float dx = minImg(A.x - B[q].x, P.region[0]);
+        const float dy = minImg(A.y - B[q].y, P.region[1]);
+        const float dz = minImg(A.z - B[q].z, P.region[2]);
+        const float rr = dx * dx + dy * dy + dz * dz;
+        if ((rr < P.rrCutEam) && (k[q] < metalEnd)) sum += SG_EAM_DENS(P, sqrtf(rr));
+      }
     }
   }
 #pragma unroll
@@ -222,29 +233,42 @@ __device__ __forceinline__ void SG_KN(forceMetalBody)(int e, const RepConst &P, 
     const int n = nn[i];
     const float dFi = dF[i];
     const int *row = nbl + (size_t)i * rowStride;
-    for (int j = sub; j < n; j += MT) {
-      const int k = row[j];
-      const float4 B = pos[k];
-      const float dx = minImg(A.x - B.x, P.region[0]);
-      const float dy = minImg(A.y - B.y, P.region[1]);
-      const float dz = minImg(A.z - B.z, P.region[2]);
-      const float rr = dx * dx + dy * dy + dz * dz;
-      if (k < metalEnd) {
-        if (rr >= P.rrCutEam) continue;  // the reference computes and then zeroes the term
-        const float r = sqrtf(rr);
-        const EamPair e = SG_EAM_PAIR(P, r);
-        float fc = -e.dphi;
-        fc = fc - e.df * (dFi + dF[k]);
-        fc = fc / r;
-        fx = fx + fc * dx; fy = fy + fc * dy; fz = fz + fc * dz;
-        u += e.phi;
-      } else {
-        if (rr >= P.rrCutLJ) continue;
-        float fc, ul;
-        ljTerms(P, rr, fc, ul);
-        u += ul;
-        fx = fx + fc * dx; fy = fy + fc * dy; fz = fz + fc * dz;
-        rx = rx + fc * dx;
+    // batches of entries as in the density pass; same order of the sums
+    for (int j0 = sub; j0 < n; j0 += kMetalBatch * MT) {
+      int k[kMetalBatch];
+      float4 B[kMetalBatch];
+      float dFk[kMetalBatch];
+#pragma unroll
+      for (int q = 0; q < kMetalBatch; q++) k[q] = (j0 + q * MT < n) ? row[j0 + q * MT] : -1;
+#pragma unroll
+      for (int q = 0; q < kMetalBatch; q++) {
+        B[q] = (k[q] >= 0) ? pos[k[q]] : A;
+        dFk[q] = (k[q] >= 0 && k[q] < metalEnd) ? dF[k[q]] : 0.f;
+      }
+#pragma unroll
+      for (int q = 0; q < kMetalBatch; q++) {
+        if (k[q] < 0) continue;
+        const float dx = minImg(A.x - B[q].x, P.region[0]);
+        const float dy = minImg(A.y - B[q].y, P.region[1]);
+        const float dz = minImg(A.z - B[q].z, P.region[2]);
+        const float rr = dx * dx + dy * dy + dz * dz;
+        if (k[q] < metalEnd) {
+          if (rr >= P.rrCutEam) continue;  // the reference computes and then zeroes the term
+          const float r = sqrtf(rr);
+          const EamPair e = SG_EAM_PAIR(P, r);
+          float fc = -e.dphi;
+          fc = fc - e.df * (dFi + dFk[q]);
+          fc = fc / r;
+          fx = fx + fc * dx; fy = fy + fc * dy; fz = fz + fc * dz;
+          u += e.phi;
+        } else {
+          if (rr >= P.rrCutLJ) continue;
+          float fc, ul;
+          ljTerms(P, rr, fc, ul);
+          u += ul;
+          fx = fx + fc * dx; fy = fy + fc * dy; fz = fz + fc * dz;
+          rx = rx + fc * dx;
+        }
       }
     }
   }
