@@ -83,8 +83,9 @@ typedef struct sg_options {
                             * order (0: ascending) */
     int nebr_item_atoms;   /* list build: most home atoms of one work item (a warp's share); a
                             * cell of more atoms is split into near-equal items, 4..64 (0: 8) */
-    int nebr_atom_threads; /* list build: 0 a warp per cell (windows of candidates), 1 a thread
-                            * per atom; the same lists */
+    int nebr_build;        /* list build: 0 a warp per cell window, hits placed by the warp; 1 a
+                            * thread per atom; 2 a warp per cell window, hits placed by one lane
+                            * per home atom; the same lists */
     int eam_table_smem;    /* MIXED: 1 the metal passes stage the EAM table in shared memory
                             * (a grid of 4 blocks per SM), 0 read it through L1 */
     int reserved[2];
@@ -355,8 +356,8 @@ int sg_diff_force_matching(sg_diff *d, const double *theta, const float *ref_for
 /* ---- tuning ------------------------------------------------------------------------------- */
 /* Times the launch shapes of the tunable passes on the context's own state and keeps the
  * fastest: the metal lanes per atom (4, 8, 16, 32; `steps` steps each, the context's own
- * rebuild schedule), then the list build (a thread per atom, or a warp per cell with its home
- * atoms per work item 4, 6, 8, 16, blocks per SM 2, 4, 8, 16 and cell order ascending or
+ * rebuild schedule), then the list build (its three forms, then for the cell-window forms the
+ * home atoms per work item 4, 6, 8, 16, blocks per SM 2, 4, 8, 16 and cell order ascending or
  * descending), `steps` steps each with a rebuild in every step, then programmatic dependent
  * launch off and on, and (MIXED) the EAM table read through L1 or staged in shared memory.  Every device buffer and the host step counters are copied first
  * and put back after each trial, so the context continues from the state it had; the trials
@@ -371,7 +372,7 @@ typedef struct sg_launch_shape {
     int nebr_descending;    /* 0 or 1 */
     int nebr_item_atoms;    /* 4..64 */
     int programmatic_launch; /* 0 or 1 */
-    int nebr_atom_threads;  /* 0 or 1 */
+    int nebr_build;         /* 0, 1 or 2 */
     int eam_table_smem;     /* 0 or 1 (MIXED) */
     int reserved[1];
 } sg_launch_shape;

@@ -274,7 +274,11 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
   setNebrBlocks(c, c->opt.nebr_blocks_per_sm ? c->opt.nebr_blocks_per_sm : 8);
   c->nebrDescending = c->opt.nebr_descending ? 1 : 0;
   c->nebrItemAtoms = c->opt.nebr_item_atoms ? c->opt.nebr_item_atoms : kItemAtoms;
-  c->nebrAlgo = c->opt.nebr_atom_threads ? 1 : 0;
+  if (c->opt.nebr_build < 0 || c->opt.nebr_build > 2) {
+    sg_destroy(c);
+    return sg_fail(SG_ERR_INVALID, "nebr_build %d: 0, 1 or 2", c->opt.nebr_build);
+  }
+  c->nebrAlgo = c->opt.nebr_build;
   c->eamStaged = c->opt.mode == SG_MODE_MIXED && c->opt.eam_table_smem != 0;  // sg_mixed_init may clear it
   if (c->nebrItemAtoms < kMinItemAtoms || c->nebrItemAtoms > 64) {
     sg_destroy(c);
@@ -523,7 +527,8 @@ static int enqueueRebuild(sg_ctx *c, int force) {
                c->cellOf, c->cellStart, c->sortPos, c->nn, c->nbl, c->ns, c->sl, c->nrl, c->rl, c->rowStride,
                c->nebrMax, c->nebrWork, fr));
   else
-    CK(launchK(c->pdl, k_build_nebr, c->nebrGrid, kNebrWarps * 32, 0, c->stream, c->tileTab.rep, c->activeCells,
+    CK(launchK(c->pdl, c->nebrAlgo == 2 ? k_build_nebr_lanes : k_build_nebr, c->nebrGrid, kNebrWarps * 32, 0,
+               c->stream, c->tileTab.rep, c->activeCells,
                c->heavyItems, c->nebrWork, c->rc, c->st, c->cellStart, c->sortPos, c->nn, c->nbl, c->ns, c->sl,
                c->nrl, c->rl, c->rowStride, c->nebrMax, c->nebrDescending));
   return SG_OK;
@@ -1092,7 +1097,7 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
   const int algo0 = c->nebrAlgo;
   const bool staged0 = c->eamStaged;
   const int laneChoice[4] = {4, 8, 16, 32}, bpsChoice[4] = {2, 4, 8, 16}, itemChoice[4] = {4, 6, 8, 16};
-  float laneMs[4] = {}, bpsMs[4] = {}, orderMs[2] = {}, itemMs[4] = {}, pdlMs[2] = {}, algoMs[2] = {};
+  float laneMs[4] = {}, bpsMs[4] = {}, orderMs[2] = {}, itemMs[4] = {}, pdlMs[2] = {}, algoMs[3] = {};
   float stagedMs[2] = {};
   bool bestStaged = staged0;
   int bestLanes = lanes0, bestBps = bps0, bestDesc = desc0, bestItem = item0, bestAlgo = algo0;
@@ -1111,15 +1116,19 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
   if (!rc && !(rc = setMetalLanes(c, bestLanes))) {
     c->opt.force_rebuild = 1;
     destroyGraphs(c);
-    for (int a = 0; a < 2 && !rc; a++) {
+    for (int a = 0; a < 3 && !rc; a++) {
       if ((rc = restoreSnapshot(c, snap))) break;
       c->nebrAlgo = a;
       destroyGraphs(c);
       rc = timeSteps(c, steps, &algoMs[a]);
     }
-    if (!rc) bestAlgo = algoMs[1] < algoMs[0] ? 1 : 0;
-    c->nebrAlgo = 0;
-    if (!rc && bestAlgo == 0) {
+    if (!rc) {
+      bestAlgo = 0;
+      for (int a = 1; a < 3; a++)
+        if (algoMs[a] < algoMs[bestAlgo]) bestAlgo = a;
+    }
+    c->nebrAlgo = bestAlgo;
+    if (!rc && bestAlgo != 1) {
       float best = 0.f;
       for (int k = 0; k < 4 && !rc; k++) {
         if ((rc = restoreSnapshot(c, snap))) break;
@@ -1204,14 +1213,14 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
              "\"8\": %.6g, \"16\": %.6g}, \"nebr_order_ms_per_step_rebuilding\": {\"ascending\": %.6g, "
              "\"descending\": %.6g}, \"nebr_item_atoms_ms_per_step_rebuilding\": {\"4\": %.6g, "
              "\"6\": %.6g, \"8\": %.6g, \"16\": %.6g}, \"programmatic_launch_ms_per_step\": {\"0\": %.6g, "
-             "\"1\": %.6g}, \"nebr_atom_threads_ms_per_step_rebuilding\": {\"0\": %.6g, \"1\": %.6g}, "
+             "\"1\": %.6g}, \"nebr_build_ms_per_step_rebuilding\": {\"0\": %.6g, \"1\": %.6g, \"2\": %.6g}, "
              "\"eam_table_smem_ms_per_step\": {\"0\": %.6g, \"1\": %.6g}, "
              "\"metal_lanes\": %d, \"nebr_blocks_per_sm\": %d, \"nebr_descending\": %d, "
-             "\"nebr_item_atoms\": %d, \"programmatic_launch\": %d, \"nebr_atom_threads\": %d, "
+             "\"nebr_item_atoms\": %d, \"programmatic_launch\": %d, \"nebr_build\": %d, "
              "\"eam_table_smem\": %d, \"nebr_grid\": %d}",
              steps, laneMs[0], laneMs[1], laneMs[2], laneMs[3], bpsMs[0], bpsMs[1], bpsMs[2], bpsMs[3],
              orderMs[0], orderMs[1], itemMs[0], itemMs[1], itemMs[2], itemMs[3], pdlMs[0], pdlMs[1],
-             algoMs[0], algoMs[1], stagedMs[0], stagedMs[1], c->metalLanes, c->nebrBlocksPerSM,
+             algoMs[0], algoMs[1], algoMs[2], stagedMs[0], stagedMs[1], c->metalLanes, c->nebrBlocksPerSM,
              c->nebrDescending, c->nebrItemAtoms, c->pdl ? 1 : 0, c->nebrAlgo, c->eamStaged ? 1 : 0, c->nebrGrid);
   }
   return SG_OK;
@@ -1227,8 +1236,8 @@ extern "C" int sg_set_launch_shape(sg_ctx *c, const sg_launch_shape *shape) {
     return sg_fail(SG_ERR_INVALID, "nebr_item_atoms %d: %d..64", shape->nebr_item_atoms, kMinItemAtoms);
   if (shape->programmatic_launch != 0 && shape->programmatic_launch != 1)
     return sg_fail(SG_ERR_INVALID, "programmatic_launch %d: 0 or 1", shape->programmatic_launch);
-  if (shape->nebr_atom_threads != 0 && shape->nebr_atom_threads != 1)
-    return sg_fail(SG_ERR_INVALID, "nebr_atom_threads %d: 0 or 1", shape->nebr_atom_threads);
+  if (shape->nebr_build < 0 || shape->nebr_build > 2)
+    return sg_fail(SG_ERR_INVALID, "nebr_build %d: 0, 1 or 2", shape->nebr_build);
   if (shape->eam_table_smem != 0 && shape->eam_table_smem != 1)
     return sg_fail(SG_ERR_INVALID, "eam_table_smem %d: 0 or 1", shape->eam_table_smem);
   if (shape->eam_table_smem && !(c->opt.mode == SG_MODE_MIXED && sg_mixed_staging_ok(c)))
@@ -1238,9 +1247,9 @@ extern "C" int sg_set_launch_shape(sg_ctx *c, const sg_launch_shape *shape) {
   if (rc) return rc;
   setNebrBlocks(c, shape->nebr_blocks_per_sm);
   if (shape->nebr_descending != c->nebrDescending || shape->nebr_item_atoms != c->nebrItemAtoms ||
-      (shape->programmatic_launch != 0) != c->pdl || shape->nebr_atom_threads != c->nebrAlgo)
+      (shape->programmatic_launch != 0) != c->pdl || shape->nebr_build != c->nebrAlgo)
     destroyGraphs(c);
-  c->nebrAlgo = shape->nebr_atom_threads;
+  c->nebrAlgo = shape->nebr_build;
   if ((shape->eam_table_smem != 0) != c->eamStaged) destroyGraphs(c);
   c->eamStaged = shape->eam_table_smem != 0;
   c->nebrDescending = shape->nebr_descending;
@@ -1257,7 +1266,7 @@ extern "C" int sg_get_launch_shape(sg_ctx *c, sg_launch_shape *shape) {
   shape->nebr_descending = c->nebrDescending;
   shape->nebr_item_atoms = c->nebrItemAtoms;
   shape->programmatic_launch = c->pdl ? 1 : 0;
-  shape->nebr_atom_threads = c->nebrAlgo;
+  shape->nebr_build = c->nebrAlgo;
   shape->eam_table_smem = c->eamStaged ? 1 : 0;
   return SG_OK;
 }

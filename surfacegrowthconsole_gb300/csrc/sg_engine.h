@@ -61,7 +61,9 @@ struct sg_ctx {
   DevTab metalLaneTab[4];
   DevTab metalRun;
   int numSMs = 0, nebrBlocksPerSM = 8, nebrDescending = 0, nebrItemAtoms = sg::kItemAtoms;
-  int nebrAlgo = 0;  // list build: 0 cell windows (k_build_nebr), 1 atom threads (k_build_nebr_atoms)
+  // list build: 0 cell windows, warp-placed hits (k_build_nebr); 1 atom threads
+  // (k_build_nebr_atoms); 2 cell windows, lane-placed hits (k_build_nebr_lanes)
+  int nebrAlgo = 0;
   bool eamStaged = false;  // MIXED: metal passes with the EAM table staged in shared memory
   bool pdl = false;  // programmatic dependent launch between the kernels of a step
   std::vector<std::pair<void *, size_t>> regions;  // every device buffer with its size

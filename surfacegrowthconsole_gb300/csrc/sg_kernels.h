@@ -43,6 +43,9 @@ __global__ void k_rank(BlockTab tab, const RepConst *rc, const RepState *st, con
 __global__ void k_build_nebr(const int *tileRep, const int *active, const int2 *heavy, int *work, const RepConst *rc, RepState *st,
                              const int *cellStart, const float4 *sortPos, int *nn, int *nbl, int *ns, int *sl,
                              int *nrl, int2 *rl, int rowStride, int nebrMax, int descending);
+__global__ void k_build_nebr_lanes(const int *tileRep, const int *active, const int2 *heavy, int *work, const RepConst *rc, RepState *st,
+                             const int *cellStart, const float4 *sortPos, int *nn, int *nbl, int *ns, int *sl,
+                             int *nrl, int2 *rl, int rowStride, int nebrMax, int descending);
 
 // ---- PLAIN force and step kernels ----
 __global__ void k_rho(BlockTab tab, const RepConst *rc, const float4 *pos, const int *nn,

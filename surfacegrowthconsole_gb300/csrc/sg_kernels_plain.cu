@@ -576,17 +576,16 @@ __device__ __forceinline__ void stIf2(bool p, int2 *a, int x, int y) {
                : "memory");
 }
 
-__global__ void __launch_bounds__(kNebrWarps * 32) k_build_nebr(const int *__restrict__ tileRep,
-                                                                const int *__restrict__ active,
-                                                                const int2 *__restrict__ heavy, int *work,
-                                                                const RepConst *__restrict__ rc, RepState *st,
-                                                                const int *__restrict__ cellStart,
-                                                                const float4 *__restrict__ sortPos,
-                                                                int *__restrict__ nn, int *__restrict__ nbl,
-                                                                int *__restrict__ ns, int *__restrict__ sl,
-                                                                int *__restrict__ nrl, int2 *__restrict__ rl,
-                                                                int rowStride, int nebrMax, int descending) {
-  pdlEnter();
+// LANE_EMIT: the emit pass with one lane per home atom walking its own hits (the lists are the
+// same; k_build_nebr_lanes), instead of the warp placing every word's hits cooperatively.
+template <bool LANE_EMIT>
+__device__ __forceinline__ void nebrBody(const int *__restrict__ tileRep, const int *__restrict__ active,
+                                         const int2 *__restrict__ heavy, int *work,
+                                         const RepConst *__restrict__ rc, RepState *st,
+                                         const int *__restrict__ cellStart, const float4 *__restrict__ sortPos,
+                                         int *__restrict__ nn, int *__restrict__ nbl, int *__restrict__ ns,
+                                         int *__restrict__ sl, int *__restrict__ nrl, int2 *__restrict__ rl,
+                                         int rowStride, int nebrMax, int descending) {
   __shared__ int sK[kNebrWarps][kWin];                 // atom index of each window position
   __shared__ uint2 sMask[kNebrWarps][kWin / 32][32];   // [word][home atom]: {hit, close}
   __shared__ unsigned sMetal[kNebrWarps][kWin / 32];   // [word]: candidate is a metal atom
@@ -706,6 +705,42 @@ __global__ void __launch_bounds__(kNebrWarps * 32) k_build_nebr(const int *__res
         }
         __syncwarp();
         // ---- emit pass
+        if constexpr (LANE_EMIT) {
+          // lane a walks the set bits of home atom a's masks, word by word: its entries in list
+          // order, with the same limits and the same close and relevant entries
+          if (lane < nh) {
+            const int g = ga;
+            int n = nMy, m = mMy, r = rMy;
+            int *row = nbl + (size_t)g * rowStride;
+            const bool carbonHome = g >= metalEnd;
+            int *srow = sl + (size_t)g * kShortMax;
+            int2 *rrow = rl + (size_t)g * kRelMax;
+            for (int i = 0; i < nw; i++) {
+              const uint2 hc = sMask[w][i][lane];
+              const unsigned metalW = sMetal[w][i];
+              unsigned bits = hc.x;
+              while (bits) {
+                const int b = __ffs(bits) - 1;
+                bits &= bits - 1;
+                const int k = sK[w][32 * i + b];
+                if (n < nebrMax) row[n] = k;
+                if (carbonHome) {
+                  const bool close = (hc.y >> b) & 1u;
+                  if (close) {
+                    if (m < kShortMax) srow[m] = k;
+                    m++;
+                  }
+                  if (close || ((metalW >> b) & 1u)) {
+                    if (r < kRelMax) rrow[r] = make_int2(k, n);
+                    r++;
+                  }
+                }
+                n++;
+              }
+            }
+            nMy = n; mMy = m; rMy = r;
+          }
+        } else {
         for (int a = 0; a < nh; a++) {
           const int g = __float_as_int(sHome[w][a].w);
           int n = __shfl_sync(full, nMy, a);
@@ -743,6 +778,7 @@ __global__ void __launch_bounds__(kNebrWarps * 32) k_build_nebr(const int *__res
           }
           nMy = (lane == a) ? n : nMy;
         }
+        }
         __syncwarp();
       }
       if (lane < nh) {
@@ -768,6 +804,25 @@ __global__ void __launch_bounds__(kNebrWarps * 32) k_build_nebr(const int *__res
     __syncwarp();
   }
 }
+
+#define SG_NEBR_PARAMS                                                                                 \
+  const int *__restrict__ tileRep, const int *__restrict__ active, const int2 *__restrict__ heavy,      \
+      int *work, const RepConst *__restrict__ rc, RepState *st, const int *__restrict__ cellStart,     \
+      const float4 *__restrict__ sortPos, int *__restrict__ nn, int *__restrict__ nbl,                 \
+      int *__restrict__ ns, int *__restrict__ sl, int *__restrict__ nrl, int2 *__restrict__ rl,        \
+      int rowStride, int nebrMax, int descending
+#define SG_NEBR_ARGS \
+  tileRep, active, heavy, work, rc, st, cellStart, sortPos, nn, nbl, ns, sl, nrl, rl, rowStride, nebrMax, descending
+__global__ void __launch_bounds__(kNebrWarps * 32) k_build_nebr(SG_NEBR_PARAMS) {
+  pdlEnter();
+  nebrBody<false>(SG_NEBR_ARGS);
+}
+__global__ void __launch_bounds__(kNebrWarps * 32) k_build_nebr_lanes(SG_NEBR_PARAMS) {
+  pdlEnter();
+  nebrBody<true>(SG_NEBR_ARGS);
+}
+#undef SG_NEBR_PARAMS
+#undef SG_NEBR_ARGS
 
 // The force passes (sg_forces.cuh) under their PLAIN names.
 }  // namespace sg

@@ -48,12 +48,13 @@ def _lists(p, r, v, **shape):
 
 @pytest.mark.parametrize("which", ["small", "production", "bulk"])
 def test_list_builds_and_shapes_change_nothing(which):
-    """Both list builds (cell windows in any grid, order and item size; atom threads) give the
-    same full, close and relevant lists."""
+    """The three list builds (cell windows with warp- or lane-placed hits in any grid, order and
+    item size; atom threads) give the same full, close and relevant lists."""
     p, r, v = {"small": lambda: workloads.small(seed=3), "production": lambda: workloads.production(seed=2, steps=10),
                "bulk": lambda: workloads.bulk_metal(8, 600.0, 7)}[which]()
     ref = _lists(p, r, v)
-    for kw in ({"nebr_atom_threads": 1}, {"nebr_blocks_per_sm": 1, "nebr_item_atoms": 16},
+    for kw in ({"nebr_build": 1}, {"nebr_build": 2}, {"nebr_build": 2, "nebr_item_atoms": 4, "nebr_descending": 1},
+               {"nebr_blocks_per_sm": 1, "nebr_item_atoms": 16},
                {"nebr_blocks_per_sm": 4, "nebr_descending": 1, "nebr_item_atoms": 4},
                {"nebr_blocks_per_sm": 32, "nebr_descending": 1, "nebr_item_atoms": 64}):
         got = _lists(p, r, v, **kw)
@@ -63,14 +64,14 @@ def test_list_builds_and_shapes_change_nothing(which):
 
 def test_bad_shapes_are_refused():
     p, r, v = workloads.small(seed=3)
-    for kw in ({"metal_lanes": 6}, {"nebr_blocks_per_sm": 33}, {"nebr_item_atoms": 3}):
+    for kw in ({"metal_lanes": 6}, {"nebr_blocks_per_sm": 33}, {"nebr_item_atoms": 3}, {"nebr_build": 3}):
         with pytest.raises(Exception):
             Simulation(p, **kw)
     sim = Simulation(p)
     with pytest.raises(Exception):
         sim.set_launch_shape({"metal_lanes": 64})
     assert sim.launch_shape() == {"metal_lanes": 16, "nebr_blocks_per_sm": 8, "nebr_descending": 0,
-                                  "nebr_item_atoms": 8, "programmatic_launch": 0, "nebr_atom_threads": 0,
+                                  "nebr_item_atoms": 8, "programmatic_launch": 0, "nebr_build": 0,
                                   "eam_table_smem": 0}
     sim.close()
 
@@ -86,7 +87,7 @@ def test_autotune_restores_the_state(mode):
     shape = tuned.launch_shape()
     assert shape == {f: rep[f] for f in Simulation.SHAPE_FIELDS}
     assert shape["metal_lanes"] in (4, 8, 16, 32) and shape["nebr_blocks_per_sm"] in (2, 4, 8, 16)
-    assert shape["nebr_item_atoms"] in (4, 6, 8, 16) and shape["nebr_atom_threads"] in (0, 1)
+    assert shape["nebr_item_atoms"] in (4, 6, 8, 16) and shape["nebr_build"] in (0, 1, 2)
     for k in ("4", "8", "16", "32"):
         assert rep["metal_lanes_ms_per_step"][k] > 0
     plain = Simulation(p, mode=mode)
