@@ -128,6 +128,8 @@ int sg_get_params(sg_ctx *ctx, int rep, sg_simparams *out);
  * reductions, nanoparticle diffusion sample, momentum/max-v2/Sum mv2, Berendsen thermostat,
  * potential energy, rebuild criterion, shear, RDF sample, property accumulation. */
 int sg_step(sg_ctx *ctx, int nsteps);
+/* Bytes sg_step copies back to the host after its steps (the replicas' state records). */
+long long sg_step_readback_bytes(const sg_ctx *ctx);
 /* The same steps, launched on the context's stream without waiting for them (no status from
  * the device is checked; call sg_step(ctx, 0) to synchronise and collect it). */
 int sg_step_async(sg_ctx *ctx, int nsteps);
@@ -158,6 +160,8 @@ typedef struct sg_thermo {
     sg_prop props[7];  /* totEnergy, potEnergy, kinEnergy, oneStep, centerOfMass, cmVel, frictForce */
 } sg_thermo;
 int sg_get_thermo(sg_ctx *ctx, int rep, sg_thermo *out);
+/* sg_step, then replica rep's thermo record (as sg_get_thermo) from the same synchronisation. */
+int sg_step_thermo(sg_ctx *ctx, int nsteps, int rep, sg_thermo *thermo);
 
 /* ---- single phases on the current state (parity checks, harness) ---------------------- */
 /* Cell binning + neighbour list from the current positions

@@ -317,7 +317,12 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
   if (c->opt.rdf_ext_bins > 0) AL(c->histExt, (size_t)n_replicas * c->opt.rdf_ext_bins);
   AL(c->diffBuf, std::max<size_t>(diffOff, 1));
   AL(c->dDiffOff, n_replicas);
-  AL(c->stage, 3 * N);
+  AL(c->stage, 6 * N);  // two float3 arrays in transit at once
+  if (cudaMallocHost(&c->hostSt, sizeof(RepState) * n_replicas) != cudaSuccess) {
+    c->hostSt = nullptr;
+    sg_destroy(c);
+    return sg_fail(SG_ERR_NOMEM, "cudaMallocHost(%zu)", sizeof(RepState) * n_replicas);
+  }
 #undef AL
   if (c->opt.phase_timing)
     for (auto &e : c->phaseEv) cudaEventCreate(&e);
@@ -425,6 +430,7 @@ extern "C" int sg_destroy(sg_ctx *c) {
   for (auto &e : c->phaseEv)
     if (e) cudaEventDestroy(e);
   for (void *p : c->allocs) cudaFree(p);
+  if (c->hostSt) cudaFreeHost(c->hostSt);
   if (c->side) cudaStreamSynchronize(c->side);
   if (c->evFork) cudaEventDestroy(c->evFork);
   if (c->evJoin) cudaEventDestroy(c->evJoin);
@@ -455,9 +461,11 @@ static int repRange(sg_ctx *c, int rep, int &off, int &n) {
 // Host float4 arrays have the device layout and are copied directly; float3 arrays go through
 // a device staging buffer and a widening kernel.  With pinned host buffers every copy is a
 // single DMA transfer.
-static int upload3(sg_ctx *c, const sg_float3 *h, float4 *d, int n) {
-  CK(cudaMemcpyAsync(c->stage, h, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-  k_unpack3<<<(n + 255) / 256, 256, 0, c->stream>>>(c->stage, d, n);
+// slot 0 or 1: which half of the staging buffer (3 floats per atom each)
+static int upload3(sg_ctx *c, const sg_float3 *h, float4 *d, int n, int slot = 0) {
+  float *st = c->stage + (size_t)slot * 3 * c->ntot;
+  CK(cudaMemcpyAsync(st, h, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  k_unpack3<<<(n + 255) / 256, 256, 0, c->stream>>>(st, d, n);
   CK(cudaGetLastError());
   return SG_OK;
 }
@@ -477,9 +485,8 @@ extern "C" int sg_set_state(sg_ctx *c, int rep, const sg_float4 *r, const sg_flo
     CK(cudaMemcpyAsync(c->pos + off, r, (size_t)n * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
     if (c->posLo) CK(cudaMemsetAsync(c->posLo + off, 0, (size_t)n * sizeof(float4), c->stream));
   }
-  if (v && (rc = upload3(c, v, c->vel + off, n))) return rc;
-  if (v) CK(cudaStreamSynchronize(c->stream));  // the staging buffer is reused below
-  if (a && (rc = upload3(c, a, c->acc + off, n))) return rc;
+  if (v && (rc = upload3(c, v, c->vel + off, n, 0))) return rc;
+  if (a && (rc = upload3(c, a, c->acc + off, n, 1))) return rc;
   // a new state cancels any thermostat rescale still pending from the previous step
   k_clear_pending<<<(c->nrep + 127) / 128, 128, 0, c->stream>>>(c->st, c->nrep);
   CK(cudaGetLastError());
@@ -711,6 +718,16 @@ static int checkFlags(sg_ctx *c) {
   return SG_OK;
 }
 
+static void thermoFromState(sg_ctx *c, int rep, const RepState &S, sg_thermo *t);
+
+// Flags of the replica states already copied to the host mirror: status, clearing them on the
+// device (rare) as checkFlags does.
+static int flagsFromMirror(sg_ctx *c) {
+  int flags = 0;
+  for (int r = 0; r < c->nrep; r++) flags |= c->hostSt[r].flags;
+  return flags ? checkFlags(c) : SG_OK;
+}
+
 extern "C" int sg_step(sg_ctx *c, int nsteps) {
   if (!c) return sg_fail(SG_ERR_INVALID, "null context");
   for (int s = 0; s < nsteps; s++) {
@@ -719,8 +736,22 @@ extern "C" int sg_step(sg_ctx *c, int nsteps) {
     if (rc) return rc;
     advanceSchedule(c, v, nullptr);
   }
+  // the replica states come back in the same synchronisation (flags, and sg_step_thermo's record)
+  CK(cudaMemcpyAsync(c->hostSt, c->st, sizeof(RepState) * c->nrep, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
-  return checkFlags(c);
+  return flagsFromMirror(c);
+}
+
+extern "C" long long sg_step_readback_bytes(const sg_ctx *c) {
+  return c ? (long long)sizeof(RepState) * c->nrep : 0;
+}
+
+extern "C" int sg_step_thermo(sg_ctx *c, int nsteps, int rep, sg_thermo *t) {
+  if (!c || !t || rep < 0 || rep >= c->nrep) return sg_fail(SG_ERR_INVALID, "sg_step_thermo: bad arguments");
+  const int rc = sg_step(c, nsteps);
+  if (rc) return rc;
+  thermoFromState(c, rep, c->hostSt[rep], t);
+  return SG_OK;
 }
 
 extern "C" int sg_kernels_per_step(sg_ctx *c) {
@@ -807,6 +838,11 @@ extern "C" int sg_get_thermo(sg_ctx *c, int rep, sg_thermo *t) {
   RepState S;
   int rc = sg_read_state(c, rep, &S);
   if (rc) return rc;
+  thermoFromState(c, rep, S, t);
+  return SG_OK;
+}
+
+static void thermoFromState(sg_ctx *c, int rep, const RepState &S, sg_thermo *t) {
   memset(t, 0, sizeof(*t));
   t->stepCount = S.stepCount;
   t->nebrNow = S.nebrNow;
@@ -829,7 +865,6 @@ extern "C" int sg_get_thermo(sg_ctx *c, int rep, sg_thermo *t) {
   t->virial64 = S.virial64;
   for (int k = 0; k < 7; k++) t->props[k] = sg_prop{S.props[k][0], S.props[k][1], S.props[k][2]};
   t->props[3] = c->oneStep[rep];
-  return SG_OK;
 }
 
 extern "C" int sg_get_params(sg_ctx *c, int rep, sg_simparams *out) {

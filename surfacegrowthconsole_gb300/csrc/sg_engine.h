@@ -75,7 +75,8 @@ struct sg_ctx {
   int countRdf = 0;
   std::vector<sg_prop> oneStep;  // per replica, host-accumulated step times
   void *mixed = nullptr;         // MIXED-mode buffers (sg_kernels_mixed.cu)
-  float *stage = nullptr;        // 3 floats per atom: host float3 arrays in transit
+  float *stage = nullptr;        // 6 floats per atom: two host float3 arrays in transit
+  RepState *hostSt = nullptr;    // pinned host mirror of the replica states (read with sg_step)
   cudaEvent_t phaseEv[9] = {};   // phase boundaries of a step (phase_timing)
   cudaStream_t side = nullptr;   // second stream: the metal force chain runs beside the carbon pass
   cudaEvent_t evFork = nullptr, evJoin = nullptr;

@@ -187,6 +187,15 @@ class Simulation:
             check(-n)
         return out[:n]
 
+    def step_thermo(self, nsteps: int = 1, rep: int = 0) -> Thermo:
+        """nsteps steps and replica rep's thermo record, with one synchronisation."""
+        t = Thermo()
+        check(lib().sg_step_thermo(self._h, nsteps, rep, C.byref(t)))
+        return t
+
+    def step_readback_bytes(self) -> int:
+        return int(lib().sg_step_readback_bytes(self._h))
+
     def thermo(self, rep: int = 0) -> Thermo:
         t = Thermo()
         check(lib().sg_get_thermo(self._h, rep, C.byref(t)))
