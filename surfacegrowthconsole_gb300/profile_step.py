@@ -8,8 +8,8 @@ of its fields, e.g. the one the benchmark's autotuning chose; default: the libra
 defaults), steps it `warmup` times (graph capture, caches), then runs `steps` steps
 between cudaProfilerStart and cudaProfilerStop, so that a profiler started with its
 from-start profiling off (ncu --profile-from-start off) sees exactly those steps' kernels.
-Lists are rebuilt every step, as in the production benchmark.  Prints the kernel launches per
-step.
+Lists are rebuilt every step for the production workload (as its benchmark does) and by the
+reference's rule for the others.  Prints the kernel launches per step.
 """
 from __future__ import annotations
 
@@ -54,7 +54,8 @@ def main() -> None:
         r = np.concatenate([w[1] for w in reps])
         v = np.concatenate([w[2] for w in reps])
     n = int(sum(q.nMol for q in plist))
-    sim = Simulation(plist, mode=MODE_MIXED if a.mode == "mixed" else MODE_PLAIN, force_rebuild=True)
+    sim = Simulation(plist, mode=MODE_MIXED if a.mode == "mixed" else MODE_PLAIN,
+                     force_rebuild=a.workload == "production")
     sim.set_state(r, v, np.zeros((n, 3), np.float32))
     if a.shape:
         sim.set_launch_shape(json.loads(a.shape))
