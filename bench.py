@@ -14,7 +14,8 @@ LJ, graphene, reductions, thermostat, RDF/diffusion when due).
   nve_drift : the total-energy drift of both forms on bulk Ni (4,000 atoms, 300 K, 10 ps NVE),
           the "stated drift" the two forms are compared at.
   e2e   : the same metric through the public C ABI with host buffers: every step uploads the
-          state (r, v, a) from pinned host memory, steps, and reads the step's thermo record.
+          state (r, v, a) from pinned host memory, steps, and reads the step's thermo record, in
+          one sg_step_from_host call (one synchronisation per step).
   roofline : the neighbour-list build (the largest share of the step): its compulsory bytes per
           launch / its mean duration (CUDA events around it on the library's stream), against
           the measured HBM copy peak.  The phase durations come from a second pass of the same
@@ -508,8 +509,9 @@ def run_production(args, rank: int, world: int, local: int, dist):
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        sim.set_state(hr, hv, ha)   # r, v, a from pinned host memory
-        th = sim.step_thermo(1)     # one step, the state record back in the same synchronisation
+        # r, v, a from pinned host memory, one step, the thermo record back: one call, one
+        # synchronisation (sg_step_from_host)
+        th = sim.step_from_host(hr, hv, ha, nsteps=1)
     barrier()
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     e2e = {"value": atoms_all * e2e_steps / e2e_s, "unit": "atom-steps/s",

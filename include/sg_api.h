@@ -162,6 +162,12 @@ typedef struct sg_thermo {
 int sg_get_thermo(sg_ctx *ctx, int rep, sg_thermo *out);
 /* sg_step, then replica rep's thermo record (as sg_get_thermo) from the same synchronisation. */
 int sg_step_thermo(sg_ctx *ctx, int nsteps, int rep, sg_thermo *thermo);
+/* A step from host buffers in one call: sg_set_state(ctx, rep, r, v, a), then sg_step(ctx,
+ * nsteps) and, if thermo is not NULL, replica thermo_rep's record, with one synchronisation
+ * for the whole (the copies are enqueued on the context's stream ahead of the steps; the host
+ * buffers are free again when the call returns).  Results equal those of the three calls. */
+int sg_step_from_host(sg_ctx *ctx, int rep, const sg_float4 *r, const sg_float3 *v, const sg_float3 *a,
+                      int nsteps, int thermo_rep, sg_thermo *thermo);
 
 /* ---- single phases on the current state (parity checks, harness) ---------------------- */
 /* Cell binning + neighbour list from the current positions

@@ -214,6 +214,8 @@ _SIGS = {
     "sg_compute_forces_noalloc": (C.c_int, [C.POINTER(SimParams), C.c_void_p, C.c_void_p, C.c_void_p]),
     "sg_autotune": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p, C.c_int]),
     "sg_step_thermo": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
+    "sg_step_from_host": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                    C.c_void_p]),
     "sg_step_readback_bytes": (C.c_longlong, [C.c_void_p]),
     "sg_get_launch_shape": (C.c_int, [C.c_void_p, C.POINTER(LaunchShape)]),
     "sg_set_launch_shape": (C.c_int, [C.c_void_p, C.POINTER(LaunchShape)]),

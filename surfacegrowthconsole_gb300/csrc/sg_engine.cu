@@ -462,13 +462,6 @@ static int repRange(sg_ctx *c, int rep, int &off, int &n) {
 // a device staging buffer and a widening kernel.  With pinned host buffers every copy is a
 // single DMA transfer.
 // slot 0 or 1: which half of the staging buffer (3 floats per atom each)
-static int upload3(sg_ctx *c, const sg_float3 *h, float4 *d, int n, int slot = 0) {
-  float *st = c->stage + (size_t)slot * 3 * c->ntot;
-  CK(cudaMemcpyAsync(st, h, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-  k_unpack3<<<(n + 255) / 256, 256, 0, c->stream>>>(st, d, n);
-  CK(cudaGetLastError());
-  return SG_OK;
-}
 static int download3(sg_ctx *c, const float4 *d, sg_float3 *h, int n) {
   k_pack3<<<(n + 255) / 256, 256, 0, c->stream>>>(d, c->stage, n);
   CK(cudaGetLastError());
@@ -477,19 +470,29 @@ static int download3(sg_ctx *c, const float4 *d, sg_float3 *h, int n) {
   return SG_OK;
 }
 
-extern "C" int sg_set_state(sg_ctx *c, int rep, const sg_float4 *r, const sg_float3 *v, const sg_float3 *a) {
-  if (!c) return sg_fail(SG_ERR_INVALID, "null context");
+// A state upload, enqueued: r straight into pos, v and a through the staging buffer and one
+// unpack kernel (which also clears the low position words and cancels any thermostat rescale
+// still pending from the previous step).  The host buffers must stay valid until the stream
+// has passed the copies.
+static int enqueueSetState(sg_ctx *c, int rep, const sg_float4 *r, const sg_float3 *v, const sg_float3 *a) {
   int off, n, rc;
   if ((rc = repRange(c, rep, off, n))) return rc;
-  if (r) {
-    CK(cudaMemcpyAsync(c->pos + off, r, (size_t)n * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
-    if (c->posLo) CK(cudaMemsetAsync(c->posLo + off, 0, (size_t)n * sizeof(float4), c->stream));
-  }
-  if (v && (rc = upload3(c, v, c->vel + off, n, 0))) return rc;
-  if (a && (rc = upload3(c, a, c->acc + off, n, 1))) return rc;
-  // a new state cancels any thermostat rescale still pending from the previous step
-  k_clear_pending<<<(c->nrep + 127) / 128, 128, 0, c->stream>>>(c->st, c->nrep);
+  float *sv = v ? c->stage : nullptr, *sa = a ? c->stage + 3 * (size_t)c->ntot : nullptr;
+  if (r) CK(cudaMemcpyAsync(c->pos + off, r, (size_t)n * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
+  if (v) CK(cudaMemcpyAsync(sv, v, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  if (a) CK(cudaMemcpyAsync(sa, a, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  const int m = std::max(n, c->nrep);
+  k_unpack_state<<<(m + 255) / 256, 256, 0, c->stream>>>(sv, sa, c->vel + off, c->acc + off,
+                                                         (r && c->posLo) ? c->posLo + off : nullptr, n, c->st,
+                                                         c->nrep);
   CK(cudaGetLastError());
+  return SG_OK;
+}
+
+extern "C" int sg_set_state(sg_ctx *c, int rep, const sg_float4 *r, const sg_float3 *v, const sg_float3 *a) {
+  if (!c) return sg_fail(SG_ERR_INVALID, "null context");
+  const int rc = enqueueSetState(c, rep, r, v, a);
+  if (rc) return rc;
   CK(cudaStreamSynchronize(c->stream));
   return SG_OK;
 }
@@ -751,6 +754,18 @@ extern "C" int sg_step_thermo(sg_ctx *c, int nsteps, int rep, sg_thermo *t) {
   const int rc = sg_step(c, nsteps);
   if (rc) return rc;
   thermoFromState(c, rep, c->hostSt[rep], t);
+  return SG_OK;
+}
+
+extern "C" int sg_step_from_host(sg_ctx *c, int rep, const sg_float4 *r, const sg_float3 *v, const sg_float3 *a,
+                                 int nsteps, int thermo_rep, sg_thermo *t) {
+  if (!c || (t && (thermo_rep < 0 || thermo_rep >= c->nrep)) || nsteps < 0)
+    return sg_fail(SG_ERR_INVALID, "sg_step_from_host: bad arguments");
+  int rc = enqueueSetState(c, rep, r, v, a);
+  if (rc) return rc;
+  // the upload, the steps and the state records back in one synchronisation
+  if ((rc = sg_step(c, nsteps))) return rc;
+  if (t) thermoFromState(c, thermo_rep, c->hostSt[thermo_rep], t);
   return SG_OK;
 }
 

@@ -1547,6 +1547,19 @@ __global__ void k_pack3(const float4 *src, float *dst, int n) {
   }
 }
 
+// A state upload's device half: v and a (host float3 rows, staged) to float4, the low position
+// words cleared (MIXED), and any pending thermostat rescale of every replica cancelled.
+__global__ void k_unpack_state(const float *sv, const float *sa, float4 *vel, float4 *acc, float4 *posLo,
+                               int n, RepState *st, int nrep) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    if (sv) vel[i] = make_float4(sv[3 * i], sv[3 * i + 1], sv[3 * i + 2], 0.f);
+    if (sa) acc[i] = make_float4(sa[3 * i], sa[3 * i + 1], sa[3 * i + 2], 0.f);
+    if (posLo) posLo[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  if (i < nrep) st[i].thermoPending = 0;
+}
+
 __global__ void k_clear_pending(RepState *st, int nrep) {
   pdlEnter();
   const int r = blockIdx.x * blockDim.x + threadIdx.x;

@@ -141,8 +141,7 @@ class Simulation:
         return lib().sg_num_atoms(self._h, rep)
 
     # -- state
-    def set_state(self, r: np.ndarray | None, v: np.ndarray | None = None, a: np.ndarray | None = None,
-                  rep: int = -1) -> None:
+    def _state_args(self, r, v, a, rep):
         n = self.natoms(rep)
         def prep(x, w):
             if x is None:
@@ -151,8 +150,23 @@ class Simulation:
             if x.shape != (n, w):
                 raise ValueError(f"expected shape {(n, w)}, got {x.shape}")
             return x
-        r_, v_, a_ = prep(r, 4), prep(v, 3), prep(a, 3)
+        return prep(r, 4), prep(v, 3), prep(a, 3)
+
+    def set_state(self, r: np.ndarray | None, v: np.ndarray | None = None, a: np.ndarray | None = None,
+                  rep: int = -1) -> None:
+        r_, v_, a_ = self._state_args(r, v, a, rep)
         check(lib().sg_set_state(self._h, rep, _ptr(r_), _ptr(v_), _ptr(a_)))
+
+    def step_from_host(self, r: np.ndarray | None, v: np.ndarray | None = None, a: np.ndarray | None = None,
+                       nsteps: int = 1, rep: int = -1, thermo_rep: int | None = 0) -> Thermo | None:
+        """set_state(r, v, a, rep), nsteps steps and replica thermo_rep's thermo record (None:
+        no record) in one call with one synchronisation (sg_step_from_host)."""
+        r_, v_, a_ = self._state_args(r, v, a, rep)
+        t = Thermo() if thermo_rep is not None else None
+        check(lib().sg_step_from_host(self._h, rep, _ptr(r_), _ptr(v_), _ptr(a_), nsteps,
+                                      0 if thermo_rep is None else thermo_rep,
+                                      C.byref(t) if t is not None else None))
+        return t
 
     def get_state(self, rep: int = -1):
         n = self.natoms(rep)

@@ -1,5 +1,6 @@
-"""The host-buffer calls of the sg_* C ABI: state uploads and downloads round-trip exactly, and
-sg_step_thermo's record is the one sg_get_thermo reads after sg_step."""
+"""The host-buffer calls of the sg_* C ABI: state uploads and downloads round-trip exactly,
+sg_step_thermo's record is the one sg_get_thermo reads after sg_step, and sg_step_from_host is
+sg_set_state + sg_step + that record."""
 import numpy as np
 import pytest
 
@@ -54,5 +55,53 @@ def test_step_thermo_is_step_then_thermo(mode):
         else:
             assert x == y, f
     assert one.step_readback_bytes() > 0
+    one.close()
+    two.close()
+
+
+def _same_thermo(t1, t2):
+    for f, _ in t1._fields_:
+        if f == "props":
+            continue
+        x, y = getattr(t1, f), getattr(t2, f)
+        if hasattr(x, "x"):
+            assert (x.x, x.y, x.z) == (y.x, y.y, y.z), f
+        else:
+            assert x == y, f
+
+
+@pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_MIXED])
+def test_step_from_host_is_set_state_then_step(mode):
+    """One replica or all at once: the same states and thermo records as sg_set_state followed by
+    sg_step / sg_step_thermo, over several calls in a row."""
+    reps = [workloads.small(seed=s) for s in (64, 65)]
+    plist = [w[0] for w in reps]
+    r_all = np.concatenate([w[1] for w in reps])
+    v_all = np.concatenate([w[2] for w in reps])
+    rng = np.random.RandomState(9)
+    a_all = rng.normal(scale=0.01, size=(len(r_all), 3)).astype(np.float32)
+    one = Simulation(plist, mode=mode)
+    two = Simulation(plist, mode=mode)
+    for sim in (one, two):
+        sim.set_state(r_all, v_all, a_all)
+        sim.step(24)
+    r1, v1, a1 = one.get_state(1)
+    r1 = r1.copy()
+    r1[:, :3] += rng.normal(scale=1e-3, size=(len(r1), 3)).astype(np.float32)
+    for k in range(3):
+        t1 = one.step_from_host(r1, v1, a1, nsteps=3, rep=1, thermo_rep=1)
+        two.set_state(r1, v1, a1, rep=1)
+        t2 = two.step_thermo(3, rep=1)
+        _same_thermo(t1, t2)
+        for x, y in zip(one.get_state(), two.get_state()):
+            assert np.array_equal(x, y)
+        r1, v1, a1 = one.get_state(1)
+    ra, va, aa = one.get_state()
+    assert one.step_from_host(ra, va, aa, nsteps=2, thermo_rep=None) is None
+    two.set_state(ra, va, aa)
+    two.step(2)
+    for x, y in zip(one.get_state(), two.get_state()):
+        assert np.array_equal(x, y)
+    _same_thermo(one.thermo(0), two.thermo(0))
     one.close()
     two.close()
