@@ -553,7 +553,8 @@ __global__ void k_rank_cells(BlockTab tab, const RepConst *__restrict__ rc, RepS
 //    give the word's "within the list radius" and "within rCutC + skin" masks of each home
 //    atom, kept in shared memory with the word's "metal candidate" mask.  Words without a
 //    periodic shift that cannot hold a home atom take a loop without the shift and the
-//    self-pair test (subtracting a zero shift changes no bit).
+//    self-pair test (subtracting a zero shift changes no bit).  Each lane loads its candidate
+//    of the next word while the current word is tested.
 //  Emit pass: per home atom and word with hits, lane l places candidate l at its rank among
 //    the word's set bits, so consecutive entries of the atom's row nbl[g*rowStride + j] come
 //    from one coalesced store; for a carbon atom the same ranks place its close list (entries
@@ -658,18 +659,36 @@ __device__ __forceinline__ void nebrBody(const int *__restrict__ tileRep, const 
       for (int base = 0; base < total; base += kWin) {
         const int nw = (min(kWin, total - base) + 31) >> 5;
         // ---- test pass
+        // this lane's candidate of the next word (window position eN, stencil cell oN: the last
+        // one whose segment starts at or before eN), loaded while the current word is tested
+        int oN = 0;
+        float4 BN = make_float4(0.f, 0.f, 0.f, 0.f);
+        {
+          const int eN = base + lane;
+          if (eN < total) {
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1)
+              if (oN + step < 27 && sOff[w][oN + step] <= eN) oN += step;
+            BN = sortPos[sQb[w][oN] + eN - sOff[w][oN]];
+          }
+        }
         for (int i = 0; i < nw; i++) {
           const int e = base + 32 * i + lane;
+          const int o = oN;
+          const float4 B = BN;
+          if (i + 1 < nw && e + 32 < total) {
+            const int eN = e + 32;
+            oN = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1)
+              if (oN + step < 27 && sOff[w][oN + step] <= eN) oN += step;
+            BN = sortPos[sQb[w][oN] + eN - sOff[w][oN]];
+          }
           // this lane's candidate; past the window end it sits at 1e30 and never matches
           float bx = 1e30f, by = 1e30f, bz = 1e30f, sx = 0.f, sy = 0.f, sz = 0.f;
           int k = -1;
           bool shifted = false;
           if (e < total) {
-            int o = 0;  // the last stencil cell whose segment starts at or before e
-#pragma unroll
-            for (int step = 16; step > 0; step >>= 1)
-              if (o + step < 27 && sOff[w][o + step] <= e) o += step;
-            const float4 B = sortPos[sQb[w][o] + e - sOff[w][o]];
             k = __float_as_int(B.w);
             bx = B.x; by = B.y; bz = B.z;
             const float4 sh = sSh[w][o];
