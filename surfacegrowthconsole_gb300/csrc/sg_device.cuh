@@ -43,6 +43,7 @@ constexpr int kScanCells = 512;   // cells per block of the single-pass cell sca
 constexpr int kScanThreads = 128;
 constexpr int kMixThreads = 128;  // MIXED step reduction: threads per block
 constexpr int kMixAtoms = 256;    // and atoms per block (2 per thread)
+constexpr int kUnpackAtoms = 256; // state upload: atoms (threads) per block
 constexpr int kMinItemAtoms = 4;  // smallest home atoms per work item the engine allows
 constexpr int kItemAtoms = 8;     // the engine's default home atoms per work item
 constexpr int kMetalPerBlock = 128 / kMT;   // atoms per 128-thread block

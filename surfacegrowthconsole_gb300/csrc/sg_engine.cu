@@ -470,21 +470,43 @@ static int download3(sg_ctx *c, const float4 *d, sg_float3 *h, int n) {
   return SG_OK;
 }
 
-// A state upload, enqueued: r straight into pos, v and a through the staging buffer and one
-// unpack kernel (which also clears the low position words and cancels any thermostat rescale
-// still pending from the previous step).  The host buffers must stay valid until the stream
-// has passed the copies.
+// The device address of a host array the GPU can read in place (page-locked, mapped into the
+// unified address space: cudaMallocHost, cudaHostAlloc, cudaHostRegister), else nullptr.
+static const void *mappedHost(const void *h) {
+  if (!h) return nullptr;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, h) != cudaSuccess) {
+    cudaGetLastError();  // not a pointer the runtime knows: an ordinary host array
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
+// A state upload, enqueued.  Host arrays in page-locked memory are read in place by one kernel
+// (over the host link, without a copy-engine transfer per array); others are copied first, r
+// straight into pos, v and a into the staging buffer.  The same kernel unpacks v and a to
+// float4, clears the low position words and cancels any thermostat rescale still pending from
+// the previous step.  The host arrays must stay valid until the stream has passed the kernel.
 static int enqueueSetState(sg_ctx *c, int rep, const sg_float4 *r, const sg_float3 *v, const sg_float3 *a) {
   int off, n, rc;
   if ((rc = repRange(c, rep, off, n))) return rc;
-  float *sv = v ? c->stage : nullptr, *sa = a ? c->stage + 3 * (size_t)c->ntot : nullptr;
-  if (r) CK(cudaMemcpyAsync(c->pos + off, r, (size_t)n * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
-  if (v) CK(cudaMemcpyAsync(sv, v, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-  if (a) CK(cudaMemcpyAsync(sa, a, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  const float4 *sr = static_cast<const float4 *>(mappedHost(r));
+  const float *sv = static_cast<const float *>(mappedHost(v));
+  const float *sa = static_cast<const float *>(mappedHost(a));
+  if (r && !sr) CK(cudaMemcpyAsync(c->pos + off, r, (size_t)n * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
+  if (v && !sv) {
+    CK(cudaMemcpyAsync(c->stage, v, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    sv = c->stage;
+  }
+  if (a && !sa) {
+    float *st = c->stage + 3 * (size_t)c->ntot;
+    CK(cudaMemcpyAsync(st, a, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    sa = st;
+  }
   const int m = std::max(n, c->nrep);
-  k_unpack_state<<<(m + 255) / 256, 256, 0, c->stream>>>(sv, sa, c->vel + off, c->acc + off,
-                                                         (r && c->posLo) ? c->posLo + off : nullptr, n, c->st,
-                                                         c->nrep);
+  k_unpack_state<<<(m + kUnpackAtoms - 1) / kUnpackAtoms, kUnpackAtoms, 0, c->stream>>>(
+      sr, sv, sa, c->pos + off, c->vel + off, c->acc + off, (r && c->posLo) ? c->posLo + off : nullptr, n, c->st,
+      c->nrep);
   CK(cudaGetLastError());
   return SG_OK;
 }

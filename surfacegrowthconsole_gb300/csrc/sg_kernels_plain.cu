@@ -1566,14 +1566,40 @@ __global__ void k_pack3(const float4 *src, float *dst, int n) {
   }
 }
 
-// A state upload's device half: v and a (host float3 rows, staged) to float4, the low position
-// words cleared (MIXED), and any pending thermostat rescale of every replica cancelled.
-__global__ void k_unpack_state(const float *sv, const float *sa, float4 *vel, float4 *acc, float4 *posLo,
-                               int n, RepState *st, int nrep) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+// Floats [3 a0, 3 min(n, a0 + kUnpackAtoms)) of a float3 array into shared memory, read as
+// float4 where the array is 16-byte aligned (3 a0 is a multiple of 4), each float once.
+__device__ __forceinline__ void stageRows3(const float *src, int n, int a0, float *sm) {
+  const int f0 = 3 * a0, f1 = 3 * min(n, a0 + kUnpackAtoms);
+  const bool aligned = (reinterpret_cast<uintptr_t>(src) & 15) == 0;
+  for (int q = threadIdx.x; 4 * q < f1 - f0; q += blockDim.x) {
+    const int f = f0 + 4 * q;
+    if (aligned && f + 4 <= f1) {
+      const float4 x = reinterpret_cast<const float4 *>(src)[f >> 2];
+      sm[4 * q] = x.x; sm[4 * q + 1] = x.y; sm[4 * q + 2] = x.z; sm[4 * q + 3] = x.w;
+    } else {
+      for (int k = 0; k < 4 && f + k < f1; k++) sm[4 * q + k] = src[f + k];
+    }
+  }
+}
+
+// A state upload's device half, kUnpackAtoms atoms per block: r (sr, when the host array is
+// mapped) to pos, v and a (host float3 rows, mapped or staged) to float4 through shared
+// memory (coalesced reads over the host link), the low position words cleared (MIXED), and any
+// pending thermostat rescale of every replica cancelled.
+__global__ void __launch_bounds__(kUnpackAtoms) k_unpack_state(const float4 *sr, const float *sv, const float *sa,
+                                                               float4 *pos, float4 *vel, float4 *acc, float4 *posLo,
+                                                               int n, RepState *st, int nrep) {
+  __shared__ float sV[3 * kUnpackAtoms], sA[3 * kUnpackAtoms];
+  const int a0 = blockIdx.x * kUnpackAtoms, t = threadIdx.x, i = a0 + t;
+  if (a0 < n) {
+    if (sv) stageRows3(sv, n, a0, sV);
+    if (sa) stageRows3(sa, n, a0, sA);
+  }
+  __syncthreads();
   if (i < n) {
-    if (sv) vel[i] = make_float4(sv[3 * i], sv[3 * i + 1], sv[3 * i + 2], 0.f);
-    if (sa) acc[i] = make_float4(sa[3 * i], sa[3 * i + 1], sa[3 * i + 2], 0.f);
+    if (sr) pos[i] = sr[i];
+    if (sv) vel[i] = make_float4(sV[3 * t], sV[3 * t + 1], sV[3 * t + 2], 0.f);
+    if (sa) acc[i] = make_float4(sA[3 * t], sA[3 * t + 1], sA[3 * t + 2], 0.f);
     if (posLo) posLo[i] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   if (i < nrep) st[i].thermoPending = 0;

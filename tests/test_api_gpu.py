@@ -10,20 +10,31 @@ from surfacegrowthconsole_gb300.engine import Simulation
 pytestmark = pytest.mark.gpu
 
 
+def _pinned(x):
+    """A page-locked copy of x (the upload kernel reads such arrays in place)."""
+    torch = pytest.importorskip("torch")
+    y = torch.empty(x.shape, dtype=torch.float32, pin_memory=True).numpy()
+    y[:] = x
+    return y
+
+
+@pytest.mark.parametrize("pinned", [False, True])
 @pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_MIXED])
-def test_state_round_trip(mode):
+def test_state_round_trip(mode, pinned):
     reps = [workloads.small(seed=s) for s in (61, 62)]
     plist = [w[0] for w in reps]
     sim = Simulation(plist, mode=mode)
     rng = np.random.RandomState(5)
+    host = _pinned if pinned else (lambda x: x)
     for k, (q, r, v) in enumerate(reps):  # one replica at a time
         a = rng.normal(size=(q.nMol, 3)).astype(np.float32)
+        r, v, a = host(r), host(v), host(a)
         sim.set_state(r, v, a, rep=k)
         rg, vg, ag = sim.get_state(k)
         assert np.array_equal(rg, r) and np.array_equal(vg, v) and np.array_equal(ag, a)
-    r_all = np.concatenate([w[1] for w in reps])
-    v_all = np.concatenate([w[2] for w in reps])
-    a_all = rng.normal(size=(len(r_all), 3)).astype(np.float32)
+    r_all = host(np.concatenate([w[1] for w in reps]))
+    v_all = host(np.concatenate([w[2] for w in reps]))
+    a_all = host(rng.normal(size=(len(r_all), 3)).astype(np.float32))
     sim.set_state(r_all, v_all, a_all)  # all replicas at once
     off = 0
     for k, (q, _, _) in enumerate(reps):
@@ -70,8 +81,9 @@ def _same_thermo(t1, t2):
             assert x == y, f
 
 
+@pytest.mark.parametrize("pinned", [False, True])
 @pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_MIXED])
-def test_step_from_host_is_set_state_then_step(mode):
+def test_step_from_host_is_set_state_then_step(mode, pinned):
     """One replica or all at once: the same states and thermo records as sg_set_state followed by
     sg_step / sg_step_thermo, over several calls in a row."""
     reps = [workloads.small(seed=s) for s in (64, 65)]
@@ -85,10 +97,12 @@ def test_step_from_host_is_set_state_then_step(mode):
     for sim in (one, two):
         sim.set_state(r_all, v_all, a_all)
         sim.step(24)
+    host = _pinned if pinned else (lambda x: x)
     r1, v1, a1 = one.get_state(1)
     r1 = r1.copy()
     r1[:, :3] += rng.normal(scale=1e-3, size=(len(r1), 3)).astype(np.float32)
     for k in range(3):
+        r1, v1, a1 = host(r1), host(v1), host(a1)
         t1 = one.step_from_host(r1, v1, a1, nsteps=3, rep=1, thermo_rep=1)
         two.set_state(r1, v1, a1, rep=1)
         t2 = two.step_thermo(3, rep=1)
@@ -96,7 +110,7 @@ def test_step_from_host_is_set_state_then_step(mode):
         for x, y in zip(one.get_state(), two.get_state()):
             assert np.array_equal(x, y)
         r1, v1, a1 = one.get_state(1)
-    ra, va, aa = one.get_state()
+    ra, va, aa = (host(x) for x in one.get_state())
     assert one.step_from_host(ra, va, aa, nsteps=2, thermo_rep=None) is None
     two.set_state(ra, va, aa)
     two.step(2)
