@@ -577,8 +577,10 @@ __device__ __forceinline__ void stIf2(bool p, int2 *a, int x, int y) {
                : "memory");
 }
 
-// LANE_EMIT: the emit pass with one lane per home atom walking its own hits (the lists are the
-// same; k_build_nebr_lanes), instead of the warp placing every word's hits cooperatively.
+// LANE_EMIT: the emit pass with lanes walking the hits of one home atom each (the lists are
+// the same; k_build_nebr_lanes), instead of the warp placing every word's hits cooperatively:
+// G = 32 / nh' lanes per home atom (nh' = nh rounded up to a power of two), lane q of a group
+// taking a contiguous share of the window's words after the hits of the group's earlier lanes.
 template <bool LANE_EMIT>
 __device__ __forceinline__ void nebrBody(const int *__restrict__ tileRep, const int *__restrict__ active,
                                          const int2 *__restrict__ heavy, int *work,
@@ -725,17 +727,42 @@ __device__ __forceinline__ void nebrBody(const int *__restrict__ tileRep, const 
         __syncwarp();
         // ---- emit pass
         if constexpr (LANE_EMIT) {
-          // lane a walks the set bits of home atom a's masks, word by word: its entries in list
-          // order, with the same limits and the same close and relevant entries
-          if (lane < nh) {
-            const int g = ga;
-            int n = nMy, m = mMy, r = rMy;
+          // lane q of home atom a's group walks the set bits of a's masks in words [i0, i1):
+          // its share of a's entries in list order, with the same limits and the same close and
+          // relevant entries; the group's exclusive prefix of the hit counts places them
+          const int lg = 32 - __clz(nh - 1);  // log2 of nh rounded up to a power of two
+          const int G = 32 >> lg;
+          const int a = lane >> (5 - lg), q = lane & (G - 1);
+          const int i0 = q * nw / G, i1 = (q + 1) * nw / G;
+          int cn = 0, cm = 0, cr = 0;  // this lane's hits, close hits and relevant hits
+          for (int i = i0; i < i1; i++) {
+            const uint2 hc = sMask[w][i][a];
+            cn += __popc(hc.x);
+            cm += __popc(hc.x & hc.y);
+            cr += __popc(hc.x & (hc.y | sMetal[w][i]));
+          }
+          int pn = cn, pm = cm, pr = cr;  // inclusive prefix inside the group
+          for (int d = 1; d < G; d <<= 1) {
+            const int yn = __shfl_up_sync(full, pn, d, G);
+            const int ym = __shfl_up_sync(full, pm, d, G);
+            const int yr = __shfl_up_sync(full, pr, d, G);
+            if (q >= d) { pn += yn; pm += ym; pr += yr; }
+          }
+          const int g = __shfl_sync(full, ga, a);
+          int n = __shfl_sync(full, nMy, a) + pn - cn;
+          int m = __shfl_sync(full, mMy, a) + pm - cm;
+          int r = __shfl_sync(full, rMy, a) + pr - cr;
+          const int lastOfGroup = ((lane * G) & 31) + G - 1;  // for lane < nh: home `lane`'s group
+          const int tn = __shfl_sync(full, pn, lastOfGroup);
+          const int tm = __shfl_sync(full, pm, lastOfGroup);
+          const int tr = __shfl_sync(full, pr, lastOfGroup);
+          if (a < nh) {
             int *row = nbl + (size_t)g * rowStride;
             const bool carbonHome = g >= metalEnd;
             int *srow = sl + (size_t)g * kShortMax;
             int2 *rrow = rl + (size_t)g * kRelMax;
-            for (int i = 0; i < nw; i++) {
-              const uint2 hc = sMask[w][i][lane];
+            for (int i = i0; i < i1; i++) {
+              const uint2 hc = sMask[w][i][a];
               const unsigned metalW = sMetal[w][i];
               unsigned bits = hc.x;
               while (bits) {
@@ -757,8 +784,8 @@ __device__ __forceinline__ void nebrBody(const int *__restrict__ tileRep, const 
                 n++;
               }
             }
-            nMy = n; mMy = m; rMy = r;
           }
+          if (lane < nh) { nMy += tn; mMy += tm; rMy += tr; }
         } else {
         for (int a = 0; a < nh; a++) {
           const int g = __float_as_int(sHome[w][a].w);
