@@ -369,7 +369,9 @@ int sg_diff_force_matching(sg_diff *d, const double *theta, const float *ref_for
  * rebuild schedule), then the list build (its three forms, then for the cell-window forms the
  * home atoms per work item 4, 6, 8, 16, blocks per SM 2, 4, 8, 16 and cell order ascending or
  * descending), `steps` steps each with a rebuild in every step, then programmatic dependent
- * launch off and on, and (MIXED) the EAM table read through L1 or staged in shared memory.  Every device buffer and the host step counters are copied first
+ * launch off and on, and (MIXED) the EAM table read through L1 or staged in shared memory.  A
+ * trial keeps the setting the context had unless another choice is more than 1% faster (each
+ * timing is the faster of two runs).  Every device buffer and the host step counters are copied first
  * and put back after each trial, so the context continues from the state it had; the trials
  * change no results but the summation order of the metal passes.  `report` (if not NULL)
  * receives a JSON object with the milliseconds per step of every trial and the choice.

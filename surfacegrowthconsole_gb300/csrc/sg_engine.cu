@@ -1134,26 +1134,42 @@ int restoreSnapshot(sg_ctx *c, const Snapshot &s) {
   return SG_OK;
 }
 
-// Milliseconds per step of `steps` steps after three warm-up steps (which capture the graphs).
+// Milliseconds per step: the faster of two runs of `steps` steps, after three warm-up steps
+// (which capture the graphs).
 int timeSteps(sg_ctx *c, int steps, float *msPerStep) {
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
   int rc = sg_step_async(c, 3);
   if (!rc) rc = checkFlags(c);
-  if (!rc) {
+  float best = 0.f;
+  for (int run = 0; run < 2 && !rc; run++) {
     CK(cudaEventRecord(e0, c->stream));
     rc = sg_step_async(c, steps);
     CK(cudaEventRecord(e1, c->stream));
     CK(cudaEventSynchronize(e1));
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, e0, e1));
-    *msPerStep = ms / steps;
+    if (run == 0 || ms < best) best = ms;
     if (!rc) rc = checkFlags(c);
   }
+  *msPerStep = best / steps;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return rc;
+}
+
+// The choice a trial keeps: the incumbent (the setting before tuning) unless the fastest choice
+// beats it by more than kTuneMargin, about the spread of the timings themselves.
+constexpr float kTuneMargin = 0.01f;
+int pickChoice(const float *ms, const int *choice, int n, int incumbent) {
+  int fast = 0, inc = -1;
+  for (int k = 0; k < n; k++) {
+    if (ms[k] < ms[fast]) fast = k;
+    if (choice[k] == incumbent) inc = k;
+  }
+  if (inc < 0 || ms[fast] < ms[inc] * (1.f - kTuneMargin)) return choice[fast];
+  return choice[inc];
 }
 }  // namespace
 
@@ -1169,6 +1185,7 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
   const int algo0 = c->nebrAlgo;
   const bool staged0 = c->eamStaged;
   const int laneChoice[4] = {4, 8, 16, 32}, bpsChoice[4] = {2, 4, 8, 16}, itemChoice[4] = {4, 6, 8, 16};
+  const int algoChoice[3] = {0, 1, 2}, offOn[2] = {0, 1};
   float laneMs[4] = {}, bpsMs[4] = {}, orderMs[2] = {}, itemMs[4] = {}, pdlMs[2] = {}, algoMs[3] = {};
   float stagedMs[2] = {};
   bool bestStaged = staged0;
@@ -1176,12 +1193,11 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
   bool bestPdl = pdl0;
   // 1. lanes per metal atom, on the context's own schedule
   if (c->metalRun.n > 0) {
-    float best = 0.f;
     for (int k = 0; k < 4 && !rc; k++) {
       if ((rc = restoreSnapshot(c, snap)) || (rc = setMetalLanes(c, laneChoice[k]))) break;
       rc = timeSteps(c, steps, &laneMs[k]);
-      if (!rc && (k == 0 || laneMs[k] < best)) { best = laneMs[k]; bestLanes = laneChoice[k]; }
     }
+    if (!rc) bestLanes = pickChoice(laneMs, laneChoice, 4, lanes0);
   }
   // 2. the list build (atom threads or cell windows; for cell windows the home atoms per item,
   //    blocks per SM and cell order), with a rebuild in every step
@@ -1194,30 +1210,24 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
       destroyGraphs(c);
       rc = timeSteps(c, steps, &algoMs[a]);
     }
-    if (!rc) {
-      bestAlgo = 0;
-      for (int a = 1; a < 3; a++)
-        if (algoMs[a] < algoMs[bestAlgo]) bestAlgo = a;
-    }
+    if (!rc) bestAlgo = pickChoice(algoMs, algoChoice, 3, algo0);
     c->nebrAlgo = bestAlgo;
     if (!rc && bestAlgo != 1) {
-      float best = 0.f;
       for (int k = 0; k < 4 && !rc; k++) {
         if ((rc = restoreSnapshot(c, snap))) break;
         c->nebrItemAtoms = itemChoice[k];
         destroyGraphs(c);
         rc = timeSteps(c, steps, &itemMs[k]);
-        if (!rc && (k == 0 || itemMs[k] < best)) { best = itemMs[k]; bestItem = itemChoice[k]; }
       }
+      if (!rc) bestItem = pickChoice(itemMs, itemChoice, 4, item0);
       c->nebrItemAtoms = bestItem;
       destroyGraphs(c);
-      best = 0.f;
       for (int k = 0; k < 4 && !rc; k++) {
         if ((rc = restoreSnapshot(c, snap))) break;
         setNebrBlocks(c, bpsChoice[k]);
         rc = timeSteps(c, steps, &bpsMs[k]);
-        if (!rc && (k == 0 || bpsMs[k] < best)) { best = bpsMs[k]; bestBps = bpsChoice[k]; }
       }
+      if (!rc) bestBps = pickChoice(bpsMs, bpsChoice, 4, bps0);
       if (!rc) setNebrBlocks(c, bestBps);
       for (int d = 0; d < 2 && !rc; d++) {
         if ((rc = restoreSnapshot(c, snap))) break;
@@ -1225,7 +1235,7 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
         destroyGraphs(c);
         rc = timeSteps(c, steps, &orderMs[d]);
       }
-      if (!rc) bestDesc = orderMs[1] < orderMs[0] ? 1 : 0;
+      if (!rc) bestDesc = pickChoice(orderMs, offOn, 2, desc0);
     }
     c->opt.force_rebuild = fr0;
     destroyGraphs(c);
@@ -1242,7 +1252,7 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
       destroyGraphs(c);
       rc = timeSteps(c, steps, &pdlMs[k]);
     }
-    if (!rc) bestPdl = pdlMs[1] < pdlMs[0];
+    if (!rc) bestPdl = pickChoice(pdlMs, offOn, 2, pdl0 ? 1 : 0) == 1;
   }
   // 4. (MIXED) the EAM table through L1 or staged in shared memory
   if (!rc && c->opt.mode == SG_MODE_MIXED && sg_mixed_staging_ok(c) && c->metalRun.n > 0) {
@@ -1253,7 +1263,7 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
       destroyGraphs(c);
       rc = timeSteps(c, steps, &stagedMs[k]);
     }
-    if (!rc) bestStaged = stagedMs[1] < stagedMs[0];
+    if (!rc) bestStaged = pickChoice(stagedMs, offOn, 2, staged0 ? 1 : 0) == 1;
   }
   // the state as it was, with the chosen shape (the starting shape if a trial failed)
   const int rc2 = restoreSnapshot(c, snap);
