@@ -293,65 +293,76 @@ __global__ void __launch_bounds__(kMixThreads) k_step_reduce_mixed(
   __threadfence();
   // block partials in a fixed order (whichever block finished last), as double-floats on the
   // FP32 pipes (FP64 runs at a small fraction of their rate on this GPU; a double-float sum of
-  // a few hundred partials keeps ~1e-14 relative, far below the FP32 warp sums' own rounding):
-  // thread t adds rows t, t + kMixThreads, ... (independent loads, in flight together); then 8
-  // threads per value each add 16 of those sums, and one thread per value the 8 results.
-  constexpr int kParts = kMixThreads / 16;
-  __shared__ DF s1[kMixThreads][kMixAcc];
-  __shared__ float s1F[kMixThreads][kMixMax];
-  __shared__ DF s2[kParts][kMixAcc];
+  // a few hundred partials keeps ~1e-14 relative, far below the FP32 warp sums' own rounding).
+  // Sums: thread t adds value t % 16 of rows t / 16 + kG * i (kG = kMixThreads / 16 row groups,
+  // four rows of predicated loads in flight, two chains), then the row groups of a warp meet in
+  // a shuffle and the warps in one step.  Extremes: value t % 8 of rows t / 8 + kG2 * i.
+  static_assert(kMixThreads % 32 == 0 && kMixAcc <= 16 && kMixMax <= 8, "final sums: 16 and 8 values per row");
+  constexpr int kG = kMixThreads / 16, kG2 = kMixThreads / 8;
+  __shared__ DF sW[kMixThreads / 32][16];
+  __shared__ float sWF[kMixThreads / 32][8];
   __shared__ double tot[kMixAcc];
   __shared__ float totF[kMixMax];
   const int p0 = P.redFirstM, nb = P.nRedBlocksM;
   {
-    DF x[kMixAcc];
-    float y[kMixMax];
-#pragma unroll
-    for (int k = 0; k < kMixAcc; k++) x[k] = DF{0.f, 0.f};
-#pragma unroll
-    for (int k = 0; k < kMixMax; k++) y[k] = (k == MM_VVMAX || k >= MM_MAX_X) ? -3.4e38f : 3.4e38f;
-    for (int j = t; j < nb; j += kMixThreads) {
-      const float2 *row = partDF + (size_t)(p0 + j) * kMixAcc;
-      const float *rowF = partF + (size_t)(p0 + j) * kMixMax;
-#pragma unroll
-      for (int k = 0; k < kMixAcc; k++) {
-        const float2 v = __ldcg(row + k);
-        x[k] = dfAdd(x[k], DF{v.x, v.y});
-      }
-#pragma unroll
-      for (int k = 0; k < kMixMax; k++) {
-        const float z = __ldcg(rowF + k);
-        y[k] = (k == MM_VVMAX || k >= MM_MAX_X) ? fmaxf(y[k], z) : fminf(y[k], z);
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < kMixAcc; k++) s1[t][k] = x[k];
-#pragma unroll
-    for (int k = 0; k < kMixMax; k++) s1F[t][k] = y[k];
-  }
-  __syncthreads();
-  {
-    const int k = t & 15, part = t >> 4;
+    const int k = t & 15;
+    DF x0{0.f, 0.f}, x1{0.f, 0.f};
     if (k < kMixAcc) {
-      DF x{0.f, 0.f};
+      for (int j0 = t >> 4; j0 < nb; j0 += 4 * kG) {
+        float2 v[4];
 #pragma unroll
-      for (int q = 0; q < 16; q++) x = dfAdd(x, s1[part * 16 + q][k]);
-      s2[part][k] = x;
+        for (int u = 0; u < 4; u++) {
+          const int j = j0 + u * kG;
+          v[u] = j < nb ? __ldcg(partDF + (size_t)(p0 + j) * kMixAcc + k) : make_float2(0.f, 0.f);
+        }
+        x0 = dfAdd(x0, DF{v[0].x, v[0].y});
+        x1 = dfAdd(x1, DF{v[1].x, v[1].y});
+        x0 = dfAdd(x0, DF{v[2].x, v[2].y});
+        x1 = dfAdd(x1, DF{v[3].x, v[3].y});
+      }
     }
+    DF x = dfAdd(x0, x1);
+    const DF y{__shfl_xor_sync(0xffffffffu, x.hi, 16), __shfl_xor_sync(0xffffffffu, x.lo, 16)};
+    x = dfAdd(x, y);
+    if (lane < 16) sW[w][lane] = x;
   }
-  if (t >= 96 && t < 96 + kMixMax) {
-    const int k = t - 96;
+  {
+    const int k = t & 7;
     const bool isMax = (k == MM_VVMAX || k >= MM_MAX_X);
-    float y = s1F[0][k];
-    for (int q = 1; q < kMixThreads; q++) y = isMax ? fmaxf(y, s1F[q][k]) : fminf(y, s1F[q][k]);
-    totF[k] = y;
+    const float neutral = isMax ? -3.4e38f : 3.4e38f;
+    float y = neutral;
+    if (k < kMixMax) {
+      for (int j0 = t >> 3; j0 < nb; j0 += 4 * kG2) {
+        float z[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int j = j0 + u * kG2;
+          z[u] = j < nb ? __ldcg(partF + (size_t)(p0 + j) * kMixMax + k) : neutral;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) y = isMax ? fmaxf(y, z[u]) : fminf(y, z[u]);
+      }
+    }
+#pragma unroll
+    for (int o = 8; o < 32; o <<= 1) {
+      const float z = __shfl_xor_sync(0xffffffffu, y, o);
+      y = isMax ? fmaxf(y, z) : fminf(y, z);
+    }
+    if (lane < 8) sWF[w][lane] = y;
   }
   __syncthreads();
   if (t < kMixAcc) {
-    DF x{0.f, 0.f};
+    DF x = sW[0][t];
 #pragma unroll
-    for (int q = 0; q < kParts; q++) x = dfAdd(x, s2[q][t]);
+    for (int q = 1; q < kMixThreads / 32; q++) x = dfAdd(x, sW[q][t]);
     tot[t] = (double)x.hi + (double)x.lo;
+  } else if (t >= 32 && t < 32 + kMixMax) {
+    const int k = t - 32;
+    const bool isMax = (k == MM_VVMAX || k >= MM_MAX_X);
+    float y = sWF[0][k];
+#pragma unroll
+    for (int q = 1; q < kMixThreads / 32; q++) y = isMax ? fmaxf(y, sWF[q][k]) : fminf(y, sWF[q][k]);
+    totF[k] = y;
   }
   __syncthreads();
   if (t == 0) counter[rep] = 0;
@@ -476,8 +487,11 @@ __device__ void stepControlMixed(const RepConst &P, RepState *S, const double (&
   float *tbF = diffF;                      // nB x 7, element 0 = count (int bits)
   float *avF = diffF + (size_t)nB * 7 + (size_t)nB * nV;
   float *prF = avF + nV;
-  if (t == 0) {
-    for (int nb = 0; nb < nB; nb++) {
+  // one thread per buffer (the buffers are independent); the accumulation below runs only in
+  // a step where a buffer fills
+  int filled = 0;
+  {
+    for (int nb = t; nb < nB; nb += blockDim.x) {
       double *o = org + 6 * nb;
       const int count = __float_as_int(tbF[7 * nb]);
       if (count == 0) {
@@ -497,9 +511,10 @@ __device__ void stepControlMixed(const RepConst &P, RepState *S, const double (&
         rrb[count] = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
       }
       tbF[7 * nb] = __int_as_float(count + 1);
+      filled |= (count + 1 == nV) ? 1 : 0;
     }
   }
-  __syncthreads();
+  if (!__syncthreads_or(filled)) return;
   for (int nb = 0; nb < nB; nb++) {
     if (t == 0) {
       accumNow = (__float_as_int(tbF[7 * nb]) == nV);

@@ -1301,8 +1301,11 @@ __device__ void stepControl(const RepConst &P, RepState *S, const float (&red)[k
   float *rr = diff + (size_t)nB * 7;       // nB x nV
   float *av = rr + (size_t)nB * nV;        // nV
   float *pr = av + nV;                     // nV (last finished table)
-  if (t == 0) {
-    for (int nb = 0; nb < nB; nb++) {
+  // one thread per buffer (the buffers are independent); the accumulation below runs only in
+  // a step where a buffer fills
+  int filled = 0;
+  {
+    for (int nb = t; nb < nB; nb += blockDim.x) {
       float *b = tb + 7 * nb;
       int count = __float_as_int(b[0]);
       if (count == 0) {
@@ -1322,9 +1325,10 @@ __device__ void stepControl(const RepConst &P, RepState *S, const float (&red)[k
         rrb[ni] += dx * dx + dy * dy + dz * dz;
       }
       b[0] = __int_as_float(count + 1);
+      filled |= (count + 1 == nV) ? 1 : 0;
     }
   }
-  __syncthreads();
+  if (!__syncthreads_or(filled)) return;
   for (int nb = 0; nb < nB; nb++) {
     if (t == 0) {
       accumNb[0] = (__float_as_int(tb[7 * nb]) == nV);
