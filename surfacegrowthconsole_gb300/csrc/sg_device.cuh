@@ -220,6 +220,15 @@ __device__ __forceinline__ void stateToShared(const RepState *g, RepState *s) {
   for (int i = threadIdx.x; i < (int)(sizeof(RepState) / 4); i += blockDim.x) dst[i] = __ldcg(src + i);
   __syncthreads();
 }
+// The same for the replica's constants, which the step control's single thread reads field by
+// field (from shared memory each read costs tens of cycles instead of an L2 round trip); the
+// copy and the state's share one barrier when this runs first.
+static_assert(sizeof(RepConst) % 4 == 0, "RepConst is copied as 32-bit words");
+__device__ __forceinline__ void constToShared(const RepConst *g, RepConst *s) {
+  const int *src = reinterpret_cast<const int *>(g);
+  int *dst = reinterpret_cast<int *>(s);
+  for (int i = threadIdx.x; i < (int)(sizeof(RepConst) / 4); i += blockDim.x) dst[i] = src[i];
+}
 __device__ __forceinline__ void stateFromShared(const RepState *s, RepState *g) {
   __syncthreads();
   const int *src = reinterpret_cast<const int *>(s);

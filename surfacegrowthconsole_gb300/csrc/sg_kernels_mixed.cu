@@ -373,8 +373,10 @@ __global__ void __launch_bounds__(kMixThreads) k_step_reduce_mixed(
 #pragma unroll
   for (int k = 0; k < kMixMax; k++) M[k] = totF[k];
   __shared__ RepState sS;
+  __shared__ RepConst sP;
+  constToShared(&P, &sP);
   stateToShared(S, &sS);
-  stepControlMixed(P, &sS, A, M, diff64 ? diff64 + diffOff64[rep] : nullptr,
+  stepControlMixed(sP, &sS, A, M, diff64 ? diff64 + diffOff64[rep] : nullptr,
                    diffF ? diffF + diffOffF[rep] : nullptr, forceRebuild);
   stateFromShared(&sS, S);
 }

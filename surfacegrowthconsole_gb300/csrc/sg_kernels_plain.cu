@@ -1199,9 +1199,11 @@ __global__ void __launch_bounds__(kRedThreads) k_step_reduce(
 #pragma unroll
   for (int s = 0; s < kNumRed; s++) redv[s] = red[s];
   __shared__ RepState sS;
+  __shared__ RepConst sP;
+  constToShared(&P, &sP);
   stateToShared(S, &sS);
   if (t == 0) sS.redCounter = 0;  // every block has counted in: ready for the next step
-  stepControl(P, &sS, redv, diffBuf ? diffBuf + diffOff[rep] : nullptr, forceRebuild);
+  stepControl(sP, &sS, redv, diffBuf ? diffBuf + diffOff[rep] : nullptr, forceRebuild);
   stateFromShared(&sS, S);
 }
 
