@@ -10,6 +10,10 @@
 #error "define SG_KN(name) before including sg_forces.cuh"
 #endif
 
+// SG_FAST_ANGLES (MIXED): the graphene angle and radial terms divide through reciprocals and
+// reciprocal square roots (__fdividef, rsqrtf: a few ulp) shared between the terms of a pair,
+// instead of one IEEE division per quotient of the reference's expressions (PLAIN keeps those
+// for bit parity).  Fewer instructions for the carbon pass, which is bound by instruction issue.
 // SG_EAM_TABLE (MIXED): the EAM pair functions come from cubic Hermite tables instead of the
 // analytic forms; the table buffer is one more kernel parameter, and the force bodies take the
 // start of the replica's table (in global memory, or staged in shared memory).
@@ -528,6 +532,9 @@ __global__ void __launch_bounds__(128, 8) SG_KN(k_force_carbon)(BlockTab tab, co
     const int k = sK[a][q];
     const float rnx = sD[a][q][0], rny = sD[a][q][1], rnz = sD[a][q][2], absR = sD[a][q][3];
     const float4 B = pos[k];
+#ifdef SG_FAST_ANGLES
+    const float invR2 = __fdividef(1.f, absR * absR);
+#endif
     // the neighbour's close list holds, in list order, every entry that can pass the rCutC test
     // below; four entries per load (a close-list row is 32 bytes, aligned)
     const int nk = ns[k];
@@ -561,6 +568,18 @@ __global__ void __launch_bounds__(128, 8) SG_KN(k_force_carbon)(BlockTab tab, co
         const float rr2 = ex * ex + ey * ey + ez * ez;
         if ((rr2 < P.rrCutC) && (m != i)) {
           ex = ex * (-1.f); ey = ey * (-1.f); ez = ez * (-1.f);
+#ifdef SG_FAST_ANGLES
+          const float inv = __fdividef(1.f, absR * rr2);
+          const float cs = (rnx * ex + rny * ey + rnz * ez) * inv;
+          const float th = acosf(cs);
+          const float dth = th - P.theta_0;
+          const float tmp = P.mu_theta * dth * rsqrtf(1.f - cs * cs);
+          float f = tmp * inv;
+          fx = fx + f * ex; fy = fy + f * ey; fz = fz + f * ez;
+          f = -tmp * cs * invR2;
+          fx = fx + f * rnx; fy = fy + f * rny; fz = fz + f * rnz;
+          f = -P.mu_p * (rm.z - P.z_0) * (1.f / 9.f);
+#else
           const float cs = (rnx * ex + rny * ey + rnz * ez) / (absR * rr2);
           const float th = acosf(cs);
           const float dth = th - P.theta_0;
@@ -570,6 +589,7 @@ __global__ void __launch_bounds__(128, 8) SG_KN(k_force_carbon)(BlockTab tab, co
           f = -tmp * cs / (absR * absR);
           fx = fx + f * rnx; fy = fy + f * rny; fz = fz + f * rnz;
           f = -P.mu_p * (rm.z - P.z_0) / 9.f;
+#endif
           fz = fz + f;
           ++countk;
         }
@@ -584,9 +604,18 @@ __global__ void __launch_bounds__(128, 8) SG_KN(k_force_carbon)(BlockTab tab, co
       rnx[q] = sD[a][q][0]; rny[q] = sD[a][q][1]; rnz[q] = sD[a][q][2]; absR[q] = sD[a][q][3];
       dzs[q] = sZ[a][q];
     }
+#ifdef SG_FAST_ANGLES
+    float invR[3];
+#pragma unroll
+    for (int q = 0; q < 3; q++) invR[q] = __fdividef(1.f, absR[q]);
+#endif
 #pragma unroll
     for (int q = 0; q < 3; q++) {
+#ifdef SG_FAST_ANGLES
+      const float f = -P.mu_r * (absR[q] - 1.f) * invR[q];
+#else
       const float f = -P.mu_r * (absR[q] - 1.f) / absR[q];
+#endif
       fx = fx + f * rnx[q]; fy = fy + f * rny[q]; fz = fz + f * rnz[q];
       u += P.mu_r * (absR[q] - 1.f) * (absR[q] - 1.f);
     }
@@ -597,6 +626,16 @@ __global__ void __launch_bounds__(128, 8) SG_KN(k_force_carbon)(BlockTab tab, co
 #pragma unroll
     for (int q = 0; q < 3; q++) {
       const int p0 = q, p1 = (q == 2) ? 0 : q + 1;
+#ifdef SG_FAST_ANGLES
+      const float inv01 = invR[p0] * invR[p1];
+      const float cs = (rnx[p0] * rnx[p1] + rny[p0] * rny[p1] + rnz[p0] * rnz[p1]) * inv01;
+      const float th = acosf(cs);
+      const float dth = th - P.theta_0;
+      const float tmp = P.mu_theta * dth * rsqrtf(1.f - cs * cs);
+      float f = tmp * (1.f - absR[p0] * cs * invR[p1]) * inv01;
+      fx = fx + f * rnx[p1]; fy = fy + f * rny[p1]; fz = fz + f * rnz[p1];
+      f = tmp * (1.f - absR[p1] * cs * invR[p0]) * inv01;
+#else
       const float cs = (rnx[p0] * rnx[p1] + rny[p0] * rny[p1] + rnz[p0] * rnz[p1]) / (absR[p0] * absR[p1]);
       const float th = acosf(cs);
       const float dth = th - P.theta_0;
@@ -604,6 +643,7 @@ __global__ void __launch_bounds__(128, 8) SG_KN(k_force_carbon)(BlockTab tab, co
       float f = tmp * (1.f - absR[p0] * cs / absR[p1]) / (absR[p0] * absR[p1]);
       fx = fx + f * rnx[p1]; fy = fy + f * rny[p1]; fz = fz + f * rnz[p1];
       f = tmp * (1.f - absR[p1] * cs / absR[p0]) / (absR[p0] * absR[p1]);
+#endif
       fx = fx + f * rnx[p0]; fy = fy + f * rny[p0]; fz = fz + f * rnz[p0];
       u += P.mu_theta * dth * dth;
     }
