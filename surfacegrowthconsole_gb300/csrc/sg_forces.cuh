@@ -10,10 +10,11 @@
 #error "define SG_KN(name) before including sg_forces.cuh"
 #endif
 
-// SG_FAST_ANGLES (MIXED): the graphene angle and radial terms divide through reciprocals and
-// reciprocal square roots (__fdividef, rsqrtf: a few ulp) shared between the terms of a pair,
-// instead of one IEEE division per quotient of the reference's expressions (PLAIN keeps those
-// for bit parity).  Fewer instructions for the carbon pass, which is bound by instruction issue.
+// SG_FAST_RECIP (MIXED): quotients through reciprocals and reciprocal square roots (__fdividef,
+// rsqrtf: a few ulp) shared between the terms that use them — the graphene angle and radial
+// terms, the EAM pair distance and force, the LJ terms — instead of an IEEE division or square
+// root per quotient of the reference's expressions (PLAIN keeps those for bit parity).  Fewer
+// instructions for passes that are bound by instruction issue.
 // SG_EAM_TABLE (MIXED): the EAM pair functions come from cubic Hermite tables instead of the
 // analytic forms; the table buffer is one more kernel parameter, and the force bodies take the
 // start of the replica's table (in global memory, or staged in shared memory).
@@ -175,7 +176,11 @@ __device__ __forceinline__ void SG_KN(rhoBody)(int e, const RepConst &P, BlockTa
         const float dy = minImg(A.y - B[q].y, P.region[1]);
         const float dz = minImg(A.z - B[q].z, P.region[2]);
         const float rr = dx * dx + dy * dy + dz * dz;
+#ifdef SG_FAST_RECIP
+        if ((rr < P.rrCutEam) && (k[q] < metalEnd)) sum += SG_EAM_DENS(P, rr * rsqrtf(rr));
+#else
         if ((rr < P.rrCutEam) && (k[q] < metalEnd)) sum += SG_EAM_DENS(P, sqrtf(rr));
+#endif
       }
     }
   }
@@ -210,9 +215,16 @@ __global__ void __launch_bounds__(128) SG_KN(k_rho_tpa)(BlockTab tab, const RepC
 
 // Lennard-Jones metal-carbon term (cu:880-884).
 __device__ __forceinline__ void ljTerms(const RepConst &P, float rr, float &fc, float &u) {
+#ifdef SG_FAST_RECIP
+  const float irr = __fdividef(1.f, rr);
+  const float rri = P.sigmaLJ * P.sigmaLJ * irr;
+  const float rri3 = rri * rri * rri;
+  fc = 48.f * P.epsLJ * rri3 * (rri3 - 0.5f) * irr;
+#else
   const float rri = P.sigmaLJ * P.sigmaLJ / rr;
   const float rri3 = rri * rri * rri;
   fc = 48.f * P.epsLJ * rri3 * (rri3 - 0.5f) * rri / (P.sigmaLJ * P.sigmaLJ);
+#endif
   u = 4.f * P.epsLJ * rri3 * (rri3 - 1.f);
 }
 
@@ -258,11 +270,20 @@ __device__ __forceinline__ void SG_KN(forceMetalBody)(int e, const RepConst &P, 
         const float rr = dx * dx + dy * dy + dz * dz;
         if (k[q] < metalEnd) {
           if (rr >= P.rrCutEam) continue;  // the reference computes and then zeroes the term
+#ifdef SG_FAST_RECIP
+          const float ri = rsqrtf(rr);
+          const float r = rr * ri;
+#else
           const float r = sqrtf(rr);
+#endif
           const EamPair e = SG_EAM_PAIR(P, r);
           float fc = -e.dphi;
           fc = fc - e.df * (dFi + dFk[q]);
+#ifdef SG_FAST_RECIP
+          fc = fc * ri;
+#else
           fc = fc / r;
+#endif
           fx = fx + fc * dx; fy = fy + fc * dy; fz = fz + fc * dz;
           u += e.phi;
         } else {
@@ -532,7 +553,7 @@ __global__ void __launch_bounds__(128, 8) SG_KN(k_force_carbon)(BlockTab tab, co
     const int k = sK[a][q];
     const float rnx = sD[a][q][0], rny = sD[a][q][1], rnz = sD[a][q][2], absR = sD[a][q][3];
     const float4 B = pos[k];
-#ifdef SG_FAST_ANGLES
+#ifdef SG_FAST_RECIP
     const float invR2 = __fdividef(1.f, absR * absR);
 #endif
     // the neighbour's close list holds, in list order, every entry that can pass the rCutC test
@@ -568,7 +589,7 @@ __global__ void __launch_bounds__(128, 8) SG_KN(k_force_carbon)(BlockTab tab, co
         const float rr2 = ex * ex + ey * ey + ez * ez;
         if ((rr2 < P.rrCutC) && (m != i)) {
           ex = ex * (-1.f); ey = ey * (-1.f); ez = ez * (-1.f);
-#ifdef SG_FAST_ANGLES
+#ifdef SG_FAST_RECIP
           const float inv = __fdividef(1.f, absR * rr2);
           const float cs = (rnx * ex + rny * ey + rnz * ez) * inv;
           const float th = acosf(cs);
@@ -604,14 +625,14 @@ __global__ void __launch_bounds__(128, 8) SG_KN(k_force_carbon)(BlockTab tab, co
       rnx[q] = sD[a][q][0]; rny[q] = sD[a][q][1]; rnz[q] = sD[a][q][2]; absR[q] = sD[a][q][3];
       dzs[q] = sZ[a][q];
     }
-#ifdef SG_FAST_ANGLES
+#ifdef SG_FAST_RECIP
     float invR[3];
 #pragma unroll
     for (int q = 0; q < 3; q++) invR[q] = __fdividef(1.f, absR[q]);
 #endif
 #pragma unroll
     for (int q = 0; q < 3; q++) {
-#ifdef SG_FAST_ANGLES
+#ifdef SG_FAST_RECIP
       const float f = -P.mu_r * (absR[q] - 1.f) * invR[q];
 #else
       const float f = -P.mu_r * (absR[q] - 1.f) / absR[q];
@@ -626,7 +647,7 @@ __global__ void __launch_bounds__(128, 8) SG_KN(k_force_carbon)(BlockTab tab, co
 #pragma unroll
     for (int q = 0; q < 3; q++) {
       const int p0 = q, p1 = (q == 2) ? 0 : q + 1;
-#ifdef SG_FAST_ANGLES
+#ifdef SG_FAST_RECIP
       const float inv01 = invR[p0] * invR[p1];
       const float cs = (rnx[p0] * rnx[p1] + rny[p0] * rny[p1] + rnz[p0] * rnz[p1]) * inv01;
       const float th = acosf(cs);

@@ -31,7 +31,7 @@
 
 #define SG_KN(name) name##_mixed
 #define SG_EAM_TABLE
-#define SG_FAST_ANGLES
+#define SG_FAST_RECIP
 #include "sg_forces.cuh"
 
 namespace sg {
