@@ -447,8 +447,10 @@ void SG_KN(launchMetalChain)(bool pdl, int mt, int grid, int stagedGrid, size_t 
 // The reference reuses its list counter for the bonded loop (cu:989), so after the third close
 // carbon its walk resumes at entry 4: metal entries at positions 4..p2 contribute their LJ term
 // twice, and entry 3 is skipped when p2 == 2.  After the walk, lane q < 3 adds the
-// second-neighbour terms of close carbon q (walking that neighbour's close list) and lane 3 the
-// radial, out-of-plane and angle terms; the four partial sums meet in a shuffle tree.
+// second-neighbour terms of close carbon q (walking that neighbour's close list) and the
+// own-angle term of close carbons q, q + 1, and lane 3 the radial and out-of-plane terms (the
+// lanes 0..2 run one angle each, converged, instead of lane 3 running all three); the four
+// partial sums meet in a shuffle tree.
 __device__ __forceinline__ void relEntry(bool full, const int *row, const int2 *rrow, int e, int &k, int &j) {
   if (full) { k = row[e]; j = e; }
   else { const int2 v = rrow[e]; k = v.x; j = v.y; }
@@ -617,56 +619,54 @@ __global__ void __launch_bounds__(128, 8) SG_KN(k_force_carbon)(BlockTab tab, co
         if (countk == 2) break;
       }
     }
-  } else if (sub == 3 && counti == 3) {
-    // radial, out-of-plane and own-angle terms (cu:985-1061)
-    float rnx[3], rny[3], rnz[3], absR[3], dzs[3];
-#pragma unroll
-    for (int q = 0; q < 3; q++) {
-      rnx[q] = sD[a][q][0]; rny[q] = sD[a][q][1]; rnz[q] = sD[a][q][2]; absR[q] = sD[a][q][3];
-      dzs[q] = sZ[a][q];
-    }
+  }
+  if (counti == 3) {
+    if (sub < 3) {
+      // own-angle term of close carbons q, q + 1 (cu:1020-1061): one per lane 0..2
+      const int p0 = sub, p1 = (sub == 2) ? 0 : sub + 1;
+      const float rx0 = sD[a][p0][0], ry0 = sD[a][p0][1], rz0 = sD[a][p0][2], ar0 = sD[a][p0][3];
+      const float rx1 = sD[a][p1][0], ry1 = sD[a][p1][1], rz1 = sD[a][p1][2], ar1 = sD[a][p1][3];
 #ifdef SG_FAST_RECIP
-    float invR[3];
-#pragma unroll
-    for (int q = 0; q < 3; q++) invR[q] = __fdividef(1.f, absR[q]);
-#endif
-#pragma unroll
-    for (int q = 0; q < 3; q++) {
-#ifdef SG_FAST_RECIP
-      const float f = -P.mu_r * (absR[q] - 1.f) * invR[q];
-#else
-      const float f = -P.mu_r * (absR[q] - 1.f) / absR[q];
-#endif
-      fx = fx + f * rnx[q]; fy = fy + f * rny[q]; fz = fz + f * rnz[q];
-      u += P.mu_r * (absR[q] - 1.f) * (absR[q] - 1.f);
-    }
-    float dZ = 2.f * (A.z - P.z_0) - (dzs[0] + dzs[1] + dzs[2]);
-    fz = fz + -0.666666667f * P.mu_p * dZ;
-    dZ = (A.z - P.z_0) - 0.33333333f * (dzs[0] + dzs[1] + dzs[2]);
-    u += P.mu_p * dZ * dZ;
-#pragma unroll
-    for (int q = 0; q < 3; q++) {
-      const int p0 = q, p1 = (q == 2) ? 0 : q + 1;
-#ifdef SG_FAST_RECIP
-      const float inv01 = invR[p0] * invR[p1];
-      const float cs = (rnx[p0] * rnx[p1] + rny[p0] * rny[p1] + rnz[p0] * rnz[p1]) * inv01;
+      const float i0 = __fdividef(1.f, ar0), i1 = __fdividef(1.f, ar1);
+      const float inv01 = i0 * i1;
+      const float cs = (rx0 * rx1 + ry0 * ry1 + rz0 * rz1) * inv01;
       const float th = acosf(cs);
       const float dth = th - P.theta_0;
       const float tmp = P.mu_theta * dth * rsqrtf(1.f - cs * cs);
-      float f = tmp * (1.f - absR[p0] * cs * invR[p1]) * inv01;
-      fx = fx + f * rnx[p1]; fy = fy + f * rny[p1]; fz = fz + f * rnz[p1];
-      f = tmp * (1.f - absR[p1] * cs * invR[p0]) * inv01;
+      float f = tmp * (1.f - ar0 * cs * i1) * inv01;
+      fx = fx + f * rx1; fy = fy + f * ry1; fz = fz + f * rz1;
+      f = tmp * (1.f - ar1 * cs * i0) * inv01;
 #else
-      const float cs = (rnx[p0] * rnx[p1] + rny[p0] * rny[p1] + rnz[p0] * rnz[p1]) / (absR[p0] * absR[p1]);
+      const float cs = (rx0 * rx1 + ry0 * ry1 + rz0 * rz1) / (ar0 * ar1);
       const float th = acosf(cs);
       const float dth = th - P.theta_0;
       const float tmp = P.mu_theta * dth / sqrtf(1.f - cs * cs);
-      float f = tmp * (1.f - absR[p0] * cs / absR[p1]) / (absR[p0] * absR[p1]);
-      fx = fx + f * rnx[p1]; fy = fy + f * rny[p1]; fz = fz + f * rnz[p1];
-      f = tmp * (1.f - absR[p1] * cs / absR[p0]) / (absR[p0] * absR[p1]);
+      float f = tmp * (1.f - ar0 * cs / ar1) / (ar0 * ar1);
+      fx = fx + f * rx1; fy = fy + f * ry1; fz = fz + f * rz1;
+      f = tmp * (1.f - ar1 * cs / ar0) / (ar0 * ar1);
 #endif
-      fx = fx + f * rnx[p0]; fy = fy + f * rny[p0]; fz = fz + f * rnz[p0];
+      fx = fx + f * rx0; fy = fy + f * ry0; fz = fz + f * rz0;
       u += P.mu_theta * dth * dth;
+    } else {
+      // radial and out-of-plane terms (cu:985-1019): lane 3
+      float dzs = 0.f;
+#pragma unroll
+      for (int q = 0; q < 3; q++) {
+        const float rx = sD[a][q][0], ry = sD[a][q][1], rz = sD[a][q][2], ar = sD[a][q][3];
+#ifdef SG_FAST_RECIP
+        const float f = -P.mu_r * (ar - 1.f) * __fdividef(1.f, ar);
+#else
+        const float f = -P.mu_r * (ar - 1.f) / ar;
+#endif
+        fx = fx + f * rx; fy = fy + f * ry; fz = fz + f * rz;
+        u += P.mu_r * (ar - 1.f) * (ar - 1.f);
+      }
+      const float z0 = sZ[a][0], z1 = sZ[a][1], z2 = sZ[a][2];
+      dzs = z0 + z1 + z2;
+      float dZ = 2.f * (A.z - P.z_0) - dzs;
+      fz = fz + -0.666666667f * P.mu_p * dZ;
+      dZ = (A.z - P.z_0) - 0.33333333f * dzs;
+      u += P.mu_p * dZ * dZ;
     }
   }
 #pragma unroll
