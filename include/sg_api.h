@@ -88,7 +88,9 @@ typedef struct sg_options {
                             * per home atom; the same lists */
     int eam_table_smem;    /* MIXED: 1 the metal passes stage the EAM table in shared memory
                             * (a grid of 4 blocks per SM), 0 read it through L1 */
-    int reserved[2];
+    int carbon_blocks_per_sm; /* carbon pass compiled for 8, 12 or 16 resident 128-thread blocks
+                            * per SM (64, 40 or 32 registers a thread; 0: 8) */
+    int reserved[1];
 } sg_options;
 
 /* Initialise *opt with the defaults (PLAIN mode, graphs on, device 0). */
@@ -369,7 +371,8 @@ int sg_diff_force_matching(sg_diff *d, const double *theta, const float *ref_for
  * rebuild schedule), then the list build (its three forms, then for the cell-window forms the
  * home atoms per work item 4, 6, 8, 16, blocks per SM 2, 4, 8, 16 and cell order ascending or
  * descending), `steps` steps each with a rebuild in every step, then programmatic dependent
- * launch off and on, and (MIXED) the EAM table read through L1 or staged in shared memory.  A
+ * launch off and on, (MIXED) the EAM table read through L1 or staged in shared memory, and the
+ * carbon pass's resident blocks per SM 8, 12, 16.  A
  * trial keeps the setting the context had unless another choice is more than 1% faster (each
  * timing is the faster of two runs).  Every device buffer and the host step counters are copied first
  * and put back after each trial, so the context continues from the state it had; the trials
@@ -386,7 +389,7 @@ typedef struct sg_launch_shape {
     int programmatic_launch; /* 0 or 1 */
     int nebr_build;         /* 0, 1 or 2 */
     int eam_table_smem;     /* 0 or 1 (MIXED) */
-    int reserved[1];
+    int carbon_blocks_per_sm; /* 8, 12 or 16 */
 } sg_launch_shape;
 /* The launch shape in use (from the options, or as sg_autotune chose it). */
 int sg_get_launch_shape(sg_ctx *ctx, sg_launch_shape *shape);

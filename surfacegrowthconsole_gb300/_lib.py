@@ -90,14 +90,15 @@ class Options(C.Structure):
         ("eam_table_knots", C.c_int), ("metal_lanes", C.c_int), ("nebr_blocks_per_sm", C.c_int),
         ("phase_timing", C.c_int),
         ("programmatic_launch", C.c_int), ("nebr_descending", C.c_int), ("nebr_item_atoms", C.c_int),
-        ("nebr_build", C.c_int), ("eam_table_smem", C.c_int), ("reserved", C.c_int * 2),
+        ("nebr_build", C.c_int), ("eam_table_smem", C.c_int), ("carbon_blocks_per_sm", C.c_int),
+        ("reserved", C.c_int * 1),
     ]
 
 
 class LaunchShape(C.Structure):
     _fields_ = [("metal_lanes", C.c_int), ("nebr_blocks_per_sm", C.c_int), ("nebr_descending", C.c_int),
                 ("nebr_item_atoms", C.c_int), ("programmatic_launch", C.c_int), ("nebr_build", C.c_int),
-                ("eam_table_smem", C.c_int), ("reserved", C.c_int * 1)]
+                ("eam_table_smem", C.c_int), ("carbon_blocks_per_sm", C.c_int)]
 
 
 class Thermo(C.Structure):

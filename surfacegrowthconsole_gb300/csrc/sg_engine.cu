@@ -280,6 +280,14 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
   }
   c->nebrAlgo = c->opt.nebr_build;
   c->eamStaged = c->opt.mode == SG_MODE_MIXED && c->opt.eam_table_smem != 0;  // sg_mixed_init may clear it
+  {
+    const int cb = c->opt.carbon_blocks_per_sm ? c->opt.carbon_blocks_per_sm : 8;
+    if (cb != 8 && cb != 12 && cb != 16) {
+      sg_destroy(c);
+      return sg_fail(SG_ERR_INVALID, "carbon_blocks_per_sm %d: 0 (default), 8, 12 or 16", c->opt.carbon_blocks_per_sm);
+    }
+    c->carbonBlocks = cb;
+  }
   if (c->nebrItemAtoms < kMinItemAtoms || c->nebrItemAtoms > 64) {
     sg_destroy(c);
     return sg_fail(SG_ERR_INVALID, "nebr_item_atoms %d: 0 (default) or %d..64", c->opt.nebr_item_atoms,
@@ -584,8 +592,8 @@ static int enqueueForces(sg_ctx *c, bool withCmVel) {
     LAUNCH_OK();
   }
   if (c->carbonTabT.n)
-    CK(launchK(c->pdl, k_force_carbon, c->carbonTabT.n, 128, 0, c->stream, c->carbonTabT.view(), c->rc, c->pos, c->acc, c->nn,
-                                                           c->nbl, c->ns, c->sl, c->nrl, c->rl, c->rowStride));
+    CK(launchCarbon(c->pdl, c->carbonBlocks, c->carbonTabT.n, c->stream, c->carbonTabT.view(), c->rc, c->pos, c->acc,
+                    c->nn, c->nbl, c->ns, c->sl, c->nrl, c->rl, c->rowStride));
   if (c->opt.phase_timing) cudaEventRecordWithFlags(c->phaseEv[3], c->stream, cudaEventRecordExternal);
   LAUNCH_OK();
   if (fork) {
@@ -1184,11 +1192,13 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
   const bool pdl0 = c->pdl;
   const int algo0 = c->nebrAlgo;
   const bool staged0 = c->eamStaged;
+  const int cb0 = c->carbonBlocks;
   const int laneChoice[4] = {4, 8, 16, 32}, bpsChoice[4] = {2, 4, 8, 16}, itemChoice[4] = {4, 6, 8, 16};
-  const int algoChoice[3] = {0, 1, 2}, offOn[2] = {0, 1};
+  const int algoChoice[3] = {0, 1, 2}, offOn[2] = {0, 1}, cbChoice[3] = {8, 12, 16};
   float laneMs[4] = {}, bpsMs[4] = {}, orderMs[2] = {}, itemMs[4] = {}, pdlMs[2] = {}, algoMs[3] = {};
-  float stagedMs[2] = {};
+  float stagedMs[2] = {}, cbMs[3] = {};
   bool bestStaged = staged0;
+  int bestCb = cb0;
   int bestLanes = lanes0, bestBps = bps0, bestDesc = desc0, bestItem = item0, bestAlgo = algo0;
   bool bestPdl = pdl0;
   // 1. lanes per metal atom, on the context's own schedule
@@ -1265,6 +1275,18 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
     }
     if (!rc) bestStaged = pickChoice(stagedMs, offOn, 2, staged0 ? 1 : 0) == 1;
   }
+  // 5. the carbon pass's resident blocks per SM, on the context's own schedule
+  if (!rc && c->carbonTabT.n > 0) {
+    c->pdl = bestPdl;
+    c->eamStaged = bestStaged;
+    for (int k = 0; k < 3 && !rc; k++) {
+      if ((rc = restoreSnapshot(c, snap))) break;
+      c->carbonBlocks = cbChoice[k];
+      destroyGraphs(c);
+      rc = timeSteps(c, steps, &cbMs[k]);
+    }
+    if (!rc) bestCb = pickChoice(cbMs, cbChoice, 3, cb0);
+  }
   // the state as it was, with the chosen shape (the starting shape if a trial failed)
   const int rc2 = restoreSnapshot(c, snap);
   if (snap.dev) cudaFree(snap.dev);
@@ -1276,6 +1298,7 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
     c->pdl = pdl0;
     c->nebrAlgo = algo0;
     c->eamStaged = staged0;
+    c->carbonBlocks = cb0;
     destroyGraphs(c);
     return rc;
   }
@@ -1287,6 +1310,7 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
   c->pdl = bestPdl;
   c->nebrAlgo = bestAlgo;
   c->eamStaged = bestStaged;
+  c->carbonBlocks = bestCb;
   destroyGraphs(c);
   if (report && report_len > 0) {
     snprintf(report, report_len,
@@ -1297,13 +1321,15 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
              "\"6\": %.6g, \"8\": %.6g, \"16\": %.6g}, \"programmatic_launch_ms_per_step\": {\"0\": %.6g, "
              "\"1\": %.6g}, \"nebr_build_ms_per_step_rebuilding\": {\"0\": %.6g, \"1\": %.6g, \"2\": %.6g}, "
              "\"eam_table_smem_ms_per_step\": {\"0\": %.6g, \"1\": %.6g}, "
+             "\"carbon_blocks_per_sm_ms_per_step\": {\"8\": %.6g, \"12\": %.6g, \"16\": %.6g}, "
              "\"metal_lanes\": %d, \"nebr_blocks_per_sm\": %d, \"nebr_descending\": %d, "
              "\"nebr_item_atoms\": %d, \"programmatic_launch\": %d, \"nebr_build\": %d, "
-             "\"eam_table_smem\": %d, \"nebr_grid\": %d}",
+             "\"eam_table_smem\": %d, \"carbon_blocks_per_sm\": %d, \"nebr_grid\": %d}",
              steps, laneMs[0], laneMs[1], laneMs[2], laneMs[3], bpsMs[0], bpsMs[1], bpsMs[2], bpsMs[3],
              orderMs[0], orderMs[1], itemMs[0], itemMs[1], itemMs[2], itemMs[3], pdlMs[0], pdlMs[1],
-             algoMs[0], algoMs[1], algoMs[2], stagedMs[0], stagedMs[1], c->metalLanes, c->nebrBlocksPerSM,
-             c->nebrDescending, c->nebrItemAtoms, c->pdl ? 1 : 0, c->nebrAlgo, c->eamStaged ? 1 : 0, c->nebrGrid);
+             algoMs[0], algoMs[1], algoMs[2], stagedMs[0], stagedMs[1], cbMs[0], cbMs[1], cbMs[2], c->metalLanes,
+             c->nebrBlocksPerSM, c->nebrDescending, c->nebrItemAtoms, c->pdl ? 1 : 0, c->nebrAlgo,
+             c->eamStaged ? 1 : 0, c->carbonBlocks, c->nebrGrid);
   }
   return SG_OK;
 }
@@ -1324,6 +1350,8 @@ extern "C" int sg_set_launch_shape(sg_ctx *c, const sg_launch_shape *shape) {
     return sg_fail(SG_ERR_INVALID, "eam_table_smem %d: 0 or 1", shape->eam_table_smem);
   if (shape->eam_table_smem && !(c->opt.mode == SG_MODE_MIXED && sg_mixed_staging_ok(c)))
     return sg_fail(SG_ERR_UNSUPPORTED, "eam_table_smem: MIXED mode with tabulated EAM only");
+  if (shape->carbon_blocks_per_sm != 8 && shape->carbon_blocks_per_sm != 12 && shape->carbon_blocks_per_sm != 16)
+    return sg_fail(SG_ERR_INVALID, "carbon_blocks_per_sm %d: 8, 12 or 16", shape->carbon_blocks_per_sm);
   CK(cudaStreamSynchronize(c->stream));
   const int rc = setMetalLanes(c, shape->metal_lanes);
   if (rc) return rc;
@@ -1337,6 +1365,8 @@ extern "C" int sg_set_launch_shape(sg_ctx *c, const sg_launch_shape *shape) {
   c->nebrDescending = shape->nebr_descending;
   c->nebrItemAtoms = shape->nebr_item_atoms;
   c->pdl = shape->programmatic_launch != 0;
+  if (shape->carbon_blocks_per_sm != c->carbonBlocks) destroyGraphs(c);
+  c->carbonBlocks = shape->carbon_blocks_per_sm;
   return SG_OK;
 }
 
@@ -1350,5 +1380,6 @@ extern "C" int sg_get_launch_shape(sg_ctx *c, sg_launch_shape *shape) {
   shape->programmatic_launch = c->pdl ? 1 : 0;
   shape->nebr_build = c->nebrAlgo;
   shape->eam_table_smem = c->eamStaged ? 1 : 0;
+  shape->carbon_blocks_per_sm = c->carbonBlocks;
   return SG_OK;
 }

@@ -66,6 +66,7 @@ struct sg_ctx {
   int nebrAlgo = 0;
   bool eamStaged = false;  // MIXED: metal passes with the EAM table staged in shared memory
   bool pdl = false;  // programmatic dependent launch between the kernels of a step
+  int carbonBlocks = 8;  // carbon pass: resident blocks per SM of its register budget (8, 12, 16)
   std::vector<std::pair<void *, size_t>> regions;  // every device buffer with its size
   int anyMetal = 0, anyCarbon = 0, maxHist = 0;
   // graphs keyed by variant bits

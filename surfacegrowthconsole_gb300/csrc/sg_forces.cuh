@@ -456,7 +456,11 @@ __device__ __forceinline__ void relEntry(bool full, const int *row, const int2 *
   else { const int2 v = rrow[e]; k = v.x; j = v.y; }
 }
 
-__global__ void __launch_bounds__(128, 8) SG_KN(k_force_carbon)(BlockTab tab, const RepConst *__restrict__ rc,
+// MINB: resident blocks per SM the register budget is cut for (8: 64 registers, 12: 40, 16:
+// 32); more warps hide more of the gathers' latency at large sizes, fewer registers cost
+// instructions (launchCarbon picks one, the autotuner times them).
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) SG_KN(k_force_carbon)(BlockTab tab, const RepConst *__restrict__ rc,
                                                       float4 *__restrict__ pos, float4 *__restrict__ acc,
                                                       const int *__restrict__ nn, const int *__restrict__ nbl,
                                                       const int *__restrict__ ns, const int *__restrict__ sl,
@@ -679,6 +683,23 @@ __global__ void __launch_bounds__(128, 8) SG_KN(k_force_carbon)(BlockTab tab, co
   if (valid && sub == 0) {
     acc[i] = make_float4(fx, fy, fz, 0.f);
     pos[i].w = 0.5f * u;
+  }
+}
+
+// The carbon pass with minBlocks (8, 12 or 16; others: 8) resident blocks per SM.
+cudaError_t SG_KN(launchCarbon)(bool pdl, int minBlocks, int grid, cudaStream_t s, BlockTab tab,
+                                const RepConst *rc, float4 *pos, float4 *acc, const int *nn, const int *nbl,
+                                const int *ns, const int *sl, const int *nrl, const int2 *rl, int rowStride) {
+  switch (minBlocks) {
+    case 12:
+      return launchK(pdl, SG_KN(k_force_carbon)<12>, grid, 128, 0, s, tab, rc, pos, acc, nn, nbl, ns, sl, nrl, rl,
+                     rowStride);
+    case 16:
+      return launchK(pdl, SG_KN(k_force_carbon)<16>, grid, 128, 0, s, tab, rc, pos, acc, nn, nbl, ns, sl, nrl, rl,
+                     rowStride);
+    default:
+      return launchK(pdl, SG_KN(k_force_carbon)<8>, grid, 128, 0, s, tab, rc, pos, acc, nn, nbl, ns, sl, nrl, rl,
+                     rowStride);
   }
 }
 

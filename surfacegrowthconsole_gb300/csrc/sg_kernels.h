@@ -58,9 +58,10 @@ __global__ void k_force_metal(BlockTab tab, const RepConst *rc, float4 *pos, flo
 void launchMetalChain(bool pdl, int mt, int grid, int stagedGrid, size_t stagedSmem, cudaStream_t s, BlockTab tab, const RepConst *rc, float4 *pos,
                       float4 *acc, const int *nn, const int *nbl, float *rho, float *dF, float *Fv,
                       float *fric, int rowStride);
-__global__ void k_force_carbon(BlockTab tab, const RepConst *rc, float4 *pos, float4 *acc,
-                               const int *nn, const int *nbl, const int *ns, const int *sl,
-                               const int *nrl, const int2 *rl, int rowStride);
+// the carbon pass with minBlocks (8, 12, 16) resident 128-thread blocks per SM
+cudaError_t launchCarbon(bool pdl, int minBlocks, int grid, cudaStream_t s, BlockTab tab, const RepConst *rc,
+                         float4 *pos, float4 *acc, const int *nn, const int *nbl, const int *ns, const int *sl,
+                         const int *nrl, const int2 *rl, int rowStride);
 __global__ void k_cmvel(BlockTab tab, const RepConst *rc, RepState *st, const float4 *vel,
                         const float4 *acc, float *partial, const int *redFirst);
 __global__ void k_step_reduce(BlockTab tab, const RepConst *rc, RepState *st, const float4 *pos,

@@ -717,10 +717,9 @@ int sg_mixed_enqueue_forces(sg_ctx *c) {
     MCK(cudaGetLastError());
   }
   if (c->carbonTabT.n) {
-    MCK(launchK(c->pdl, k_force_carbon_mixed, c->carbonTabT.n, 128, 0, c->stream, c->carbonTabT.view(), c->rc, c->pos, c->acc,
-                                                                 c->nn, c->nbl, c->ns, c->sl, c->nrl, c->rl,
-                                                                 c->rowStride));
-    }
+    MCK(launchCarbon_mixed(c->pdl, c->carbonBlocks, c->carbonTabT.n, c->stream, c->carbonTabT.view(), c->rc, c->pos,
+                           c->acc, c->nn, c->nbl, c->ns, c->sl, c->nrl, c->rl, c->rowStride));
+  }
   if (c->opt.phase_timing) cudaEventRecordWithFlags(c->phaseEv[3], c->stream, cudaEventRecordExternal);
   MCK(cudaGetLastError());
   if (fork) {

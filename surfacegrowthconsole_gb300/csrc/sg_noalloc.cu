@@ -212,7 +212,7 @@ extern "C" int sg_compute_forces_noalloc(const sg_simparams *p, sg_float4 *d_pos
     k_rho<<<nMetalBlk, kBs, 0, s>>>(metalTab, rc, pos, nn, nbl, rho, dF, Fv, rowStride);
     k_force_metal<<<nMetalBlk, kBs, 0, s>>>(metalTab, rc, pos, acc, nn, nbl, dF, Fv, fric, rowStride);
   }
-  if (nCarbBlk) k_force_carbon<<<nCarbBlk, kBs, 0, s>>>(carbTab, rc, pos, acc, nn, nbl, ns, sl, nrl, rl, rowStride);
+  if (nCarbBlk) launchCarbon(false, 8, nCarbBlk, s, carbTab, rc, pos, acc, nn, nbl, ns, sl, nrl, rl, rowStride);
   e = cudaGetLastError();
   if (e != cudaSuccess) return sg_fail(SG_ERR_CUDA, "sg_compute_forces_noalloc launch: %s", cudaGetErrorString(e));
   int flags = 0;

@@ -88,7 +88,8 @@ class Simulation:
                  use_graphs: bool = True, device: int = 0, rdf_ext_bins: int = 0, rdf_ext_range: float = 0.0,
                  eam_table_knots: int = 0, stream: int = 0, phase_timing: bool = False, metal_lanes: int = 0,
                  nebr_blocks_per_sm: int = 0, programmatic_launch: bool = False, nebr_descending: int = 0,
-                 nebr_item_atoms: int = 0, nebr_build: int = 0, eam_table_smem: int = 0):
+                 nebr_item_atoms: int = 0, nebr_build: int = 0, eam_table_smem: int = 0,
+                 carbon_blocks_per_sm: int = 0):
         plist = [params] if isinstance(params, SimParams) else list(params)
         arr = (SimParams * len(plist))(*plist)
         opt = Options()
@@ -109,6 +110,7 @@ class Simulation:
         opt.nebr_item_atoms = nebr_item_atoms
         opt.nebr_build = nebr_build
         opt.eam_table_smem = eam_table_smem
+        opt.carbon_blocks_per_sm = carbon_blocks_per_sm
         h = C.c_void_p()
         check(lib().sg_create(arr, len(plist), C.byref(opt), C.byref(h)))
         self._h = h
@@ -304,7 +306,8 @@ class Simulation:
         return json.loads(buf.value.decode())
 
     SHAPE_FIELDS = ("metal_lanes", "nebr_blocks_per_sm", "nebr_descending", "nebr_item_atoms",
-                    "programmatic_launch", "nebr_build", "eam_table_smem")
+                    "programmatic_launch", "nebr_build", "eam_table_smem",
+                    "carbon_blocks_per_sm")
 
     def launch_shape(self) -> dict:
         """The launch shape in use: the fields of sg_launch_shape."""

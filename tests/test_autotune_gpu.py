@@ -64,15 +64,18 @@ def test_list_builds_and_shapes_change_nothing(which):
 
 def test_bad_shapes_are_refused():
     p, r, v = workloads.small(seed=3)
-    for kw in ({"metal_lanes": 6}, {"nebr_blocks_per_sm": 33}, {"nebr_item_atoms": 3}, {"nebr_build": 3}):
+    for kw in ({"metal_lanes": 6}, {"nebr_blocks_per_sm": 33}, {"nebr_item_atoms": 3}, {"nebr_build": 3},
+               {"carbon_blocks_per_sm": 10}):
         with pytest.raises(Exception):
             Simulation(p, **kw)
     sim = Simulation(p)
     with pytest.raises(Exception):
         sim.set_launch_shape({"metal_lanes": 64})
+    with pytest.raises(Exception):
+        sim.set_launch_shape({"carbon_blocks_per_sm": 9})
     assert sim.launch_shape() == {"metal_lanes": 16, "nebr_blocks_per_sm": 8, "nebr_descending": 0,
                                   "nebr_item_atoms": 8, "programmatic_launch": 0, "nebr_build": 0,
-                                  "eam_table_smem": 0}
+                                  "eam_table_smem": 0, "carbon_blocks_per_sm": 8}
     sim.close()
 
 
@@ -141,3 +144,26 @@ def test_staged_eam_table_changes_nothing(lanes):
     for a, b in zip(out[0], out[1]):
         for x, y in zip(a, b) if isinstance(a, tuple) else [(a, b)]:
             assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_MIXED])
+def test_carbon_blocks_per_sm_change_nothing(mode):
+    """The carbon pass compiled for 8, 12 or 16 resident blocks per SM (another register budget,
+    the same source): PLAIN (no contraction) is bit-identical, MIXED agrees to FP32 rounding."""
+    p, r, v = workloads.production(seed=2, steps=10)
+    out = {}
+    for cb in (8, 12, 16):
+        sim = Simulation(p, mode=mode, carbon_blocks_per_sm=cb)
+        assert sim.launch_shape()["carbon_blocks_per_sm"] == cb
+        sim.set_state(r, v, np.zeros((p.nMol, 3), np.float32))
+        sim.build_lists()
+        sim.compute_forces()
+        out[cb] = sim.get_state()
+        sim.close()
+    for cb in (12, 16):
+        for x, y in zip(out[cb], out[8]):
+            if mode == MODE_PLAIN:
+                assert np.array_equal(x, y), cb
+            else:
+                err = np.abs(x.astype(np.float64) - y).max() / max(np.abs(y).max(), 1e-30)
+                assert err <= SUM_ORDER_RTOL, (cb, err)
