@@ -1624,13 +1624,16 @@ __global__ void __launch_bounds__(kUnpackAtoms) k_unpack_state(const float4 *sr,
                                                                int n, RepState *st, int nrep) {
   __shared__ float sV[3 * kUnpackAtoms], sA[3 * kUnpackAtoms];
   const int a0 = blockIdx.x * kUnpackAtoms, t = threadIdx.x, i = a0 + t;
+  // every read over the host link is issued before the barrier: one round trip
+  float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (sr && i < n) r = sr[i];
   if (a0 < n) {
     if (sv) stageRows3(sv, n, a0, sV);
     if (sa) stageRows3(sa, n, a0, sA);
   }
   __syncthreads();
   if (i < n) {
-    if (sr) pos[i] = sr[i];
+    if (sr) pos[i] = r;
     if (sv) vel[i] = make_float4(sV[3 * t], sV[3 * t + 1], sV[3 * t + 2], 0.f);
     if (sa) acc[i] = make_float4(sA[3 * t], sA[3 * t + 1], sA[3 * t + 2], 0.f);
     if (posLo) posLo[i] = make_float4(0.f, 0.f, 0.f, 0.f);
