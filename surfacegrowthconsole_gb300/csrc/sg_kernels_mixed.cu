@@ -59,6 +59,7 @@ struct MixedBufs {
   std::vector<size_t> diffOff64;
   unsigned *counter = nullptr;  // per replica: blocks done
   float4 *eamTab = nullptr;     // per replica nTab intervals x 2: cubic coefficients of phi, of f
+  int mixAtoms = kMixAtoms;     // atoms per step-reduction block (1024, 2048 or 4096)
   int *redRep = nullptr, *redStart = nullptr;  // reduction blocks: replica, block index in it
   int redN = 0;
   size_t stagedSmem = 0;        // shared memory of the staged metal kernels (the largest table)
@@ -188,6 +189,8 @@ __device__ void stepControlMixed(const RepConst &P, RepState *S, const double (&
                                  const float (&M)[kMixMax], double *diff, float *diffF,
                                  int forceRebuild);
 
+// APT atoms per thread: APT * kMixThreads atoms per block (the engine picks 2, 4 or 8 by size).
+template <int APT>
 __global__ void __launch_bounds__(kMixThreads) k_step_reduce_mixed(
     BlockTab tab, const RepConst *__restrict__ rc, RepState *st, const float4 *__restrict__ pos,
     const float4 *__restrict__ posLo, float4 *__restrict__ vel, const float4 *__restrict__ acc4,
@@ -210,8 +213,8 @@ __global__ void __launch_bounds__(kMixThreads) k_step_reduce_mixed(
   DF cm[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
   float mm[kMixMax] = {0.f, 3.4e38f, 3.4e38f, 3.4e38f, -3.4e38f, -3.4e38f, -3.4e38f};
 #pragma unroll
-  for (int half = 0; half < 2; half++) {
-    const int local = kMixAtoms * b + half * kMixThreads + t;
+  for (int half = 0; half < APT; half++) {
+    const int local = APT * kMixThreads * b + half * kMixThreads + t;
     if (local >= P.nMol) continue;
     const int g = P.atomOff + local;
     const float4 r = pos[g];
@@ -633,12 +636,23 @@ int sg_mixed_init(sg_ctx *c) {
     MCK(cudaMemcpyAsync(m->eamTab, tab.data(), sizeof(float4) * tab.size(), cudaMemcpyHostToDevice, c->stream));
   MCK(cudaMemcpyAsync(c->rc, c->hrc.data(), sizeof(RepConst) * c->nrep, cudaMemcpyHostToDevice, c->stream));
   MCK(cudaStreamSynchronize(c->stream));
-  // reduction blocks of kMixAtoms atoms
+  // reduction blocks of m->mixAtoms atoms: the largest of 1024, 2048, 4096 that still gives two
+  // blocks per SM (more atoms per thread: fewer, longer blocks and fewer partials, faster at the
+  // batched size; a single small system keeps 1024 for its parallelism)
   {
+    m->mixAtoms = kMixAtoms;
+    for (int a = 4 * kMixAtoms; a > kMixAtoms; a /= 2) {
+      long long blocks = 0;
+      for (int r = 0; r < c->nrep; r++) blocks += (c->hrc[r].nMol + a - 1) / a;
+      if (blocks >= 2LL * std::max(c->numSMs, 1)) {
+        m->mixAtoms = a;
+        break;
+      }
+    }
     std::vector<int> rr, ss;
     for (int r = 0; r < c->nrep; r++) {
       RepConst &P = c->hrc[r];
-      P.nRedBlocksM = (P.nMol + kMixAtoms - 1) / kMixAtoms;
+      P.nRedBlocksM = (P.nMol + m->mixAtoms - 1) / m->mixAtoms;
       P.redFirstM = (int)rr.size();
       for (int b = 0; b < P.nRedBlocksM; b++) { rr.push_back(r); ss.push_back(b); }
     }
@@ -734,7 +748,10 @@ int sg_mixed_enqueue_forces(sg_ctx *c) {
 int sg_mixed_enqueue_reduce(sg_ctx *c, int forceRebuild) {
   MixedBufs *m = static_cast<MixedBufs *>(c->mixed);
   if (!c->redTab.n) return SG_OK;
-  MCK(launchK(c->pdl, k_step_reduce_mixed, m->redN, kMixThreads, 0, c->stream,
+  auto kern = m->mixAtoms == 8 * kMixThreads   ? k_step_reduce_mixed<8>
+              : m->mixAtoms == 4 * kMixThreads ? k_step_reduce_mixed<4>
+                                               : k_step_reduce_mixed<2>;
+  MCK(launchK(c->pdl, kern, m->redN, kMixThreads, 0, c->stream,
       BlockTab{m->redRep, m->redStart, m->redN}, c->rc, c->st, c->pos, c->posLo, c->vel, c->acc, c->fric, m->partDF, m->partF,
       c->dRedFirst, m->counter, m->diff64, m->dDiffOff64, c->diffBuf, c->dDiffOff, forceRebuild));
   MCK(cudaGetLastError());
