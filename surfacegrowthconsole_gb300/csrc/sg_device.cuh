@@ -241,14 +241,14 @@ __device__ __forceinline__ void setFlag(RepState *st, int code) {
 }
 
 // Programmatic dependent launch.  A kernel of the step chain, launched with the
-// programmatic-serialization attribute, may be scheduled while its predecessor in the stream
-// still runs; it waits here, before its first global memory access, for the predecessor grid to
-// complete with its memory visible, then allows its own successor to be scheduled.  Every kernel
-// of the chain waits, so completion is transitive.  Launched without the attribute, both
-// instructions return at once.
+// programmatic-serialization attribute, is scheduled once every block of its predecessor in the
+// stream has exited (the implicit trigger: no kernel calls launch_dependents, so waiting blocks
+// never hold SM slots the predecessor still needs), overlapping its launch with the
+// predecessor's completion; it waits here, before its first global memory access, for the
+// predecessor grid to complete with its memory visible.  Every kernel of the chain waits, so
+// completion is transitive.  Launched without the attribute, the wait returns at once.
 __device__ __forceinline__ void pdlEnter() {
   asm volatile("griddepcontrol.wait;" ::: "memory");
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
 }  // namespace sg
