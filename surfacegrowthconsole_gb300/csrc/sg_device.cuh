@@ -42,7 +42,7 @@ constexpr int kHeavyChunk = 8;    // sizes the item list of the fixed-size scrat
 constexpr int kScanCells = 512;   // cells per block of the single-pass cell scan (kCellTile / 4)
 constexpr int kScanThreads = 128;
 constexpr int kMixThreads = 512;  // MIXED step reduction: threads per block
-constexpr int kMixAtoms = 1024;   // and the fewest atoms per block (2 per thread; up to 8 at large sizes)
+constexpr int kMixAtoms = 512;    // and the fewest atoms per block (1 per thread; up to 8 at large sizes)
 constexpr int kUnpackAtoms = 256; // state upload: atoms (threads) per block
 constexpr int kMinItemAtoms = 4;  // smallest home atoms per work item the engine allows
 constexpr int kItemAtoms = 8;     // the engine's default home atoms per work item

@@ -59,7 +59,7 @@ struct MixedBufs {
   std::vector<size_t> diffOff64;
   unsigned *counter = nullptr;  // per replica: blocks done
   float4 *eamTab = nullptr;     // per replica nTab intervals x 2: cubic coefficients of phi, of f
-  int mixAtoms = kMixAtoms;     // atoms per step-reduction block (1024, 2048 or 4096)
+  int mixAtoms = kMixAtoms;     // atoms per step-reduction block (512, 1024, 2048 or 4096)
   int *redRep = nullptr, *redStart = nullptr;  // reduction blocks: replica, block index in it
   int redN = 0;
   size_t stagedSmem = 0;        // shared memory of the staged metal kernels (the largest table)
@@ -189,7 +189,7 @@ __device__ void stepControlMixed(const RepConst &P, RepState *S, const double (&
                                  const float (&M)[kMixMax], double *diff, float *diffF,
                                  int forceRebuild);
 
-// APT atoms per thread: APT * kMixThreads atoms per block (the engine picks 2, 4 or 8 by size).
+// APT atoms per thread: APT * kMixThreads atoms per block (the engine picks 1, 2, 4 or 8 by size).
 template <int APT>
 __global__ void __launch_bounds__(kMixThreads) k_step_reduce_mixed(
     BlockTab tab, const RepConst *__restrict__ rc, RepState *st, const float4 *__restrict__ pos,
@@ -637,11 +637,11 @@ int sg_mixed_init(sg_ctx *c) {
   MCK(cudaMemcpyAsync(c->rc, c->hrc.data(), sizeof(RepConst) * c->nrep, cudaMemcpyHostToDevice, c->stream));
   MCK(cudaStreamSynchronize(c->stream));
   // reduction blocks of m->mixAtoms atoms: the largest of 1024, 2048, 4096 that still gives two
-  // blocks per SM (more atoms per thread: fewer, longer blocks and fewer partials, faster at the
-  // batched size; a single small system keeps 1024 for its parallelism)
+  // blocks per SM, else 512 (more atoms per thread: fewer, longer blocks and fewer partials,
+  // faster at the batched size; a single small system keeps 512 for its parallelism)
   {
     m->mixAtoms = kMixAtoms;
-    for (int a = 4 * kMixAtoms; a > kMixAtoms; a /= 2) {
+    for (int a = 8 * kMixAtoms; a > kMixAtoms; a /= 2) {
       long long blocks = 0;
       for (int r = 0; r < c->nrep; r++) blocks += (c->hrc[r].nMol + a - 1) / a;
       if (blocks >= 2LL * std::max(c->numSMs, 1)) {
@@ -750,7 +750,8 @@ int sg_mixed_enqueue_reduce(sg_ctx *c, int forceRebuild) {
   if (!c->redTab.n) return SG_OK;
   auto kern = m->mixAtoms == 8 * kMixThreads   ? k_step_reduce_mixed<8>
               : m->mixAtoms == 4 * kMixThreads ? k_step_reduce_mixed<4>
-                                               : k_step_reduce_mixed<2>;
+              : m->mixAtoms == 2 * kMixThreads ? k_step_reduce_mixed<2>
+                                               : k_step_reduce_mixed<1>;
   MCK(launchK(c->pdl, kern, m->redN, kMixThreads, 0, c->stream,
       BlockTab{m->redRep, m->redStart, m->redN}, c->rc, c->st, c->pos, c->posLo, c->vel, c->acc, c->fric, m->partDF, m->partF,
       c->dRedFirst, m->counter, m->diff64, m->dDiffOff64, c->diffBuf, c->dDiffOff, forceRebuild));
