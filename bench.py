@@ -84,8 +84,28 @@ def parse():
 
 
 def workload(rank: int):
+    """Rank r's system: the production workload with its own seed (independent replicas, no
+    collective on the data path)."""
     from surfacegrowthconsole_gb300 import workloads
     return workloads.production(seed=2 + rank)
+
+
+def over_ranks(dist, x: float, op: str, device: str) -> float:
+    """x reduced over the ranks ("max" for times, "sum" for atom counts); x itself with one
+    rank.  device: where the one-element tensor lives for the backend (cuda:N for NCCL, cpu for
+    gloo)."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def job_value(atoms_all: float, steps: int, seconds_max: float) -> float:
+    """Whole-job throughput: the atoms of all ranks times the steps, over the slowest rank's
+    time."""
+    return atoms_all * steps / seconds_max
 
 
 class Clocks:
@@ -228,9 +248,10 @@ def run_reference(args, rank: int, world: int):
     print(json.dumps(line, default=float))
 
 
-def run_batched(args, rank: int, world: int, local: int):
+def run_batched(args, rank: int, world: int, local: int, dist=None):
     """The batched form: all replicas in one context, in both forms (the headline --mode and the
-    other), against the same replicas one by one in the headline form."""
+    other), against the same replicas one by one in the headline form.  With several ranks each
+    steps its own seeded batch; the values are all ranks' atoms over the slowest rank's time."""
     import torch
     from surfacegrowthconsole_gb300 import MODE_MIXED, MODE_PLAIN, workloads
     from surfacegrowthconsole_gb300.engine import Simulation
@@ -239,6 +260,7 @@ def run_batched(args, rank: int, world: int, local: int):
     r = np.concatenate([w[1] for w in reps])
     v = np.concatenate([w[2] for w in reps])
     natoms = int(sum(q.nMol for q in plist))
+    natoms_all = over_ranks(dist, float(natoms), "sum", f"cuda:{local}")
     stream = torch.cuda.Stream(device=local)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     head = args.mode
@@ -250,6 +272,8 @@ def run_batched(args, rank: int, world: int, local: int):
         tune = None if args.no_tune else sim.autotune(steps=10)
         sim.step(args.warmup)
         torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
         launches = 0
         with Clocks(local) as clk:
             with torch.cuda.stream(stream):
@@ -260,8 +284,8 @@ def run_batched(args, rank: int, world: int, local: int):
                 ev1.record(stream)
             torch.cuda.synchronize()
         sim.step(0)
-        t = ev0.elapsed_time(ev1) * 1e-3
-        forms[name] = {"value": natoms * args.steps / t, "ms_per_step": 1e3 * t / args.steps,
+        t = over_ranks(dist, ev0.elapsed_time(ev1) * 1e-3, "max", f"cuda:{local}")
+        forms[name] = {"value": job_value(natoms_all, args.steps, t), "ms_per_step": 1e3 * t / args.steps,
                        "gpu_launches": launches, "clocks": clk.summary(), "launch_shape": tune,
                        "rebuilds_all_replicas": int(sum(sim.thermo(k).rebuilds for k in range(len(plist))))}
         sim.close()
@@ -284,7 +308,8 @@ def run_batched(args, rank: int, world: int, local: int):
         t_one += ev0.elapsed_time(ev1) * 1e-3
         atoms_one += q.nMol
         s1.close()
-    one = atoms_one * k1 / t_one
+    one = job_value(over_ranks(dist, float(atoms_one), "sum", f"cuda:{local}"), k1,
+                    over_ranks(dist, t_one, "max", f"cuda:{local}"))
     if rank == 0:
         f = forms[head]
         other = "plain" if head == "mixed" else "mixed"
@@ -361,7 +386,10 @@ def main():
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     if args.workload in ("batched", "diff"):
-        (run_batched if args.workload == "batched" else run_diff)(args, rank, world, local)
+        if args.workload == "batched":
+            run_batched(args, rank, world, local, dist)
+        else:
+            run_diff(args, rank, world, local)
         if dist:
             dist.destroy_process_group()
         return
@@ -407,11 +435,7 @@ def run_production(args, rank: int, world: int, local: int, dist):
         torch.cuda.synchronize()
 
     def max_over_ranks(x: float) -> float:
-        if not dist:
-            return x
-        t = torch.tensor([x], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return over_ranks(dist, x, "max", f"cuda:{local}")
 
     def make(mode, phase_timing=False):
         return Simulation(p, mode=mode, force_rebuild=True, device=local, stream=stream.cuda_stream,
@@ -451,14 +475,9 @@ def run_production(args, rank: int, world: int, local: int, dist):
         forms[name] = {"total_s": total_s, "launches": launches, "launch_shape": tune,
                        "shape": sim.launch_shape(), "clocks": clk.summary()}
         sims[name] = sim
-    if dist:
-        n_all = torch.tensor([float(p.nMol)], device=f"cuda:{local}")
-        dist.all_reduce(n_all)
-        atoms_all = float(n_all.item())
-    else:
-        atoms_all = float(p.nMol)
+    atoms_all = over_ranks(dist, float(p.nMol), "sum", f"cuda:{local}")
     for f in forms.values():
-        f["value"] = atoms_all * args.steps / f["total_s"]
+        f["value"] = job_value(atoms_all, args.steps, f["total_s"])
         f["ms_per_step"] = 1e3 * f["total_s"] / args.steps
     sim = sims[head]
     sims["plain" if head == "mixed" else "mixed"].close()
