@@ -555,22 +555,20 @@ enum { V_SHEAR = 1, V_RDF = 2, V_RDF_ZERO = 4 };
 
 static int enqueueRebuild(sg_ctx *c, int force) {
   const int fr = force;
-  CK(launchK(c->pdl, k_scan_cells, c->nScanBlocks, kScanThreads, 0, c->stream, c->tileTab.rep, c->tileTab.start,
+  CK(launchK(c->pdl, k_scan_rank, c->nScanBlocks, kScanRankThreads, 0, c->stream, c->tileTab.rep, c->tileTab.start,
              c->dTileFirst, c->rc, c->st, c->cellCount, c->cellStart, c->bucketCap, fr, c->activeCells,
-             c->heavyItems, c->nebrWork, c->nebrItemAtoms, c->blockCount));
-  CK(launchK(c->pdl, k_rank_cells, c->atomTab.n, 128, 0, c->stream, c->atomTab.view(), c->rc, c->st, c->cellOf,
-             c->slot, c->cellStart, c->bucket, c->bucketCap, c->pos, c->sortIdx, c->sortPos, c->nn, c->ns, c->nrl,
-             fr, c->blockCount, c->nScanBlocks));
+             c->heavyItems, c->nebrWork, c->nebrItemAtoms, c->blockCount, c->bucket, c->cellOf, c->pos,
+             c->sortIdx, c->sortPos, c->nn, c->ns, c->nrl));
   if (c->opt.phase_timing) cudaEventRecordWithFlags(c->phaseEv[8], c->stream, cudaEventRecordExternal);
   if (c->nebrAlgo == 1)
     CK(launchK(c->pdl, k_build_nebr_atoms, c->atomTab.n, 128, 0, c->stream, c->atomTab.view(), c->rc, c->st,
                c->cellOf, c->cellStart, c->sortPos, c->nn, c->nbl, c->ns, c->sl, c->nrl, c->rl, c->rowStride,
-               c->nebrMax, c->nebrWork, fr));
+               c->nebrMax, c->nebrWork, fr, c->blockCount, c->nScanBlocks));
   else
     CK(launchK(c->pdl, c->nebrAlgo == 2 ? k_build_nebr_lanes : k_build_nebr, c->nebrGrid, kNebrWarps * 32, 0,
                c->stream, c->tileTab.rep, c->activeCells,
                c->heavyItems, c->nebrWork, c->rc, c->st, c->cellStart, c->sortPos, c->nn, c->nbl, c->ns, c->sl,
-               c->nrl, c->rl, c->rowStride, c->nebrMax, c->nebrDescending));
+               c->nrl, c->rl, c->rowStride, c->nebrMax, c->nebrDescending, c->blockCount, c->nScanBlocks));
   return SG_OK;
 }
 

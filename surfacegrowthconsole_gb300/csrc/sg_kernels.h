@@ -16,15 +16,13 @@ __global__ void k_cell_bucket(BlockTab tab, const RepConst *rc, const float4 *po
 __global__ void k_build_nebr_atoms(BlockTab tab, const RepConst *rc, RepState *st, const int *cellOf,
                                    const int *cellStart, const float4 *sortPos, int *nn, int *nbl, int *ns,
                                    int *sl, int *nrl, int2 *rl, int rowStride, int nebrMax, int *work,
-                                   int forceRebuild);
-// one block of kScanThreads threads per kScanCells cells
-__global__ void k_scan_cells(const int *tileRep, const int *tileStart, const int *tileFirst, const RepConst *rc,
-                             RepState *st, int *cellCount, int *cellStart, int cap, int forceRebuild, int *active,
-                             int2 *heavy, int *work, int itemAtoms, const int *blockCount);
-__global__ void k_rank_cells(BlockTab tab, const RepConst *rc, RepState *st, const int *cellOf, const int *slot,
-                             const int *cellStart, const int *bucket, int cap, const float4 *pos, int *sortIdx,
-                             float4 *sortPos, int *nn, int *ns, int *nrl, int forceRebuild, int *blockCount,
-                             int nBlockCount);
+                                   int forceRebuild, int *blockCount, int nBlockCount);
+// one block of kScanRankThreads threads per kScanCells cells
+__global__ void k_scan_rank(const int *tileRep, const int *tileStart, const int *tileFirst, const RepConst *rc,
+                            RepState *st, int *cellCount, int *cellStart, int cap, int forceRebuild, int *active,
+                            int2 *heavy, int *work, int itemAtoms, const int *blockCount, const int *bucket,
+                            const int *cellOf, const float4 *pos, int *sortIdx, float4 *sortPos, int *nn, int *ns,
+                            int *nrl);
 __global__ void k_scan_tiles(BlockTab tab, const RepConst *rc, const RepState *st,
                              const int *cellCount, int *tileSum, int forceRebuild);
 __global__ void k_scan_tile_prefix(const RepConst *rc, const RepState *st, const int *tileFirst,
@@ -42,10 +40,12 @@ __global__ void k_rank(BlockTab tab, const RepConst *rc, const RepState *st, con
 // of the home-chunk list `heavy` (all reset before the scan of every rebuild).
 __global__ void k_build_nebr(const int *tileRep, const int *active, const int2 *heavy, int *work, const RepConst *rc, RepState *st,
                              const int *cellStart, const float4 *sortPos, int *nn, int *nbl, int *ns, int *sl,
-                             int *nrl, int2 *rl, int rowStride, int nebrMax, int descending);
+                             int *nrl, int2 *rl, int rowStride, int nebrMax, int descending, int *blockCount,
+                             int nBlockCount);
 __global__ void k_build_nebr_lanes(const int *tileRep, const int *active, const int2 *heavy, int *work, const RepConst *rc, RepState *st,
                              const int *cellStart, const float4 *sortPos, int *nn, int *nbl, int *ns, int *sl,
-                             int *nrl, int2 *rl, int rowStride, int nebrMax, int descending);
+                             int *nrl, int2 *rl, int rowStride, int nebrMax, int descending, int *blockCount,
+                             int nBlockCount);
 
 // ---- PLAIN force and step kernels ----
 __global__ void k_rho(BlockTab tab, const RepConst *rc, const float4 *pos, const int *nn,

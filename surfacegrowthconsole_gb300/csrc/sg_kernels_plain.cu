@@ -357,78 +357,76 @@ __global__ void k_rank(BlockTab tab, const RepConst *__restrict__ rc, const RepS
 // ============================================================================================
 // Counting sort in two passes (the engine's path).  The histogram pass (binAtom) files each
 // atom in its cell's bucket and counts the filed atoms per block of kScanCells cells
-// (blockCount).  k_scan_cells: one block per kScanCells cells takes its exclusive offset from
-// the counts of the replica's earlier blocks (no wait on another block), scans its cells and
-// writes cellStart and the list build's work items.  k_rank_cells orders each cell from its
-// bucket and clears blockCount for the next rebuild.
+// (blockCount).  k_scan_rank: one block per kScanCells cells takes its exclusive offset from
+// the counts of the replica's earlier blocks (no wait on another block), scans its cells,
+// writes cellStart and the list build's work items and orders each of its cells from its
+// bucket; the list build clears blockCount for the next rebuild.
 // ============================================================================================
-__global__ void __launch_bounds__(kScanThreads) k_scan_cells(const int *__restrict__ tileRep,
-                                                             const int *__restrict__ tileStart,
-                                                             const int *__restrict__ tileFirst,
-                                                             const RepConst *__restrict__ rc, RepState *st,
-                                                             int *__restrict__ cellCount, int *__restrict__ cellStart,
-                                                             int cap, int forceRebuild, int *__restrict__ active,
-                                                             int2 *__restrict__ heavy, int *__restrict__ work,
-                                                             int itemAtoms, const int *__restrict__ blockCount) {
+// The cell scan and the in-cell ordering in one pass: one block of kScanRankThreads threads per
+// kScanCells cells takes its exclusive atom offset from the replica's earlier blocks' counts
+// (blockCount), scans its cells (a thread per cell), writes cellStart and the list build's work
+// items, then orders the atoms of its cells with all its threads: block entry e (cell j, bucket
+// slot s) goes to position cellStart[j] + (number of atoms of j's bucket with a smaller index),
+// a few entries per thread with their loads in flight together.  Atoms outside the grid get
+// empty lists.  blockCount is cleared by the list build (all blocks have read it then).
+__global__ void __launch_bounds__(kScanRankThreads) k_scan_rank(const int *__restrict__ tileRep,
+                                                          const int *__restrict__ tileStart,
+                                                          const int *__restrict__ tileFirst,
+                                                          const RepConst *__restrict__ rc, RepState *st,
+                                                          int *__restrict__ cellCount, int *__restrict__ cellStart,
+                                                          int cap, int forceRebuild, int *__restrict__ active,
+                                                          int2 *__restrict__ heavy, int *__restrict__ work,
+                                                          int itemAtoms, const int *__restrict__ blockCount,
+                                                          const int *__restrict__ bucket, const int *__restrict__ cellOf,
+                                                          const float4 *__restrict__ pos, int *__restrict__ sortIdx,
+                                                          float4 *__restrict__ sortPos, int *__restrict__ nn,
+                                                          int *__restrict__ ns, int *__restrict__ nrl) {
   pdlEnter();
   constexpr int kSub = kCellTile / kScanCells;  // scan blocks per tile of the tile table
-  constexpr int kPer = kScanCells / kScanThreads;
-  constexpr int kWarps = kScanThreads / 32;
-  __shared__ int ws[kWarps], wp[kWarps];
-  __shared__ int wl[kWarps], wh[kWarps], wOcc[kWarps], wOver[kWarps], sBaseL, sBaseH;
+  constexpr int kWarps = kScanRankThreads / 32;
+  static_assert(kScanCells % 32 == 0 && kScanCells <= kScanRankThreads, "one cell per scan thread");
+  __shared__ int ws[kWarps], wp[kWarps], wl[kWarps], wh[kWarps], wOcc[kWarps], wOver[kWarps];
+  __shared__ int sEx[kScanCells + 1];  // exclusive prefix of the block's cell counts
+  __shared__ int sBaseL, sBaseH, sBase;
   const int t = blockIdx.x;
   const int rep = tileRep[t / kSub];
   RepState *S = st + rep;
   if (!rebuilding(S, forceRebuild)) return;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const RepConst &P = rc[rep];
   const int first = tileFirst[rep] * kSub;  // the replica's first scan block
   const int c0 = tileStart[t / kSub] + (t % kSub) * kScanCells;
-  int v[kPer];
-  int sum = 0, occ = 0, over = 0;
-  const int cb = P.cellOff + c0 + threadIdx.x * kPer;
-#pragma unroll
-  for (int i = 0; i < kPer; i++) {
-    const int n = cellCount[cb + i];
-    occ = max(occ, n);
-    over += (n > cap) ? 1 : 0;
-    v[i] = min(n, cap);  // atoms past the cap are not in the bucket (SG_ERR_CELL_OVERFLOW)
-    sum += v[i];
+  const int cb = P.cellOff + c0;  // the block's first global cell
+  const bool own = tid < kScanCells;  // this thread scans cell tid of the block
+  const int n = own ? cellCount[cb + tid] : 0;
+  const int v = min(n, cap);  // atoms past the cap are not in the bucket (SG_ERR_CELL_OVERFLOW)
+  int pre = 0;                // atoms filed in the replica's earlier blocks
+  for (int q = first + tid; q < t; q += kScanRankThreads) pre += blockCount[q];
+  // atoms outside the grid: empty lists (the reference clears their NN), counted in cellRange
+  {
+    const int lb = t - first, nb = P.ncellsPad / kScanCells;
+    int outside = 0;
+    for (int g = P.atomOff + lb * kScanRankThreads + tid; g < P.atomOff + P.nMol; g += nb * kScanRankThreads)
+      if (cellOf[g] < 0) {
+        nn[g] = 0;
+        ns[g] = 0;
+        nrl[g] = 0;
+        outside++;
+      }
+    if (outside) atomicAdd(&S->cellRange, outside);
   }
-  int pre = 0;  // atoms filed in the replica's earlier blocks
-  for (int q = first + threadIdx.x; q < t; q += kScanThreads) pre += blockCount[q];
-  int x = sum;
+  int x = v;  // inclusive prefix inside the warp
   for (int o = 1; o < 32; o <<= 1) {
     const int y = __shfl_up_sync(0xffffffffu, x, o);
     if (lane >= o) x += y;
   }
   for (int o = 16; o > 0; o >>= 1) pre += __shfl_xor_sync(0xffffffffu, pre, o);
-  if (lane == 31) ws[wid] = x;
-  if (lane == 0) wp[wid] = pre;
-  __syncthreads();
-  int warpOff = 0, excl = 0;
-#pragma unroll
-  for (int k = 0; k < kWarps; k++) {
-    warpOff += (k < wid) ? ws[k] : 0;
-    excl += wp[k];
-  }
-  int run = P.atomOff + excl + warpOff + x - sum;
-#pragma unroll
-  for (int i = 0; i < kPer; i++) {
-    cellStart[cb + i] = run;
-    run += v[i];
-    cellCount[cb + i] = 0;
-  }
-  // work items of the list build, as in k_scan_final; one atomic per list for the block
-  int nLight = 0, nHeavy = 0;
-#pragma unroll
-  for (int i = 0; i < kPer; i++) {
-    if (v[i] > 0 && c0 + threadIdx.x * kPer + i < P.ncells) {
-      if (v[i] > itemAtoms) nHeavy += (v[i] + itemAtoms - 1) / itemAtoms;
-      else nLight++;
-    }
-  }
-  int preL = nLight, preH = nHeavy;
+  // work items of the list build: a cell of more than itemAtoms atoms splits into near-equal
+  // items {cell, first << 16 | count}, the others are listed whole
+  const bool live = own && v > 0 && c0 + tid < P.ncells;
+  const int nHeavy = (live && v > itemAtoms) ? (v + itemAtoms - 1) / itemAtoms : 0;
+  const int nLight = (live && v <= itemAtoms) ? 1 : 0;
+  int preL = nLight, preH = nHeavy, occ = n, over = (n > cap) ? 1 : 0;
   for (int o = 1; o < 32; o <<= 1) {
     const int yl = __shfl_up_sync(0xffffffffu, preL, o);
     const int yh = __shfl_up_sync(0xffffffffu, preH, o);
@@ -439,21 +437,26 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_cells(const int *__restri
     over += __shfl_xor_sync(0xffffffffu, over, o);
   }
   if (lane == 31) {
+    ws[wid] = x;
     wl[wid] = preL;
     wh[wid] = preH;
     wOcc[wid] = occ;
     wOver[wid] = over;
   }
+  if (lane == 0) wp[wid] = pre;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int tl = 0, th = 0, to = 0, tv = 0;
+  if (tid == 0) {
+    int tl = 0, th = 0, to = 0, tv = 0, ta = 0, tp = 0;
     for (int k = 0; k < kWarps; k++) {
-      const int l = wl[k], h = wh[k];
-      wl[k] = tl; wh[k] = th;  // exclusive warp offsets
-      tl += l; th += h;
+      const int a = ws[k], l = wl[k], h = wh[k];
+      ws[k] = ta; wl[k] = tl; wh[k] = th;  // exclusive warp offsets
+      ta += a; tl += l; th += h;
       to = max(to, wOcc[k]);
       tv += wOver[k];
+      tp += wp[k];
     }
+    sEx[kScanCells] = ta;
+    sBase = P.atomOff + tp;
     sBaseL = tl > 0 ? atomicAdd(&work[1], tl) : 0;
     sBaseH = th > 0 ? atomicAdd(&work[2], th) : 0;
     if (to > 0) atomicMax(&S->maxCellOcc, to);
@@ -463,79 +466,42 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_cells(const int *__restri
     }
   }
   __syncthreads();
-  int outL = sBaseL + wl[wid] + preL - nLight;
-  int outH = sBaseH + wh[wid] + preH - nHeavy;
-#pragma unroll
-  for (int i = 0; i < kPer; i++) {
-    if (v[i] > 0 && c0 + threadIdx.x * kPer + i < P.ncells) {
-      if (v[i] > itemAtoms) {
-        const int k = (v[i] + itemAtoms - 1) / itemAtoms;
-        for (int j = 0; j < k; j++) {
-          const int h0 = j * v[i] / k, h1 = (j + 1) * v[i] / k;
-          heavy[outH++] = make_int2(cb + i, (h0 << 16) | (h1 - h0));
-        }
-      } else {
-        active[outL++] = cb + i;
+  const int ex = ws[wid] + x - v;  // exclusive prefix inside the block
+  if (own) {
+    sEx[tid] = ex;
+    cellStart[cb + tid] = sBase + ex;
+    cellCount[cb + tid] = 0;
+  }
+  if (live) {
+    if (nHeavy) {
+      int outH = sBaseH + wh[wid] + preH - nHeavy;
+      for (int j = 0; j < nHeavy; j++) {
+        const int h0 = j * v / nHeavy, h1 = (j + 1) * v / nHeavy;
+        heavy[outH++] = make_int2(cb + tid, (h0 << 16) | (h1 - h0));
       }
+    } else {
+      active[sBaseL + wl[wid] + preL - nLight] = cb + tid;
     }
   }
-}
-
-// Orders each cell by ascending atom index, from the cell's bucket: the rank of an atom is the
-// number of atoms of its bucket with a smaller index.  Also clears blockCount.  Writes the sorted index and a sorted
-// position copy whose w holds the atom index (as int bits); an atom outside the grid gets
-// empty lists (the reference clears its NN) and is counted in cellRange.
-__global__ void k_rank_cells(BlockTab tab, const RepConst *__restrict__ rc, RepState *st,
-                             const int *__restrict__ cellOf, const int *__restrict__ slot,
-                             const int *__restrict__ cellStart, const int *__restrict__ bucket, int cap,
-                             const float4 *__restrict__ pos, int *__restrict__ sortIdx,
-                             float4 *__restrict__ sortPos, int *__restrict__ nn, int *__restrict__ ns,
-                             int *__restrict__ nrl, int forceRebuild, int *__restrict__ blockCount,
-                             int nBlockCount) {
-  pdlEnter();
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nBlockCount; i += gridDim.x * blockDim.x)
-    blockCount[i] = 0;  // k_scan_cells has read them
-  const int rep = tab.rep[blockIdx.x];
-  RepState *S = st + rep;
-  const RepConst &P = rc[rep];
-  const int g = tab.start[blockIdx.x] + threadIdx.x;
-  if (g >= P.atomOff + P.nMol) return;
-  // independent loads first: one round trip for all of them
-  const int c = cellOf[g];
-  const int sg = slot[g];
-  float4 r = pos[g];
-  if (!rebuilding(S, forceRebuild)) return;
-  if (c < 0) {
-    nn[g] = 0;
-    ns[g] = 0;
-    nrl[g] = 0;
-    atomicAdd(&S->cellRange, 1);
-    return;
-  }
-  if (sg >= cap) return;  // not filed: the cell overflowed
-  const int gc = P.cellOff + c;
-  const int b = cellStart[gc], n = cellStart[gc + 1] - b;
-  const int *bk = bucket + (size_t)gc * cap;
-  int rank = 0;
-  if ((cap & 3) == 0) {  // rows of a multiple of 4 slots: 16-byte loads, four at a time
-    for (int q = 0; q < n; q += 16) {
-      int4 u[4];
+  __syncthreads();
+  // ordering: block entry e is slot s of cell j (the last cell whose prefix is <= e)
+  const int nBlk = sEx[kScanCells];
+#pragma unroll 4
+  for (int e = tid; e < nBlk; e += kScanRankThreads) {
+    int j = 0;
 #pragma unroll
-      for (int k = 0; k < 4; k++)
-        u[k] = (q + 4 * k < n) ? *reinterpret_cast<const int4 *>(bk + q + 4 * k) : make_int4(g, g, g, g);
-#pragma unroll
-      for (int k = 0; k < 4; k++) {
-        const int q0 = q + 4 * k;
-        rank += (q0 < n && u[k].x < g) + (q0 + 1 < n && u[k].y < g) + (q0 + 2 < n && u[k].z < g) +
-                (q0 + 3 < n && u[k].w < g);
-      }
-    }
-  } else {
-    for (int q = 0; q < n; q++) rank += (bk[q] < g) ? 1 : 0;
+    for (int step = kScanCells / 2; step > 0; step >>= 1)
+      if (sEx[j + step] <= e) j += step;
+    const int b = sEx[j], m = sEx[j + 1] - b, s = e - b;
+    const int *bk = bucket + (size_t)(cb + j) * cap;
+    const int g = bk[s];
+    int rank = 0;
+    for (int q = 0; q < m; q++) rank += (bk[q] < g) ? 1 : 0;
+    float4 r = pos[g];
+    r.w = __int_as_float(g);
+    sortIdx[sBase + b + rank] = g;
+    sortPos[sBase + b + rank] = r;
   }
-  sortIdx[b + rank] = g;
-  r.w = __int_as_float(g);
-  sortPos[b + rank] = r;
 }
 
 // ============================================================================================
@@ -856,15 +822,21 @@ __device__ __forceinline__ void nebrBody(const int *__restrict__ tileRep, const 
       int *work, const RepConst *__restrict__ rc, RepState *st, const int *__restrict__ cellStart,     \
       const float4 *__restrict__ sortPos, int *__restrict__ nn, int *__restrict__ nbl,                 \
       int *__restrict__ ns, int *__restrict__ sl, int *__restrict__ nrl, int2 *__restrict__ rl,        \
-      int rowStride, int nebrMax, int descending
+      int rowStride, int nebrMax, int descending, int *__restrict__ blockCount, int nBlockCount
 #define SG_NEBR_ARGS \
   tileRep, active, heavy, work, rc, st, cellStart, sortPos, nn, nbl, ns, sl, nrl, rl, rowStride, nebrMax, descending
+// the binning's per-block counts, read by k_scan_rank, start the next rebuild at zero
+__device__ __forceinline__ void clearBlockCount(int *blockCount, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) blockCount[i] = 0;
+}
 __global__ void __launch_bounds__(kNebrWarps * 32) k_build_nebr(SG_NEBR_PARAMS) {
   pdlEnter();
+  clearBlockCount(blockCount, nBlockCount);
   nebrBody<false>(SG_NEBR_ARGS);
 }
 __global__ void __launch_bounds__(kNebrWarps * 32) k_build_nebr_lanes(SG_NEBR_PARAMS) {
   pdlEnter();
+  clearBlockCount(blockCount, nBlockCount);
   nebrBody<true>(SG_NEBR_ARGS);
 }
 #undef SG_NEBR_PARAMS
@@ -893,8 +865,11 @@ __global__ void __launch_bounds__(128) k_build_nebr_atoms(BlockTab tab, const Re
                                                           int *__restrict__ ns, int *__restrict__ sl,
                                                           int *__restrict__ nrl, int2 *__restrict__ rl,
                                                           int rowStride, int nebrMax, int *__restrict__ work,
-                                                          int forceRebuild) {
+                                                          int forceRebuild, int *__restrict__ blockCount,
+                                                          int nBlockCount) {
   pdlEnter();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nBlockCount; i += gridDim.x * blockDim.x)
+    blockCount[i] = 0;  // k_scan_rank has read them
   if (blockIdx.x == 0 && threadIdx.x < 3) work[threadIdx.x] = 0;
   const int rep = tab.rep[blockIdx.x];
   RepState *S = st + rep;

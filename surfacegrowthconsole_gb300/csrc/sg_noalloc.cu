@@ -207,7 +207,8 @@ extern "C" int sg_compute_forces_noalloc(const sg_simparams *p, sg_float4 *d_pos
   k_rank<<<nAtomBlk, kBs, 0, s>>>(atomTab, rc, st, cellOf, cellStart, tmpIdx, pos, sortIdx, sortPos, 1);
   const int rowStride = (p->iNebrMax + 3) & ~3;
   k_build_nebr<<<256, kNebrWarps * 32, 0, s>>>(tileRep, active, heavy, work, rc, st, cellStart, sortPos, nn, nbl, ns,
-                                               sl, nrl, rl, rowStride, p->iNebrMax, 0);
+                                               sl, nrl, rl, rowStride, p->iNebrMax, 0,
+                                               nullptr, 0);
   if (nMetalBlk) {
     k_rho<<<nMetalBlk, kBs, 0, s>>>(metalTab, rc, pos, nn, nbl, rho, dF, Fv, rowStride);
     k_force_metal<<<nMetalBlk, kBs, 0, s>>>(metalTab, rc, pos, acc, nn, nbl, dF, Fv, fric, rowStride);
