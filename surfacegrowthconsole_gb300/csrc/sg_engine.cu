@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <chrono>
 #include <cstring>
 #include <map>
 #include <string>
@@ -326,10 +327,16 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
   AL(c->diffBuf, std::max<size_t>(diffOff, 1));
   AL(c->dDiffOff, n_replicas);
   AL(c->stage, 6 * N);  // two float3 arrays in transit at once
-  if (cudaMallocHost(&c->hostSt, sizeof(RepState) * n_replicas) != cudaSuccess) {
+  if (cudaMallocHost(&c->hostSt, sizeof(RepState) * n_replicas + 64) != cudaSuccess) {
     c->hostSt = nullptr;
     sg_destroy(c);
-    return sg_fail(SG_ERR_NOMEM, "cudaMallocHost(%zu)", sizeof(RepState) * n_replicas);
+    return sg_fail(SG_ERR_NOMEM, "cudaMallocHost(%zu)", sizeof(RepState) * n_replicas + 64);
+  }
+  c->hostSeq = reinterpret_cast<volatile unsigned *>(reinterpret_cast<char *>(c->hostSt) + sizeof(RepState) * n_replicas);
+  *c->hostSeq = 0u;
+  if (cudaMalloc(&c->devSeq, sizeof(unsigned)) != cudaSuccess || cudaMemset(c->devSeq, 0, sizeof(unsigned)) != cudaSuccess) {
+    sg_destroy(c);
+    return sg_fail(SG_ERR_NOMEM, "cudaMalloc(sequence counter)");
   }
 #undef AL
   if (c->opt.phase_timing)
@@ -439,6 +446,7 @@ extern "C" int sg_destroy(sg_ctx *c) {
     if (e) cudaEventDestroy(e);
   for (void *p : c->allocs) cudaFree(p);
   if (c->hostSt) cudaFreeHost(c->hostSt);
+  if (c->devSeq) cudaFree(c->devSeq);
   if (c->side) cudaStreamSynchronize(c->side);
   if (c->evFork) cudaEventDestroy(c->evFork);
   if (c->evJoin) cudaEventDestroy(c->evJoin);
@@ -767,9 +775,28 @@ extern "C" int sg_step(sg_ctx *c, int nsteps) {
     if (rc) return rc;
     advanceSchedule(c, v, nullptr);
   }
-  // the replica states come back in the same synchronisation (flags, and sg_step_thermo's record)
-  CK(cudaMemcpyAsync(c->hostSt, c->st, sizeof(RepState) * c->nrep, cudaMemcpyDeviceToHost, c->stream));
-  CK(cudaStreamSynchronize(c->stream));
+  // the replica states come back to the page-locked mirror (flags, and sg_step_thermo's record),
+  // followed by a sequence number the host waits for: a stream synchronisation's wake-up costs
+  // more than this wait.  If the number does not come (a failed launch), the synchronisation
+  // reports why.
+  const int nwords = (int)(sizeof(RepState) * c->nrep / 4);
+  k_publish_state<<<1, 256, 0, c->stream>>>(reinterpret_cast<const int *>(c->st), reinterpret_cast<int *>(c->hostSt),
+                                            nwords, c->devSeq, c->hostSeq);
+  CK(cudaGetLastError());
+  const unsigned want = ++c->pubSeq;
+  const auto t0 = std::chrono::steady_clock::now();
+  bool seen = false;
+  for (unsigned spin = 0;; spin++) {
+    if (*c->hostSeq == want) {
+      seen = true;
+      break;
+    }
+    if ((spin & 1023u) == 1023u && std::chrono::steady_clock::now() - t0 > std::chrono::seconds(2)) break;
+  }
+  if (!seen) {
+    CK(cudaStreamSynchronize(c->stream));
+    if (*c->hostSeq != want) return sg_fail(SG_ERR_CUDA, "step results not published");
+  }
   return flagsFromMirror(c);
 }
 

@@ -1616,6 +1616,21 @@ __global__ void __launch_bounds__(kUnpackAtoms) k_unpack_state(const float4 *sr,
   if (i < nrep) st[i].thermoPending = 0;
 }
 
+// The replica states to the host's page-locked mirror (dst, its device address), then a new
+// sequence number next to it: the host waits for that number instead of a stream
+// synchronisation.  Every thread's copy is made visible system-wide before the number is.
+__global__ void k_publish_state(const int *src, int *dst, int nwords, unsigned *devSeq, volatile unsigned *hostSeq) {
+  for (int i = threadIdx.x; i < nwords; i += blockDim.x) dst[i] = __ldcg(src + i);
+  __threadfence_system();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned seq = *devSeq + 1u;
+    *devSeq = seq;
+    __threadfence_system();
+    *hostSeq = seq;
+  }
+}
+
 __global__ void k_clear_pending(RepState *st, int nrep) {
   pdlEnter();
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
