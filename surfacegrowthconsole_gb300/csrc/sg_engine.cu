@@ -776,9 +776,9 @@ extern "C" int sg_step(sg_ctx *c, int nsteps) {
     advanceSchedule(c, v, nullptr);
   }
   // the replica states come back to the page-locked mirror (flags, and sg_step_thermo's record),
-  // followed by a sequence number the host waits for: a stream synchronisation's wake-up costs
-  // more than this wait.  If the number does not come (a failed launch), the synchronisation
-  // reports why.
+  // followed by a sequence number the host polls for: a stream synchronisation's wake-up costs
+  // more than this wait.  After 5 ms of polling (long batches of steps, or a failed launch) the
+  // host synchronises the stream instead, which also reports any error.
   const int nwords = (int)(sizeof(RepState) * c->nrep / 4);
   k_publish_state<<<1, 256, 0, c->stream>>>(reinterpret_cast<const int *>(c->st), reinterpret_cast<int *>(c->hostSt),
                                             nwords, c->devSeq, c->hostSeq);
@@ -791,7 +791,7 @@ extern "C" int sg_step(sg_ctx *c, int nsteps) {
       seen = true;
       break;
     }
-    if ((spin & 1023u) == 1023u && std::chrono::steady_clock::now() - t0 > std::chrono::seconds(2)) break;
+    if ((spin & 1023u) == 1023u && std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(5)) break;
   }
   if (!seen) {
     CK(cudaStreamSynchronize(c->stream));
