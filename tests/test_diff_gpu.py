@@ -62,7 +62,7 @@ def test_torch_autograd_harness_carries_the_adjoint_gradient_and_fits():
     loss.backward()
     L, g = model.force_matching(theta0, ref)
     # two evaluations: the parameter sums use atomics, whose order varies (~1e-7 relative)
-    assert abs(float(loss) - L) <= 1e-6 * L
+    assert abs(float(loss.detach()) - L) <= 1e-6 * L
     assert rel_inf(t.grad.numpy(), g) < 1e-5
     _, hist = fit(model, theta0, ref, steps=30, lr=5e-3)
     assert hist[-1] < 0.5 * hist[0], hist[::10]
