@@ -39,7 +39,7 @@ constexpr int kRelMax = 48;       // relevant-list capacity per carbon atom
 constexpr int kShortMax = 8;      // close-list capacity per carbon atom (a multiple of 4)
 constexpr int kHeavyCell = 16;    // list build: default home atoms per work item (larger cells split)
 constexpr int kHeavyChunk = 8;    // sizes the item list of the fixed-size scratch (>= kHeavyCell / 2)
-constexpr int kScanCells = 128;   // cells per block of the single-pass cell scan and ordering
+constexpr int kScanCells = 128;   // cells per block of the single-pass cell scan and ordering (or 2x)
 constexpr int kScanRankThreads = 512;  // threads of that block (the ordering uses all of them)
 constexpr int kMixThreads = 512;  // MIXED step reduction: threads per block
 constexpr int kMixAtoms = 512;    // and the fewest atoms per block (1 per thread; up to 8 at large sizes)
@@ -67,6 +67,7 @@ struct RepConst {
   int cells[3], ncells, ncellsPad;
   int atomOff, nMol, nMolMe, cellOff;
   int nRedBlocks;  // ceil(nMol / 1024)
+  int scanCells;   // cells per block of the scan and ordering (kScanCells or 2 kScanCells)
   int nRedBlocksM, redFirstM;  // MIXED reduction: blocks of kMixAtoms atoms, first partial slot
   // integrator
   float deltaT, rrNebr, rNebrShell, rrShort;
@@ -182,7 +183,7 @@ __device__ __forceinline__ int cellIndex(const RepConst &P, float x, float y, fl
 // Minimum image of one component as the force kernels do it (SurfaceGrowth.cu:750-759).
 // Cell of atom g and its arrival slot in the cell; with a bucket (cap slots per cell, the
 // reference's blockSize) the atom is also filed there, and counted in blockCount per block of
-// kScanCells cells (one atomic per block among the warp's atoms), for k_scan_rank.
+// P.scanCells cells (one atomic per block among the warp's atoms), for k_scan_rank.
 __device__ __forceinline__ void binAtom(const RepConst &P, int g, const float4 &r, int *cellOf, int *slot,
                                         int *cellCount, int *bucket, int cap, int *blockCount) {
   const int c = cellIndex(P, r.x, r.y, r.z);
@@ -193,7 +194,7 @@ __device__ __forceinline__ void binAtom(const RepConst &P, int g, const float4 &
     slot[g] = s;
     if (bucket && s < cap) {
       bucket[(size_t)(P.cellOff + c) * cap + s] = g;
-      key = (P.cellOff + c) / kScanCells;
+      if (blockCount) key = (P.cellOff + c) / P.scanCells;
     }
   }
   if (blockCount) {

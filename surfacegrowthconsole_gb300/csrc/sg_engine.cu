@@ -108,6 +108,7 @@ static RepConst makeConst(const sg_simparams &p) {
   P.nMol = p.nMol;
   P.nMolMe = p.nMolMe;
   P.nRedBlocks = (p.nMol + kRedElems - 1) / kRedElems;
+  P.scanCells = kScanCells;
   P.deltaT = p.deltaT;
   P.rrNebr = p.rrNebr;
   P.rNebrShell = p.rNebrShell;
@@ -363,7 +364,12 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
       for (int t = 0; t < P.ncellsPad; t += kCellTile) { tr.push_back(r); ts.push_back(t); }
     }
     c->ntiles = (int)tr.size();
-    c->nScanBlocks = c->ntiles * (kCellTile / kScanCells);
+    // cells per scan block: 2 kScanCells when that still gives two blocks per SM (large and
+    // batched systems: fewer, fuller blocks), else kScanCells
+    c->scanCells = ((long long)c->ntiles * (kCellTile / (2 * kScanCells)) >= 2LL * std::max(numSMs, 1))
+                       ? 2 * kScanCells : kScanCells;
+    for (auto &P : c->hrc) P.scanCells = c->scanCells;
+    c->nScanBlocks = c->ntiles * (kCellTile / c->scanCells);
     if ((rc = uploadTab(c, c->redTab, rr, ss)) || (rc = uploadTab(c, c->cmvTab, cr, cs)) ||
         (rc = uploadTab(c, c->tileTab, tr, ts))) {
       sg_destroy(c);
@@ -563,7 +569,7 @@ enum { V_SHEAR = 1, V_RDF = 2, V_RDF_ZERO = 4 };
 
 static int enqueueRebuild(sg_ctx *c, int force) {
   const int fr = force;
-  CK(launchK(c->pdl, k_scan_rank, c->nScanBlocks, kScanRankThreads, 0, c->stream, c->tileTab.rep, c->tileTab.start,
+  CK(launchScanRank(c->pdl, c->scanCells, c->nScanBlocks, c->stream, c->tileTab.rep, c->tileTab.start,
              c->dTileFirst, c->rc, c->st, c->cellCount, c->cellStart, c->bucketCap, fr, c->activeCells,
              c->heavyItems, c->nebrWork, c->nebrItemAtoms, c->blockCount, c->bucket, c->cellOf, c->pos,
              c->sortIdx, c->sortPos, c->nn, c->ns, c->nrl));

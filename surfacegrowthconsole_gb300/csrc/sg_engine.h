@@ -42,7 +42,8 @@ struct sg_ctx {
   int nebrGrid = 0;
   int *activeCells = nullptr, *nebrWork = nullptr;
   int *bucket = nullptr, bucketCap = 64;  // atoms of each cell in arrival order, bucketCap slots per cell
-  int *blockCount = nullptr;  // filed atoms per block of kScanCells cells (zero between rebuilds)
+  int *blockCount = nullptr;  // filed atoms per block of scanCells cells (zero between rebuilds)
+  int scanCells = sg::kScanCells;  // cells per block of the scan and ordering
   int nScanBlocks = 0;
   int2 *heavyItems = nullptr;
   float *rho = nullptr, *dF = nullptr, *Fv = nullptr, *fric = nullptr;

@@ -17,12 +17,12 @@ __global__ void k_build_nebr_atoms(BlockTab tab, const RepConst *rc, RepState *s
                                    const int *cellStart, const float4 *sortPos, int *nn, int *nbl, int *ns,
                                    int *sl, int *nrl, int2 *rl, int rowStride, int nebrMax, int *work,
                                    int forceRebuild, int *blockCount, int nBlockCount);
-// one block of kScanRankThreads threads per kScanCells cells
-__global__ void k_scan_rank(const int *tileRep, const int *tileStart, const int *tileFirst, const RepConst *rc,
-                            RepState *st, int *cellCount, int *cellStart, int cap, int forceRebuild, int *active,
-                            int2 *heavy, int *work, int itemAtoms, const int *blockCount, const int *bucket,
-                            const int *cellOf, const float4 *pos, int *sortIdx, float4 *sortPos, int *nn, int *ns,
-                            int *nrl);
+// the cell scan and in-cell ordering: one block of kScanRankThreads threads per `cells` cells
+cudaError_t launchScanRank(bool pdl, int cells, int grid, cudaStream_t s, const int *tileRep, const int *tileStart,
+                           const int *tileFirst, const RepConst *rc, RepState *st, int *cellCount, int *cellStart,
+                           int cap, int forceRebuild, int *active, int2 *heavy, int *work, int itemAtoms,
+                           const int *blockCount, const int *bucket, const int *cellOf, const float4 *pos,
+                           int *sortIdx, float4 *sortPos, int *nn, int *ns, int *nrl);
 __global__ void k_scan_tiles(BlockTab tab, const RepConst *rc, const RepState *st,
                              const int *cellCount, int *tileSum, int forceRebuild);
 __global__ void k_scan_tile_prefix(const RepConst *rc, const RepState *st, const int *tileFirst,

@@ -356,19 +356,20 @@ __global__ void k_rank(BlockTab tab, const RepConst *__restrict__ rc, const RepS
 
 // ============================================================================================
 // Counting sort in two passes (the engine's path).  The histogram pass (binAtom) files each
-// atom in its cell's bucket and counts the filed atoms per block of kScanCells cells
-// (blockCount).  k_scan_rank: one block per kScanCells cells takes its exclusive offset from
+// atom in its cell's bucket and counts the filed atoms per block of P.scanCells cells
+// (blockCount).  k_scan_rank: one block per P.scanCells cells takes its exclusive offset from
 // the counts of the replica's earlier blocks (no wait on another block), scans its cells,
 // writes cellStart and the list build's work items and orders each of its cells from its
 // bucket; the list build clears blockCount for the next rebuild.
 // ============================================================================================
 // The cell scan and the in-cell ordering in one pass: one block of kScanRankThreads threads per
-// kScanCells cells takes its exclusive atom offset from the replica's earlier blocks' counts
+// CELLS cells takes its exclusive atom offset from the replica's earlier blocks' counts
 // (blockCount), scans its cells (a thread per cell), writes cellStart and the list build's work
 // items, then orders the atoms of its cells with all its threads: block entry e (cell j, bucket
 // slot s) goes to position cellStart[j] + (number of atoms of j's bucket with a smaller index),
 // a few entries per thread with their loads in flight together.  Atoms outside the grid get
 // empty lists.  blockCount is cleared by the list build (all blocks have read it then).
+template <int CELLS>
 __global__ void __launch_bounds__(kScanRankThreads) k_scan_rank(const int *__restrict__ tileRep,
                                                           const int *__restrict__ tileStart,
                                                           const int *__restrict__ tileFirst,
@@ -382,11 +383,11 @@ __global__ void __launch_bounds__(kScanRankThreads) k_scan_rank(const int *__res
                                                           float4 *__restrict__ sortPos, int *__restrict__ nn,
                                                           int *__restrict__ ns, int *__restrict__ nrl) {
   pdlEnter();
-  constexpr int kSub = kCellTile / kScanCells;  // scan blocks per tile of the tile table
+  constexpr int kSub = kCellTile / CELLS;  // scan blocks per tile of the tile table
   constexpr int kWarps = kScanRankThreads / 32;
-  static_assert(kScanCells % 32 == 0 && kScanCells <= kScanRankThreads, "one cell per scan thread");
+  static_assert(CELLS % 32 == 0 && CELLS <= kScanRankThreads, "one cell per scan thread");
   __shared__ int ws[kWarps], wp[kWarps], wl[kWarps], wh[kWarps], wOcc[kWarps], wOver[kWarps];
-  __shared__ int sEx[kScanCells + 1];  // exclusive prefix of the block's cell counts
+  __shared__ int sEx[CELLS + 1];  // exclusive prefix of the block's cell counts
   __shared__ int sBaseL, sBaseH, sBase;
   const int t = blockIdx.x;
   const int rep = tileRep[t / kSub];
@@ -395,16 +396,16 @@ __global__ void __launch_bounds__(kScanRankThreads) k_scan_rank(const int *__res
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const RepConst &P = rc[rep];
   const int first = tileFirst[rep] * kSub;  // the replica's first scan block
-  const int c0 = tileStart[t / kSub] + (t % kSub) * kScanCells;
+  const int c0 = tileStart[t / kSub] + (t % kSub) * CELLS;
   const int cb = P.cellOff + c0;  // the block's first global cell
-  const bool own = tid < kScanCells;  // this thread scans cell tid of the block
+  const bool own = tid < CELLS;  // this thread scans cell tid of the block
   const int n = own ? cellCount[cb + tid] : 0;
   const int v = min(n, cap);  // atoms past the cap are not in the bucket (SG_ERR_CELL_OVERFLOW)
   int pre = 0;                // atoms filed in the replica's earlier blocks
   for (int q = first + tid; q < t; q += kScanRankThreads) pre += blockCount[q];
   // atoms outside the grid: empty lists (the reference clears their NN), counted in cellRange
   {
-    const int lb = t - first, nb = P.ncellsPad / kScanCells;
+    const int lb = t - first, nb = P.ncellsPad / CELLS;
     int outside = 0;
     for (int g = P.atomOff + lb * kScanRankThreads + tid; g < P.atomOff + P.nMol; g += nb * kScanRankThreads)
       if (cellOf[g] < 0) {
@@ -455,7 +456,7 @@ __global__ void __launch_bounds__(kScanRankThreads) k_scan_rank(const int *__res
       tv += wOver[k];
       tp += wp[k];
     }
-    sEx[kScanCells] = ta;
+    sEx[CELLS] = ta;
     sBase = P.atomOff + tp;
     sBaseL = tl > 0 ? atomicAdd(&work[1], tl) : 0;
     sBaseH = th > 0 ? atomicAdd(&work[2], th) : 0;
@@ -485,12 +486,12 @@ __global__ void __launch_bounds__(kScanRankThreads) k_scan_rank(const int *__res
   }
   __syncthreads();
   // ordering: block entry e is slot s of cell j (the last cell whose prefix is <= e)
-  const int nBlk = sEx[kScanCells];
+  const int nBlk = sEx[CELLS];
 #pragma unroll 4
   for (int e = tid; e < nBlk; e += kScanRankThreads) {
     int j = 0;
 #pragma unroll
-    for (int step = kScanCells / 2; step > 0; step >>= 1)
+    for (int step = CELLS / 2; step > 0; step >>= 1)
       if (sEx[j + step] <= e) j += step;
     const int b = sEx[j], m = sEx[j + 1] - b, s = e - b;
     const int *bk = bucket + (size_t)(cb + j) * cap;
@@ -502,6 +503,21 @@ __global__ void __launch_bounds__(kScanRankThreads) k_scan_rank(const int *__res
     sortIdx[sBase + b + rank] = g;
     sortPos[sBase + b + rank] = r;
   }
+}
+
+// k_scan_rank with `cells` (kScanCells or 2 kScanCells) cells per block.
+cudaError_t launchScanRank(bool pdl, int cells, int grid, cudaStream_t s, const int *tileRep, const int *tileStart,
+                           const int *tileFirst, const RepConst *rc, RepState *st, int *cellCount, int *cellStart,
+                           int cap, int forceRebuild, int *active, int2 *heavy, int *work, int itemAtoms,
+                           const int *blockCount, const int *bucket, const int *cellOf, const float4 *pos,
+                           int *sortIdx, float4 *sortPos, int *nn, int *ns, int *nrl) {
+  if (cells == 2 * kScanCells)
+    return launchK(pdl, k_scan_rank<2 * kScanCells>, grid, kScanRankThreads, 0, s, tileRep, tileStart, tileFirst, rc,
+                   st, cellCount, cellStart, cap, forceRebuild, active, heavy, work, itemAtoms, blockCount, bucket,
+                   cellOf, pos, sortIdx, sortPos, nn, ns, nrl);
+  return launchK(pdl, k_scan_rank<kScanCells>, grid, kScanRankThreads, 0, s, tileRep, tileStart, tileFirst, rc, st,
+                 cellCount, cellStart, cap, forceRebuild, active, heavy, work, itemAtoms, blockCount, bucket, cellOf,
+                 pos, sortIdx, sortPos, nn, ns, nrl);
 }
 
 // ============================================================================================
