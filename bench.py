@@ -15,7 +15,7 @@ LJ, graphene, reductions, thermostat, RDF/diffusion when due).
           the "stated drift" the two forms are compared at.
   e2e   : the same metric through the public C ABI with host buffers: every step uploads the
           state (r, v, a) from pinned host memory, steps, and reads the step's thermo record, in
-          one sg_step_from_host call (one synchronisation per step).
+          one sg_step_from_host call (one wait per step).
   roofline : the neighbour-list build (the largest share of the step): its compulsory bytes per
           launch / its mean duration (CUDA events around it on the library's stream), against
           the measured HBM copy peak.  The phase durations come from a second pass of the same
@@ -529,7 +529,7 @@ def run_production(args, rank: int, world: int, local: int, dist):
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         # r, v, a from pinned host memory, one step, the thermo record back: one call, one
-        # synchronisation (sg_step_from_host)
+        # wait (sg_step_from_host)
         th = sim.step_from_host(hr, hv, ha, nsteps=1)
     barrier()
     e2e_s = max_over_ranks(time.perf_counter() - t0)

@@ -128,7 +128,10 @@ int sg_get_params(sg_ctx *ctx, int rep, sg_simparams *out);
  * (SurfaceGrowth.cu:2141-2489) without file output: Verlet part 1 + wrap, cell/neighbour
  * rebuild when nebrNow, EAM density, forces, friction sum, Verlet part 2, tribology
  * reductions, nanoparticle diffusion sample, momentum/max-v2/Sum mv2, Berendsen thermostat,
- * potential energy, rebuild criterion, shear, RDF sample, property accumulation. */
+ * potential energy, rebuild criterion, shear, RDF sample, property accumulation.  Returns
+ * when the steps are done: a one-block kernel copies the replica states to a page-locked host
+ * mirror followed by a sequence number, which the call polls for up to 5 ms before it falls back
+ * to synchronising the stream (which also reports a failed launch). */
 int sg_step(sg_ctx *ctx, int nsteps);
 /* Bytes sg_step copies back to the host after its steps (the replicas' state records). */
 long long sg_step_readback_bytes(const sg_ctx *ctx);
@@ -162,12 +165,12 @@ typedef struct sg_thermo {
     sg_prop props[7];  /* totEnergy, potEnergy, kinEnergy, oneStep, centerOfMass, cmVel, frictForce */
 } sg_thermo;
 int sg_get_thermo(sg_ctx *ctx, int rep, sg_thermo *out);
-/* sg_step, then replica rep's thermo record (as sg_get_thermo) from the same synchronisation. */
+/* sg_step, then replica rep's thermo record (as sg_get_thermo) from the same wait. */
 int sg_step_thermo(sg_ctx *ctx, int nsteps, int rep, sg_thermo *thermo);
 /* A step from host buffers in one call: sg_set_state(ctx, rep, r, v, a), then sg_step(ctx,
- * nsteps) and, if thermo is not NULL, replica thermo_rep's record, with one synchronisation
- * for the whole (the copies are enqueued on the context's stream ahead of the steps; the host
- * buffers are free again when the call returns).  Results equal those of the three calls. */
+ * nsteps) and, if thermo is not NULL, replica thermo_rep's record, with one wait for the
+ * whole (the copies are enqueued on the context's stream ahead of the steps; the host buffers
+ * are free again when the call returns).  Results equal those of the three calls. */
 int sg_step_from_host(sg_ctx *ctx, int rep, const sg_float4 *r, const sg_float3 *v, const sg_float3 *a,
                       int nsteps, int thermo_rep, sg_thermo *thermo);
 

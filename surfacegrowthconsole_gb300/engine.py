@@ -162,7 +162,7 @@ class Simulation:
     def step_from_host(self, r: np.ndarray | None, v: np.ndarray | None = None, a: np.ndarray | None = None,
                        nsteps: int = 1, rep: int = -1, thermo_rep: int | None = 0) -> Thermo | None:
         """set_state(r, v, a, rep), nsteps steps and replica thermo_rep's thermo record (None:
-        no record) in one call with one synchronisation (sg_step_from_host)."""
+        no record) in one call with one wait (sg_step_from_host)."""
         r_, v_, a_ = self._state_args(r, v, a, rep)
         t = Thermo() if thermo_rep is not None else None
         check(lib().sg_step_from_host(self._h, rep, _ptr(r_), _ptr(v_), _ptr(a_), nsteps,
@@ -204,7 +204,7 @@ class Simulation:
         return out[:n]
 
     def step_thermo(self, nsteps: int = 1, rep: int = 0) -> Thermo:
-        """nsteps steps and replica rep's thermo record, with one synchronisation."""
+        """nsteps steps and replica rep's thermo record, with one wait."""
         t = Thermo()
         check(lib().sg_step_thermo(self._h, nsteps, rep, C.byref(t)))
         return t
