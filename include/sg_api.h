@@ -77,8 +77,9 @@ typedef struct sg_options {
     int nebr_blocks_per_sm;/* resident 128-thread blocks per SM of the list build's work queue,
                             * 1..32 (0: 8) */
     int phase_timing;      /* 1: record CUDA events between the phases of every step */
-    int programmatic_launch; /* 1: launch the kernels of a step with programmatic dependent launch
-                            * (a kernel is scheduled while its predecessor drains); 0: off */
+    int programmatic_launch; /* 1 (default): launch the kernels of a step with programmatic
+                            * dependent launch (a kernel is launched once its predecessor's blocks
+                            * have exited and waits for its completion); 0: off */
     int nebr_descending;   /* 1: the list build takes the non-crowded cells in descending cell
                             * order (0: ascending) */
     int nebr_item_atoms;   /* list build: most home atoms of one work item (a warp's share); a

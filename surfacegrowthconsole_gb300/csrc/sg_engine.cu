@@ -55,6 +55,7 @@ extern "C" void sg_default_options(sg_options *o) {
   memset(o, 0, sizeof(*o));
   o->mode = SG_MODE_PLAIN;
   o->use_graphs = 1;
+  o->programmatic_launch = 1;
   o->rdf_ext_range = 0.f;
 }
 

@@ -87,7 +87,7 @@ class Simulation:
     def __init__(self, params: SimParams | Sequence[SimParams], mode: int = MODE_PLAIN, force_rebuild: bool = False,
                  use_graphs: bool = True, device: int = 0, rdf_ext_bins: int = 0, rdf_ext_range: float = 0.0,
                  eam_table_knots: int = 0, stream: int = 0, phase_timing: bool = False, metal_lanes: int = 0,
-                 nebr_blocks_per_sm: int = 0, programmatic_launch: bool = False, nebr_descending: int = 0,
+                 nebr_blocks_per_sm: int = 0, programmatic_launch: bool = True, nebr_descending: int = 0,
                  nebr_item_atoms: int = 0, nebr_build: int = 0, eam_table_smem: int = 0,
                  carbon_blocks_per_sm: int = 0):
         plist = [params] if isinstance(params, SimParams) else list(params)

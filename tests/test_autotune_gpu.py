@@ -74,7 +74,7 @@ def test_bad_shapes_are_refused():
     with pytest.raises(Exception):
         sim.set_launch_shape({"carbon_blocks_per_sm": 9})
     assert sim.launch_shape() == {"metal_lanes": 16, "nebr_blocks_per_sm": 8, "nebr_descending": 0,
-                                  "nebr_item_atoms": 8, "programmatic_launch": 0, "nebr_build": 0,
+                                  "nebr_item_atoms": 8, "programmatic_launch": 1, "nebr_build": 0,
                                   "eam_table_smem": 0, "carbon_blocks_per_sm": 8}
     sim.close()
 
