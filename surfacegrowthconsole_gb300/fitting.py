@@ -41,5 +41,5 @@ def fit(model: DiffModel, theta0: np.ndarray, ref: np.ndarray, steps: int = 50, 
         loss = ForceMatchingLoss.apply(base * (1 + x), model, ref)
         loss.backward()
         opt.step()
-        hist.append(float(loss))
+        hist.append(float(loss.detach()))
     return (base * (1 + x)).detach().numpy(), hist
