@@ -313,7 +313,9 @@ int sg_read_backup(const char *path, sg_simparams *p, sg_float4 *r, sg_float3 *v
  * lives in one static device array of SG_NOALLOC_SCRATCH_BYTES that every GPU loading the
  * library holds until the process exits; systems above the SG_NOALLOC_MAX_* limits are
  * rejected with SG_ERR_INVALID.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress), so make it before any stream capture.  All calls share the
+ * address (cudaGetSymbolAddress), so make it before any stream capture.  That address is kept
+ * for the device's primary context (the CUDA runtime's): do not call this after a
+ * cudaDeviceReset, or with another driver-API context current.  All calls share the
  * array: calls that overlap on the GPU (other streams, other host threads) race and corrupt
  * each other's results.  The call synchronises `stream` (a cudaStream_t, NULL: the default
  * stream) to report device-side conditions.  It calls no cudaMalloc/cudaFree. */

@@ -54,6 +54,10 @@ def lib():
             "orc_eam_eval": (C.c_double, [C.POINTER(SimParams), C.c_int, C.c_double, C.c_int]),
             "orc_rdf_allpairs": (None, [C.POINTER(SimParams), V, C.c_int, C.c_double, V]),
             "orc_diff_eval": (C.c_int, [V, C.c_int, V, V, V, V, V, V, V, V]),
+            "orc_get_last_avg": (None, [V, V]),
+            "orc_num_prints": (C.c_int, [V, C.c_int]),
+            "orc_get_rdf_print": (None, [V, V]),
+            "orc_get_diffuse_print": (C.c_int, [V, C.c_int, V]),
         }
         for n, (r, a) in sigs.items():
             f = getattr(L, n)
@@ -168,6 +172,32 @@ class OracleSim:
         cav = C.c_int()
         lib().orc_get_diffusion(self._h, _p(rr), _p(counts), C.byref(cav))
         return rr, counts, cav.value
+
+    def last_avg(self):
+        """The seven property accumulators {val, sum, sum2} of the last averaging step, before
+        they were zeroed: totEnergy, potEnergy, kinEnergy, oneStep, centerOfMass, cmVel,
+        frictForce (PrintSummary's inputs)."""
+        from surfacegrowthconsole_gb300._lib import Prop
+        out = (Prop * 7)()
+        lib().orc_get_last_avg(self._h, C.cast(out, C.c_void_p))
+        return list(out)
+
+    def num_rdf_prints(self) -> int:
+        return lib().orc_num_prints(self._h, 0)
+
+    def num_diffusion_tables(self) -> int:
+        return lib().orc_num_prints(self._h, 1)
+
+    def rdf_print(self):
+        out = np.zeros(self.p.sizeHistRdf, np.uint32)
+        lib().orc_get_rdf_print(self._h, _p(out))
+        return out
+
+    def diffusion_table(self, k: int):
+        out = np.zeros(self.p.nValDiffuse, np.float32)
+        if lib().orc_get_diffuse_print(self._h, k, _p(out)) != 0:
+            raise IndexError(k)
+        return out
 
     def diag(self):
         from surfacegrowthconsole_gb300._lib import Diag

@@ -11,9 +11,13 @@
 # cudaDeviceReset.  SurfaceGrowth.cpp's calls into the CUDA wrappers are renamed to
 # sgref_* stubs (the harness) so that parameter derivation, RNG and the result-file header
 # run without a GPU.  It also builds the reference kernels as cubins (end of file).
-# Usage: oracle/ref/build_ref.sh [REFERENCE_ROOT]
+# Usage: oracle/ref/build_ref.sh REFERENCE_ROOT   (or SG_REFERENCE_ROOT in the environment)
 set -euo pipefail
-REF=${1:-/root/reference}
+REF=${1:-${SG_REFERENCE_ROOT:-}}
+if [ -z "$REF" ]; then
+  echo "usage: build_ref.sh REFERENCE_ROOT (or set SG_REFERENCE_ROOT)" >&2
+  exit 3
+fi
 SRC="$REF/SurfaceGrowthConsole"
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/../_ref"

@@ -14,7 +14,7 @@
 // Globals and functions defined by SurfaceGrowth.cpp.
 extern cudaDeviceProp g_hDeviceProp;
 extern SimParams g_hSimParams;
-extern float3 *g_hv;
+extern float3 *g_hv, *g_ha;
 extern TCHAR g_szResult[MAX_PATH];
 int ReadInputFile(TCHAR *szInpFile);
 int SetParams();
@@ -33,7 +33,7 @@ void InitDiffusion(TBuf *tBuf, real *rrDiffuseAv, SimParams *hparams);
 void EvalDiffusion(TBuf *tBuf, real *rrDiffuseAv, FILE *file, SimParams *hparams, float3 centerOfMass);
 
 static int s_seed = 0;
-static std::vector<float3> s_vels;
+static std::vector<float3> s_vels, s_accels;
 
 extern "C" {
 
@@ -62,11 +62,14 @@ int sgref_setup(const char *inpath, int seed, SimParams *after_setparams, SimPar
   if (!SetupJob()) return -3;
   *after_setup = g_hSimParams;
   s_vels.assign(g_hv, g_hv + g_hSimParams.nMol);
+  s_accels.assign(g_ha, g_ha + g_hSimParams.nMol);
   strcpy(result_name, g_szResult);
   FreeArrays();  // also closes the result file holding the header
   return g_hSimParams.nMol;
 }
 void sgref_get_vels(float3 *out) { memcpy(out, s_vels.data(), s_vels.size() * sizeof(float3)); }
+// The accelerations SetupJob hands to DoComputationsW (InitAccels, SurfaceGrowth.cpp:622-630).
+void sgref_get_accels(float3 *out) { memcpy(out, s_accels.data(), s_accels.size() * sizeof(float3)); }
 
 // RandR / VRand / VRandRfloat4 streams from a seed.
 void sgref_rand(int seed, int n, float *out) {

@@ -42,10 +42,12 @@ Fn g_fn[] = {
     {"20ComputeParticleSizeK", nullptr},   {"16ComputeNetForceK", nullptr},
     {"24ApplyBerendsenThermostat", nullptr}, {"11ApplyShearK", nullptr},
     {"8EvalRdfK", nullptr},                {"12InsertAtomsK", nullptr},
+    {"14InitFccCoordsK", nullptr},         {"15InitSlabCoordsK", nullptr},
+    {"19InitGrapheneCoordsK", nullptr},
 };
 enum {
   F_LEAP, F_BOUND, F_BIN, F_NEBR, F_RHO, F_FORCES, F_VSUM, F_VVMAX, F_VVSUM, F_POT, F_CM, F_CMVEL,
-  F_SIZE, F_NET, F_THERMO, F_SHEAR, F_RDF, F_INSERT, F_COUNT
+  F_SIZE, F_NET, F_THERMO, F_SHEAR, F_RDF, F_INSERT, F_INIT_FCC, F_INIT_SLAB, F_INIT_GRAPHENE, F_COUNT
 };
 
 CUcontext g_ctx = nullptr;
@@ -295,6 +297,95 @@ int rk_thermostat(int stepCount) {
   CUdeviceptr vv = hlp;
   void *args[] = {&dv, &vv, &stepCount};
   return launchCells(F_THERMO, args);
+}
+
+// ApplyShearK alone on the current state (SurfaceGrowth.cu:517-534), with the step loop's
+// launch shape and counter (the first word of molsInCells, zeroed first, cu:2405-2411).
+// Writes the number of metal atoms the shear was added to.
+int rk_shear(float shear, float centerOfMassX, unsigned *count) {
+  CU(cuMemsetD32(mic, 0, 1));
+  CUdeviceptr cnt = mic;
+  void *args[] = {&dr, &da, &shear, &centerOfMassX, &cnt};
+  if (int rc = launchCells(F_SHEAR, args)) return rc;
+  CU(cuMemcpyDtoH(count, mic, 4));
+  return 0;
+}
+
+// The step loop's host-side scalars after rk_run_steps (stepCount, nebrNow, dispHi, shear,
+// totalShear, countRdf as DoComputationsW keeps them in hparams).
+int rk_get_params(sg_simparams *out) {
+  *out = g_p;
+  return 0;
+}
+
+// The device half of InitCoordsW (SurfaceGrowth.cu:2532-2609) with the reference's own lattice
+// kernels and launch shapes: InitFccCoordsK for regime 0, InitGrapheneCoordsK for the sheet of
+// regimes 1 and 2, and InitSlabCoordsK for the regime-2 metal slab (initUcellMeX/Y and the
+// layer count computed as the wrapper does, and written back to *p like the wrapper does).
+// The regime-1 metal atoms come from the host generator and are left as zeros here.  Loads
+// *p into the constant block; needs no rk_setup.  The shapes are checked against the CUDA
+// launch limits and the kernels' writes against the nMol-entry array before any launch.
+int rk_init_coords(sg_simparams *p, float *hr) {
+  const size_t N = (size_t)p->nMol;
+  if (p->nMol <= 0 || p->nMolMe < 0 || p->nMolMe > p->nMol) {
+    g_err = "rk_init_coords: bad atom counts";
+    return -1;
+  }
+  unsigned fcc[3] = {0, 0, 0}, gr = 0, slab[3] = {0, 0, 0};
+  if (p->iRegime == 0) {
+    fcc[0] = p->initUcell.x; fcc[1] = p->initUcell.y; fcc[2] = p->initUcell.z;
+    // InitFccCoordsK writes 4 atoms from n = 4 * (cell index) while n <= nMol - 4
+    if ((size_t)4 * fcc[0] * fcc[1] * fcc[2] != N || fcc[2] == 0 || fcc[2] > 64 || fcc[1] > 65535) {
+      g_err = "rk_init_coords: fcc shape outside the launch limits or nMol != 4 cells";
+      return -1;
+    }
+  } else if (p->iRegime == 1 || p->iRegime == 2) {
+    const int nC = p->nMol - p->nMolMe;
+    if (nC % 32 != 0 || nC <= 0) {
+      g_err = "rk_init_coords: carbon count not a positive multiple of 32";
+      return -1;
+    }
+    gr = (unsigned)(nC / 32);
+    if (p->iRegime == 2 && p->nMolMe != 0) {
+      // integer conversions as the wrapper's (cu:2577-2579)
+      const int ux = (int)((p->region.x - 2 * p->a) / p->a);
+      const int uy = (int)((p->region.y - 2 * p->a) / p->a);
+      if (ux <= 0 || uy <= 0) {
+        g_err = "rk_init_coords: box too small for the metal slab";
+        return -1;
+      }
+      const int layers = (int)ceil(p->nMolMe * 0.25 / (ux * uy));
+      if (layers <= 0 || layers > 64 || uy > 65535) {
+        g_err = "rk_init_coords: slab shape outside the launch limits";
+        return -1;
+      }
+      p->initUcellMeX = ux;
+      p->initUcellMeY = uy;
+      slab[0] = (unsigned)ux; slab[1] = (unsigned)uy; slab[2] = (unsigned)layers;
+    }
+  } else {
+    g_err = "rk_init_coords: unknown regime";
+    return -1;
+  }
+  CU(cuMemcpyHtoD(g_dparams, p, sizeof(sg_simparams)));
+  CUdeviceptr d = 0;
+  CU(cuMemAlloc(&d, N * 16));
+  int rc = 0;
+  CUresult e = cuMemsetD32(d, 0, N * 4);
+  void *args[] = {&d};
+  if (e == CUDA_SUCCESS && p->iRegime == 0)
+    e = cuLaunchKernel(g_fn[F_INIT_FCC].f, fcc[0], fcc[1], 1, 1, 1, fcc[2], 0, nullptr, args, nullptr);
+  if (e == CUDA_SUCCESS && gr)
+    e = cuLaunchKernel(g_fn[F_INIT_GRAPHENE].f, gr, 1, 1, 32, 1, 1, 0, nullptr, args, nullptr);
+  if (e == CUDA_SUCCESS && slab[0])
+    e = cuLaunchKernel(g_fn[F_INIT_SLAB].f, slab[0], slab[1], 1, 1, 1, slab[2], 0, nullptr, args, nullptr);
+  if (e == CUDA_SUCCESS) e = cuCtxSynchronize();
+  if (e == CUDA_SUCCESS) e = cuMemcpyDtoH(hr, d, N * 16);
+  if (e != CUDA_SUCCESS) rc = fail(e, "rk_init_coords");
+  cuMemFree(d);
+  // the constant block goes back to the arrays' parameters, if a system is set up
+  if (!rc && g_p.nMol > 0) CU(cuMemcpyHtoD(g_dparams, &g_p, sizeof(sg_simparams)));
+  return rc;
 }
 
 int rk_rdf(int countRdf) {

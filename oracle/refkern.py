@@ -74,6 +74,9 @@ def _L():
             "rk_rdf": (I, [I]),
             "rk_get_rdf": (I, [V]),
             "rk_run_steps": (I, [I, I, C.POINTER(C.c_float)]),
+            "rk_shear": (I, [C.c_float, C.c_float, C.POINTER(C.c_uint)]),
+            "rk_get_params": (I, [V]),
+            "rk_init_coords": (I, [V, V]),
         }
         for n, (r, a) in sigs.items():
             f = getattr(L, n)
@@ -228,8 +231,40 @@ class RefKernels:
         _ck(_L().rk_get_state(_p(r), _p(v), _p(a)))
         return r, v, a
 
+    def shear(self, shear, center_of_mass_x):
+        """ApplyShearK on the current state; returns the number of sheared metal atoms."""
+        cnt = C.c_uint(0)
+        _ck(_L().rk_shear(shear, center_of_mass_x, C.byref(cnt)))
+        return cnt.value
+
+    def params(self):
+        """The step loop's host-side parameter block after run_steps."""
+        out = self.p.copy()
+        _ck(_L().rk_get_params(C.byref(out)))
+        return out
+
     def run_steps(self, steps, force_rebuild=True):
         """The reference step loop's device work; returns elapsed ms."""
         ms = C.c_float(0)
         _ck(_L().rk_run_steps(steps, 1 if force_rebuild else 0, C.byref(ms)))
         return ms.value
+
+
+def init_coords(params, kind: str = "nofma"):
+    """The reference's lattice kernels as InitCoordsW launches them (SurfaceGrowth.cu:2532-2609):
+    returns (positions (nMol, 4) float32, the parameter block with initUcellMeX/Y as the wrapper
+    writes them).  Regime-1 metal rows are zeros (the reference fills them on the host)."""
+    global _open
+    why = available(kind)
+    if why:
+        raise RefKernelError(why)
+    L = _L()
+    if _open != kind:
+        if _open is not None:
+            L.rk_close()
+        _ck(L.rk_open(str(CUBINS[kind]).encode()))
+        _open = kind
+    q = params.copy()
+    out = np.zeros((q.nMol, 4), np.float32)
+    _ck(L.rk_init_coords(C.byref(q), _p(out)))
+    return out, q

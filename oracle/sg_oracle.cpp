@@ -244,6 +244,7 @@ template <class R> struct Sim : SimBase {
     fric.assign(std::max(nMolMe, 1), 0);
     hist.assign(std::max(p.sizeHistRdf, 1), 0);
     memset(&diag, 0, sizeof(diag));
+    P.nebrNow = 1;  // no lists exist yet (a state resumed from a backup starts with a rebuild)
     if (P.iRegime == 2 || forceDiffusion) {
       tbuf.resize(P.nBuffDiffuse);
       for (int nb = 0; nb < P.nBuffDiffuse; nb++) {
@@ -604,6 +605,7 @@ template <class R> struct Sim : SimBase {
           float fac = 1. / (3 * 2 * P.stepDiffuse * P.deltaT * P.limitDiffuseAv);
           for (int j = 1; j < P.nValDiffuse; j++) rrDiffuseAv[j] *= fac / j;
           lastDiffusePrint = rrDiffuseAv;
+          diffuseTables.push_back(rrDiffuseAv);
           diffusePrints++;
           P.countDiffuseAv = 0;
           std::fill(rrDiffuseAv.begin(), rrDiffuseAv.end(), 0.f);
@@ -612,6 +614,7 @@ template <class R> struct Sim : SimBase {
     }
   }
   std::vector<float> lastDiffusePrint;
+  std::vector<std::vector<float>> diffuseTables;  // every printed table, in order
   int diffusePrints = 0;
 
   // ---- property accumulators (cu:2659-2686) -------------------------------------------------
@@ -816,6 +819,9 @@ template <class R> struct Sim : SimBase {
     propAccum(P.centerOfMass); propAccum(P.cmVel); propAccum(P.frictForce);
     if (sc % P.stepAvg == 0) {
       lastAvg[0] = P.totEnergy; lastAvg[1] = P.potEnergy; lastAvg[2] = P.kinEnergy;
+      // the seven accumulators as PrintSummary receives them (before AccumProps(0))
+      lastAvg7[0] = P.totEnergy; lastAvg7[1] = P.potEnergy; lastAvg7[2] = P.kinEnergy; lastAvg7[3] = P.oneStep;
+      lastAvg7[4] = P.centerOfMass; lastAvg7[5] = P.cmVel; lastAvg7[6] = P.frictForce;
       propZero(P.totEnergy); propZero(P.potEnergy); propZero(P.kinEnergy); propZero(P.oneStep);
       propZero(P.centerOfMass); propZero(P.cmVel); propZero(P.frictForce);
     }
@@ -825,6 +831,7 @@ template <class R> struct Sim : SimBase {
   std::vector<unsigned> lastRdfPrint;
   int rdfPrints = 0;
   sg_prop lastAvg[3];
+  sg_prop lastAvg7[7];
 };
 
 struct Handle {
@@ -1075,6 +1082,27 @@ void orc_get_rdf(orc_sim *s, unsigned int *hist) {
 void orc_get_diffusion(orc_sim *s, float *rr, int *counts, int *cav) {
   if (s->h.prec == 32) getDiff(*s->h.f, rr, counts, cav);
   else getDiff(*s->h.d, rr, counts, cav);
+}
+// Output bookkeeping of the step loop, for driving the reference's writers from an oracle run:
+// the seven property accumulators of the last averaging step (totEnergy, potEnergy, kinEnergy,
+// oneStep, centerOfMass, cmVel, frictForce, before they were zeroed), the number of RDF prints
+// and diffusion tables so far (kind 0 / 1), the last printed RDF histogram and table k.
+void orc_get_last_avg(orc_sim *s, sg_prop *out7) {
+  for (int k = 0; k < 7; k++) out7[k] = (s->h.prec == 32) ? s->h.f->lastAvg7[k] : s->h.d->lastAvg7[k];
+}
+int orc_num_prints(orc_sim *s, int kind) {
+  if (s->h.prec == 32) return kind == 0 ? s->h.f->rdfPrints : (int)s->h.f->diffuseTables.size();
+  return kind == 0 ? s->h.d->rdfPrints : (int)s->h.d->diffuseTables.size();
+}
+void orc_get_rdf_print(orc_sim *s, unsigned *hist) {
+  const std::vector<unsigned> &h = (s->h.prec == 32) ? s->h.f->lastRdfPrint : s->h.d->lastRdfPrint;
+  std::copy(h.begin(), h.end(), hist);
+}
+int orc_get_diffuse_print(orc_sim *s, int k, float *table) {
+  const auto &t = (s->h.prec == 32) ? s->h.f->diffuseTables : s->h.d->diffuseTables;
+  if (k < 0 || k >= (int)t.size()) return -1;
+  std::copy(t[k].begin(), t[k].end(), table);
+  return 0;
 }
 void orc_get_diag(orc_sim *s, sg_diag *d) { *d = (s->h.prec == 32) ? s->h.f->diag : s->h.d->diag; }
 

@@ -793,8 +793,13 @@ extern "C" int sg_step(sg_ctx *c, int nsteps) {
   const unsigned want = ++c->pubSeq;
   const auto t0 = std::chrono::steady_clock::now();
   bool seen = false;
+  // The sequence number is read with acquire semantics: the mirror's words are plain loads, and
+  // on a weakly ordered host (the Grace CPU of a GB300 node is Arm) nothing else would stop them
+  // from being satisfied before the sequence load and returning the previous publish.  The
+  // device side stores the words, fences system-wide, then stores the sequence number.
+  const unsigned *seqp = const_cast<const unsigned *>(c->hostSeq);
   for (unsigned spin = 0;; spin++) {
-    if (*c->hostSeq == want) {
+    if (__atomic_load_n(seqp, __ATOMIC_ACQUIRE) == want) {
       seen = true;
       break;
     }
@@ -802,7 +807,7 @@ extern "C" int sg_step(sg_ctx *c, int nsteps) {
   }
   if (!seen) {
     CK(cudaStreamSynchronize(c->stream));
-    if (*c->hostSeq != want) return sg_fail(SG_ERR_CUDA, "step results not published");
+    if (__atomic_load_n(seqp, __ATOMIC_ACQUIRE) != want) return sg_fail(SG_ERR_CUDA, "step results not published");
   }
   return flagsFromMirror(c);
 }

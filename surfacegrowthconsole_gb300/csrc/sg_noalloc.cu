@@ -81,7 +81,10 @@ constexpr Carve carve() {
 constexpr Carve kCarve = carve();
 static_assert(kCarve.total <= kScratchBytes, "scratch layout exceeds the static array");
 
-// Device address of g_scratch per device ordinal, set up once per device.
+// Device address of g_scratch per device ordinal, set up once per device.  The address belongs
+// to the context that was current at set-up: the device's primary context, the one the CUDA
+// runtime uses.  A caller that resets the device (cudaDeviceReset) or drives the device through
+// another driver-API context is outside what this cache supports.
 constexpr int kMaxDevices = 64;
 unsigned char *g_base[kMaxDevices] = {};
 std::mutex g_mu;
@@ -139,16 +142,19 @@ RepConst constFor(const sg_simparams &p) {
 
 extern "C" int sg_compute_forces_noalloc(const sg_simparams *p, sg_float4 *d_pos, sg_float4 *d_acc, void *stream) {
   if (!p || !d_pos || !d_acc) return sg_fail(SG_ERR_INVALID, "sg_compute_forces_noalloc: null argument");
-  const int ncells = p->cells.x * p->cells.y * p->cells.z;
-  const int ncellsPad = ((ncells + 1 + kCellTile - 1) / kCellTile) * kCellTile;
   if (p->nMol <= 0 || p->nMolMe < 0 || p->nMolMe > p->nMol || p->cells.x < 1 || p->cells.y < 1 || p->cells.z < 1)
     return sg_fail(SG_ERR_INVALID, "sg_compute_forces_noalloc: inconsistent parameter block");
-  if (p->nMol > SG_NOALLOC_MAX_ATOMS || ncellsPad > SG_NOALLOC_MAX_CELLS || p->iNebrMax > SG_NOALLOC_MAX_NEBR ||
+  // the cell count in 64 bits: a parameter block from outside may hold any extents, and an int
+  // product could wrap to a small value that passes the limit
+  const long long ncells64 = (long long)p->cells.x * p->cells.y * p->cells.z;
+  const long long ncellsPad64 = ((ncells64 + 1 + kCellTile - 1) / kCellTile) * kCellTile;
+  if (p->nMol > SG_NOALLOC_MAX_ATOMS || ncellsPad64 > SG_NOALLOC_MAX_CELLS || p->iNebrMax > SG_NOALLOC_MAX_NEBR ||
       p->iNebrMax < 1)
     return sg_fail(SG_ERR_INVALID,
                    "sg_compute_forces_noalloc: system exceeds the static scratch (nMol %d of max %d, "
-                   "padded cells %d of max %d, iNebrMax %d of max %d)",
-                   p->nMol, SG_NOALLOC_MAX_ATOMS, ncellsPad, SG_NOALLOC_MAX_CELLS, p->iNebrMax, SG_NOALLOC_MAX_NEBR);
+                   "padded cells %lld of max %d, iNebrMax %d of max %d)",
+                   p->nMol, SG_NOALLOC_MAX_ATOMS, ncellsPad64, SG_NOALLOC_MAX_CELLS, p->iNebrMax, SG_NOALLOC_MAX_NEBR);
+  const int ncellsPad = (int)ncellsPad64;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices)

@@ -1,7 +1,7 @@
 """Generate golden fixtures from the reference's own host code.
 
-Runs in a container that has the reference tree (default /root/reference) and a built
-oracle/_ref/libsgref_host.so (oracle/ref/build_ref.sh).  Each case runs in a fresh
+Runs where the reference tree is present and oracle/ref/build_ref.sh has built
+oracle/_ref/libsgref_host.so from it.  Each case runs in a fresh
 subprocess because the reference keeps its configuration in process globals.  Writes
 tests/golden/ref_host.json plus the output files under tests/golden/ref_files/.
 

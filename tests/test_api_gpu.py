@@ -119,3 +119,20 @@ def test_step_from_host_is_set_state_then_step(mode, pinned):
     _same_thermo(one.thermo(0), two.thermo(0))
     one.close()
     two.close()
+
+
+@pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_MIXED])
+def test_published_record_is_the_current_step_over_many_calls(mode):
+    """sg_step_thermo returns once the host sees the step's sequence number in the page-locked
+    mirror; the record it then reads must be that step's, never the previous publish (the host
+    reads the sequence number with acquire ordering: the Grace host is weakly ordered).  Over
+    300 single-step calls every record equals sg_get_thermo's after a stream synchronisation."""
+    p, r, v = workloads.small(seed=64)
+    sim = Simulation(p, mode=mode)
+    sim.set_state(r, v, np.zeros((p.nMol, 3), np.float32))
+    for i in range(300):
+        t1 = sim.step_thermo(1)
+        t2 = sim.thermo()
+        assert t1.stepCount == t2.stepCount == i + 1
+        _same_thermo(t1, t2)
+    sim.close()

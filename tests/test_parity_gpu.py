@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import oracle
-from surfacegrowthconsole_gb300 import workloads
+from surfacegrowthconsole_gb300 import MODE_MIXED, MODE_PLAIN, workloads
 from surfacegrowthconsole_gb300.engine import Simulation, default_input, init_coords, init_vels, set_params
 
 pytestmark = pytest.mark.gpu
@@ -294,3 +294,38 @@ def test_diffusion_matches_oracle():
     assert np.array_equal(cnt_g, cnt_o) and cav_g == cav_o
     ok, err = close(rr_g, rr_o, rtol=1e-3, atol=1e-6); assert ok, err
     sim.close()
+
+
+@pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_MIXED], ids=["plain", "mixed"])
+def test_batched_uneven_replicas_equal_single_runs(mode):
+    """Twelve replicas of the batched configuration (graphene of 1,000-20,000 C, one Ni cluster
+    of 50-2,000 atoms, 300-1,500 K, each from its own seed) stepped together in one context
+    against each replica stepped alone.  PLAIN: bit for bit.  MIXED sums each replica's
+    reductions in blocks whose size follows the launch's total atom count, so the batch and a
+    single run may round a double-float sum differently (about 1e-14 relative): close, not
+    identical."""
+    systems = workloads.batched(n=12, seed=4, steps=5000)
+    sizes = [s[0].nMol for s in systems]
+    assert max(sizes) > 3 * min(sizes)  # uneven
+    batch = Simulation([s[0] for s in systems], mode=mode)
+    for k, (p, r, v) in enumerate(systems):
+        batch.set_state(r, v, np.zeros((p.nMol, 3), np.float32), rep=k)
+    steps = 30  # across the thermostat step 25
+    batch.step(steps)
+    for k, (p, r, v) in enumerate(systems):
+        single = Simulation(p, mode=mode)
+        single.set_state(r, v, np.zeros((p.nMol, 3), np.float32))
+        single.step(steps)
+        rb, vb, ab = batch.get_state(rep=k)
+        rs, vs, as_ = single.get_state()
+        tb, ts = batch.thermo(k), single.thermo()
+        assert tb.stepCount == ts.stepCount == steps and tb.rebuilds == ts.rebuilds, k
+        if mode == MODE_PLAIN:
+            assert np.array_equal(rb, rs) and np.array_equal(vb, vs) and np.array_equal(ab, as_), k
+            assert tb.totEnergy == ts.totEnergy, k
+        else:
+            assert np.abs(rb[:, :3] - rs[:, :3]).max() < 1e-4, k
+            ok, err = close(vb, vs, rtol=1e-4); assert ok, (k, err)
+            assert abs(tb.totEnergy - ts.totEnergy) <= 1e-5 * abs(ts.totEnergy), k
+        single.close()
+    batch.close()

@@ -1,0 +1,107 @@
+"""The shear drive with a non-zero increment, against the reference's kernels and the oracle.
+
+Regime 2 applies the shear after equilibration and cooling (SurfaceGrowth.cu:2397-2415): every
+step past stepEquil + stepCool, while the metal centre-of-mass x velocity is below 0.005, the
+shear grows by deltaF; ApplyShearK (cu:517-534) then adds it to a.x of every metal atom left of
+the centre of mass and counts them, and totalShear = count * shear.  The next step's first
+half-kick carries it into the velocities.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import refkern
+from surfacegrowthconsole_gb300 import MODE_MIXED, MODE_PLAIN, workloads
+from surfacegrowthconsole_gb300.engine import Simulation
+
+pytestmark = pytest.mark.gpu
+
+STEPS = 40
+
+
+def shear_system(seed=61, delta_pN=2.0, cool=10):
+    """The 2,217-atom nanoparticle-on-graphene system with the shear drive on from step cool+1."""
+    p, r, v = workloads.small(seed=seed)
+    p.stepEquil = 0
+    p.stepCool = cool
+    p.deltaF = np.float32(delta_pN) * np.float32(p.forceU) * np.float32(0.001)
+    return p, r, v, np.zeros((p.nMol, 3), np.float32)
+
+
+def test_apply_shear_kernel_alone():
+    """ApplyShearK on a snapshot: the reference's kernel against the rule restated on the host."""
+    if refkern.available("nofma"):
+        pytest.skip(refkern.available("nofma"))
+    p, r, v, _ = shear_system()
+    a = np.random.RandomState(3).normal(0, 1, size=(p.nMol, 3)).astype(np.float32)
+    rk = refkern.RefKernels(p, r, v, a)
+    cm_x = np.float32(r[:p.nMolMe, 0].astype(np.float64).mean())
+    shear = np.float32(0.0371)
+    n = rk.shear(float(shear), float(cm_x))
+    _, _, a_ref = rk.state()
+    left = (cm_x - r[:p.nMolMe, 0]) > 0
+    assert n == int(left.sum()) > 0
+    exp = a.copy()
+    exp[:p.nMolMe, 0][left] += shear
+    assert np.array_equal(a_ref, exp)
+
+
+@pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_MIXED], ids=["plain", "mixed"])
+def test_shear_ramp_matches_oracle(mode):
+    p, r, v, a = shear_system()
+    sim = Simulation(p, mode=mode)
+    sim.set_state(r, v, a)
+    orc = oracle.OracleSim(p, 32)
+    orc.set_state(r, v, a)
+    shear_g, shear_o = [], []
+    for _ in range(STEPS):
+        sim.step(1)
+        orc.step(1)
+        tg, to = sim.thermo(), orc.thermo()
+        shear_g.append((tg.shear, tg.totalShear))
+        shear_o.append((to.shear, to.totalShear))
+    sg, so = np.array(shear_g), np.array(shear_o)
+    # off through the cooling interval, then the ramp
+    assert (so[:p.stepCool] == 0).all() and so[-1, 0] > 0 and so[-1, 1] > 0
+    if mode == MODE_PLAIN:
+        assert np.array_equal(sg, so)
+    else:
+        # MIXED decides the ramp on its FP64 centre-of-mass velocity: the same decisions here
+        assert np.array_equal(sg[:, 0], so[:, 0])
+        assert np.allclose(sg[:, 1], so[:, 1], rtol=0, atol=2 * float(so[-1, 0]))
+    rg, vg, _ = sim.get_state()
+    ro, vo, _ = orc.get_state()
+    assert np.abs(rg[:, :3] - ro[:, :3]).max() < 1e-3
+    assert np.abs(vg - vo).max() < 1e-3 * float(np.abs(vo).max())
+    # the drive moved the metal: its x velocity differs from a run without shear
+    q = p.copy()
+    q.deltaF = 0.0
+    free = oracle.OracleSim(q, 32)
+    free.set_state(r, v, a)
+    free.step(STEPS)
+    vf = free.get_state()[1]
+    assert vo[:p.nMolMe, 0].mean() > vf[:p.nMolMe, 0].mean()
+    sim.close()
+
+
+def test_shear_trajectory_against_the_reference_step_loop():
+    """The reference's own step loop on its kernels (oracle/refkern.py run_steps: the launches of
+    DoComputationsW, cu:2141-2430, including the shear schedule) against the library."""
+    if refkern.available("nofma"):
+        pytest.skip(refkern.available("nofma"))
+    p, r, v, a = shear_system(seed=62)
+    rk = refkern.RefKernels(p, r, v, a)
+    rk.run_steps(STEPS, force_rebuild=False)
+    pr = rk.params()
+    rr, vr, _ = rk.state()
+    sim = Simulation(p)
+    sim.set_state(r, v, a)
+    sim.step(STEPS)
+    t = sim.thermo()
+    assert pr.stepCount == t.stepCount == STEPS
+    assert pr.shear == t.shear and t.shear > 0
+    assert pr.totalShear == t.totalShear and t.totalShear > 0
+    rg, vg, _ = sim.get_state()
+    assert np.abs(rg[:, :3] - rr[:, :3]).max() < 1e-3
+    assert np.abs(vg - vr).max() < 1e-3 * float(np.abs(vr).max())
+    sim.close()

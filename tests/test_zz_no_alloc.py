@@ -58,6 +58,36 @@ def test_noalloc_forces_match_context_path_two_calls():
         assert _close(u_na, u_ctx), "per-atom energies differ from the context path"
 
 
+def test_noalloc_call_allocates_no_device_memory():
+    """After a first call (which looks up the static array's address), a call leaves the
+    device's free memory exactly as it was: no allocation, no growth of any pool."""
+    import torch
+    p, r, v = workloads.small(seed=63)
+    dpos = torch.from_numpy(np.ascontiguousarray(r, np.float32)).cuda()
+    dacc = torch.zeros((p.nMol, 4), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    args = (C.byref(p), C.c_void_p(dpos.data_ptr()), C.c_void_p(dacc.data_ptr()), C.c_void_p(stream))
+    L.check(L.lib().sg_compute_forces_noalloc(*args))
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        L.check(L.lib().sg_compute_forces_noalloc(*args))
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+
+
+def test_noalloc_rejects_cell_extents_whose_product_wraps():
+    """A parameter block from outside with cell extents whose product overflows 32 bits is
+    rejected, not wrapped into a small count that would pass the limit."""
+    p, r, _ = workloads.small(seed=64)
+    q = p.copy()
+    q.cells.x, q.cells.y, q.cells.z = 65536, 65536, 2  # 2^33 cells: 0 in 32-bit arithmetic
+    with pytest.raises(L.SgError) as e:
+        _noalloc_forces(q, r)
+    assert e.value.code == 1 and "exceeds the static scratch" in str(e.value)
+
+
 def test_noalloc_rejects_systems_above_its_limit():
     p, r, _ = workloads.production(seed=62, steps=10)  # 45,546 atoms > SG_NOALLOC_MAX_ATOMS
     with pytest.raises(L.SgError) as e:
