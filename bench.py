@@ -9,8 +9,15 @@ LJ, graphene, reductions, thermostat, RDF/diffusion when due).
   value : atom-steps/s of the chosen form (MIXED: hi/lo positions, FP64 sums; --mode plain
           makes the PLAIN FP32 drop-in the headline) with the state resident in HBM, each step
           timed with CUDA events on the library's stream; the L2 is flushed (a 512 MB write)
-          between timed steps because the whole state fits in the 129 MB L2.  The other form is
-          timed the same way and reported beside it (`plain` / `mixed`, `mixed_over_plain`).
+          between timed steps because the whole state fits in the 129 MB L2.  The RDF is sampled
+          every stepRdf = 100 steps, which a short window may or may not hold: its extra device
+          time is measured on RDF steps against the steps just before them and added as
+          rdf_extra_ms / 100 to the window's steps without RDF work (window_ms_per_step is the
+          raw window).  The other form is timed the same way and reported beside it (`plain` /
+          `mixed`, `mixed_over_plain`).
+  batched : the batched form beside it (256 replicas in one context, MIXED and PLAIN, each
+          autotuned, and the same replicas one by one), so that the comparison of the two forms
+          at the batched size is in every run (--no-batched leaves it out).
   nve_drift : the total-energy drift of both forms on bulk Ni (4,000 atoms, 300 K, 10 ps NVE),
           the "stated drift" the two forms are compared at.
   e2e   : the same metric through the public C ABI with host buffers: every step uploads the
@@ -18,7 +25,9 @@ LJ, graphene, reductions, thermostat, RDF/diffusion when due).
           one sg_step_from_host call (one wait per step).
   roofline : the neighbour-list build (the largest share of the step): its compulsory bytes per
           launch / its mean duration (CUDA events around it on the library's stream), against
-          the measured HBM copy peak.  The phase durations come from a second pass of the same
+          the measured HBM copy peak; the kernel is bound by instruction issue, so its issue-slot,
+          FP32-pipe and L1 fractions from an ncu capture (profiles/k_build_nebr_traffic.json)
+          ride beside the HBM fraction.  The phase durations come from a second pass of the same
           steps with event-record nodes between the phases of every step; those nodes cost a few
           microseconds each, so the headline pass carries none.
   step_roofline : the whole step's lower bound, sum over its parts of max(bytes / HBM peak,
@@ -78,6 +87,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="leave out the batched comparison of the production line")
     ap.add_argument("--workload", default="production", choices=["production", "batched", "diff"])
     ap.add_argument("--replicas", type=int, default=256)
     return ap.parse_args()
@@ -248,10 +258,12 @@ def run_reference(args, rank: int, world: int):
     print(json.dumps(line, default=float))
 
 
-def run_batched(args, rank: int, world: int, local: int, dist=None):
-    """The batched form: all replicas in one context, in both forms (the headline --mode and the
-    other), against the same replicas one by one in the headline form.  With several ranks each
-    steps its own seeded batch; the values are all ranks' atoms over the slowest rank's time."""
+def batched_forms(args, rank: int, world: int, local: int, dist, steps: int, warmup: int, tune_steps: int,
+                  one_steps: int) -> dict:
+    """The batched form: all replicas in one context, timed in both forms (MIXED and PLAIN, each
+    autotuned first), and the same replicas one by one in the headline form, each in its own
+    context.  With several ranks each steps its own seeded batch; the values are all ranks'
+    atoms over the slowest rank's time."""
     import torch
     from surfacegrowthconsole_gb300 import MODE_MIXED, MODE_PLAIN, workloads
     from surfacegrowthconsole_gb300.engine import Simulation
@@ -269,8 +281,8 @@ def run_batched(args, rank: int, world: int, local: int, dist=None):
     for name in (head, "plain" if head == "mixed" else "mixed"):
         sim = Simulation(plist, mode=modes[name], device=local, stream=stream.cuda_stream)
         sim.set_state(r, v, np.zeros((natoms, 3), np.float32))
-        tune = None if args.no_tune else sim.autotune(steps=10)
-        sim.step(args.warmup)
+        tune = None if args.no_tune else sim.autotune(steps=tune_steps)
+        sim.step(warmup)
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
@@ -278,19 +290,18 @@ def run_batched(args, rank: int, world: int, local: int, dist=None):
         with Clocks(local) as clk:
             with torch.cuda.stream(stream):
                 ev0.record(stream)
-                for _ in range(args.steps):
+                for _ in range(steps):
                     sim.step_async(1)
                     launches += sim.kernels_per_step()
                 ev1.record(stream)
             torch.cuda.synchronize()
         sim.step(0)
         t = over_ranks(dist, ev0.elapsed_time(ev1) * 1e-3, "max", f"cuda:{local}")
-        forms[name] = {"value": job_value(natoms_all, args.steps, t), "ms_per_step": 1e3 * t / args.steps,
-                       "gpu_launches": launches, "clocks": clk.summary(), "launch_shape": tune,
+        forms[name] = {"value": job_value(natoms_all, steps, t), "ms_per_step": 1e3 * t / steps,
+                       "steps": steps, "gpu_launches": launches, "clocks": clk.summary(), "launch_shape": tune,
                        "rebuilds_all_replicas": int(sum(sim.thermo(k).rebuilds for k in range(len(plist))))}
         sim.close()
-    # the same replicas one by one, each in its own context (fewer steps: 256 contexts)
-    k1 = max(1, min(args.steps, 20))
+    # the same replicas one by one, each in its own context
     t_one = 0.0
     atoms_one = 0
     for w in reps:
@@ -301,33 +312,45 @@ def run_batched(args, rank: int, world: int, local: int, dist=None):
         torch.cuda.synchronize()
         with torch.cuda.stream(stream):
             ev0.record(stream)
-            s1.step_async(k1)
+            s1.step_async(one_steps)
             ev1.record(stream)
         torch.cuda.synchronize()
         s1.step(0)
         t_one += ev0.elapsed_time(ev1) * 1e-3
         atoms_one += q.nMol
         s1.close()
-    one = job_value(over_ranks(dist, float(atoms_one), "sum", f"cuda:{local}"), k1,
+    one = job_value(over_ranks(dist, float(atoms_one), "sum", f"cuda:{local}"), one_steps,
                     over_ranks(dist, t_one, "max", f"cuda:{local}"))
+    return {"replicas": len(plist), "atoms": natoms, "forms": forms, "head": head,
+            "mixed_over_plain": forms["mixed"]["value"] / forms["plain"]["value"],
+            "one_by_one": {"value": one, "unit": "atom-steps/s", "steps": one_steps, "mode": head,
+                           "ms_all_replicas_per_step": 1e3 * t_one / one_steps}}
+
+
+BATCHED_WORKLOAD = ("{n} replicas, {atoms} atoms in all, graphene 1,000-20,000 C + one Ni cluster of 50-2,000 "
+                    "atoms each, 300-1,500 K, lists rebuilt by the reference's rule")
+
+
+def run_batched(args, rank: int, world: int, local: int, dist=None):
+    """--workload batched: the batched form as the headline."""
+    b = batched_forms(args, rank, world, local, dist, args.steps, args.warmup, 10, max(1, min(args.steps, 20)))
     if rank == 0:
-        f = forms[head]
+        head = b["head"]
+        f = b["forms"][head]
         other = "plain" if head == "mixed" else "mixed"
         line = {"metric": "atom-steps/s", "value": f["value"], "unit": "atom-steps/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": f["ms_per_step"],
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded replicas: graphene + one fcc Ni cluster each, Maxwell velocities)",
-                "config": {"workload": f"{len(plist)} replicas, {natoms} atoms in all, graphene 1,000-20,000 C + "
-                                       "one Ni cluster of 50-2,000 atoms each, 300-1,500 K, lists rebuilt by the "
-                                       "reference's rule", "replicas": len(plist), "atoms": natoms, "mode": head,
+                "config": {"workload": BATCHED_WORKLOAD.format(n=b["replicas"], atoms=b["atoms"]),
+                           "replicas": b["replicas"], "atoms": b["atoms"], "mode": head,
                            "l2": "state larger than L2 (no flush)", "parallelism": f"replicas x{world}",
                            "launch_shape": f["launch_shape"]},
                 "clocks": f["clocks"], "gpu_launches": f["gpu_launches"],
                 "rebuilds_all_replicas": f["rebuilds_all_replicas"],
-                other: forms[other],
-                "mixed_over_plain": forms["mixed"]["value"] / forms["plain"]["value"],
-                "one_by_one": {"value": one, "unit": "atom-steps/s", "steps": k1, "mode": head,
-                               "ms_all_replicas_per_step": 1e3 * t_one / k1}}
+                other: b["forms"][other],
+                "mixed_over_plain": b["mixed_over_plain"],
+                "one_by_one": b["one_by_one"]}
         print(json.dumps(line, default=float))
 
 
@@ -443,10 +466,11 @@ def run_production(args, rank: int, world: int, local: int, dist):
 
     def timed(sim, phases=None):
         """args.steps steps, each bracketed by CUDA events on the library's stream, the L2 flushed
-        before each; returns (seconds, kernel launches)."""
+        before each; returns (seconds, kernel launches, RDF steps among them)."""
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
               for _ in range(args.steps)]
         launches = 0
+        s0 = sim.thermo().stepCount
         barrier()
         with torch.cuda.stream(stream):
             for k in range(args.steps):
@@ -459,7 +483,40 @@ def run_production(args, rank: int, world: int, local: int, dist):
                 launches += sim.kernels_per_step()
         barrier()
         sim.step(0)  # collects device status (overflow flags)
-        return max_over_ranks(sum(e0.elapsed_time(e1) for e0, e1 in ev) * 1e-3), launches
+        n_rdf = sum(1 for k in range(1, args.steps + 1) if (s0 + k) % p.stepRdf == 0)
+        return max_over_ranks(sum(e0.elapsed_time(e1) for e0, e1 in ev) * 1e-3), launches, n_rdf
+
+    def rdf_extra_s(sim, samples=3):
+        """Device time an RDF step (k_rdf and the 0-15 A extension, every stepRdf steps) adds to a
+        step: RDF steps against the steps just before them, each timed alone after an L2 flush,
+        the steps between them run untimed."""
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t_rdf, t_plain = [], []
+        for _ in range(samples):
+            # run untimed to two steps before the next RDF step, then time the step before it
+            # (no RDF work) and the RDF step itself
+            sc = sim.thermo().stepCount
+            nxt = (sc // p.stepRdf + 1) * p.stepRdf
+            if nxt - 2 < sc:
+                nxt += p.stepRdf
+            if nxt - 2 - sc > 0:
+                sim.step(nxt - 2 - sc)
+            for out in (t_plain, t_rdf):
+                barrier()
+                with torch.cuda.stream(stream):
+                    flush.zero_()
+                    e0.record(stream)
+                    sim.step_async(1)
+                    e1.record(stream)
+                barrier()
+                out.append(e0.elapsed_time(e1) * 1e-3)
+        sim.step(0)
+        return max_over_ranks(max(statistics.median(t_rdf) - statistics.median(t_plain), 0.0))
+
+    def amortised_s(total_s, n_steps, n_rdf, extra_s):
+        """Seconds per step with one RDF sample every stepRdf steps: the window's steps without
+        their RDF work, plus extra_s / stepRdf."""
+        return (total_s - n_rdf * extra_s) / n_steps + extra_s / p.stepRdf
 
     head = args.mode
     forms = {}
@@ -471,14 +528,18 @@ def run_production(args, rank: int, world: int, local: int, dist):
         tune = None if args.no_tune else sim.autotune(steps=20)
         sim.step(args.warmup)
         with Clocks(local) as clk:
-            total_s, launches = timed(sim)
+            total_s, launches, n_rdf = timed(sim)
+        extra = rdf_extra_s(sim)
         forms[name] = {"total_s": total_s, "launches": launches, "launch_shape": tune,
-                       "shape": sim.launch_shape(), "clocks": clk.summary()}
+                       "shape": sim.launch_shape(), "clocks": clk.summary(), "window_rdf_steps": n_rdf,
+                       "rdf_extra_ms": 1e3 * extra,
+                       "step_s": amortised_s(total_s, args.steps, n_rdf, extra)}
         sims[name] = sim
     atoms_all = over_ranks(dist, float(p.nMol), "sum", f"cuda:{local}")
     for f in forms.values():
-        f["value"] = job_value(atoms_all, args.steps, f["total_s"])
-        f["ms_per_step"] = 1e3 * f["total_s"] / args.steps
+        f["value"] = atoms_all / f["step_s"]
+        f["ms_per_step"] = 1e3 * f["step_s"]
+        f["window_ms_per_step"] = 1e3 * f["total_s"] / args.steps
     sim = sims[head]
     sims["plain" if head == "mixed" else "mixed"].close()
     total_s = forms[head]["total_s"]
@@ -491,7 +552,7 @@ def run_production(args, rank: int, world: int, local: int, dist):
     psim.set_launch_shape(forms[head]["shape"])
     psim.step(args.warmup)
     phases = []
-    phase_total_s, _ = timed(psim, phases)
+    phase_total_s, _, _ = timed(psim, phases)
     psim.close()
     # integrate, rebuild, metal chain, carbon, forces, reduce, extra, list build
     ph = np.mean(np.array(phases), axis=0)
@@ -512,9 +573,15 @@ def run_production(args, rank: int, world: int, local: int, dist):
                          "forces_fork_to_join": float(ph[4]), "reduce": float(ph[5]), "rdf_shear": float(ph[6])}}
     prof = ROOT / "profiles" / "k_build_nebr_traffic.json"
     if prof.exists():
-        roof["traffic"] = json.loads(prof.read_text()).get("dram_bytes_per_launch")
+        pj = json.loads(prof.read_text())
+        roof["traffic"] = pj.get("dram_bytes_per_launch")
+        # the list build is bound by instruction issue, not by bytes: its issue-slot, FP32-pipe
+        # and L1 fractions from the same ncu capture
+        for k in ("issue_slot_frac", "fp32_pipe_frac", "l1_frac", "ipc_per_sm", "ncu_command"):
+            if k in pj:
+                roof[k] = pj[k]
     t_lb, counts = step_lower_bound_ms(p, pi, pk, prr, peak)
-    step_ms = 1e3 * total_s / args.steps
+    step_ms = forms[head]["ms_per_step"]
     step_roof = {"lower_bound_ms": t_lb, "measured_ms": step_ms, "frac": t_lb / step_ms,
                  "hbm_peak_gbs": peak, "fp32_peak_tflops": FP32_NOMINAL_TFLOPS, "fp32_peak_kind": "nominal",
                  **counts}
@@ -525,6 +592,7 @@ def run_production(args, rank: int, world: int, local: int, dist):
     ha = torch.empty((p.nMol, 3), dtype=torch.float32, pin_memory=True).numpy()
     hr[:], hv[:], ha[:] = sim.get_state()
     e2e_steps = max(1, min(args.e2e_steps, args.steps))
+    s0 = sim.thermo().stepCount
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
@@ -533,10 +601,30 @@ def run_production(args, rank: int, world: int, local: int, dist):
         th = sim.step_from_host(hr, hv, ha, nsteps=1)
     barrier()
     e2e_s = max_over_ranks(time.perf_counter() - t0)
-    e2e = {"value": atoms_all * e2e_steps / e2e_s, "unit": "atom-steps/s",
+    n_rdf_e2e = sum(1 for k in range(1, e2e_steps + 1) if (s0 + k) % p.stepRdf == 0)
+    e2e_step_s = amortised_s(e2e_s, e2e_steps, n_rdf_e2e, forms[head]["rdf_extra_ms"] * 1e-3)
+    e2e = {"value": atoms_all / e2e_step_s, "unit": "atom-steps/s",
            "h2d_bytes_per_step": p.nMol * (16 + 12 + 12), "d2h_bytes_per_step": sim.step_readback_bytes(),
-           "steps": e2e_steps, "result": f"total energy {float(th.totEnergy):.6g} (the step's thermo record)"}
+           "steps": e2e_steps, "ms_per_step": 1e3 * e2e_step_s, "window_ms_per_step": 1e3 * e2e_s / e2e_steps,
+           "window_rdf_steps": n_rdf_e2e,
+           "result": f"total energy {float(th.totEnergy):.6g} (the step's thermo record)"}
     sim.close()
+
+    # the batched form beside the production line (256 replicas in one context, both forms,
+    # and one by one), so that the comparison the chosen form is judged on is in every run
+    batched = None
+    if not args.no_batched:
+        bsteps = max(10, min(args.steps, 40))
+        b = batched_forms(args, rank, world, local, dist, bsteps, max(3, min(args.warmup, 5)), 5,
+                          max(1, min(args.steps, 10)))
+        batched = {"workload": BATCHED_WORKLOAD.format(n=b["replicas"], atoms=b["atoms"]), "unit": "atom-steps/s",
+                   "mixed": {k: b["forms"]["mixed"][k] for k in ("value", "ms_per_step", "steps", "gpu_launches",
+                                                                 "launch_shape", "clocks")},
+                   "plain": {k: b["forms"]["plain"][k] for k in ("value", "ms_per_step", "steps", "gpu_launches",
+                                                                 "launch_shape", "clocks")},
+                   "mixed_over_plain": b["mixed_over_plain"], "one_by_one": b["one_by_one"],
+                   "timing": "device time of the steps with CUDA events on the library's stream; state larger "
+                             "than L2 (no flush)"}
 
     drift = None
     if args.drift_steps > 0:
@@ -557,13 +645,22 @@ def run_production(args, rank: int, world: int, local: int, dist):
                            "atoms_per_gpu": p.nMol, "mode": head,
                            "form": "chosen (MIXED)" if head == "mixed" else "plain FP32 drop-in",
                            "l2": "flushed between timed steps", "parallelism": f"replicas x{world}",
+                           "rdf": f"one RDF sample (reference bins + the 0-15 A / 300-bin extension) every "
+                                  f"{p.stepRdf} steps, amortised: its extra device time, measured on RDF steps "
+                                  f"against the steps just before them, is added as rdf_extra_ms / {p.stepRdf} "
+                                  "to the timed window's steps without RDF work (value, ms_per_step, e2e)",
                            "launch_shape": forms[head]["launch_shape"]},
+                "window_ms_per_step": forms[head]["window_ms_per_step"],
+                "window_rdf_steps": forms[head]["window_rdf_steps"], "rdf_extra_ms": forms[head]["rdf_extra_ms"],
                 "clocks": forms[head]["clocks"], "gpu_launches": forms[head]["launches"], "roofline": roof,
                 "step_roofline": step_roof, "e2e": e2e,
                 other: {"value": forms[other]["value"], "ms_per_step": forms[other]["ms_per_step"],
+                        "window_ms_per_step": forms[other]["window_ms_per_step"],
+                        "rdf_extra_ms": forms[other]["rdf_extra_ms"],
                         "gpu_launches": forms[other]["launches"], "clocks": forms[other]["clocks"],
                         "launch_shape": forms[other]["launch_shape"]},
                 "mixed_over_plain": forms["mixed"]["value"] / forms["plain"]["value"],
+                "batched": batched,
                 "nve_drift": drift,
                 "cpu_baseline": cpu}
         print(json.dumps(line, default=float))

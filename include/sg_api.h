@@ -46,7 +46,8 @@ enum {
     SG_ERR_TIMEOUT = 8,        /* a bounded device-side wait gave up */
     SG_ERR_IO = 9,             /* output file could not be written */
     SG_ERR_UNSUPPORTED = 10,   /* feature not available in this mode */
-    SG_ERR_CELL_OVERFLOW = 11, /* more than blockSize (64) atoms in one cell (reference cap) */
+    SG_ERR_CELL_OVERFLOW = 11, /* PLAIN: more than blockSize (64) atoms in one cell (the reference's
+                                  cap); MIXED: more than 4 x blockSize (256) */
     SG_ERR_BAD_FILE = 12       /* malformed input or checkpoint file */
 };
 
@@ -370,6 +371,15 @@ int sg_diff_forces(sg_diff *d, const double *theta, float *forces);
  * NULL, dL/dtheta. */
 int sg_diff_force_matching(sg_diff *d, const double *theta, const float *ref_forces, double *loss,
                            double *grad);
+/* A fitted theta into the simulated model: replica rep's (rep == -1: every replica's) MIXED EAM
+ * tables become the B-splines phi(r) and f(r) of theta, its metal-carbon LJ epsilon and sigma
+ * theta[0], theta[1]; the embedding function and the graphene terms stay.  The metal forces of
+ * the context then equal sg_diff_forces(theta) on the same positions (with a list radius that
+ * covers the LJ cutoff, as sg_diff_frame_params gives).  With eam_table_knots - 1 a multiple of
+ * SG_DIFF_SPLINE_INTERVALS (1016, say) every table piece is a spline piece; with other knot
+ * counts the table interpolates the spline.  MIXED only (SG_ERR_UNSUPPORTED in PLAIN, which
+ * evaluates the reference's analytic functions). */
+int sg_load_diff_theta(sg_ctx *ctx, int rep, const double *theta);
 
 /* ---- tuning ------------------------------------------------------------------------------- */
 /* Times the launch shapes of the tunable passes on the context's own state and keeps the

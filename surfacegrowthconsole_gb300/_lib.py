@@ -229,6 +229,7 @@ _SIGS = {
     "sg_diff_energy": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "sg_diff_forces": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "sg_diff_force_matching": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "sg_load_diff_theta": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "CudaInitW": (None, [C.c_int, C.c_void_p]),
     "SetParametersW": (None, [C.POINTER(SimParams)]),
     "InitCoordsW": (C.c_char_p, [C.c_void_p, C.c_void_p, C.POINTER(SimParams)]),

@@ -1,6 +1,6 @@
-"""In-tree build of the native parts: libsgmd.so (CUDA kernels + C ABI, sm_103a), the sgmd
-command-line driver, and the test infrastructure: the CPU oracle (oracle/liboracle.so) and the
-loader of the reference kernels' cubin (oracle/librefkern.so).
+"""In-tree build of the native parts: libsgmd.so (CUDA kernels + C ABI, sm_103a) and the test
+infrastructure: the CPU oracle (oracle/liboracle.so) and the loader of the reference kernels'
+cubin (oracle/librefkern.so).
 
 Each translation unit compiles in its own process, all in parallel; a unit is rebuilt only
 when a source or header it may include is newer than its object.  No CMake, one -gencode.
@@ -19,7 +19,6 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 INC = ROOT / "include"
 LIBDIR = PKG / "lib"
-BINDIR = PKG / "bin"
 ORACLE = ROOT / "oracle"
 CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 NVCC = str(CUDA_HOME / "bin" / "nvcc")
@@ -29,7 +28,6 @@ HOSTFLAGS = "-fPIC,-ffp-contract=off,-O2"
 LIBSGMD = LIBDIR / "libsgmd.so"
 LIBORACLE = ORACLE / "liboracle.so"
 LIBREFKERN = ORACLE / "librefkern.so"  # loads the reference kernels' cubin (tests only)
-SGMD_BIN = BINDIR / "sgmd"
 
 # (source, extra flags): the PLAIN kernels are compiled without FMA contraction so their
 # arithmetic follows the reference's operation order exactly.
@@ -68,7 +66,6 @@ def _obj(src: str) -> Path:
 def build(verbose: bool = False, force: bool = False) -> None:
     """Compile everything that is out of date."""
     (LIBDIR / "obj").mkdir(parents=True, exist_ok=True)
-    BINDIR.mkdir(parents=True, exist_ok=True)
     hdrs = _headers()
     jobs = []
     for src, extra in CUDA_UNITS:
@@ -102,16 +99,10 @@ def build(verbose: bool = False, force: bool = False) -> None:
     if force or _stale(LIBSGMD, objs):
         _run(["g++", "-shared", "-o", str(LIBSGMD), *map(str, objs), "-L" + cudalib, "-lcudart",
               "-Wl,-rpath," + cudalib, "-Wl,--no-undefined"])
-    main_src = CSRC / "sgmd_main.cpp"
-    if main_src.exists() and (force or _stale(SGMD_BIN, [main_src, LIBSGMD] + hdrs)):
-        _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", str(INC), str(main_src), "-o", str(SGMD_BIN),
-              "-L" + str(LIBDIR), "-lsgmd", "-Wl,-rpath,$ORIGIN/../lib", "-L" + cudalib, "-lcudart",
-              "-Wl,-rpath," + cudalib])
 
 
 def clean() -> None:
     shutil.rmtree(LIBDIR, ignore_errors=True)
-    shutil.rmtree(BINDIR, ignore_errors=True)
     for f in (LIBORACLE, LIBREFKERN):
         if f.exists():
             f.unlink()

@@ -46,6 +46,9 @@ constexpr int kMixAtoms = 512;    // and the fewest atoms per block (1 per threa
 constexpr int kUnpackAtoms = 256; // state upload: atoms (threads) per block
 constexpr int kMinItemAtoms = 4;  // smallest home atoms per work item the engine allows
 constexpr int kItemAtoms = 8;     // the engine's default home atoms per work item
+constexpr int kMixedCellCapFactor = 4;  // MIXED: atoms per cell up to 4 x blockSize (256)
+constexpr int kRdfAtoms = 4;      // RDF sample: metal atoms per 128-thread block (a warp each)
+constexpr int kRdfTile = 64;      // RDF extension: metal atoms per tile (and threads per block)
 constexpr int kMetalPerBlock = 128 / kMT;   // atoms per 128-thread block
 constexpr int kCarbonPerBlock = 128 / kCT;
 

@@ -265,8 +265,14 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
   }
   c->ntot = atomOff;
   c->ctot = cellOff;
+  // Cell capacity of the counting sort.  PLAIN keeps the reference's cap of blockSize (64) atoms
+  // per cell (SurfaceGrowth.h:35, cu:582-583) and reports a cell above it as SG_ERR_CELL_OVERFLOW
+  // where the reference would write past its cell array.  MIXED, which is not held to that
+  // limit, files up to kMixedCellCapFactor times as many atoms per cell, so a crowded cell (a hot
+  // system pressing atoms together) stays in the lists.
   c->bucketCap = 1;
   for (int r = 0; r < n_replicas; r++) c->bucketCap = std::max(c->bucketCap, (int)params[r].blockSize);
+  if (c->opt.mode == SG_MODE_MIXED) c->bucketCap *= kMixedCellCapFactor;
   // list build: one warp per home cell, a grid of a few resident blocks per SM walking the cells
   c->numSMs = numSMs;
   c->pdl = c->opt.programmatic_launch != 0;
@@ -346,7 +352,7 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
   // tables
   if ((rc = makeRangeTab(c, c->atomTab, 128, 0)) || (rc = makeRangeTab(c, c->metalTab, 128, 1)) ||
       (rc = makeRangeTab(c, c->carbonTab, 128, 2)) || (rc = makeRangeTab(c, c->metalTabT, kMetalPerBlock, 1)) ||
-      (rc = makeRangeTab(c, c->carbonTabT, kCarbonPerBlock, 2))) {
+      (rc = makeRangeTab(c, c->carbonTabT, kCarbonPerBlock, 2)) || (rc = makeRangeTab(c, c->rdfTab, kRdfAtoms, 1))) {
     sg_destroy(c);
     return rc;
   }
@@ -354,6 +360,27 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
   if ((rc = setMetalLanes(c, c->opt.metal_lanes ? c->opt.metal_lanes : kMT))) {
     sg_destroy(c);
     return rc;
+  }
+  if (c->histExt) {
+    // RDF extension: every pair (A, B >= A) of 64-atom metal tiles of each replica
+    std::vector<int4> pairs;
+    for (int r = 0; r < n_replicas; r++) {
+      const RepConst &P = c->hrc[r];
+      const int nt = (P.nMolMe + kRdfTile - 1) / kRdfTile;
+      for (int a = 0; a < nt; a++)
+        for (int b = a; b < nt; b++)
+          pairs.push_back(make_int4(r, P.atomOff + a * kRdfTile, P.atomOff + b * kRdfTile, 0));
+    }
+    c->nRdfPairs = (int)pairs.size();
+    if ((rc = devAllocT(c, &c->rdfPairs, std::max<size_t>(pairs.size(), 1)))) {
+      sg_destroy(c);
+      return rc;
+    }
+    if (!pairs.empty() && cudaMemcpy(c->rdfPairs, pairs.data(), pairs.size() * sizeof(int4),
+                                     cudaMemcpyHostToDevice) != cudaSuccess) {
+      sg_destroy(c);
+      return sg_fail(SG_ERR_CUDA, "upload of the RDF tile pairs");
+    }
   }
   {
     std::vector<int> rr, ss, cr, cs, tr, ts;
@@ -624,14 +651,14 @@ static int enqueueRdf(sg_ctx *c, bool zero) {
     if (c->histExt)
       CK(cudaMemsetAsync(c->histExt, 0, sizeof(unsigned long long) * c->nrep * c->opt.rdf_ext_bins, c->stream));
   }
-  if (c->metalTab.n && c->maxHist > 0) {
-    CK(launchK(c->pdl, k_rdf, c->metalTab.n, 128, c->maxHist * sizeof(unsigned), c->stream, 
-        c->metalTab.view(), c->rc, c->st, c->pos, c->cellOf, c->cellStart, c->sortIdx, c->hist, c->histStride));
+  if (c->rdfTab.n && c->maxHist > 0) {
+    CK(launchK(c->pdl, k_rdf, c->rdfTab.n, 32 * kRdfAtoms, c->maxHist * sizeof(unsigned), c->stream,
+               c->rdfTab.view(), c->rc, c->st, c->pos, c->cellOf, c->cellStart, c->sortIdx, c->hist, c->histStride));
     LAUNCH_OK();
   }
-  if (c->histExt && c->metalTab.n) {
-    CK(launchK(c->pdl, k_rdf_ext, c->metalTab.n, 128, c->opt.rdf_ext_bins * sizeof(unsigned), c->stream, 
-        c->rc, c->pos, c->metalTab.rep, c->metalTab.start, c->histExt, c->opt.rdf_ext_bins, c->opt.rdf_ext_range));
+  if (c->histExt && c->nRdfPairs) {
+    CK(launchK(c->pdl, k_rdf_ext, c->nRdfPairs, kRdfTile, c->opt.rdf_ext_bins * sizeof(unsigned), c->stream,
+               c->rc, c->pos, c->rdfPairs, c->histExt, c->opt.rdf_ext_bins, c->opt.rdf_ext_range));
     LAUNCH_OK();
   }
   return SG_OK;

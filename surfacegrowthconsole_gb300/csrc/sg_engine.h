@@ -51,11 +51,14 @@ struct sg_ctx {
   int *dRedFirst = nullptr, *dCmvFirst = nullptr, *tileSum = nullptr, *dTileFirst = nullptr;
   unsigned *hist = nullptr;
   unsigned long long *histExt = nullptr;
+  int4 *rdfPairs = nullptr;  // RDF extension: {replica, first A atom, first B atom} per tile pair
+  int nRdfPairs = 0;
   int histStride = 0;
   float *diffBuf = nullptr;
   size_t *dDiffOff = nullptr;
   DevTab atomTab, metalTab, carbonTab, redTab, cmvTab, tileTab;
   DevTab metalTabT, carbonTabT;  // blocks of kMetalPerBlock / kCarbonPerBlock atoms
+  DevTab rdfTab;                 // blocks of kRdfAtoms metal atoms (the RDF sample)
   // launch shape of the metal chain: lanes per atom and its block table (128 / lanes atoms per
   // block; lanes 4, 8, 16, 32 -> slot 0..3, made on first use, slot 2 is metalTabT)
   int metalLanes = sg::kMT;

@@ -73,8 +73,8 @@ __global__ void k_shear(BlockTab tab, const RepConst *rc, RepState *st, const fl
 __global__ void k_rdf(BlockTab tab, const RepConst *rc, RepState *st, const float4 *pos,
                       const int *cellOf, const int *cellStart, const int *sortIdx, unsigned *hist,
                       int histStride);
-__global__ void k_rdf_ext(const RepConst *rc, const float4 *pos, const int *tileRep,
-                          const int *tileStart, unsigned long long *hist, int nbins, float range);
+__global__ void k_rdf_ext(const RepConst *rc, const float4 *pos, const int4 *pairs, unsigned long long *hist,
+                          int nbins, float range);
 __global__ void k_apply_pending(BlockTab tab, const RepConst *rc, RepState *st, float4 *vel);
 __global__ void k_clear_pending(RepState *st, int nrep);
 __global__ void k_publish_state(const int *src, int *dst, int nwords, unsigned *devSeq, volatile unsigned *hostSeq);

@@ -583,6 +583,15 @@ static void eamPairExact(const RepConst &P, double r, double out[4]) {
   out[3] = -(double)P.fe * rei * eB * tB / dB;
 }
 
+// Interval of width h with values g0, g1 and slopes d0, d1 at its ends: the coefficients of
+// g(r_k + s) = c0 + c1 s + c2 s^2 + c3 s^3 (the cubic Hermite interpolant), expanded around the
+// left end in FP64.
+static float4 hermite(double g0, double d0, double g1, double d1, double h) {
+  const double c2 = (3.0 * (g1 - g0) / h - 2.0 * d0 - d1) / h;
+  const double c3 = (d0 + d1 - 2.0 * (g1 - g0) / h) / (h * h);
+  return make_float4((float)g0, (float)d0, (float)c2, (float)c3);
+}
+
 bool sg_mixed_staging_ok(sg_ctx *c) {
   const MixedBufs *m = static_cast<const MixedBufs *>(c->mixed);
   return m && m->stagedOk;
@@ -612,12 +621,7 @@ int sg_mixed_init(sg_ctx *c) {
       double a[4], b[4];
       eamPairExact(P, rmin + k * h, a);
       eamPairExact(P, rmin + (k + 1) * h, b);
-      for (int fn = 0; fn < 2; fn++) {
-        const double g0 = a[2 * fn], d0 = a[2 * fn + 1], g1 = b[2 * fn], d1 = b[2 * fn + 1];
-        const double c2 = (3.0 * (g1 - g0) / h - 2.0 * d0 - d1) / h;
-        const double c3 = (d0 + d1 - 2.0 * (g1 - g0) / h) / (h * h);
-        tab.push_back(make_float4((float)g0, (float)d0, (float)c2, (float)c3));
-      }
+      for (int fn = 0; fn < 2; fn++) tab.push_back(hermite(a[2 * fn], a[2 * fn + 1], b[2 * fn], b[2 * fn + 1], h));
     }
   }
   // the staged metal kernels hold the largest replica table in shared memory
@@ -756,5 +760,59 @@ int sg_mixed_enqueue_reduce(sg_ctx *c, int forceRebuild) {
       BlockTab{m->redRep, m->redStart, m->redN}, c->rc, c->st, c->pos, c->posLo, c->vel, c->acc, c->fric, m->partDF, m->partF,
       c->dRedFirst, m->counter, m->diff64, m->dDiffOff64, c->diffBuf, c->dDiffOff, forceRebuild));
   MCK(cudaGetLastError());
+  return SG_OK;
+}
+
+// The differentiation form's fitted model in a MIXED context: phi and f become the uniform cubic
+// B-splines of theta (SG_DIFF_SPLINE_COEFFS coefficients each on SG_DIFF_SPLINE_INTERVALS equal
+// intervals from 0.6 r_e to the EAM cutoff, the piece of the end interval continuing past it),
+// and the metal-carbon Lennard-Jones epsilon and sigma become theta[0], theta[1] (its cutoff
+// stays the parameter block's).  Each table interval takes the values and slopes of the spline
+// piece that holds its midpoint at both ends, so when the table's knots include the spline's
+// (intervals - 1 a multiple of SG_DIFF_SPLINE_INTERVALS, e.g. eam_table_knots 1016) every table
+// cubic is the spline's own piece; otherwise the table is the spline's Hermite interpolant.
+extern "C" int sg_load_diff_theta(sg_ctx *c, int rep, const double *theta) {
+  if (!c || !theta || rep < -1 || rep >= c->nrep) return sg_fail(SG_ERR_INVALID, "sg_load_diff_theta: bad arguments");
+  if (c->opt.mode != SG_MODE_MIXED || !c->mixed)
+    return sg_fail(SG_ERR_UNSUPPORTED, "sg_load_diff_theta: tables exist in MIXED mode only");
+  MixedBufs *m = static_cast<MixedBufs *>(c->mixed);
+  constexpr int kSC = SG_DIFF_SPLINE_COEFFS, kSI = SG_DIFF_SPLINE_INTERVALS;
+  for (int r = (rep < 0 ? 0 : rep); r < (rep < 0 ? c->nrep : rep + 1); r++) {
+    RepConst &P = c->hrc[r];
+    if (P.nMolMe == 0) continue;
+    if (P.nTab == 0) return sg_fail(SG_ERR_UNSUPPORTED, "sg_load_diff_theta: replica %d has no EAM table", r);
+    const int knots = P.nTab;
+    const double rmin = 0.6 / P.rei, rmax = std::sqrt((double)P.rrCutEam);
+    const double h = (rmax - rmin) / (knots - 1);
+    const double hs = (rmax - rmin) / kSI;
+    // value and slope of spline `fn` (0: phi, 1: f) at r, on piece k
+    auto spline = [&](int fn, int k, double r, double &g, double &d) {
+      const double *cf = theta + 2 + fn * kSC + k;
+      const double t = (r - rmin) / hs - k, t2 = t * t, t3 = t2 * t, u = 1.0 - t;
+      g = (cf[0] * u * u * u + cf[1] * (3.0 * t3 - 6.0 * t2 + 4.0) + cf[2] * (-3.0 * t3 + 3.0 * t2 + 3.0 * t + 1.0) +
+           cf[3] * t3) / 6.0;
+      d = (cf[0] * (-0.5 * u * u) + cf[1] * (1.5 * t2 - 2.0 * t) + cf[2] * (-1.5 * t2 + t + 0.5) + cf[3] * (0.5 * t2)) / hs;
+    };
+    std::vector<float4> tab;
+    tab.reserve((size_t)2 * knots);
+    for (int k = 0; k < knots; k++) {
+      const double ra = rmin + k * h, rb = rmin + (k + 1) * h;
+      const int piece = std::max(0, std::min((int)std::floor((0.5 * (ra + rb) - rmin) / hs), kSI - 1));
+      for (int fn = 0; fn < 2; fn++) {
+        double g0, d0, g1, d1;
+        spline(fn, piece, ra, g0, d0);
+        spline(fn, piece, rb, g1, d1);
+        tab.push_back(hermite(g0, d0, g1, d1, h));
+      }
+    }
+    P.epsLJ = (float)theta[0];
+    P.sigmaLJ = (float)theta[1];
+    c->hp[r].epsLJ = P.epsLJ;
+    c->hp[r].sigmaLJ = P.sigmaLJ;
+    MCK(cudaMemcpyAsync(m->eamTab + (size_t)2 * P.tabOff, tab.data(), sizeof(float4) * tab.size(),
+                        cudaMemcpyHostToDevice, c->stream));
+  }
+  MCK(cudaMemcpyAsync(c->rc, c->hrc.data(), sizeof(RepConst) * c->nrep, cudaMemcpyHostToDevice, c->stream));
+  MCK(cudaStreamSynchronize(c->stream));
   return SG_OK;
 }

@@ -1401,46 +1401,69 @@ __global__ void k_shear(BlockTab tab, const RepConst *__restrict__ rc, RepState 
 
 // ============================================================================================
 // RDF sample (EvalRdfK, cu:1895-1999): ordered metal pairs in the 27-cell stencil of the
-// last-built cells, current positions, warp-aggregated shared-memory histogram.
+// last-built cells, current positions.  One warp per metal atom (kRdfAtoms atoms per 128-thread
+// block): lanes 0..26 look up the stencil cells (the reference's visiting order), a warp scan
+// of their lengths lays the candidates out as one window, and the lanes stride over it, each
+// finding its candidate's cell by binary search over the segment offsets.  Bins of the same
+// value are merged across the warp (__match_any_sync) before one shared-memory atomic per
+// distinct bin; the block adds its histogram to the replica's.  Counts do not depend on the
+// order of the pairs, so they are the reference's bit for bit.
 // ============================================================================================
-__global__ void k_rdf(BlockTab tab, const RepConst *__restrict__ rc, RepState *st,
-                      const float4 *__restrict__ pos, const int *__restrict__ cellOf,
-                      const int *__restrict__ cellStart, const int *__restrict__ sortIdx,
-                      unsigned *__restrict__ hist, int histStride) {
+__global__ void __launch_bounds__(128) k_rdf(BlockTab tab, const RepConst *__restrict__ rc, RepState *st,
+                                             const float4 *__restrict__ pos, const int *__restrict__ cellOf,
+                                             const int *__restrict__ cellStart, const int *__restrict__ sortIdx,
+                                             unsigned *__restrict__ hist, int histStride) {
   pdlEnter();
   extern __shared__ unsigned shist[];
+  __shared__ int sQb[kRdfAtoms][27], sOff[kRdfAtoms][28];
+  __shared__ float4 sSh[kRdfAtoms][27];
   const int rep = tab.rep[blockIdx.x];
   const RepConst &P = rc[rep];
   RepState *S = st + rep;
   const int nb = P.sizeHistRdf;
   for (int b = threadIdx.x; b < nb; b += blockDim.x) shist[b] = 0u;
   __syncthreads();
-  const int i = tab.start[blockIdx.x] + threadIdx.x;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = tab.start[blockIdx.x] + w;
   const int metalEnd = P.atomOff + P.nMolMe;
   const float range2 = P.rangeRdf * P.rangeRdf;
-  const int lane = threadIdx.x & 31;
   int dropped = 0;
-  const bool active = (i < metalEnd) && (cellOf[i] >= 0);
-  const float4 A = active ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-  const int c = active ? cellOf[i] : 0;
-  for (int o = 0; o < 27; o++) {
-    float sx = 0.f, sy = 0.f, sz = 0.f;
-    int qb = 0, len = 0;
-    if (active) {
-      const int C = stencilCell(P, c, o, sx, sy, sz);
-      qb = cellStart[P.cellOff + C];
+  const bool active = (i < metalEnd) && (cellOf[i] >= 0);  // uniform across the warp
+  if (active) {
+    const float4 A = pos[i];
+    const int c = cellOf[i];
+    int len = 0;
+    if (lane < 27) {
+      float sx, sy, sz;
+      const int C = stencilCell(P, c, lane, sx, sy, sz);
+      const int qb = cellStart[P.cellOff + C];
       len = cellStart[P.cellOff + C + 1] - qb;
+      sQb[w][lane] = qb;
+      sSh[w][lane] = make_float4(sx, sy, sz, 0.f);
     }
-    // every lane runs the same trip count, so the warp is converged at the match below
-    const int maxLen = __reduce_max_sync(0xffffffffu, len);
-    for (int q = 0; q < maxLen; q++) {
+    int incl = len;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += v;
+    }
+    if (lane < 27) sOff[w][lane] = incl - len;
+    const int total = __shfl_sync(0xffffffffu, incl, 26);
+    __syncwarp();
+    for (int e0 = 0; e0 < total; e0 += 32) {  // the same trip count in every lane
+      const int e = e0 + lane;
       int bin = -1;
-      if (q < len) {
-        const int k = sortIdx[qb + q];
+      if (e < total) {
+        int o = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1)
+          if (o + step < 27 && sOff[w][o + step] <= e) o += step;
+        const int k = sortIdx[sQb[w][o] + e - sOff[w][o]];
         if (k < metalEnd && k != i) {
           const float4 B = pos[k];
+          const float4 sh = sSh[w][o];
           float dx = A.x - B.x, dy = A.y - B.y, dz = A.z - B.z;
-          dx = dx - sx; dy = dy - sy; dz = dz - sz;
+          dx = dx - sh.x; dy = dy - sh.y; dz = dz - sh.z;
           const float rr = dx * dx + dy * dy + dz * dz;
           if (rr < range2) {
             bin = (int)(sqrtf(rr) * P.intervalRdf);
@@ -1462,96 +1485,102 @@ __global__ void k_rdf(BlockTab tab, const RepConst *__restrict__ rc, RepState *s
   // a pair just inside rangeRdf whose bin index rounds up to sizeHistRdf: the reference adds it
   // one element past its histogram (SurfaceGrowth.cu:1988-1989), outside every printed bin; it
   // is dropped here and only counted (sg_diag.rdf_range), not reported as an error
-  if (dropped) atomicAdd(&S->rdfRange, dropped);
+  for (int o = 16; o > 0; o >>= 1) dropped += __shfl_xor_sync(0xffffffffu, dropped, o);
+  if (dropped && lane == 0) atomicAdd(&S->rdfRange, dropped);
 }
 
-__device__ __forceinline__ void blockBox(float4 p, bool valid, float *out6, float (*red)[6]) {
-  // min x, y, z and max x, y, z of the valid points of a 128-thread block
-  float v[6] = {valid ? p.x : 3.4e38f, valid ? p.y : 3.4e38f, valid ? p.z : 3.4e38f,
-                valid ? p.x : -3.4e38f, valid ? p.y : -3.4e38f, valid ? p.z : -3.4e38f};
+
+// RDF extension: all metal pairs of a replica within `range` into nbins (0-15 A / 300 bins in
+// the benchmark), ordered pairs counted twice like the reference's histogram.  One 64-thread
+// block per (A tile, B tile) pair of 64-atom metal tiles with B >= A (the pair table, built
+// once per context): the block loads both tiles, takes their bounding boxes and leaves at once
+// when the boxes are farther apart in the minimum image than the range (with a margin far above
+// rounding) -- metal atoms are numbered cluster by cluster, so most tile pairs of a
+// multi-cluster system drop out.  A surviving block walks its 64 x 64 pairs (j > i inside a
+// self tile): per B atom every lane has its A atom's bin, lanes with the same bin are merged
+// by __match_any_sync and their leader adds the merged count to a shared-memory histogram,
+// which the block adds to the replica's global histogram at the end.  The pair tiles spread
+// the work over every SM (the former one-block-per-A-tile form ran a serial walk over the
+// remaining tiles in 44 blocks).
+__global__ void __launch_bounds__(kRdfTile) k_rdf_ext(const RepConst *__restrict__ rc, const float4 *__restrict__ pos,
+                                                      const int4 *__restrict__ pairs,
+                                                      unsigned long long *__restrict__ hist, int nbins, float range) {
+  pdlEnter();
+  extern __shared__ unsigned eh[];
+  __shared__ float4 tileB[kRdfTile];
+  __shared__ float box[kRdfTile / 32][12];
+  const int4 w = pairs[blockIdx.x];  // replica, first A atom, first B atom
+  const RepConst &P = rc[w.x];
+  const int me = P.atomOff + P.nMolMe;
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const bool haveA = w.y + t < me, haveB = w.z + t < me;
+  const float4 A = haveA ? pos[w.y + t] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 Bt = haveB ? pos[w.z + t] : make_float4(0.f, 0.f, 0.f, 0.f);
+  tileB[t] = Bt;
+  // bounding boxes of the two tiles: min x, y, z, max x, y, z of A, then of B
+  float v[12] = {haveA ? A.x : 3.4e38f, haveA ? A.y : 3.4e38f, haveA ? A.z : 3.4e38f,
+                 haveA ? A.x : -3.4e38f, haveA ? A.y : -3.4e38f, haveA ? A.z : -3.4e38f,
+                 haveB ? Bt.x : 3.4e38f, haveB ? Bt.y : 3.4e38f, haveB ? Bt.z : 3.4e38f,
+                 haveB ? Bt.x : -3.4e38f, haveB ? Bt.y : -3.4e38f, haveB ? Bt.z : -3.4e38f};
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
-    for (int c = 0; c < 6; c++) {
-      const float w = __shfl_xor_sync(0xffffffffu, v[c], o);
-      v[c] = (c < 3) ? fminf(v[c], w) : fmaxf(v[c], w);
+    for (int c = 0; c < 12; c++) {
+      const float u = __shfl_xor_sync(0xffffffffu, v[c], o);
+      v[c] = (c % 6 < 3) ? fminf(v[c], u) : fmaxf(v[c], u);
     }
-  const int wid = threadIdx.x >> 5;
-  if ((threadIdx.x & 31) == 0)
-    for (int c = 0; c < 6; c++) red[wid][c] = v[c];
+  if (lane == 0)
+#pragma unroll
+    for (int c = 0; c < 12; c++) box[wid][c] = v[c];
   __syncthreads();
-  if (threadIdx.x < 6) {
-    float m = red[0][threadIdx.x];
-    for (int w = 1; w < 4; w++) m = (threadIdx.x < 3) ? fminf(m, red[w][threadIdx.x]) : fmaxf(m, red[w][threadIdx.x]);
-    out6[threadIdx.x] = m;
+#pragma unroll
+  for (int c = 0; c < 12; c++) {
+    float m = box[0][c];
+#pragma unroll
+    for (int k = 1; k < kRdfTile / 32; k++) m = (c % 6 < 3) ? fminf(m, box[k][c]) : fmaxf(m, box[k][c]);
+    v[c] = m;
   }
-}
-
-// RDF extension: all metal pairs of a replica within `range` into nbins (0-15 A / 300 bins in
-// the production configuration), checked against the FP64 all-pairs oracle.  Unordered pairs,
-// each counted twice (the FP32 distance of (i, k) and (k, i) is the same number).  Blocks of
-// 128 atoms against tiles of 128 atoms; a tile whose minimum-image bounding-box gap to the
-// block exceeds the range (with a margin far above rounding) is skipped whole: metal atoms are
-// numbered cluster by cluster, so most tiles of a multi-cluster system drop out.
-__global__ void __launch_bounds__(128) k_rdf_ext(const RepConst *__restrict__ rc, const float4 *__restrict__ pos,
-                                                 const int *__restrict__ tileRep,
-                                                 const int *__restrict__ tileStart,
-                                                 unsigned long long *__restrict__ hist, int nbins, float range) {
-  pdlEnter();
-  extern __shared__ unsigned eh[];
-  __shared__ float4 tileB[128];
-  __shared__ float boxA[6], boxB[6];
-  __shared__ float red[4][6];
-  const int rep = tileRep[blockIdx.x];
-  const RepConst &P = rc[rep];
-  for (int b = threadIdx.x; b < nbins; b += blockDim.x) eh[b] = 0u;
-  const int a0 = tileStart[blockIdx.x];
-  const int i = a0 + threadIdx.x;
-  const int me = P.atomOff + P.nMolMe;
-  const bool haveA = i < me;
-  const float4 A = haveA ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
   const float L[3] = {P.region[0], P.region[1], P.region[2]};
   const float invL[3] = {1.f / L[0], 1.f / L[1], 1.f / L[2]};
-  const float scale = nbins / range;
   const float r2max = range * range;
-  blockBox(A, haveA, boxA, red);
-  for (int j0 = a0; j0 < me; j0 += 128) {
-    __syncthreads();
-    const bool haveB = j0 + threadIdx.x < me;
-    const float4 Bt = haveB ? pos[j0 + threadIdx.x] : make_float4(0.f, 0.f, 0.f, 0.f);
-    tileB[threadIdx.x] = Bt;
-    blockBox(Bt, haveB, boxB, red);
-    __syncthreads();
-    // skip the tile when its boxes are farther apart than the range: per axis, no pair can be
-    // closer in the minimum image than the folded centre distance minus both half extents
-    float gap2 = 0.f;
+  // per axis, no pair can be closer in the minimum image than the folded centre distance minus
+  // both half extents (every thread computes the same value from the same shared words, so the
+  // exit below is uniform across the block)
+  float gap2 = 0.f;
 #pragma unroll
-    for (int c = 0; c < 3; c++) {
-      const float hA = 0.5f * (boxA[3 + c] - boxA[c]), hB = 0.5f * (boxB[3 + c] - boxB[c]);
-      float d = 0.5f * (boxA[3 + c] + boxA[c]) - 0.5f * (boxB[3 + c] + boxB[c]);
-      d -= L[c] * rintf(d * invL[c]);
-      const float g = fmaxf(fabsf(d) - hA - hB - 0.01f, 0.f);
-      gap2 += g * g;
-    }
-    if (gap2 <= r2max && haveA) {
-      const int nj = min(128, me - j0);
-      for (int jj = (j0 == a0) ? threadIdx.x + 1 : 0; jj < nj; jj++) {
-        const float4 B = tileB[jj];
-        float dx = A.x - B.x, dy = A.y - B.y, dz = A.z - B.z;
-        dx -= L[0] * rintf(dx * invL[0]);
-        dy -= L[1] * rintf(dy * invL[1]);
-        dz -= L[2] * rintf(dz * invL[2]);
-        const float rr = dx * dx + dy * dy + dz * dz;
-        if (rr < r2max) {
-          const int bin = (int)(sqrtf(rr) * scale);
-          if (bin < nbins) atomicAdd(&eh[bin], 2u);
-        }
+  for (int c = 0; c < 3; c++) {
+    const float hA = 0.5f * (v[3 + c] - v[c]), hB = 0.5f * (v[9 + c] - v[6 + c]);
+    float d = 0.5f * (v[3 + c] + v[c]) - 0.5f * (v[9 + c] + v[6 + c]);
+    d -= L[c] * rintf(d * invL[c]);
+    const float g = fmaxf(fabsf(d) - hA - hB - 0.01f, 0.f);
+    gap2 += g * g;
+  }
+  if (gap2 > r2max) return;
+  for (int b = t; b < nbins; b += kRdfTile) eh[b] = 0u;
+  __syncthreads();
+  const float scale = nbins / range;
+  const bool self = (w.y == w.z);
+  const int nj = min(kRdfTile, me - w.z);
+  for (int jj = 0; jj < nj; jj++) {
+    const float4 B = tileB[jj];
+    int bin = -1;
+    if (haveA && (!self || jj > t)) {
+      float dx = A.x - B.x, dy = A.y - B.y, dz = A.z - B.z;
+      dx -= L[0] * rintf(dx * invL[0]);
+      dy -= L[1] * rintf(dy * invL[1]);
+      dz -= L[2] * rintf(dz * invL[2]);
+      const float rr = dx * dx + dy * dy + dz * dz;
+      if (rr < r2max) {
+        const int b = (int)(sqrtf(rr) * scale);
+        if (b < nbins) bin = b;
       }
     }
+    const unsigned m = __match_any_sync(0xffffffffu, bin);
+    if (bin >= 0 && lane == __ffs(m) - 1) atomicAdd(&eh[bin], 2u * (unsigned)__popc(m));
   }
   __syncthreads();
-  for (int b = threadIdx.x; b < nbins; b += blockDim.x)
-    if (eh[b]) atomicAdd(&hist[(size_t)rep * nbins + b], (unsigned long long)eh[b]);
+  for (int b = t; b < nbins; b += kRdfTile)
+    if (eh[b]) atomicAdd(&hist[(size_t)w.x * nbins + b], (unsigned long long)eh[b]);
 }
 
 // Apply a pending thermostat rescale now (before the state is read back).

@@ -298,6 +298,12 @@ class Simulation:
             if f:
                 L.fclose(f)
 
+    def load_diff_theta(self, theta: np.ndarray, rep: int = -1) -> None:
+        """The differentiation form's fitted parameters (66 values) into this MIXED context's
+        EAM tables and metal-carbon LJ parameters (sg_load_diff_theta)."""
+        t = np.ascontiguousarray(theta, np.float64)
+        check(lib().sg_load_diff_theta(self._h, rep, t.ctypes.data_as(C.c_void_p)))
+
     def autotune(self, steps: int = 20) -> dict:
         """Times the launch shapes (lanes per metal atom, list-build blocks per SM) on this
         context's state, keeps the fastest and restores the state; returns the timings."""

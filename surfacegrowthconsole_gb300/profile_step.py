@@ -1,7 +1,7 @@
 """Steps a benchmark workload under a CUDA profiler range, for kernel profilers.
 
     python -m surfacegrowthconsole_gb300.profile_step [--workload production|batched|precision]
-        [--mode plain|mixed] [--warmup 3] [--steps 1] [--replicas 16] [--shape JSON]
+        [--mode plain|mixed] [--warmup 3] [--steps 1] [--replicas 16] [--shape JSON] [--rdf-step]
 
 Builds the workload (--shape: a launch shape as sg_get_launch_shape reports it, a JSON object
 of its fields, e.g. the one the benchmark's autotuning chose; default: the library's
@@ -9,7 +9,9 @@ defaults), steps it `warmup` times (graph capture, caches), then runs `steps` st
 between cudaProfilerStart and cudaProfilerStop, so that a profiler started with its
 from-start profiling off (ncu --profile-from-start off) sees exactly those steps' kernels.
 Lists are rebuilt every step for the production workload (as its benchmark does) and by the
-reference's rule for the others.  Prints the kernel launches per step.
+reference's rule for the others.  --rdf-step: the production workload with the 0-15 A /
+300-bin RDF extension on, warmed up to the step before an RDF sample, so that the profiled
+step is an RDF step.  Prints the kernel launches per step.
 """
 from __future__ import annotations
 
@@ -41,6 +43,7 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--replicas", type=int, default=16)
     ap.add_argument("--shape", default="")
+    ap.add_argument("--rdf-step", action="store_true")
     a = ap.parse_args()
     if a.workload == "production":
         p, r, v = workloads.production(seed=2)
@@ -54,12 +57,17 @@ def main() -> None:
         r = np.concatenate([w[1] for w in reps])
         v = np.concatenate([w[2] for w in reps])
     n = int(sum(q.nMol for q in plist))
+    ext = {"rdf_ext_bins": 300, "rdf_ext_range": 15.0 / 1.42} if a.rdf_step else {}
     sim = Simulation(plist, mode=MODE_MIXED if a.mode == "mixed" else MODE_PLAIN,
-                     force_rebuild=a.workload == "production")
+                     force_rebuild=a.workload == "production", **ext)
     sim.set_state(r, v, np.zeros((n, 3), np.float32))
     if a.shape:
         sim.set_launch_shape(json.loads(a.shape))
-    sim.step(a.warmup)
+    warm = a.warmup
+    if a.rdf_step:  # the first profiled step is an RDF step
+        warm = max(warm, plist[0].stepRdf - 1)
+        warm += (plist[0].stepRdf - 1 - warm) % plist[0].stepRdf
+    sim.step(warm)
     rt = _cudart()
     rt.cudaProfilerStart()
     sim.step(a.steps)

@@ -34,7 +34,7 @@ def _rank(rank: int, world: int, port: int, out):
 
 def test_two_ranks_reduce_over_gloo():
     world = 2
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:  # no fork of this (threaded) test process
         out = m.dict()
         mp.spawn(_rank, args=(world, _free_port(), out), nprocs=world, join=True)
         res = dict(out)

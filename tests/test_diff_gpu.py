@@ -67,3 +67,33 @@ def test_torch_autograd_harness_carries_the_adjoint_gradient_and_fits():
     _, hist = fit(model, theta0, ref, steps=30, lr=5e-3)
     assert hist[-1] < 0.5 * hist[0], hist[::10]
     model.close()
+
+
+@pytest.mark.parametrize("knots,rtol", [(29 * 35 + 1, 2e-5), (1024, 2e-4)], ids=["aligned", "interpolated"])
+def test_fitted_theta_drives_the_mixed_step(knots, rtol):
+    """A fitted theta loaded into a MIXED context (sg_load_diff_theta) gives the metal forces of
+    the differentiation model on the same positions: EAM from the B-spline tables (each table
+    piece a spline piece when the table knots include the spline knots; the spline's Hermite
+    interpolant otherwise), LJ with theta's epsilon and sigma, the analytic embedding.  The list
+    radius of the frame parameter block covers the LJ cutoff, so both sides sum the same pairs."""
+    from surfacegrowthconsole_gb300 import MODE_MIXED
+    from surfacegrowthconsole_gb300.engine import Simulation
+    frames, r = workloads.differentiation_frames(n_frames=1, small_system=True, warm=20, every=10)
+    q = frames[0]
+    theta = perturbed(diff_init_theta(q), seed=11)
+    model = DiffModel(frames, r)
+    f_diff = model.forces(theta).reshape(-1, 3).astype(np.float64)
+    model.close()
+    sim = Simulation(q, mode=MODE_MIXED, eam_table_knots=knots)
+    sim.load_diff_theta(theta)
+    sim.set_state(r, np.zeros((q.nMol, 3), np.float32), np.zeros((q.nMol, 3), np.float32))
+    sim.build_lists()
+    sim.compute_forces()
+    a = sim.get_state()[2].astype(np.float64)
+    p = sim.params()
+    sim.close()
+    m = q.nMolMe
+    f_mixed = a[:m] * np.float64(q.massMe)
+    err = rel_inf(f_mixed, f_diff[:m])
+    assert err < rtol, err
+    assert np.isclose(p.epsLJ, np.float32(theta[0])) and np.isclose(p.sigmaLJ, np.float32(theta[1]))

@@ -111,3 +111,48 @@ def test_nve_drift_no_worse_than_plain():
     print("NVE drift eV/atom/ns: plain", drift[MODE_PLAIN], "mixed", drift[MODE_MIXED])
     assert drift[MODE_MIXED] <= drift[MODE_PLAIN] + 2e-5
     assert drift[MODE_MIXED] < 1e-3
+
+
+def crowded_cell_state(n_blob=90, seed=7):
+    """The 2,217-atom system with n_blob cluster atoms pressed into one cell of the vacuum above
+    the sheet (well above the reference's 64-atom cap, far from every other atom)."""
+    p, r, v = workloads.small(seed=seed)
+    r = r.copy()
+    L = np.array([p.region.x, p.region.y, p.region.z], np.float64)
+    inv = np.array([p.invWidth.x, p.invWidth.y, p.invWidth.z], np.float64)
+    cells = np.array([p.cells.x, p.cells.y, p.cells.z])
+    c = np.array([cells[0] // 2, cells[1] // 2, cells[2] - 2])  # high above the sheet at z_0
+    lo = c / inv - 0.5 * L
+    rng = np.random.RandomState(seed)
+    blob = lo + (0.2 + 0.6 * rng.uniform(size=(n_blob, 3))) / inv
+    r[:n_blob, :3] = blob.astype(np.float32)
+    return p, r, v
+
+
+def test_mixed_lists_a_cell_above_the_reference_cap():
+    """PLAIN keeps the reference's 64 atoms per cell and reports a fuller cell; MIXED files up to
+    256 and builds the same cells and lists as the (uncapped) oracle."""
+    p, r, v = crowded_cell_state()
+    a = np.zeros((p.nMol, 3), np.float32)
+    orc = oracle.OracleSim(p, 32)
+    orc.set_state(r, v, a)
+    orc.build_lists()
+    _, cs, _ = orc.cells()
+    assert np.diff(cs).max() == 90 > p.blockSize
+    plain = Simulation(p, mode=MODE_PLAIN)
+    plain.set_state(r, v, a)
+    with pytest.raises(Exception) as e:
+        plain.build_lists()
+    assert "CELL_OVERFLOW" in str(e.value)
+    plain.close()
+    mixed = Simulation(p, mode=MODE_MIXED)
+    mixed.set_state(r, v, a)
+    mixed.build_lists()
+    for g, o in zip(mixed.cells(), orc.cells()):
+        assert np.array_equal(g, o)
+    nn_g, nbl_g = mixed.nebr()
+    nn_o, nbl_o = orc.nebr()
+    assert np.array_equal(nn_g, nn_o) and np.array_equal(nbl_g, nbl_o)
+    d = mixed.diag()
+    assert d.max_cell_occupancy == 90 and d.cell_overflow == 0
+    mixed.close()

