@@ -18,6 +18,9 @@ LJ, graphene, reductions, thermostat, RDF/diffusion when due).
   batched : the batched form beside it (256 replicas in one context, MIXED and PLAIN, each
           autotuned, and the same replicas one by one), so that the comparison of the two forms
           at the batched size is in every run (--no-batched leaves it out).
+  persistent_step : the MIXED step as one cooperative launch with grid barriers between its
+          phases, timed like the headline (and at the batched size under `batched`), beside the
+          CUDA graph of one launch per phase that the headline runs (--no-persistent).
   nve_drift : the total-energy drift of both forms on bulk Ni (4,000 atoms, 300 K, 10 ps NVE),
           the "stated drift" the two forms are compared at.
   e2e   : the same metric through the public C ABI with host buffers: every step uploads the
@@ -88,6 +91,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="leave out the batched comparison of the production line")
+    ap.add_argument("--no-persistent", action="store_true", help="leave out the persistent-step measurements")
     ap.add_argument("--workload", default="production", choices=["production", "batched", "diff"])
     ap.add_argument("--replicas", type=int, default=256)
     return ap.parse_args()
@@ -278,8 +282,13 @@ def batched_forms(args, rank: int, world: int, local: int, dist, steps: int, war
     head = args.mode
     modes = {"plain": MODE_PLAIN, "mixed": MODE_MIXED}
     forms = {}
-    for name in (head, "plain" if head == "mixed" else "mixed"):
-        sim = Simulation(plist, mode=modes[name], device=local, stream=stream.cuda_stream)
+    names = [head, "plain" if head == "mixed" else "mixed"]
+    if not args.no_persistent:
+        names.append("mixed_persistent")
+    for name in names:
+        persistent = name == "mixed_persistent"
+        sim = Simulation(plist, mode=MODE_MIXED if persistent else modes[name], device=local,
+                         stream=stream.cuda_stream, persistent_step=persistent)
         sim.set_state(r, v, np.zeros((natoms, 3), np.float32))
         tune = None if args.no_tune else sim.autotune(steps=tune_steps)
         sim.step(warmup)
@@ -350,6 +359,7 @@ def run_batched(args, rank: int, world: int, local: int, dist=None):
                 "rebuilds_all_replicas": f["rebuilds_all_replicas"],
                 other: b["forms"][other],
                 "mixed_over_plain": b["mixed_over_plain"],
+                "mixed_persistent": b["forms"].get("mixed_persistent"),
                 "one_by_one": b["one_by_one"]}
         print(json.dumps(line, default=float))
 
@@ -460,9 +470,10 @@ def run_production(args, rank: int, world: int, local: int, dist):
     def max_over_ranks(x: float) -> float:
         return over_ranks(dist, x, "max", f"cuda:{local}")
 
-    def make(mode, phase_timing=False):
+    def make(mode, phase_timing=False, persistent=False):
         return Simulation(p, mode=mode, force_rebuild=True, device=local, stream=stream.cuda_stream,
-                          phase_timing=phase_timing, rdf_ext_bins=RDF_EXT_BINS, rdf_ext_range=RDF_EXT_RANGE)
+                          phase_timing=phase_timing, rdf_ext_bins=RDF_EXT_BINS, rdf_ext_range=RDF_EXT_RANGE,
+                          persistent_step=persistent)
 
     def timed(sim, phases=None):
         """args.steps steps, each bracketed by CUDA events on the library's stream, the L2 flushed
@@ -535,7 +546,25 @@ def run_production(args, rank: int, world: int, local: int, dist):
                        "rdf_extra_ms": 1e3 * extra,
                        "step_s": amortised_s(total_s, args.steps, n_rdf, extra)}
         sims[name] = sim
+    # the persistent step (one cooperative launch per MIXED step, grid barriers between the
+    # phases) timed the same way, beside the graph of one launch per phase
+    persist = None
+    if not args.no_persistent:
+        qsim = make(MODE_MIXED, persistent=True)
+        qsim.set_state(r, v, a)
+        qtune = None if args.no_tune else qsim.autotune(steps=20)
+        qsim.step(args.warmup)
+        with Clocks(local) as clk:
+            q_s, q_launches, q_rdf = timed(qsim)
+        q_extra = rdf_extra_s(qsim)
+        q_step = amortised_s(q_s, args.steps, q_rdf, q_extra)
+        persist = {"ms_per_step": 1e3 * q_step, "window_ms_per_step": 1e3 * q_s / args.steps,
+                   "rdf_extra_ms": 1e3 * q_extra, "gpu_launches": q_launches, "launch_shape": qtune,
+                   "clocks": clk.summary()}
+        qsim.close()
     atoms_all = over_ranks(dist, float(p.nMol), "sum", f"cuda:{local}")
+    if persist:
+        persist["value"] = atoms_all * 1e3 / persist["ms_per_step"]
     for f in forms.values():
         f["value"] = atoms_all / f["step_s"]
         f["ms_per_step"] = 1e3 * f["step_s"]
@@ -622,6 +651,9 @@ def run_production(args, rank: int, world: int, local: int, dist):
                                                                  "launch_shape", "clocks")},
                    "plain": {k: b["forms"]["plain"][k] for k in ("value", "ms_per_step", "steps", "gpu_launches",
                                                                  "launch_shape", "clocks")},
+                   "mixed_persistent": ({k: b["forms"]["mixed_persistent"][k]
+                                         for k in ("value", "ms_per_step", "steps", "gpu_launches", "launch_shape",
+                                                   "clocks")} if "mixed_persistent" in b["forms"] else None),
                    "mixed_over_plain": b["mixed_over_plain"], "one_by_one": b["one_by_one"],
                    "timing": "device time of the steps with CUDA events on the library's stream; state larger "
                              "than L2 (no flush)"}
@@ -660,6 +692,7 @@ def run_production(args, rank: int, world: int, local: int, dist):
                         "gpu_launches": forms[other]["launches"], "clocks": forms[other]["clocks"],
                         "launch_shape": forms[other]["launch_shape"]},
                 "mixed_over_plain": forms["mixed"]["value"] / forms["plain"]["value"],
+                "persistent_step": persist,
                 "batched": batched,
                 "nve_drift": drift,
                 "cpu_baseline": cpu}

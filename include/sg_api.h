@@ -92,7 +92,19 @@ typedef struct sg_options {
                             * (a grid of 4 blocks per SM), 0 read it through L1 */
     int carbon_blocks_per_sm; /* carbon pass compiled for 8, 12 or 16 resident 128-thread blocks
                             * per SM (64, 40 or 32 registers a thread; 0: 8) */
-    int reserved[1];
+    int persistent_step;   /* MIXED: 1 runs each step as one cooperative launch over all replicas,
+                            * its phases (integrate, cell scan and order, list build, density and
+                            * carbon forces, metal forces, reduction) separated by grid-wide
+                            * barriers instead of kernel boundaries; 0 (default): one launch per
+                            * phase, captured in a CUDA graph.  Metal lanes 4 or 16, the cell-window
+                            * list build. */
+    int persistent_wait_us; /* persistent step: longest wait at a grid barrier, microseconds of
+                            * the SM clock (0: 1,000,000); a launch whose wait runs out leaves with
+                            * SG_ERR_TIMEOUT and the context must be destroyed */
+    int nebr_capacity;     /* MIXED: entries per neighbour-list row, at least the parameter
+                            * block's iNebrMax (0: iNebrMax); a hot system that crowds atoms keeps
+                            * its full lists where PLAIN stops with SG_ERR_NEBR_OVERFLOW.
+                            * sg_get_nebr still returns iNebrMax columns. */
 } sg_options;
 
 /* Initialise *opt with the defaults (PLAIN mode, graphs on, device 0). */

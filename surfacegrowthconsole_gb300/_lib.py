@@ -91,7 +91,7 @@ class Options(C.Structure):
         ("phase_timing", C.c_int),
         ("programmatic_launch", C.c_int), ("nebr_descending", C.c_int), ("nebr_item_atoms", C.c_int),
         ("nebr_build", C.c_int), ("eam_table_smem", C.c_int), ("carbon_blocks_per_sm", C.c_int),
-        ("reserved", C.c_int * 1),
+        ("persistent_step", C.c_int), ("persistent_wait_us", C.c_int), ("nebr_capacity", C.c_int),
     ]
 
 

@@ -37,6 +37,8 @@ constexpr int kNebrWarps = 4;     // warps per block in the neighbour-list build
 constexpr int kWin = 512;         // candidates per shared-memory window of the list build
 constexpr int kRelMax = 48;       // relevant-list capacity per carbon atom
 constexpr int kShortMax = 8;      // close-list capacity per carbon atom (a multiple of 4)
+constexpr int kRelPosLimit = 256; // relevant-list entries record list positions below this
+constexpr int kMaxReplicaAtoms = 1 << 24;  // atoms of one replica (relevant entries index 24 bits)
 constexpr int kHeavyCell = 16;    // list build: default home atoms per work item (larger cells split)
 constexpr int kHeavyChunk = 8;    // sizes the item list of the fixed-size scratch (>= kHeavyCell / 2)
 constexpr int kScanCells = 128;   // cells per block of the single-pass cell scan and ordering (or 2x)
@@ -71,6 +73,7 @@ struct RepConst {
   int atomOff, nMol, nMolMe, cellOff;
   int nRedBlocks;  // ceil(nMol / 1024)
   int scanCells;   // cells per block of the scan and ordering (kScanCells or 2 kScanCells)
+  int uncapped;    // MIXED: a cell above the bucket capacity is ordered by compaction, not flagged
   int nRedBlocksM, redFirstM;  // MIXED reduction: blocks of kMixAtoms atoms, first partial slot
   // integrator
   float deltaT, rrNebr, rNebrShell, rrShort;
@@ -127,8 +130,17 @@ struct RepState {
   unsigned shearCounter;
   int flags;                        // sticky error bits (SG_ERR_* as 1 << code)
   int maxNeighbours, maxCellOcc, nebrOverflow, cellRange, cellOverflow, rdfRange, shortStale;
-  int pad[4];
+  int timeouts;                     // bounded device-side waits that gave up (persistent step)
+  int pad[3];
 };
+
+// Relevant-list entry of a carbon atom: the neighbour's index relative to its replica's first
+// atom (24 bits) and its position in the full list (8 bits), one 32-bit word, so that the
+// carbon pass reads a typical row of about 7 entries in one 32-byte sector.  An atom whose full
+// list holds more than kRelPosLimit entries has no relevant list (the pass walks the full list).
+__host__ __device__ __forceinline__ unsigned relPack(int kLocal, int pos) {
+  return ((unsigned)kLocal << 8) | ((unsigned)pos & 0xffu);
+}
 
 // Block-to-replica tables: block b of a launch covers [start[b], start[b] + bs) clipped to its
 // replica's range; start is a global index (atoms) or local index (cells, reductions).
@@ -186,9 +198,12 @@ __device__ __forceinline__ int cellIndex(const RepConst &P, float x, float y, fl
 // Minimum image of one component as the force kernels do it (SurfaceGrowth.cu:750-759).
 // Cell of atom g and its arrival slot in the cell; with a bucket (cap slots per cell, the
 // reference's blockSize) the atom is also filed there, and counted in blockCount per block of
-// P.scanCells cells (one atomic per block among the warp's atoms), for k_scan_rank.
+// P.scanCells cells (one atomic per block among the warp's atoms), for k_scan_rank.  An atom
+// past the cap is not filed; uncapped (MIXED) it is counted all the same and, with a spill list,
+// appended there as {global cell, atom} (spillCount: its length), where the scan finds it.
 __device__ __forceinline__ void binAtom(const RepConst &P, int g, const float4 &r, int *cellOf, int *slot,
-                                        int *cellCount, int *bucket, int cap, int *blockCount) {
+                                        int *cellCount, int *bucket, int cap, int *blockCount,
+                                        int2 *spill = nullptr, int *spillCount = nullptr) {
   const int c = cellIndex(P, r.x, r.y, r.z);
   cellOf[g] = c;
   int key = -1;
@@ -197,6 +212,9 @@ __device__ __forceinline__ void binAtom(const RepConst &P, int g, const float4 &
     slot[g] = s;
     if (bucket && s < cap) {
       bucket[(size_t)(P.cellOff + c) * cap + s] = g;
+      if (blockCount) key = (P.cellOff + c) / P.scanCells;
+    } else if (bucket && P.uncapped) {
+      if (spill) spill[atomicAdd(spillCount, 1)] = make_int2(P.cellOff + c, g);
       if (blockCount) key = (P.cellOff + c) / P.scanCells;
     }
   }

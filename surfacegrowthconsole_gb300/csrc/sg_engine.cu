@@ -178,6 +178,8 @@ static void destroyGraphs(sg_ctx *c) {
 static int setMetalLanes(sg_ctx *c, int lanes) {
   const int slot = lanes == 4 ? 0 : lanes == 8 ? 1 : lanes == 16 ? 2 : lanes == 32 ? 3 : -1;
   if (slot < 0) return sg_fail(SG_ERR_INVALID, "metal_lanes %d: 4, 8, 16 or 32", lanes);
+  if (c->persistent && lanes != 4 && lanes != kMT)
+    return sg_fail(SG_ERR_UNSUPPORTED, "metal_lanes %d: the persistent step runs 4 or %d", lanes, kMT);
   DevTab &t = c->metalLaneTab[slot];
   if (!t.rep) {
     const int rc = makeRangeTab(c, t, 128 / lanes, 1);
@@ -238,11 +240,25 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
   c->nrep = n_replicas;
   c->hp.assign(params, params + n_replicas);
   c->nebrMax = params[0].iNebrMax;
+  if (c->opt.nebr_capacity) {
+    if (c->opt.mode != SG_MODE_MIXED || c->opt.nebr_capacity < c->nebrMax) {
+      sg_destroy(c);
+      return sg_fail(SG_ERR_INVALID, "nebr_capacity %d: MIXED mode, at least iNebrMax %d", c->opt.nebr_capacity,
+                     c->nebrMax);
+    }
+    c->nebrMax = c->opt.nebr_capacity;
+  }
   c->rowStride = (c->nebrMax + 3) & ~3;
   c->stepCount = params[0].stepCount;
   c->countRdf = params[0].countRdf;
   c->oneStep.resize(n_replicas);
   for (int r = 0; r < n_replicas; r++) c->oneStep[r] = params[r].oneStep;
+  for (int r = 0; r < n_replicas; r++)
+    if (params[r].nMol >= kMaxReplicaAtoms) {
+      sg_destroy(c);
+      return sg_fail(SG_ERR_UNSUPPORTED, "replica %d: %d atoms, at most %d per replica", r, params[r].nMol,
+                     kMaxReplicaAtoms - 1);
+    }
   // layout of replicas
   int atomOff = 0, cellOff = 0, redOff = 0, cmvOff = 0;
   size_t diffOff = 0;
@@ -272,10 +288,30 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
   // system pressing atoms together) stays in the lists.
   c->bucketCap = 1;
   for (int r = 0; r < n_replicas; r++) c->bucketCap = std::max(c->bucketCap, (int)params[r].blockSize);
-  if (c->opt.mode == SG_MODE_MIXED) c->bucketCap *= kMixedCellCapFactor;
+  if (c->opt.mode == SG_MODE_MIXED) {
+    c->bucketCap *= kMixedCellCapFactor;
+    for (auto &P : c->hrc) P.uncapped = 1;
+  }
   // list build: one warp per home cell, a grid of a few resident blocks per SM walking the cells
   c->numSMs = numSMs;
   c->pdl = c->opt.programmatic_launch != 0;
+  if (c->opt.persistent_step) {
+    if (c->opt.mode != SG_MODE_MIXED) {
+      sg_destroy(c);
+      return sg_fail(SG_ERR_UNSUPPORTED, "persistent_step: MIXED mode only");
+    }
+    if (c->opt.persistent_wait_us < 0) {
+      sg_destroy(c);
+      return sg_fail(SG_ERR_INVALID, "persistent_wait_us %d: 0 (default) or more", c->opt.persistent_wait_us);
+    }
+    // one launch per step: no programmatic dependent launch, the cell-window list build
+    c->persistent = true;
+    c->pdl = false;
+    int khz = 0;
+    cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, c->opt.device);
+    const long long us = c->opt.persistent_wait_us ? c->opt.persistent_wait_us : 1000000;
+    c->persistWaitCycles = us * (long long)std::max(khz, 1000) / 1000;
+  }
   if (c->opt.nebr_blocks_per_sm < 0 || c->opt.nebr_blocks_per_sm > 32) {
     sg_destroy(c);
     return sg_fail(SG_ERR_INVALID, "nebr_blocks_per_sm %d: 0 (default) or 1..32", c->opt.nebr_blocks_per_sm);
@@ -323,7 +359,8 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
   // a cell of n > t atoms (t = home atoms per item >= kMinItemAtoms) gives ceil(n / t) < n / t + 1
   // items: at most N / t + N / (t + 1) in all
   AL(c->heavyItems, (size_t)N / kMinItemAtoms + (size_t)N / (kMinItemAtoms + 1) + 16);
-  AL(c->nebrWork, 3);
+  AL(c->nebrWork, 4);  // next item, light items, heavy items, spill-list length
+  if (c->opt.mode == SG_MODE_MIXED) AL(c->spill, std::max<size_t>(N, 1));
   AL(c->bucket, (size_t)c->ctot * c->bucketCap);
   AL(c->rho, N); AL(c->dF, N); AL(c->Fv, N); AL(c->fric, N);
   AL(c->partial, (size_t)std::max(redOff, 1) * kNumRed);
@@ -361,6 +398,23 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
     sg_destroy(c);
     return rc;
   }
+  if (c->persistent) {
+    if (c->nebrAlgo != 0) {
+      sg_destroy(c);
+      return sg_fail(SG_ERR_UNSUPPORTED, "persistent_step: the cell-window list build (nebr_build 0) only");
+    }
+    const int bps = sg_mixed_persistent_blocks_per_sm(c->metalLanes);
+    if (bps < 1) {
+      sg_destroy(c);
+      return sg_fail(SG_ERR_UNSUPPORTED, "persistent_step: the step kernel cannot be resident");
+    }
+    c->persistGrid = bps * numSMs;
+    if ((rc = devAllocT(c, &c->persistBar, 2))) {
+      sg_destroy(c);
+      return rc;
+    }
+    CK(cudaMemsetAsync(c->persistBar, 0, 2 * sizeof(unsigned), c->stream));
+  }
   if (c->histExt) {
     // RDF extension: every pair (A, B >= A) of 64-atom metal tiles of each replica
     std::vector<int4> pairs;
@@ -394,7 +448,7 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
     c->ntiles = (int)tr.size();
     // cells per scan block: 2 kScanCells when that still gives two blocks per SM (large and
     // batched systems: fewer, fuller blocks), else kScanCells
-    c->scanCells = ((long long)c->ntiles * (kCellTile / (2 * kScanCells)) >= 2LL * std::max(numSMs, 1))
+    c->scanCells = (!c->persistent && (long long)c->ntiles * (kCellTile / (2 * kScanCells)) >= 2LL * std::max(numSMs, 1))
                        ? 2 * kScanCells : kScanCells;
     for (auto &P : c->hrc) P.scanCells = c->scanCells;
     c->nScanBlocks = c->ntiles * (kCellTile / c->scanCells);
@@ -599,7 +653,7 @@ static int enqueueRebuild(sg_ctx *c, int force) {
   const int fr = force;
   CK(launchScanRank(c->pdl, c->scanCells, c->nScanBlocks, c->stream, c->tileTab.rep, c->tileTab.start,
              c->dTileFirst, c->rc, c->st, c->cellCount, c->cellStart, c->bucketCap, fr, c->activeCells,
-             c->heavyItems, c->nebrWork, c->nebrItemAtoms, c->blockCount, c->bucket, c->cellOf, c->pos,
+             c->heavyItems, c->nebrWork, c->nebrItemAtoms, c->blockCount, c->bucket, c->spill, c->cellOf, c->pos,
              c->sortIdx, c->sortPos, c->nn, c->ns, c->nrl));
   if (c->opt.phase_timing) cudaEventRecordWithFlags(c->phaseEv[8], c->stream, cudaEventRecordExternal);
   if (c->nebrAlgo == 1)
@@ -673,6 +727,18 @@ static void phaseMark(sg_ctx *c, int k) {
 static int enqueueStep(sg_ctx *c, int variant) {
   int rc;
   const int fr = c->opt.force_rebuild ? 1 : 0;
+  if (c->persistent) {
+    // the whole step in one cooperative launch, then the optional phases
+    if ((rc = sg_mixed_enqueue_persistent(c, fr))) return rc;
+    if ((variant & V_SHEAR) && c->metalTab.n) {
+      CK(launchK(false, k_shear, c->metalTab.n, 128, 0, c->stream, c->metalTab.view(), c->rc, c->st, c->pos, c->acc));
+      LAUNCH_OK();
+    }
+    if (variant & V_RDF) {
+      if ((rc = enqueueRdf(c, (variant & V_RDF_ZERO) != 0))) return rc;
+    }
+    return SG_OK;
+  }
   phaseMark(c, 0);
   if (c->opt.mode == SG_MODE_MIXED) {
     if ((rc = sg_mixed_enqueue_integrate(c, fr))) return rc;
@@ -750,7 +816,12 @@ static void advanceSchedule(sg_ctx *c, int variant, bool *rdfPrint) {
 }
 
 static int launchStep(sg_ctx *c, int variant) {
-  if (!c->opt.use_graphs) return enqueueStep(c, variant);
+  if (!c->opt.use_graphs || c->persistent) {  // the persistent step is one launch: no graph
+    c->lastVariant = variant;
+    if (c->persistent) c->kernelsPerVariant[variant] = 1 + ((variant & V_SHEAR) ? 1 : 0) +
+                                                       ((variant & V_RDF) ? 1 + (c->histExt ? 1 : 0) : 0);
+    return enqueueStep(c, variant);
+  }
   auto it = c->graphs.find(variant);
   if (it == c->graphs.end()) {
     cudaGraph_t g;
@@ -779,6 +850,9 @@ static int checkFlags(sg_ctx *c) {
   int flags = 0;
   for (auto &s : hs) flags |= s.flags;
   if (!flags) return SG_OK;
+  // a persistent step that gave up at a grid barrier left its counter mid-count
+  if ((flags & (1 << SG_ERR_TIMEOUT)) && c->persistBar)
+    CK(cudaMemsetAsync(c->persistBar, 0, 2 * sizeof(unsigned), c->stream));
   // report once, then clear
   for (int r = 0; r < c->nrep; r++) hs[r].flags = 0;
   int zero = 0;
@@ -1030,12 +1104,17 @@ extern "C" int sg_get_carbon_lists(sg_ctx *c, int rep, int *nsOut, int *slOut, i
   const RepConst &P = c->hrc[rep];
   std::vector<int> ns(P.nMol), nrl(P.nMol);
   std::vector<int> sl((size_t)P.nMol * kShortMax), rl((size_t)P.nMol * kRelMax * 2);
+  std::vector<unsigned> packed((size_t)P.nMol * kRelMax);
   int rc;
   if ((rc = readArr(c, ns.data(), c->ns + P.atomOff, P.nMol)) ||
       (rc = readArr(c, nrl.data(), c->nrl + P.atomOff, P.nMol)) ||
       (rc = readArr(c, sl.data(), c->sl + (size_t)P.atomOff * kShortMax, sl.size())) ||
-      (rc = readArr(c, rl.data(), reinterpret_cast<int *>(c->rl) + (size_t)P.atomOff * kRelMax * 2, rl.size())))
+      (rc = readArr(c, packed.data(), c->rl + (size_t)P.atomOff * kRelMax, packed.size())))
     return rc;
+  for (size_t q = 0; q < packed.size(); q++) {  // {atom, position in the full list} pairs
+    rl[2 * q] = (int)(packed[q] >> 8);
+    rl[2 * q + 1] = (int)(packed[q] & 0xffu);
+  }
   for (int i = 0; i < P.nMol; i++) {
     for (int e = 0; e < kShortMax; e++) {
       int &x = sl[(size_t)i * kShortMax + e];
@@ -1043,8 +1122,7 @@ extern "C" int sg_get_carbon_lists(sg_ctx *c, int rep, int *nsOut, int *slOut, i
     }
     for (int e = 0; e < kRelMax; e++) {
       int *x = &rl[((size_t)i * kRelMax + e) * 2];
-      if (e < nrl[i]) x[0] -= P.atomOff;
-      else x[0] = x[1] = -1;
+      if (e >= nrl[i]) x[0] = x[1] = -1;  // entries hold local indices already
     }
   }
   if (nsOut) memcpy(nsOut, ns.data(), sizeof(int) * P.nMol);
@@ -1064,7 +1142,7 @@ extern "C" int sg_get_nebr(sg_ctx *c, int rep, int *nnOut, int *nblOut) {
   if (nblOut) {
     std::vector<int> rows((size_t)P.nMol * c->rowStride);
     if ((rc = readArr(c, rows.data(), c->nbl + (size_t)P.atomOff * c->rowStride, rows.size()))) return rc;
-    for (int j = 0; j < c->nebrMax; j++)
+    for (int j = 0; j < c->hp[rep].iNebrMax; j++)  // the reference layout: iNebrMax columns
       for (int i = 0; i < P.nMol; i++)
         nblOut[(size_t)j * P.nMol + i] = (j < nn[i]) ? rows[(size_t)i * c->rowStride + j] - P.atomOff : -1;
   }
@@ -1137,6 +1215,7 @@ extern "C" int sg_get_diag(sg_ctx *c, int rep, sg_diag *d) {
   d->cell_range = S.cellRange;
   d->cell_overflow = S.cellOverflow;
   d->rdf_range = S.rdfRange;
+  d->timeouts = S.timeouts;
   d->reserved[0] = S.shortStale;
   return SG_OK;
 }
@@ -1266,8 +1345,17 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
   int bestLanes = lanes0, bestBps = bps0, bestDesc = desc0, bestItem = item0, bestAlgo = algo0;
   bool bestPdl = pdl0;
   // 1. lanes per metal atom, on the context's own schedule
+  // the persistent step runs 4 or 16 lanes, the cell-window list build on its own grid, no
+  // programmatic launch, the table through L1 and one register budget: those trials are skipped
+  // (their time reads 1e30)
+  const bool P = c->persistent;
+  const float kSkip = 1e30f;
   if (c->metalRun.n > 0) {
     for (int k = 0; k < 4 && !rc; k++) {
+      if (P && laneChoice[k] != 4 && laneChoice[k] != kMT) {
+        laneMs[k] = kSkip;
+        continue;
+      }
       if ((rc = restoreSnapshot(c, snap)) || (rc = setMetalLanes(c, laneChoice[k]))) break;
       rc = timeSteps(c, steps, &laneMs[k]);
     }
@@ -1279,6 +1367,10 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
     c->opt.force_rebuild = 1;
     destroyGraphs(c);
     for (int a = 0; a < 3 && !rc; a++) {
+      if (P && a != 0) {
+        algoMs[a] = kSkip;
+        continue;
+      }
       if ((rc = restoreSnapshot(c, snap))) break;
       c->nebrAlgo = a;
       destroyGraphs(c);
@@ -1297,6 +1389,10 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
       c->nebrItemAtoms = bestItem;
       destroyGraphs(c);
       for (int k = 0; k < 4 && !rc; k++) {
+        if (P) {
+          bpsMs[k] = kSkip;
+          continue;
+        }
         if ((rc = restoreSnapshot(c, snap))) break;
         setNebrBlocks(c, bpsChoice[k]);
         rc = timeSteps(c, steps, &bpsMs[k]);
@@ -1321,6 +1417,10 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
     c->nebrAlgo = bestAlgo;
     setNebrBlocks(c, bestBps);
     for (int k = 0; k < 2 && !rc; k++) {
+      if (P) {
+        pdlMs[k] = kSkip;
+        continue;
+      }
       if ((rc = restoreSnapshot(c, snap))) break;
       c->pdl = k == 1;
       destroyGraphs(c);
@@ -1329,7 +1429,7 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
     if (!rc) bestPdl = pickChoice(pdlMs, offOn, 2, pdl0 ? 1 : 0) == 1;
   }
   // 4. (MIXED) the EAM table through L1 or staged in shared memory
-  if (!rc && c->opt.mode == SG_MODE_MIXED && sg_mixed_staging_ok(c) && c->metalRun.n > 0) {
+  if (!rc && !P && c->opt.mode == SG_MODE_MIXED && sg_mixed_staging_ok(c) && c->metalRun.n > 0) {
     c->pdl = bestPdl;
     for (int k = 0; k < 2 && !rc; k++) {
       if ((rc = restoreSnapshot(c, snap))) break;
@@ -1340,7 +1440,7 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
     if (!rc) bestStaged = pickChoice(stagedMs, offOn, 2, staged0 ? 1 : 0) == 1;
   }
   // 5. the carbon pass's resident blocks per SM, on the context's own schedule
-  if (!rc && c->carbonTabT.n > 0) {
+  if (!rc && !P && c->carbonTabT.n > 0) {
     c->pdl = bestPdl;
     c->eamStaged = bestStaged;
     for (int k = 0; k < 3 && !rc; k++) {
@@ -1416,6 +1516,8 @@ extern "C" int sg_set_launch_shape(sg_ctx *c, const sg_launch_shape *shape) {
     return sg_fail(SG_ERR_UNSUPPORTED, "eam_table_smem: MIXED mode with tabulated EAM only");
   if (shape->carbon_blocks_per_sm != 8 && shape->carbon_blocks_per_sm != 12 && shape->carbon_blocks_per_sm != 16)
     return sg_fail(SG_ERR_INVALID, "carbon_blocks_per_sm %d: 8, 12 or 16", shape->carbon_blocks_per_sm);
+  if (c->persistent && (shape->nebr_build != 0 || shape->programmatic_launch != 0 || shape->eam_table_smem != 0))
+    return sg_fail(SG_ERR_UNSUPPORTED, "the persistent step: nebr_build 0, no programmatic launch, no staged table");
   CK(cudaStreamSynchronize(c->stream));
   const int rc = setMetalLanes(c, shape->metal_lanes);
   if (rc) return rc;

@@ -38,11 +38,12 @@ struct sg_ctx {
   int *cellOf = nullptr, *slot = nullptr, *cellCount = nullptr, *cellStart = nullptr;
   int *tmpIdx = nullptr, *sortIdx = nullptr, *nn = nullptr, *nbl = nullptr, *ns = nullptr, *sl = nullptr;
   int *nrl = nullptr;
-  int2 *rl = nullptr;
+  unsigned *rl = nullptr;  // relevant lists (relPack entries)
   int nebrGrid = 0;
   int *activeCells = nullptr, *nebrWork = nullptr;
   int *bucket = nullptr, bucketCap = 64;  // atoms of each cell in arrival order, bucketCap slots per cell
   int *blockCount = nullptr;  // filed atoms per block of scanCells cells (zero between rebuilds)
+  int2 *spill = nullptr;      // MIXED: {global cell, atom} of atoms past their cell's bucket
   int scanCells = sg::kScanCells;  // cells per block of the scan and ordering
   int nScanBlocks = 0;
   int2 *heavyItems = nullptr;
@@ -71,6 +72,11 @@ struct sg_ctx {
   bool eamStaged = false;  // MIXED: metal passes with the EAM table staged in shared memory
   bool pdl = false;  // programmatic dependent launch between the kernels of a step
   int carbonBlocks = 8;  // carbon pass: resident blocks per SM of its register budget (8, 12, 16)
+  // persistent step (MIXED): one cooperative launch per step, grid barriers between phases
+  bool persistent = false;
+  int persistGrid = 0;
+  unsigned *persistBar = nullptr;   // {arrived, generation} of the grid barrier
+  long long persistWaitCycles = 0;  // longest barrier wait, SM clock cycles
   std::vector<std::pair<void *, size_t>> regions;  // every device buffer with its size
   int anyMetal = 0, anyCarbon = 0, maxHist = 0;
   // graphs keyed by variant bits
@@ -110,4 +116,6 @@ int sg_mixed_enqueue_forces(sg_ctx *c);
 // registers a buffer the library allocated outside devAlloc (autotuner snapshots)
 void sg_register_region(sg_ctx *c, void *p, size_t bytes);
 int sg_mixed_enqueue_reduce(sg_ctx *c, int forceRebuild);
+int sg_mixed_enqueue_persistent(sg_ctx *c, int forceRebuild);
+int sg_mixed_persistent_blocks_per_sm(int metalLanes);
 bool sg_mixed_staging_ok(sg_ctx *c);

@@ -451,32 +451,32 @@ void SG_KN(launchMetalChain)(bool pdl, int mt, int grid, int stagedGrid, size_t 
 // own-angle term of close carbons q, q + 1, and lane 3 the radial and out-of-plane terms (the
 // lanes 0..2 run one angle each, converged, instead of lane 3 running all three); the four
 // partial sums meet in a shuffle tree.
-__device__ __forceinline__ void relEntry(bool full, const int *row, const int2 *rrow, int e, int &k, int &j) {
+__device__ __forceinline__ void relEntry(bool full, const int *row, const unsigned *rrow, int atomOff, int e,
+                                         int &k, int &j) {
   if (full) { k = row[e]; j = e; }
-  else { const int2 v = rrow[e]; k = v.x; j = v.y; }
+  else { const unsigned v = rrow[e]; k = atomOff + (int)(v >> 8); j = (int)(v & 0xffu); }
 }
 
 // MINB: resident blocks per SM the register budget is cut for (8: 64 registers, 12: 40, 16:
 // 32); more warps hide more of the gathers' latency at large sizes, fewer registers cost
 // instructions (launchCarbon picks one, the autotuner times them).
-template <int MINB>
-__global__ void __launch_bounds__(128, MINB) SG_KN(k_force_carbon)(BlockTab tab, const RepConst *__restrict__ rc,
-                                                      float4 *__restrict__ pos, float4 *__restrict__ acc,
-                                                      const int *__restrict__ nn, const int *__restrict__ nbl,
-                                                      const int *__restrict__ ns, const int *__restrict__ sl,
-                                                      const int *__restrict__ nrl, const int2 *__restrict__ rl,
-                                                      int rowStride) {
-  pdlEnter();
+// Block-table entry e of the carbon pass (128 / kCT carbon atoms), by a 128-thread block.
+__device__ __forceinline__ void SG_KN(carbonBody)(int e, BlockTab tab, const RepConst *__restrict__ rc,
+                                                  float4 *__restrict__ pos, float4 *__restrict__ acc,
+                                                  const int *__restrict__ nn, const int *__restrict__ nbl,
+                                                  const int *__restrict__ ns, const int *__restrict__ sl,
+                                                  const int *__restrict__ nrl, const unsigned *__restrict__ rl,
+                                                  int rowStride) {
   __shared__ float sD[128 / kCT][3][4];  // dx, dy, dz, |d| of close carbon q
   __shared__ float sZ[128 / kCT][3];     // its z - z_0
   __shared__ int sK[128 / kCT][3];       // its index
-  const int rep = tab.rep[blockIdx.x];
+  const int rep = tab.rep[e];
   const RepConst &P = rc[rep];
   const int sub = threadIdx.x & (kCT - 1);
   const int a = threadIdx.x / kCT;  // atom slot in the block
   const int glane = threadIdx.x & 31 & ~(kCT - 1);
   const unsigned gmask = ((1u << kCT) - 1) << glane;
-  const int i = tab.start[blockIdx.x] + a;
+  const int i = tab.start[e] + a;
   const int metalEnd = P.atomOff + P.nMolMe;
   const bool valid = i < P.atomOff + P.nMol;
   float fx = 0.f, fy = 0.f, fz = 0.f, u = 0.f;
@@ -486,7 +486,7 @@ __global__ void __launch_bounds__(128, MINB) SG_KN(k_force_carbon)(BlockTab tab,
   const bool full = nr < 0;
   const int nEnt = full ? nn[i] : nr;
   const int *row = nbl + (size_t)i * rowStride;
-  const int2 *rrow = rl + (size_t)i * kRelMax;
+  const unsigned *rrow = rl + (size_t)i * kRelMax;
   for (int base = 0; base < nEnt; base += kCT) {
     const int e = base + sub;
     bool closeC = false;
@@ -494,7 +494,7 @@ __global__ void __launch_bounds__(128, MINB) SG_KN(k_force_carbon)(BlockTab tab,
     float dx = 0.f, dy = 0.f, dz = 0.f, rr = 0.f, bz = 0.f;
     int k = -1, j = -1;
     if (e < nEnt) {
-      relEntry(full, row, rrow, e, k, j);
+      relEntry(full, row, rrow, P.atomOff, e, k, j);
       const float4 B = pos[k];
       bz = B.z;
       dx = minImg(A.x - B.x, P.region[0]);
@@ -537,7 +537,7 @@ __global__ void __launch_bounds__(128, MINB) SG_KN(k_force_carbon)(BlockTab tab,
   if (counti == 3 && p2 >= 4) {
     for (int e = sub; e < nEnt; e += kCT) {
       int k, j;
-      relEntry(full, row, rrow, e, k, j);
+      relEntry(full, row, rrow, P.atomOff, e, k, j);
       if (j > p2) break;
       if (j < 4 || k >= metalEnd) continue;
       const float4 B = pos[k];
@@ -686,10 +686,21 @@ __global__ void __launch_bounds__(128, MINB) SG_KN(k_force_carbon)(BlockTab tab,
   }
 }
 
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) SG_KN(k_force_carbon)(BlockTab tab, const RepConst *__restrict__ rc,
+                                                      float4 *__restrict__ pos, float4 *__restrict__ acc,
+                                                      const int *__restrict__ nn, const int *__restrict__ nbl,
+                                                      const int *__restrict__ ns, const int *__restrict__ sl,
+                                                      const int *__restrict__ nrl, const unsigned *__restrict__ rl,
+                                                      int rowStride) {
+  pdlEnter();
+  SG_KN(carbonBody)(blockIdx.x, tab, rc, pos, acc, nn, nbl, ns, sl, nrl, rl, rowStride);
+}
+
 // The carbon pass with minBlocks (8, 12 or 16; others: 8) resident blocks per SM.
 cudaError_t SG_KN(launchCarbon)(bool pdl, int minBlocks, int grid, cudaStream_t s, BlockTab tab,
                                 const RepConst *rc, float4 *pos, float4 *acc, const int *nn, const int *nbl,
-                                const int *ns, const int *sl, const int *nrl, const int2 *rl, int rowStride) {
+                                const int *ns, const int *sl, const int *nrl, const unsigned *rl, int rowStride) {
   switch (minBlocks) {
     case 12:
       return launchK(pdl, SG_KN(k_force_carbon)<12>, grid, 128, 0, s, tab, rc, pos, acc, nn, nbl, ns, sl, nrl, rl,

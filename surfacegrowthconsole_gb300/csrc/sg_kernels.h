@@ -15,14 +15,14 @@ __global__ void k_cell_bucket(BlockTab tab, const RepConst *rc, const float4 *po
                               int *cellCount, int *bucket, int cap, int *blockCount);
 __global__ void k_build_nebr_atoms(BlockTab tab, const RepConst *rc, RepState *st, const int *cellOf,
                                    const int *cellStart, const float4 *sortPos, int *nn, int *nbl, int *ns,
-                                   int *sl, int *nrl, int2 *rl, int rowStride, int nebrMax, int *work,
+                                   int *sl, int *nrl, unsigned *rl, int rowStride, int nebrMax, int *work,
                                    int forceRebuild, int *blockCount, int nBlockCount);
 // the cell scan and in-cell ordering: one block of kScanRankThreads threads per `cells` cells
 cudaError_t launchScanRank(bool pdl, int cells, int grid, cudaStream_t s, const int *tileRep, const int *tileStart,
                            const int *tileFirst, const RepConst *rc, RepState *st, int *cellCount, int *cellStart,
                            int cap, int forceRebuild, int *active, int2 *heavy, int *work, int itemAtoms,
-                           const int *blockCount, const int *bucket, const int *cellOf, const float4 *pos,
-                           int *sortIdx, float4 *sortPos, int *nn, int *ns, int *nrl);
+                           const int *blockCount, const int *bucket, const int2 *spill, const int *cellOf,
+                           const float4 *pos, int *sortIdx, float4 *sortPos, int *nn, int *ns, int *nrl);
 __global__ void k_scan_tiles(BlockTab tab, const RepConst *rc, const RepState *st,
                              const int *cellCount, int *tileSum, int forceRebuild);
 __global__ void k_scan_tile_prefix(const RepConst *rc, const RepState *st, const int *tileFirst,
@@ -40,11 +40,11 @@ __global__ void k_rank(BlockTab tab, const RepConst *rc, const RepState *st, con
 // of the home-chunk list `heavy` (all reset before the scan of every rebuild).
 __global__ void k_build_nebr(const int *tileRep, const int *active, const int2 *heavy, int *work, const RepConst *rc, RepState *st,
                              const int *cellStart, const float4 *sortPos, int *nn, int *nbl, int *ns, int *sl,
-                             int *nrl, int2 *rl, int rowStride, int nebrMax, int descending, int *blockCount,
+                             int *nrl, unsigned *rl, int rowStride, int nebrMax, int descending, int *blockCount,
                              int nBlockCount);
 __global__ void k_build_nebr_lanes(const int *tileRep, const int *active, const int2 *heavy, int *work, const RepConst *rc, RepState *st,
                              const int *cellStart, const float4 *sortPos, int *nn, int *nbl, int *ns, int *sl,
-                             int *nrl, int2 *rl, int rowStride, int nebrMax, int descending, int *blockCount,
+                             int *nrl, unsigned *rl, int rowStride, int nebrMax, int descending, int *blockCount,
                              int nBlockCount);
 
 // ---- PLAIN force and step kernels ----
@@ -61,7 +61,7 @@ void launchMetalChain(bool pdl, int mt, int grid, int stagedGrid, size_t stagedS
 // the carbon pass with minBlocks (8, 12, 16) resident 128-thread blocks per SM
 cudaError_t launchCarbon(bool pdl, int minBlocks, int grid, cudaStream_t s, BlockTab tab, const RepConst *rc,
                          float4 *pos, float4 *acc, const int *nn, const int *nbl, const int *ns, const int *sl,
-                         const int *nrl, const int2 *rl, int rowStride);
+                         const int *nrl, const unsigned *rl, int rowStride);
 __global__ void k_cmvel(BlockTab tab, const RepConst *rc, RepState *st, const float4 *vel,
                         const float4 *acc, float *partial, const int *redFirst);
 __global__ void k_step_reduce(BlockTab tab, const RepConst *rc, RepState *st, const float4 *pos,

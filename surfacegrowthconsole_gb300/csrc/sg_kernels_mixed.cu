@@ -33,6 +33,7 @@
 #define SG_EAM_TABLE
 #define SG_FAST_RECIP
 #include "sg_forces.cuh"
+#include "sg_lists.cuh"
 
 namespace sg {
 
@@ -93,17 +94,18 @@ __device__ __forceinline__ void addHiLo(float &hi, float &lo, float d) {
 // Integrator part 1 with hi/lo positions (same schedule as k_integrate_first: pending
 // thermostat, deposition, kick + drift, wrap, freeze mask, cell histogram on rebuild steps).
 // ============================================================================================
-__global__ void k_integrate_mixed(BlockTab tab, const RepConst *__restrict__ rc, RepState *st,
-                                  float4 *__restrict__ pos, float4 *__restrict__ posLo,
-                                  float4 *__restrict__ vel, const float4 *__restrict__ acc,
-                                  int *__restrict__ cellOf, int *__restrict__ slot,
-                                  int *__restrict__ cellCount, int forceRebuild, int *__restrict__ bucket,
-                                  int cap, int *__restrict__ blockCount) {
-  pdlEnter();
-  const int rep = tab.rep[blockIdx.x];
+// Block-table entry e (128 atoms), by a 128-thread block.
+__device__ __forceinline__ void integrateMixedBody(int e, BlockTab tab, const RepConst *__restrict__ rc, RepState *st,
+                                                   float4 *__restrict__ pos, float4 *__restrict__ posLo,
+                                                   float4 *__restrict__ vel, const float4 *__restrict__ acc,
+                                                   int *__restrict__ cellOf, int *__restrict__ slot,
+                                                   int *__restrict__ cellCount, int forceRebuild,
+                                                   int *__restrict__ bucket, int cap, int *__restrict__ blockCount,
+                                                   int2 *__restrict__ spill, int *__restrict__ spillCount) {
+  const int rep = tab.rep[e];
   const RepConst &P = rc[rep];
   RepState *S = st + rep;
-  const int g = tab.start[blockIdx.x] + threadIdx.x;
+  const int g = tab.start[e] + threadIdx.x;
   if (g >= P.atomOff + P.nMol) return;
   const int local = g - P.atomOff;
   const int sc = S->stepCount + 1;
@@ -155,7 +157,19 @@ __global__ void k_integrate_mixed(BlockTab tab, const RepConst *__restrict__ rc,
   pos[g] = r;
   posLo[g] = lo;
   vel[g] = v;
-  if (forceRebuild || S->nebrNow) binAtom(P, g, r, cellOf, slot, cellCount, bucket, cap, blockCount);
+  if (forceRebuild || S->nebrNow) binAtom(P, g, r, cellOf, slot, cellCount, bucket, cap, blockCount, spill, spillCount);
+}
+
+__global__ void k_integrate_mixed(BlockTab tab, const RepConst *__restrict__ rc, RepState *st,
+                                  float4 *__restrict__ pos, float4 *__restrict__ posLo,
+                                  float4 *__restrict__ vel, const float4 *__restrict__ acc,
+                                  int *__restrict__ cellOf, int *__restrict__ slot,
+                                  int *__restrict__ cellCount, int forceRebuild, int *__restrict__ bucket,
+                                  int cap, int *__restrict__ blockCount, int2 *__restrict__ spill,
+                                  int *__restrict__ spillCount) {
+  pdlEnter();
+  integrateMixedBody(blockIdx.x, tab, rc, st, pos, posLo, vel, acc, cellOf, slot, cellCount, forceRebuild, bucket, cap,
+                     blockCount, spill, spillCount);
 }
 
 // ============================================================================================
@@ -189,20 +203,22 @@ __device__ void stepControlMixed(const RepConst &P, RepState *S, const double (&
                                  const float (&M)[kMixMax], double *diff, float *diffF,
                                  int forceRebuild);
 
-// APT atoms per thread: APT * kMixThreads atoms per block (the engine picks 1, 2, 4 or 8 by size).
-template <int APT>
-__global__ void __launch_bounds__(kMixThreads) k_step_reduce_mixed(
-    BlockTab tab, const RepConst *__restrict__ rc, RepState *st, const float4 *__restrict__ pos,
+// Reduction block e of the step (APT * THREADS atoms), by a block of THREADS threads: the
+// engine's kernel runs THREADS = THREADS with APT atoms per thread (1, 2, 4 or 8, picked by
+// size); the persistent step runs its own block size with the same atoms per block (APT 0: the
+// atoms per thread `apt` at run time).
+template <int APT, int THREADS>
+__device__ __forceinline__ void reduceMixedBody(
+    int e, int apt, BlockTab tab, const RepConst *__restrict__ rc, RepState *st, const float4 *__restrict__ pos,
     const float4 *__restrict__ posLo, float4 *__restrict__ vel, const float4 *__restrict__ acc4,
     const float *__restrict__ fric, float2 *__restrict__ partDF, float *__restrict__ partF,
     const int *__restrict__ redFirst, unsigned *counter, double *__restrict__ diff64,
     const size_t *__restrict__ diffOff64, float *__restrict__ diffF, const size_t *__restrict__ diffOffF,
     int forceRebuild) {
-  pdlEnter();
-  const int rep = tab.rep[blockIdx.x];
+  const int rep = tab.rep[e];
   const RepConst &P = rc[rep];
   RepState *S = st + rep;
-  const int b = tab.start[blockIdx.x];
+  const int b = tab.start[e];
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   const float h = 0.5f * P.deltaT;
   // per thread and per warp (64 atoms) in FP32, except the centre of mass (double-float over
@@ -212,9 +228,10 @@ __global__ void __launch_bounds__(kMixThreads) k_step_reduce_mixed(
   for (int k = 0; k < kMixAcc; k++) acc[k] = 0.f;
   DF cm[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
   float mm[kMixMax] = {0.f, 3.4e38f, 3.4e38f, 3.4e38f, -3.4e38f, -3.4e38f, -3.4e38f};
+  const int atomsPerThread = APT > 0 ? APT : apt;
 #pragma unroll
-  for (int half = 0; half < APT; half++) {
-    const int local = APT * kMixThreads * b + half * kMixThreads + t;
+  for (int half = 0; half < (APT > 0 ? APT : apt); half++) {
+    const int local = atomsPerThread * THREADS * b + half * THREADS + t;
     if (local >= P.nMol) continue;
     const int g = P.atomOff + local;
     const float4 r = pos[g];
@@ -251,8 +268,8 @@ __global__ void __launch_bounds__(kMixThreads) k_step_reduce_mixed(
       acc[MA_VV_C] += vv;
     }
   }
-  __shared__ DF shDF[kMixThreads / 32][kMixAcc];
-  __shared__ float shF[kMixThreads / 32][kMixMax];
+  __shared__ DF shDF[THREADS / 32][kMixAcc];
+  __shared__ float shF[THREADS / 32][kMixMax];
 #pragma unroll
   for (int k = 0; k < kMixAcc; k++) {
     if (k >= MA_CM_X && k <= MA_CM_Z) continue;
@@ -279,12 +296,12 @@ __global__ void __launch_bounds__(kMixThreads) k_step_reduce_mixed(
   const int pb = P.redFirstM + b;
   if (t < kMixAcc) {
     DF x{0.f, 0.f};
-    for (int k = 0; k < kMixThreads / 32; k++) x = dfAdd(x, shDF[k][t]);
+    for (int k = 0; k < THREADS / 32; k++) x = dfAdd(x, shDF[k][t]);
     partDF[(size_t)pb * kMixAcc + t] = make_float2(x.hi, x.lo);
   } else if (t >= 32 && t < 32 + kMixMax) {
     const int k = t - 32;
     float x = shF[0][k];
-    for (int j = 1; j < kMixThreads / 32; j++)
+    for (int j = 1; j < THREADS / 32; j++)
       x = (k == MM_VVMAX || k >= MM_MAX_X) ? fmaxf(x, shF[j][k]) : fminf(x, shF[j][k]);
     partF[(size_t)pb * kMixMax + k] = x;
   }
@@ -298,13 +315,13 @@ __global__ void __launch_bounds__(kMixThreads) k_step_reduce_mixed(
   // block partials in a fixed order (whichever block finished last), as double-floats on the
   // FP32 pipes (FP64 runs at a small fraction of their rate on this GPU; a double-float sum of
   // a few hundred partials keeps ~1e-14 relative, far below the FP32 warp sums' own rounding).
-  // Sums: thread t adds value t % 16 of rows t / 16 + kG * i (kG = kMixThreads / 16 row groups,
+  // Sums: thread t adds value t % 16 of rows t / 16 + kG * i (kG = THREADS / 16 row groups,
   // four rows of predicated loads in flight, two chains), then the row groups of a warp meet in
   // a shuffle and the warps in one step.  Extremes: value t % 8 of rows t / 8 + kG2 * i.
-  static_assert(kMixThreads % 32 == 0 && kMixAcc <= 16 && kMixMax <= 8, "final sums: 16 and 8 values per row");
-  constexpr int kG = kMixThreads / 16, kG2 = kMixThreads / 8;
-  __shared__ DF sW[kMixThreads / 32][16];
-  __shared__ float sWF[kMixThreads / 32][8];
+  static_assert(THREADS % 32 == 0 && THREADS >= 64 && kMixAcc <= 16 && kMixMax <= 8, "final sums: 16 and 8 values per row");
+  constexpr int kG = THREADS / 16, kG2 = THREADS / 8;
+  __shared__ DF sW[THREADS / 32][16];
+  __shared__ float sWF[THREADS / 32][8];
   __shared__ double tot[kMixAcc];
   __shared__ float totF[kMixMax];
   const int p0 = P.redFirstM, nb = P.nRedBlocksM;
@@ -358,14 +375,14 @@ __global__ void __launch_bounds__(kMixThreads) k_step_reduce_mixed(
   if (t < kMixAcc) {
     DF x = sW[0][t];
 #pragma unroll
-    for (int q = 1; q < kMixThreads / 32; q++) x = dfAdd(x, sW[q][t]);
+    for (int q = 1; q < THREADS / 32; q++) x = dfAdd(x, sW[q][t]);
     tot[t] = (double)x.hi + (double)x.lo;
   } else if (t >= 32 && t < 32 + kMixMax) {
     const int k = t - 32;
     const bool isMax = (k == MM_VVMAX || k >= MM_MAX_X);
     float y = sWF[0][k];
 #pragma unroll
-    for (int q = 1; q < kMixThreads / 32; q++) y = isMax ? fmaxf(y, sWF[q][k]) : fminf(y, sWF[q][k]);
+    for (int q = 1; q < THREADS / 32; q++) y = isMax ? fmaxf(y, sWF[q][k]) : fminf(y, sWF[q][k]);
     totF[k] = y;
   }
   __syncthreads();
@@ -383,6 +400,19 @@ __global__ void __launch_bounds__(kMixThreads) k_step_reduce_mixed(
   stepControlMixed(sP, &sS, A, M, diff64 ? diff64 + diffOff64[rep] : nullptr,
                    diffF ? diffF + diffOffF[rep] : nullptr, forceRebuild);
   stateFromShared(&sS, S);
+}
+
+template <int APT>
+__global__ void __launch_bounds__(kMixThreads) k_step_reduce_mixed(
+    BlockTab tab, const RepConst *__restrict__ rc, RepState *st, const float4 *__restrict__ pos,
+    const float4 *__restrict__ posLo, float4 *__restrict__ vel, const float4 *__restrict__ acc4,
+    const float *__restrict__ fric, float2 *__restrict__ partDF, float *__restrict__ partF,
+    const int *__restrict__ redFirst, unsigned *counter, double *__restrict__ diff64,
+    const size_t *__restrict__ diffOff64, float *__restrict__ diffF, const size_t *__restrict__ diffOffF,
+    int forceRebuild) {
+  pdlEnter();
+  reduceMixedBody<APT, kMixThreads>(blockIdx.x, APT, tab, rc, st, pos, posLo, vel, acc4, fric, partDF, partF, redFirst,
+                                    counter, diff64, diffOff64, diffF, diffOffF, forceRebuild);
 }
 
 // Step control in FP64 (same schedule as the PLAIN stepControl: properties, thermostat
@@ -560,6 +590,131 @@ __device__ void stepControlMixed(const RepConst &P, RepState *S, const double (&
   }
 }
 
+// ============================================================================================
+// The persistent step: one cooperative launch runs a whole MIXED step over all replicas, its
+// phases separated by a grid-wide barrier instead of kernel boundaries (the step loop of
+// DoComputationsW, SurfaceGrowth.cu:2141-2489, as one launch).  Every block of the grid is
+// resident (cooperative launch); each phase walks its block table with a grid stride, running
+// the same device functions as the separate kernels:
+//   integrate + cell histogram | scan + in-cell order | list build (its work queue spans the
+//   grid) | EAM density and carbon forces | metal forces | reduction + step control.
+// The barrier waits at most waitCycles clock cycles; a block that gives up sets SG_ERR_TIMEOUT
+// in every replica's flags, counts it in the replica's timeouts and leaves the kernel, so the
+// blocks still waiting give up at the same barrier in turn and the launch ends.  The context is
+// then not usable (its state is partly stepped): destroy it.
+// ============================================================================================
+struct PersistArgs {
+  BlockTab atomTab, metalTab, carbonTab, redTab;
+  const int *tileRep, *tileStart, *tileFirst;
+  int nScanBlocks;
+  const RepConst *rc;
+  RepState *st;
+  float4 *pos, *posLo, *vel, *acc;
+  int *cellOf, *slot, *cellCount, *cellStart, *bucket;
+  int cap;
+  int *blockCount, *active;
+  int2 *heavy, *spill;
+  int *work;
+  int itemAtoms;
+  int *sortIdx;
+  float4 *sortPos;
+  int *nn, *nbl, *ns, *sl, *nrl;
+  unsigned *rl;
+  int rowStride, nebrMax, descending;
+  float *rho, *dF, *Fv, *fric;
+  const float4 *eamTab;
+  float2 *partDF;
+  float *partF;
+  const int *redFirst;
+  unsigned *counter;
+  double *diff64;
+  const size_t *diffOff64;
+  float *diffF;
+  const size_t *diffOffF;
+  int apt, forceRebuild, nrep;
+  unsigned *bar;  // {arrived, generation}
+  long long waitCycles;
+};
+
+// Grid-wide barrier with a bounded wait.  Thread 0 of each block reads the generation, makes
+// the block's writes visible (fence) and arrives; the last block to arrive resets the count
+// and advances the generation, the others wait until it changes or the limit runs out.
+__device__ __noinline__ bool gridBarrier(const PersistArgs &a) {
+  __syncthreads();
+  __shared__ int sOk;
+  if (threadIdx.x == 0) {
+    volatile unsigned *gen = a.bar + 1;
+    const unsigned g0 = *gen;
+    __threadfence();
+    bool ok = true;
+    if (atomicAdd(a.bar, 1u) == gridDim.x - 1) {
+      atomicExch(a.bar, 0u);
+      __threadfence();
+      atomicAdd(a.bar + 1, 1u);
+    } else {
+      const long long t0 = clock64();
+      while (*gen == g0) {
+        if (clock64() - t0 > a.waitCycles) {
+          ok = false;
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+    if (!ok)
+      for (int r = 0; r < a.nrep; r++) {
+        setFlag(a.st + r, 8 /*SG_ERR_TIMEOUT*/);
+        atomicAdd(&a.st[r].timeouts, 1);
+      }
+    sOk = ok;
+  }
+  __syncthreads();
+  return sOk != 0;
+}
+
+template <int MT>
+__global__ void __launch_bounds__(128) k_step_persistent(PersistArgs a) {
+  const int G = gridDim.x;
+  for (int e = blockIdx.x; e < a.atomTab.nblocks; e += G)
+    integrateMixedBody(e, a.atomTab, a.rc, a.st, a.pos, a.posLo, a.vel, a.acc, a.cellOf, a.slot, a.cellCount,
+                       a.forceRebuild, a.bucket, a.cap, a.blockCount, a.spill, a.work + 3);
+  if (!gridBarrier(a)) return;
+  for (int e = blockIdx.x; e < a.nScanBlocks; e += G) {
+    scanRankBody<kScanCells, 128>(e, a.tileRep, a.tileStart, a.tileFirst, a.rc, a.st, a.cellCount, a.cellStart, a.cap,
+                                  a.forceRebuild, a.active, a.heavy, a.work, a.itemAtoms, a.blockCount, a.bucket,
+                                  a.cellOf, a.pos, a.sortIdx, a.sortPos, a.nn, a.ns, a.nrl, a.spill);
+    __syncthreads();
+  }
+  if (!gridBarrier(a)) return;
+  clearBlockCount(a.blockCount, a.nScanBlocks);
+  nebrBody<false>(a.tileRep, a.active, a.heavy, a.work, a.rc, a.st, a.cellStart, a.sortPos, a.nn, a.nbl, a.ns, a.sl,
+                  a.nrl, a.rl, a.rowStride, a.nebrMax, a.descending);
+  if (!gridBarrier(a)) return;
+  const int nm = a.metalTab.nblocks, nc = a.carbonTab.nblocks;
+  for (int e = blockIdx.x; e < nm + nc; e += G) {
+    if (e < nm) {
+      const RepConst &P = a.rc[a.metalTab.rep[e]];
+      rhoBody_mixed<MT>(e, P, a.metalTab, a.pos, a.nn, a.nbl, a.rho, a.dF, a.Fv, a.rowStride, a.eamTab + 2 * P.tabOff);
+    } else {
+      carbonBody_mixed(e - nm, a.carbonTab, a.rc, a.pos, a.acc, a.nn, a.nbl, a.ns, a.sl, a.nrl, a.rl, a.rowStride);
+    }
+    __syncthreads();
+  }
+  if (!gridBarrier(a)) return;
+  for (int e = blockIdx.x; e < nm; e += G) {
+    const RepConst &P = a.rc[a.metalTab.rep[e]];
+    forceMetalBody_mixed<MT>(e, P, a.metalTab, a.pos, a.acc, a.nn, a.nbl, a.dF, a.Fv, a.fric, a.rowStride,
+                             a.eamTab + 2 * P.tabOff);
+  }
+  if (!gridBarrier(a)) return;
+  for (int e = blockIdx.x; e < a.redTab.nblocks; e += G) {
+    reduceMixedBody<0, 128>(e, a.apt, a.redTab, a.rc, a.st, a.pos, a.posLo, a.vel, a.acc, a.fric, a.partDF, a.partF,
+                            a.redFirst, a.counter, a.diff64, a.diffOff64, a.diffF, a.diffOffF, a.forceRebuild);
+    __syncthreads();
+  }
+}
+
 }  // namespace sg
 
 using namespace sg;
@@ -715,7 +870,7 @@ int sg_mixed_enqueue_integrate(sg_ctx *c, int forceRebuild) {
   if (!c->atomTab.n) return SG_OK;
   MCK(launchK(c->pdl, k_integrate_mixed, c->atomTab.n, 128, 0, c->stream, c->atomTab.view(), c->rc, c->st, c->pos, c->posLo, c->vel,
                                                          c->acc, c->cellOf, c->slot, c->cellCount, forceRebuild,
-                c->bucket, c->bucketCap, c->blockCount));
+                c->bucket, c->bucketCap, c->blockCount, c->spill, c->nebrWork + 3));
   MCK(cudaGetLastError());
   return SG_OK;
 }
@@ -815,4 +970,60 @@ extern "C" int sg_load_diff_theta(sg_ctx *c, int rep, const double *theta) {
   MCK(cudaMemcpyAsync(c->rc, c->hrc.data(), sizeof(RepConst) * c->nrep, cudaMemcpyHostToDevice, c->stream));
   MCK(cudaStreamSynchronize(c->stream));
   return SG_OK;
+}
+
+// The persistent step (k_step_persistent) of one step on the context's stream: a cooperative
+// launch of c->persistGrid blocks of 128 threads (all resident).
+int sg_mixed_enqueue_persistent(sg_ctx *c, int forceRebuild) {
+  MixedBufs *m = static_cast<MixedBufs *>(c->mixed);
+  PersistArgs a;
+  memset(&a, 0, sizeof(a));
+  a.atomTab = c->atomTab.view();
+  a.metalTab = c->metalRun.view();
+  a.carbonTab = c->carbonTabT.view();
+  a.redTab = BlockTab{m->redRep, m->redStart, m->redN};
+  a.tileRep = c->tileTab.rep;
+  a.tileStart = c->tileTab.start;
+  a.tileFirst = c->dTileFirst;
+  a.nScanBlocks = c->nScanBlocks;
+  a.rc = c->rc;
+  a.st = c->st;
+  a.pos = c->pos; a.posLo = c->posLo; a.vel = c->vel; a.acc = c->acc;
+  a.cellOf = c->cellOf; a.slot = c->slot; a.cellCount = c->cellCount; a.cellStart = c->cellStart;
+  a.bucket = c->bucket; a.cap = c->bucketCap;
+  a.blockCount = c->blockCount; a.active = c->activeCells; a.heavy = c->heavyItems; a.work = c->nebrWork;
+  a.spill = c->spill;
+  a.itemAtoms = c->nebrItemAtoms;
+  a.sortIdx = c->sortIdx; a.sortPos = c->sortPos;
+  a.nn = c->nn; a.nbl = c->nbl; a.ns = c->ns; a.sl = c->sl; a.nrl = c->nrl; a.rl = c->rl;
+  a.rowStride = c->rowStride; a.nebrMax = c->nebrMax; a.descending = c->nebrDescending;
+  a.rho = c->rho; a.dF = c->dF; a.Fv = c->Fv; a.fric = c->fric;
+  a.eamTab = m->eamTab;
+  a.partDF = m->partDF; a.partF = m->partF; a.redFirst = c->dRedFirst; a.counter = m->counter;
+  a.diff64 = m->diff64; a.diffOff64 = m->dDiffOff64; a.diffF = c->diffBuf; a.diffOffF = c->dDiffOff;
+  a.apt = m->mixAtoms / 128;
+  a.forceRebuild = forceRebuild;
+  a.nrep = c->nrep;
+  a.bar = c->persistBar;
+  a.waitCycles = c->persistWaitCycles;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(c->persistGrid);
+  cfg.blockDim = dim3(128);
+  cfg.stream = c->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (c->metalLanes == 4) MCK(cudaLaunchKernelEx(&cfg, k_step_persistent<4>, a));
+  else MCK(cudaLaunchKernelEx(&cfg, k_step_persistent<kMT>, a));
+  return SG_OK;
+}
+
+// Blocks per SM the persistent step can keep resident (its grid is that times the SM count).
+int sg_mixed_persistent_blocks_per_sm(int metalLanes) {
+  int n = 0;
+  cudaError_t e = metalLanes == 4 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step_persistent<4>, 128, 0)
+                                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_step_persistent<kMT>, 128, 0);
+  return e == cudaSuccess ? n : 0;
 }

@@ -71,7 +71,7 @@ constexpr Carve carve() {
   c.fric = o; o += up(N * sizeof(float));
   c.nbl = o; o += up(N * SG_NOALLOC_MAX_NEBR * sizeof(int));
   c.nrl = o; o += up(N * sizeof(int));
-  c.rl = o; o += up(N * kRelMax * sizeof(int2));
+  c.rl = o; o += up(N * kRelMax * sizeof(unsigned));
   c.active = o; o += up(SG_NOALLOC_MAX_CELLS * sizeof(int));
   c.heavy = o; o += up(((size_t)N / kHeavyChunk + (size_t)N / (kHeavyCell + 1) + 16) * sizeof(int2));
   c.work = o; o += up(3 * sizeof(int));
@@ -186,7 +186,7 @@ extern "C" int sg_compute_forces_noalloc(const sg_simparams *p, sg_float4 *d_pos
   float *rho = (float *)(base + K.rho), *dF = (float *)(base + K.dF), *Fv = (float *)(base + K.Fv);
   float *fric = (float *)(base + K.fric);
   int *nbl = (int *)(base + K.nbl), *nrl = (int *)(base + K.nrl);
-  int2 *rl = (int2 *)(base + K.rl);
+  unsigned *rl = (unsigned *)(base + K.rl);
   int *active = (int *)(base + K.active), *work = (int *)(base + K.work);
   int2 *heavy = (int2 *)(base + K.heavy);
   float4 *pos = (float4 *)d_pos, *acc = (float4 *)d_acc;

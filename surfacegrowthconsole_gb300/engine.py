@@ -89,7 +89,8 @@ class Simulation:
                  eam_table_knots: int = 0, stream: int = 0, phase_timing: bool = False, metal_lanes: int = 0,
                  nebr_blocks_per_sm: int = 0, programmatic_launch: bool = True, nebr_descending: int = 0,
                  nebr_item_atoms: int = 0, nebr_build: int = 0, eam_table_smem: int = 0,
-                 carbon_blocks_per_sm: int = 0):
+                 carbon_blocks_per_sm: int = 0, persistent_step: bool = False, persistent_wait_us: int = 0,
+                 nebr_capacity: int = 0):
         plist = [params] if isinstance(params, SimParams) else list(params)
         arr = (SimParams * len(plist))(*plist)
         opt = Options()
@@ -111,6 +112,9 @@ class Simulation:
         opt.nebr_build = nebr_build
         opt.eam_table_smem = eam_table_smem
         opt.carbon_blocks_per_sm = carbon_blocks_per_sm
+        opt.persistent_step = int(persistent_step)
+        opt.persistent_wait_us = persistent_wait_us
+        opt.nebr_capacity = nebr_capacity
         h = C.c_void_p()
         check(lib().sg_create(arr, len(plist), C.byref(opt), C.byref(h)))
         self._h = h

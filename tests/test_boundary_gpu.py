@@ -127,14 +127,15 @@ def test_docomputations_replays_the_reference_programs_call(tmp_path, monkeypatc
     if not ((o[-1, 15] > 0) and (o[:5, 15] == 0).all()):  # the shear force column: off, then on
         bad.append("shear force column")
 
-    # pdb snapshots: identical atom records, coordinates to the printed 0.001 A (a few ulp of
-    # trajectory difference may flip the last printed digit)
+    # pdb snapshots: identical atom records, coordinates to one unit of the last printed digit
+    # (CreatePdbFile prints %-8.2lf angstrom, SurfaceGrowth.cu:2780-2790: a trajectory difference
+    # of a few ulp may flip it)
     for f in sorted(x for x in os.listdir(gdir) if x.endswith(".pdb")):
         hg, xg = OO.pdb_coords(str(gdir / f))
         ho, xo = OO.pdb_coords(str(odir / f))
         if hg != ho:
             bad.append(f"{f}: atom records differ")
-        elif np.abs(xg - xo).max() > 2e-3:
+        elif np.abs(xg - xo).max() > 0.01 + 1e-9:
             bad.append(f"{f}: coordinates differ by {np.abs(xg - xo).max():.3g} A")
 
     # RDF file: the normalised histogram of 100 samples

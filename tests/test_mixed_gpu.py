@@ -129,16 +129,21 @@ def crowded_cell_state(n_blob=90, seed=7):
     return p, r, v
 
 
-def test_mixed_lists_a_cell_above_the_reference_cap():
-    """PLAIN keeps the reference's 64 atoms per cell and reports a fuller cell; MIXED files up to
-    256 and builds the same cells and lists as the (uncapped) oracle."""
-    p, r, v = crowded_cell_state()
+@pytest.mark.parametrize("n_blob", [90, 300], ids=["bucket", "compaction"])
+def test_mixed_lists_a_cell_above_the_reference_cap(n_blob):
+    """PLAIN keeps the reference's 64 atoms per cell and reports a fuller cell; MIXED builds the
+    same cells and lists as the (uncapped) oracle: from its 256-slot buckets (90 atoms), or, for a
+    cell above them (300 atoms), by ordered compaction over the replica's atoms.  The 300-atom
+    cell's atoms have 299 neighbours each, so both sides take 512-entry list rows."""
+    p, r, v = crowded_cell_state(n_blob=n_blob)
+    if n_blob > 100:
+        p.iNebrMax = 512
     a = np.zeros((p.nMol, 3), np.float32)
     orc = oracle.OracleSim(p, 32)
     orc.set_state(r, v, a)
     orc.build_lists()
     _, cs, _ = orc.cells()
-    assert np.diff(cs).max() == 90 > p.blockSize
+    assert np.diff(cs).max() == n_blob > p.blockSize
     plain = Simulation(p, mode=MODE_PLAIN)
     plain.set_state(r, v, a)
     with pytest.raises(Exception) as e:
@@ -154,5 +159,6 @@ def test_mixed_lists_a_cell_above_the_reference_cap():
     nn_o, nbl_o = orc.nebr()
     assert np.array_equal(nn_g, nn_o) and np.array_equal(nbl_g, nbl_o)
     d = mixed.diag()
-    assert d.max_cell_occupancy == 90 and d.cell_overflow == 0
+    assert d.max_cell_occupancy == n_blob and d.nebr_overflow == 0
+    assert d.cell_overflow == (1 if n_blob > 4 * p.blockSize else 0)  # counted, not raised
     mixed.close()
