@@ -291,6 +291,7 @@ template <class R> struct Sim : SimBase {
 
   // ---- cell binning (cu:547-609): counting sort, ascending index within a cell -----------
   int cellIndex(const V4<R> &p) const {
+    if (!std::isfinite((double)p.x) || !std::isfinite((double)p.y) || !std::isfinite((double)p.z)) return -1;
     int cx = (int)((p.x + R(0.5f) * M.region[0]) * M.invWidth[0]);
     int cy = (int)((p.y + R(0.5f) * M.region[1]) * M.invWidth[1]);
     int cz = (int)((p.z + R(0.5f) * M.region[2]) * M.invWidth[2]);

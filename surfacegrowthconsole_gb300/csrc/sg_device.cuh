@@ -188,6 +188,9 @@ __device__ __forceinline__ int stencilCell(const RepConst &P, int c, int o, floa
 // Cell of a position (BinAtomsIntoCellsK, SurfaceGrowth.cu:594-600); -1 when the linear index
 // falls outside the grid (the reference then never bins the atom).
 __device__ __forceinline__ int cellIndex(const RepConst &P, float x, float y, float z) {
+  // a non-finite coordinate (a system that has blown up) is outside the grid, like an atom out of
+  // the box: left out of the lists and counted, not filed into whatever cell the conversion gives
+  if (!isfinite(x) || !isfinite(y) || !isfinite(z)) return -1;
   int cx = (int)((x + 0.5f * P.region[0]) * P.invWidth[0]);
   int cy = (int)((y + 0.5f * P.region[1]) * P.invWidth[1]);
   int cz = (int)((z + 0.5f * P.region[2]) * P.invWidth[2]);

@@ -976,7 +976,8 @@ extern "C" int sg_step_async(sg_ctx *c, int nsteps) {
 extern "C" int sg_build_lists(sg_ctx *c) {
   if (!c) return sg_fail(SG_ERR_INVALID, "null context");
   k_cell_bucket<<<c->atomTab.n, 128, 0, c->stream>>>(c->atomTab.view(), c->rc, c->pos, c->cellOf, c->slot,
-                                                     c->cellCount, c->bucket, c->bucketCap, c->blockCount);
+                                                     c->cellCount, c->bucket, c->bucketCap, c->blockCount,
+                                                     c->spill, c->nebrWork + 3);
   LAUNCH_OK();
   int rc = enqueueRebuild(c, 1);
   if (rc) return rc;

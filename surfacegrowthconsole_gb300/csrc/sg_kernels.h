@@ -12,7 +12,7 @@ __global__ void k_integrate_first(BlockTab tab, const RepConst *rc, RepState *st
 __global__ void k_cell_count(BlockTab tab, const RepConst *rc, const float4 *pos, int *cellOf,
                              int *slot, int *cellCount);
 __global__ void k_cell_bucket(BlockTab tab, const RepConst *rc, const float4 *pos, int *cellOf, int *slot,
-                              int *cellCount, int *bucket, int cap, int *blockCount);
+                              int *cellCount, int *bucket, int cap, int *blockCount, int2 *spill, int *spillCount);
 __global__ void k_build_nebr_atoms(BlockTab tab, const RepConst *rc, RepState *st, const int *cellOf,
                                    const int *cellStart, const float4 *sortPos, int *nn, int *nbl, int *ns,
                                    int *sl, int *nrl, unsigned *rl, int rowStride, int nebrMax, int *work,

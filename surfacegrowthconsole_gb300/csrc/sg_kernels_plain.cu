@@ -122,13 +122,14 @@ __global__ void k_cell_count(BlockTab tab, const RepConst *__restrict__ rc,
 // Histogram and bucket pass alone (lists rebuilt outside a step).
 __global__ void k_cell_bucket(BlockTab tab, const RepConst *__restrict__ rc, const float4 *__restrict__ pos,
                               int *__restrict__ cellOf, int *__restrict__ slot, int *__restrict__ cellCount,
-                              int *__restrict__ bucket, int cap, int *__restrict__ blockCount) {
+                              int *__restrict__ bucket, int cap, int *__restrict__ blockCount,
+                              int2 *__restrict__ spill, int *__restrict__ spillCount) {
   pdlEnter();
   const int rep = tab.rep[blockIdx.x];
   const RepConst &P = rc[rep];
   const int g = tab.start[blockIdx.x] + threadIdx.x;
   if (g >= P.atomOff + P.nMol) return;
-  binAtom(P, g, pos[g], cellOf, slot, cellCount, bucket, cap, blockCount);
+  binAtom(P, g, pos[g], cellOf, slot, cellCount, bucket, cap, blockCount, spill, spillCount);
 }
 
 
