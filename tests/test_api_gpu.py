@@ -136,3 +136,30 @@ def test_published_record_is_the_current_step_over_many_calls(mode):
         assert t1.stepCount == t2.stepCount == i + 1
         _same_thermo(t1, t2)
     sim.close()
+
+
+@pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_MIXED])
+def test_adjacent_state_block_equals_separate_arrays(mode):
+    """r, v, a adjacent in one page-locked block take one copy-engine transfer and an unpack on
+    the device; the state and the trajectory equal those of three separate page-locked arrays."""
+    torch = pytest.importorskip("torch")
+    p, r, v = workloads.small(seed=66)
+    n = p.nMol
+    a = np.random.RandomState(6).normal(size=(n, 3)).astype(np.float32)
+    block = torch.empty(n * 10, dtype=torch.float32, pin_memory=True).numpy()
+    br, bv, ba = block[:4 * n].reshape(n, 4), block[4 * n:7 * n].reshape(n, 3), block[7 * n:].reshape(n, 3)
+    br[:], bv[:], ba[:] = r, v, a
+    one = Simulation(p, mode=mode)
+    two = Simulation(p, mode=mode)
+    one.set_state(br, bv, ba)
+    two.set_state(_pinned(r), _pinned(v), _pinned(a))
+    for x, y in zip(one.get_state(), (r, v, a)):
+        assert np.array_equal(x, y)
+    for _ in range(3):
+        t1 = one.step_from_host(br, bv, ba, nsteps=2)
+        t2 = two.step_from_host(_pinned(r), _pinned(v), _pinned(a), nsteps=2)
+        _same_thermo(t1, t2)
+    for x, y in zip(one.get_state(), two.get_state()):
+        assert np.array_equal(x, y)
+    one.close()
+    two.close()
