@@ -19,10 +19,11 @@ at 1,000 K with the thermostat on, then NVE.  PLAIN (the reference's FP32 arithm
 The lengths are sized for a test run; SG_PRECISION=full selects the configuration's own (1,000
 equilibration steps, 100,000 NVE steps, a 2,000-step FP64 window), and SG_PRECISION_REPORT=<path>
 writes the numbers as JSON.  The reference's graphene model gains energy in NVE (it applies the
-second-neighbour angle forces without their energy), and the heated system crowds cells: PLAIN
-keeps the reference's 64-atom cell cap and stops with SG_ERR_CELL_OVERFLOW where the reference
-would write past its cell array (the steps it reached are reported); MIXED files up to 256 atoms
-per cell and runs the whole NVE leg.
+second-neighbour angle forces without their energy), and its second-neighbour angle quotient
+(the cosine divided by |r_ik| r_km^2, SurfaceGrowth.cu:957) eventually reaches +-1 in the heated
+sheet, where the force diverges: at 1,000 K both forms (and the FP32 and FP64 oracle) run until
+the energy is no longer finite, some 40,000-50,000 steps in.  The NVE test reports how far each
+form ran and the drift over the steps both ran.
 """
 import json
 import os
