@@ -24,7 +24,7 @@ LJ, graphene, reductions, thermostat, RDF/diffusion when due).
   nve_drift : the total-energy drift of both forms on bulk Ni (4,000 atoms, 300 K, 10 ps NVE),
           the "stated drift" the two forms are compared at.
   e2e   : the same metric through the public C ABI with host buffers: every step uploads the
-          state (r, v, a, adjacent in one page-locked block) from pinned host memory, steps, and
+          state (r, v, a) from pinned host memory, steps, and
           reads the step's thermo record, in one sg_step_from_host call (one wait per step).
   roofline : the neighbour-list build (the largest share of the step): its compulsory bytes per
           launch / its mean duration (CUDA events around it on the library's stream), against
@@ -616,11 +616,10 @@ def run_production(args, rank: int, world: int, local: int, dist):
                  **counts}
 
     # end to end through the C ABI with pinned host buffers
-    # r, v, a adjacent in one page-locked block: the library moves it in one copy-engine transfer
-    block = torch.empty(p.nMol * 10, dtype=torch.float32, pin_memory=True).numpy()
-    hr = block[:4 * p.nMol].reshape(p.nMol, 4)
-    hv = block[4 * p.nMol:7 * p.nMol].reshape(p.nMol, 3)
-    ha = block[7 * p.nMol:].reshape(p.nMol, 3)
+    # r, v, a in page-locked host memory: the upload kernel reads them in place
+    hr = torch.empty((p.nMol, 4), dtype=torch.float32, pin_memory=True).numpy()
+    hv = torch.empty((p.nMol, 3), dtype=torch.float32, pin_memory=True).numpy()
+    ha = torch.empty((p.nMol, 3), dtype=torch.float32, pin_memory=True).numpy()
     hr[:], hv[:], ha[:] = sim.get_state()
     e2e_steps = max(1, min(args.e2e_steps, args.steps))
     s0 = sim.thermo().stepCount

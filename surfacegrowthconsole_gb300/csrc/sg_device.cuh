@@ -13,9 +13,10 @@
 //   nn int[Ntot], nbl int[Ntot * rowStride] neighbour list, entry j of atom g at
 //                                           nbl[g * rowStride + j] (rowStride = nebrMax rounded
 //                                           up to a multiple of 4: 16-byte aligned rows)
-//   nrl int[Ntot], rl int2[Ntot * kRelMax]  relevant list of a carbon atom: its metal entries
-//                                           and entries within (rCutC+skin), {index, position
-//                                           in the full list}
+//   nrl int[Ntot], rl u32[Ntot * kRelMax]   relevant list of a carbon atom: its metal entries
+//                                           and entries within (rCutC+skin), each the index in
+//                                           the replica and the position in the full list in
+//                                           one word (relPack)
 //   ns int[Ntot], sl int[Ntot * kShortMax]  close list of a carbon atom: its entries within
 //                                           (rCutC+skin), in list order
 //   rho/dF/Fv float[Ntot]   EAM density, F'(rho), F(rho) (metal atoms)

@@ -371,7 +371,7 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
   if (c->opt.rdf_ext_bins > 0) AL(c->histExt, (size_t)n_replicas * c->opt.rdf_ext_bins);
   AL(c->diffBuf, std::max<size_t>(diffOff, 1));
   AL(c->dDiffOff, n_replicas);
-  AL(c->stage, 10 * N);  // r, v, a in transit at once (4 + 3 + 3 floats an atom)
+  AL(c->stage, 6 * N);  // v and a in transit at once
   if (cudaMallocHost(&c->hostSt, sizeof(RepState) * n_replicas + 64) != cudaSuccess) {
     c->hostSt = nullptr;
     sg_destroy(c);
@@ -597,18 +597,6 @@ static int enqueueSetState(sg_ctx *c, int rep, const sg_float4 *r, const sg_floa
   const float4 *sr = static_cast<const float4 *>(mappedHost(r));
   const float *sv = static_cast<const float *>(mappedHost(v));
   const float *sa = static_cast<const float *>(mappedHost(a));
-  // r, v and a adjacent in one page-locked block (r, then v, then a): one copy-engine transfer of
-  // the whole block into the staging buffer and the unpack from device memory.  The copy engine
-  // moves one contiguous block about twice as fast as the kernel reads three arrays in place
-  // over the host link (12.6 against 24 us for 45,546 atoms on a GB300).
-  const size_t n16 = (size_t)n * 16, n12 = (size_t)n * 12;
-  if (sr && sv && sa && reinterpret_cast<const char *>(v) == reinterpret_cast<const char *>(r) + n16 &&
-      reinterpret_cast<const char *>(a) == reinterpret_cast<const char *>(v) + n12) {
-    CK(cudaMemcpyAsync(c->stage, r, n16 + 2 * n12, cudaMemcpyHostToDevice, c->stream));
-    sr = reinterpret_cast<const float4 *>(c->stage);
-    sv = c->stage + 4 * (size_t)n;
-    sa = sv + 3 * (size_t)n;
-  }
   if (r && !sr) CK(cudaMemcpyAsync(c->pos + off, r, (size_t)n * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
   if (v && !sv) {
     CK(cudaMemcpyAsync(c->stage, v, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, c->stream));

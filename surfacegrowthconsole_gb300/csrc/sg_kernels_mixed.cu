@@ -688,7 +688,7 @@ __global__ void __launch_bounds__(128) k_step_persistent(PersistArgs a) {
   }
   if (!gridBarrier(a)) return;
   clearBlockCount(a.blockCount, a.nScanBlocks);
-  nebrBody<false>(a.tileRep, a.active, a.heavy, a.work, a.rc, a.st, a.cellStart, a.sortPos, a.nn, a.nbl, a.ns, a.sl,
+  nebrFusedBody(a.tileRep, a.active, a.heavy, a.work, a.rc, a.st, a.cellStart, a.sortPos, a.nn, a.nbl, a.ns, a.sl,
                   a.nrl, a.rl, a.rowStride, a.nebrMax, a.descending);
   if (!gridBarrier(a)) return;
   const int nm = a.metalTab.nblocks, nc = a.carbonTab.nblocks;

@@ -400,12 +400,12 @@ cudaError_t launchScanRank(bool pdl, int cells, int grid, cudaStream_t s, const 
 __global__ void __launch_bounds__(kNebrWarps * 32) k_build_nebr(SG_NEBR_PARAMS) {
   pdlEnter();
   clearBlockCount(blockCount, nBlockCount);
-  nebrBody<false>(SG_NEBR_ARGS);
+  nebrFusedBody(SG_NEBR_ARGS);
 }
 __global__ void __launch_bounds__(kNebrWarps * 32) k_build_nebr_lanes(SG_NEBR_PARAMS) {
   pdlEnter();
   clearBlockCount(blockCount, nBlockCount);
-  nebrBody<true>(SG_NEBR_ARGS);
+  nebrLanesBody(SG_NEBR_ARGS);
 }
 #undef SG_NEBR_PARAMS
 #undef SG_NEBR_ARGS

@@ -215,119 +215,293 @@ __device__ __forceinline__ void scanRankBody(int t, const int *__restrict__ tile
 
 // ============================================================================================
 // Neighbour list (BuildNebrListK, SurfaceGrowth.cu:612-711), cell-centric.  Warps take work
-// items from the lists k_scan_final wrote, through an atomic work counter: first the parts of
-// the cells split into several items, then the other non-empty cells whole, in
-// ascending cell order or (descending != 0) descending: the queue should end on cheap items,
-// and in a surface system the dense metal cells sit at the high cell indices (z-major).  Lanes
-// 0..26 look up the 27 stencil cells (reference visiting order); their segments, in that order
-// and ascending atom index inside each, form the cell's window of candidates: exactly the
-// order in which the reference's one-thread walk meets them.  A lane finds the segment of its
-// window position by binary search over the segment offsets.
-//  Test pass: per 32-candidate word of the window (one candidate per lane, in registers) the
-//    warp runs through the home atoms (positions broadcast from shared memory); two ballots
-//    give the word's "within the list radius" and "within rCutC + skin" masks of each home
-//    atom, kept in shared memory with the word's "metal candidate" mask.  Words without a
-//    periodic shift that cannot hold a home atom take a loop without the shift and the
-//    self-pair test (subtracting a zero shift changes no bit).  Each lane loads its candidate
-//    of the next word while the current word is tested.
-//  Emit pass: per home atom and word with hits, lane l places candidate l at its rank among
-//    the word's set bits, so consecutive entries of the atom's row nbl[g*rowStride + j] come
-//    from one coalesced store; for a carbon atom the same ranks place its close list (entries
-//    within rCutC + skin, read by the graphene second-neighbour walk of the atoms bonded to
-//    it) and its relevant list (every metal entry and every close entry, with its position in
-//    the full list: all the carbon-force pass needs for the atom itself).  The running lengths
-//    are uniform across the warp; stores are predicated, not branched.
-// A window pass holds kWin candidates; larger stencils take several passes, the lengths
-// carrying over in the lane of each home atom.  Close and relevant lists rest on the skin, as
-// the neighbour list itself does: no pair closes in by more than rNebrShell between rebuilds.
+// items from the lists k_scan_rank wrote, through an atomic work counter: first the parts of
+// the cells split into several items, then the other non-empty cells whole, in ascending cell
+// order or (descending != 0) descending: the queue should end on cheap items, and in a surface
+// system the dense metal cells sit at the high cell indices (z-major).  Lanes 0..26 look up
+// the 27 stencil cells (reference visiting order); their segments, in that order and ascending
+// atom index inside each, form the cell's window of candidates: exactly the order in which the
+// reference's one-thread walk meets them.  A lane finds the segment of its window position by
+// binary search over the segment offsets.  Two builds share this item set-up:
+//  k_build_nebr (nebrFusedBody): per 32-candidate word of the window (one candidate per lane,
+//    loaded while the previous word is tested) the warp tests four home atoms at a time, their
+//    positions broadcast from shared memory.  Two ballots give a home atom's "within the list
+//    radius" and "within rCutC + skin" masks, and the hits go straight to the rows: lane l
+//    stores candidate l at the home atom's running length plus its rank among the mask's set
+//    bits, so a word's entries of one row leave in one store.  For a carbon home the same
+//    ranks place its close list (entries within rCutC + skin, read by the graphene
+//    second-neighbour walk of the atoms bonded to it) and its relevant list (every metal entry
+//    and every close entry, with its position in the full list: all the carbon-force pass
+//    needs for the atom itself).  A word without hits for a home atom costs it the test only,
+//    one without close or metal hits the full-list store only.  The running lengths live in
+//    the home atom's lane.
+//  k_build_nebr_lanes (nebrLanesBody): the masks of a window of kWin candidates kept in shared
+//    memory, then lanes walking the hits of one home atom each: G = 32 / nh' lanes per home
+//    atom (nh' = nh rounded up to a power of two), lane q of a group taking a contiguous share
+//    of the window's words after the hits of the group's earlier lanes.
+// Words without a periodic shift that cannot hold a home atom take a test without the shift
+// and the self-pair test (subtracting a zero shift changes no bit).  Close and relevant lists
+// rest on the skin, as the neighbour list itself does: no pair closes in by more than
+// rNebrShell between rebuilds.
 // ============================================================================================
-__device__ __forceinline__ void stIf(bool p, int *a, int v) {
-  asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %0, 0;\n\t@q st.global.u32 [%1], %2;\n\t}" ::"r"((unsigned)p), "l"(a),
-               "r"(v)
-               : "memory");
-}
-__device__ __forceinline__ void stIf2(bool p, int2 *a, int x, int y) {
-  asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %0, 0;\n\t@q st.global.v2.u32 [%1], {%2, %3};\n\t}" ::"r"((unsigned)p),
-               "l"(a), "r"(x), "r"(y)
-               : "memory");
+struct NebrItem {
+  int rep, hFirst, hLast, total, homeLen;  // home atoms [hFirst, hLast) of sortPos; window length
+};
+
+// The warp's next work item; false once the items are exhausted (every warp takes one ticket
+// past the end, and the last one clears the counters for the next rebuild: all warps have read
+// them by then).  Fills the warp's stencil tables: start of each of the 27 cells in sortPos
+// (sQb), its offset in the window (sOff) and its periodic shift (sSh, w = 1 when non-zero).
+__device__ __forceinline__ bool nebrNextItem(int *work, int nLight, int nHeavy, const int2 *__restrict__ heavy,
+                                             const int *__restrict__ active, const int *__restrict__ tileRep,
+                                             const RepConst *__restrict__ rc, const int *__restrict__ cellStart,
+                                             int descending, int lane, float4 *sSh, int *sQb, int *sOff,
+                                             NebrItem &it) {
+  const unsigned full = 0xffffffffu;
+  int idx = 0;
+  if (lane == 0) idx = atomicAdd(&work[0], 1);
+  idx = __shfl_sync(full, idx, 0);
+  if (idx >= nHeavy + nLight) {
+    if (lane == 0 && idx == nHeavy + nLight + (int)gridDim.x * kNebrWarps - 1) {
+      work[0] = 0;
+      work[1] = 0;
+      work[2] = 0;
+      work[3] = 0;
+    }
+    return false;
+  }
+  int gc, hOff = 0, hCnt = 1 << 30;
+  if (idx < nHeavy) {
+    const int2 h = heavy[idx];
+    gc = h.x;
+    hOff = h.y >> 16;
+    hCnt = h.y & 0xffff;
+  } else {
+    gc = active[descending ? nHeavy + nLight - 1 - idx : idx - nHeavy];
+  }
+  it.rep = tileRep[gc / kCellTile];
+  const RepConst &P = rc[it.rep];
+  const int c = gc - P.cellOff;
+  const int hb = cellStart[gc], he = cellStart[gc + 1];
+  it.hFirst = hb + hOff;
+  it.hLast = min(he, it.hFirst + hCnt);
+  it.homeLen = he - hb;  // stencil cell 0 is the home cell: window positions [0, homeLen)
+  int len = 0;
+  if (lane < 27) {
+    float sx, sy, sz;
+    const int C = P.cellOff + stencilCell(P, c, lane, sx, sy, sz);
+    const int qb = cellStart[C];
+    len = cellStart[C + 1] - qb;
+    sQb[lane] = qb;
+    sSh[lane] = make_float4(sx, sy, sz, (sx != 0.f || sy != 0.f || sz != 0.f) ? 1.f : 0.f);
+  }
+  int incl = len;  // inclusive prefix of the segment lengths
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const int v = __shfl_up_sync(full, incl, d);
+    if (lane >= d) incl += v;
+  }
+  if (lane < 27) sOff[lane] = incl - len;
+  it.total = __shfl_sync(full, incl, 26);
+  __syncwarp();
+  return true;
 }
 
-// LANE_EMIT: the emit pass with lanes walking the hits of one home atom each (the lists are
-// the same; k_build_nebr_lanes), instead of the warp placing every word's hits cooperatively:
-// G = 32 / nh' lanes per home atom (nh' = nh rounded up to a power of two), lane q of a group
-// taking a contiguous share of the window's words after the hits of the group's earlier lanes.
-template <bool LANE_EMIT>
-__device__ __forceinline__ void nebrBody(const int *__restrict__ tileRep, const int *__restrict__ active,
-                                         const int2 *__restrict__ heavy, int *work,
-                                         const RepConst *__restrict__ rc, RepState *st,
-                                         const int *__restrict__ cellStart, const float4 *__restrict__ sortPos,
-                                         int *__restrict__ nn, int *__restrict__ nbl, int *__restrict__ ns,
-                                         int *__restrict__ sl, int *__restrict__ nrl, unsigned *__restrict__ rl,
-                                         int rowStride, int nebrMax, int descending) {
+// The candidate at window position e: its sortPos entry (w: the atom index) and its stencil
+// cell o, the last one whose segment starts at or before e.
+__device__ __forceinline__ float4 nebrCandidate(const float4 *__restrict__ sortPos, const int *sQb, const int *sOff,
+                                                int e, int &o) {
+  o = 0;
+#pragma unroll
+  for (int step = 16; step > 0; step >>= 1)
+    if (o + step < 27 && sOff[o + step] <= e) o += step;
+  return sortPos[sQb[o] + e - sOff[o]];
+}
+
+// The lengths of home atom `lane` (< nh) once its window is done: nn, and for a carbon atom ns
+// and nrl (-1: the carbon pass walks the full list instead); the largest list and the rows
+// that overflowed accumulate in want and over.
+__device__ __forceinline__ void nebrFinishHome(int lane, int nh, int ga, int nMy, int mMy, int rMy, int metalEnd,
+                                               int nebrMax, int *__restrict__ nn, int *__restrict__ ns,
+                                               int *__restrict__ nrl, int &want, int &over) {
+  if (lane < nh) {
+    nn[ga] = min(nMy, nebrMax);
+    ns[ga] = (ga < metalEnd) ? 0 : (mMy > kShortMax || nMy > nebrMax) ? -1 : mMy;
+    nrl[ga] = (ga < metalEnd) ? 0 : (rMy > kRelMax || nMy > nebrMax || nMy > kRelPosLimit) ? -1 : rMy;
+    want = max(want, nMy);
+    over += (nMy > nebrMax) ? 1 : 0;
+  }
+}
+
+// The item's largest list and overflowing rows into the replica's state, one atomic each.
+__device__ __forceinline__ void nebrItemStats(int lane, RepState *S, int want, int over) {
+  const unsigned full = 0xffffffffu;
+  for (int off = 16; off > 0; off >>= 1) {
+    want = max(want, __shfl_xor_sync(full, want, off));
+    over += __shfl_xor_sync(full, over, off);
+  }
+  if (lane == 0) {
+    atomicMax(&S->maxNeighbours, want);
+    if (over > 0) {
+      atomicAdd(&S->nebrOverflow, over);
+      setFlag(S, 5 /*SG_ERR_NEBR_OVERFLOW*/);
+    }
+  }
+  __syncwarp();
+}
+
+// Four home atoms (a0 .. a0+3 of the warp's sHome) against this lane's candidate: the hit and
+// close masks of each.  SHIFTED: the word holds a periodic image or the home cell, so the
+// shift is subtracted and the self pair left out.
+template <bool SHIFTED>
+__device__ __forceinline__ void nebrTest4(const float4 *sHome, int a0, int nh, float bx, float by, float bz, float sx,
+                                          float sy, float sz, int k, float rrNebr, float rrShort, unsigned (&mh)[4],
+                                          unsigned (&mc)[4], int (&gh)[4]) {
+  const unsigned full = 0xffffffffu;
+#pragma unroll
+  for (int u = 0; u < 4; u++) {
+    const float4 H = sHome[a0 + u];
+    gh[u] = __float_as_int(H.w);
+    float dx = H.x - bx, dy = H.y - by, dz = H.z - bz;
+    bool hit;
+    float rr;
+    if (SHIFTED) {
+      // the reference subtracts the cell shift after the difference: both roundings kept
+      dx = dx - sx;
+      dy = dy - sy;
+      dz = dz - sz;
+      rr = sqDist(dx, dy, dz);
+      hit = (rr < rrNebr) && (gh[u] != k);
+    } else {
+      rr = sqDist(dx, dy, dz);
+      hit = rr < rrNebr;
+    }
+    mh[u] = __ballot_sync(full, hit && a0 + u < nh);
+    mc[u] = __ballot_sync(full, rr < rrShort);
+  }
+}
+
+__device__ __forceinline__ void nebrFusedBody(const int *__restrict__ tileRep, const int *__restrict__ active,
+                                              const int2 *__restrict__ heavy, int *work,
+                                              const RepConst *__restrict__ rc, RepState *st,
+                                              const int *__restrict__ cellStart, const float4 *__restrict__ sortPos,
+                                              int *__restrict__ nn, int *__restrict__ nbl, int *__restrict__ ns,
+                                              int *__restrict__ sl, int *__restrict__ nrl, unsigned *__restrict__ rl,
+                                              int rowStride, int nebrMax, int descending) {
+  __shared__ float4 sHome[kNebrWarps][32];
+  __shared__ float4 sSh[kNebrWarps][27];
+  __shared__ int sQb[kNebrWarps][27], sOff[kNebrWarps][27];
+  const unsigned full = 0xffffffffu;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned lower = (1u << lane) - 1u;
+  const int nLight = work[1], nHeavy = work[2];
+  NebrItem it;
+  while (nebrNextItem(work, nLight, nHeavy, heavy, active, tileRep, rc, cellStart, descending, lane, sSh[w], sQb[w],
+                      sOff[w], it)) {
+    const RepConst &P = rc[it.rep];
+    const int atomOff = P.atomOff, metalEnd = P.atomOff + P.nMolMe;
+    const float rrNebr = P.rrNebr, rrShort = P.rrShort;
+    const int total = it.total, nw = (total + 31) >> 5;
+    int want = 0, over = 0;
+    for (int h0 = it.hFirst; h0 < it.hLast; h0 += 32) {
+      const int nh = min(32, it.hLast - h0);
+      float4 Ah = make_float4(0.f, 0.f, 0.f, __int_as_float(-2));
+      if (lane < nh) Ah = sortPos[h0 + lane];
+      sHome[w][lane] = Ah;
+      const int ga = __float_as_int(Ah.w);
+      int nMy = 0, mMy = 0, rMy = 0;  // list, close-list and relevant-list lengths of home atom `lane`
+      __syncwarp();
+      // this lane's candidate of the next word, loaded while the current word is tested
+      int oN = 0;
+      float4 BN = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (lane < total) BN = nebrCandidate(sortPos, sQb[w], sOff[w], lane, oN);
+      for (int i = 0; i < nw; i++) {
+        const int e = 32 * i + lane;
+        const int o = oN;
+        const float4 B = BN;
+        if (e + 32 < total) BN = nebrCandidate(sortPos, sQb[w], sOff[w], e + 32, oN);
+        // this lane's candidate; past the window end it sits at 1e30 and never matches
+        float bx = 1e30f, by = 1e30f, bz = 1e30f, sx = 0.f, sy = 0.f, sz = 0.f;
+        int k = -1;
+        bool shifted = false;
+        if (e < total) {
+          k = __float_as_int(B.w);
+          bx = B.x;
+          by = B.y;
+          bz = B.z;
+          const float4 sh = sSh[w][o];
+          sx = sh.x;
+          sy = sh.y;
+          sz = sh.z;
+          shifted = sh.w != 0.f;
+        }
+        const unsigned metalW = __ballot_sync(full, k >= 0 && k < metalEnd);
+        const bool plainWord = !__any_sync(full, shifted) && 32 * i >= it.homeLen;
+        for (int a0 = 0; a0 < nh; a0 += 4) {
+          unsigned mh[4], mc[4];
+          int gh[4];
+          if (plainWord)
+            nebrTest4<false>(sHome[w], a0, nh, bx, by, bz, sx, sy, sz, k, rrNebr, rrShort, mh, mc, gh);
+          else
+            nebrTest4<true>(sHome[w], a0, nh, bx, by, bz, sx, sy, sz, k, rrNebr, rrShort, mh, mc, gh);
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            const unsigned h = mh[u];
+            if (h == 0u) continue;  // warp-uniform
+            const int a = a0 + u, g = gh[u];
+            const int n = __shfl_sync(full, nMy, a);
+            const int j = n + __popc(h & lower);
+            if (((h >> lane) & 1u) && j < nebrMax) nbl[(size_t)g * rowStride + j] = k;
+            if (g >= metalEnd) {
+              const unsigned cl = h & mc[u], rv = h & (mc[u] | metalW);
+              if (rv != 0u) {
+                const int m = __shfl_sync(full, mMy, a), r = __shfl_sync(full, rMy, a);
+                const int jm = m + __popc(cl & lower), jr = r + __popc(rv & lower);
+                if (((cl >> lane) & 1u) && jm < kShortMax) sl[(size_t)g * kShortMax + jm] = k;
+                if (((rv >> lane) & 1u) && jr < kRelMax) rl[(size_t)g * kRelMax + jr] = relPack(k - atomOff, j);
+                if (lane == a) {
+                  mMy += __popc(cl);
+                  rMy += __popc(rv);
+                }
+              }
+            }
+            if (lane == a) nMy += __popc(h);
+          }
+        }
+      }
+      nebrFinishHome(lane, nh, ga, nMy, mMy, rMy, metalEnd, nebrMax, nn, ns, nrl, want, over);
+      __syncwarp();
+    }
+    nebrItemStats(lane, st + it.rep, want, over);
+  }
+}
+
+__device__ __forceinline__ void nebrLanesBody(const int *__restrict__ tileRep, const int *__restrict__ active,
+                                              const int2 *__restrict__ heavy, int *work,
+                                              const RepConst *__restrict__ rc, RepState *st,
+                                              const int *__restrict__ cellStart, const float4 *__restrict__ sortPos,
+                                              int *__restrict__ nn, int *__restrict__ nbl, int *__restrict__ ns,
+                                              int *__restrict__ sl, int *__restrict__ nrl, unsigned *__restrict__ rl,
+                                              int rowStride, int nebrMax, int descending) {
   __shared__ int sK[kNebrWarps][kWin];                 // atom index of each window position
   __shared__ uint2 sMask[kNebrWarps][kWin / 32][32];   // [word][home atom]: {hit, close}
   __shared__ unsigned sMetal[kNebrWarps][kWin / 32];   // [word]: candidate is a metal atom
   __shared__ float4 sHome[kNebrWarps][32];
-  __shared__ float4 sSh[kNebrWarps][27];               // periodic shift, w = 1 when non-zero
+  __shared__ float4 sSh[kNebrWarps][27];
   __shared__ int sQb[kNebrWarps][27], sOff[kNebrWarps][27];
   const unsigned full = 0xffffffffu;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const unsigned lower = (1u << lane) - 1u, laneBit = 1u << lane;
   const int nLight = work[1], nHeavy = work[2];
-  while (true) {
-    int idx = 0;
-    if (lane == 0) idx = atomicAdd(&work[0], 1);
-    idx = __shfl_sync(full, idx, 0);
-    if (idx >= nHeavy + nLight) {
-      // every warp takes one ticket past the end; the last one clears the counters for the
-      // next rebuild (all warps have read them by then)
-      if (lane == 0 && idx == nHeavy + nLight + (int)gridDim.x * kNebrWarps - 1) {
-        work[0] = 0;
-        work[1] = 0;
-        work[2] = 0;
-        work[3] = 0;
-      }
-      break;
-    }
-    int gc, hOff = 0, hCnt = 1 << 30;
-    if (idx < nHeavy) {
-      const int2 it = heavy[idx];
-      gc = it.x;
-      hOff = it.y >> 16;
-      hCnt = it.y & 0xffff;
-    } else {
-      gc = active[descending ? nHeavy + nLight - 1 - idx : idx - nHeavy];
-    }
-    const int rep = tileRep[gc / kCellTile];
-    RepState *S = st + rep;
-    const RepConst &P = rc[rep];
-    const int c = gc - P.cellOff;
-    const int hb = cellStart[gc], he = cellStart[gc + 1];
-    const int hFirst = hb + hOff, hLast = min(he, hFirst + hCnt);  // home atoms of this item
+  NebrItem it;
+  while (nebrNextItem(work, nLight, nHeavy, heavy, active, tileRep, rc, cellStart, descending, lane, sSh[w], sQb[w],
+                      sOff[w], it)) {
+    const RepConst &P = rc[it.rep];
     const int metalEnd = P.atomOff + P.nMolMe;
     const float rrNebr = P.rrNebr, rrShort = P.rrShort;
-    int len = 0;
-    if (lane < 27) {
-      float sx, sy, sz;
-      const int C = P.cellOff + stencilCell(P, c, lane, sx, sy, sz);
-      const int qb = cellStart[C];
-      len = cellStart[C + 1] - qb;
-      sQb[w][lane] = qb;
-      sSh[w][lane] = make_float4(sx, sy, sz, (sx != 0.f || sy != 0.f || sz != 0.f) ? 1.f : 0.f);
-    }
-    int incl = len;  // inclusive prefix of the segment lengths
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const int v = __shfl_up_sync(full, incl, d);
-      if (lane >= d) incl += v;
-    }
-    if (lane < 27) sOff[w][lane] = incl - len;
-    const int total = __shfl_sync(full, incl, 26);
-    const int homeLen = he - hb;  // stencil cell 0 is the home cell: window positions [0, homeLen)
-    __syncwarp();
+    const int total = it.total;
     int want = 0, over = 0;
-    for (int h0 = hFirst; h0 < hLast; h0 += 32) {
-      const int nh = min(32, hLast - h0);
+    for (int h0 = it.hFirst; h0 < it.hLast; h0 += 32) {
+      const int nh = min(32, it.hLast - h0);
       float4 Ah = make_float4(0.f, 0.f, 0.f, __int_as_float(-2));
       if (lane < nh) Ah = sortPos[h0 + lane];
       sHome[w][lane] = Ah;
@@ -336,194 +510,119 @@ __device__ __forceinline__ void nebrBody(const int *__restrict__ tileRep, const 
       __syncwarp();
       for (int base = 0; base < total; base += kWin) {
         const int nw = (min(kWin, total - base) + 31) >> 5;
-        // ---- test pass
-        // this lane's candidate of the next word (window position eN, stencil cell oN: the last
-        // one whose segment starts at or before eN), loaded while the current word is tested
+        // ---- test pass: the hit and close masks of every home atom and word of the window
         int oN = 0;
         float4 BN = make_float4(0.f, 0.f, 0.f, 0.f);
-        {
-          const int eN = base + lane;
-          if (eN < total) {
-#pragma unroll
-            for (int step = 16; step > 0; step >>= 1)
-              if (oN + step < 27 && sOff[w][oN + step] <= eN) oN += step;
-            BN = sortPos[sQb[w][oN] + eN - sOff[w][oN]];
-          }
-        }
+        if (base + lane < total) BN = nebrCandidate(sortPos, sQb[w], sOff[w], base + lane, oN);
         for (int i = 0; i < nw; i++) {
           const int e = base + 32 * i + lane;
           const int o = oN;
           const float4 B = BN;
-          if (i + 1 < nw && e + 32 < total) {
-            const int eN = e + 32;
-            oN = 0;
-#pragma unroll
-            for (int step = 16; step > 0; step >>= 1)
-              if (oN + step < 27 && sOff[w][oN + step] <= eN) oN += step;
-            BN = sortPos[sQb[w][oN] + eN - sOff[w][oN]];
-          }
-          // this lane's candidate; past the window end it sits at 1e30 and never matches
+          if (i + 1 < nw && e + 32 < total) BN = nebrCandidate(sortPos, sQb[w], sOff[w], e + 32, oN);
           float bx = 1e30f, by = 1e30f, bz = 1e30f, sx = 0.f, sy = 0.f, sz = 0.f;
           int k = -1;
           bool shifted = false;
           if (e < total) {
             k = __float_as_int(B.w);
-            bx = B.x; by = B.y; bz = B.z;
+            bx = B.x;
+            by = B.y;
+            bz = B.z;
             const float4 sh = sSh[w][o];
-            sx = sh.x; sy = sh.y; sz = sh.z;
+            sx = sh.x;
+            sy = sh.y;
+            sz = sh.z;
             shifted = sh.w != 0.f;
             sK[w][32 * i + lane] = k;
           }
           sMetal[w][i] = __ballot_sync(full, k >= 0 && k < metalEnd);
-          if (!__any_sync(full, shifted) && base + 32 * i >= homeLen) {
-#pragma unroll 4
-            for (int a = 0; a < nh; a++) {
-              const float4 H = sHome[w][a];
-              const float dx = H.x - bx, dy = H.y - by, dz = H.z - bz;
-              const float rr = sqDist(dx, dy, dz);
-              const unsigned mh = __ballot_sync(full, rr < rrNebr);
-              const unsigned mc = __ballot_sync(full, rr < rrShort);
-              sMask[w][i][a] = make_uint2(mh, mc);
-            }
-          } else {
-#pragma unroll 4
-            for (int a = 0; a < nh; a++) {
-              const float4 H = sHome[w][a];
-              // the reference subtracts the cell shift after the difference: both roundings kept
-              float dx = H.x - bx, dy = H.y - by, dz = H.z - bz;
-              dx = dx - sx; dy = dy - sy; dz = dz - sz;
-              const float rr = sqDist(dx, dy, dz);
-              const bool hit = (rr < rrNebr) && (__float_as_int(H.w) != k);
-              const unsigned mh = __ballot_sync(full, hit);
-              const unsigned mc = __ballot_sync(full, rr < rrShort);
-              sMask[w][i][a] = make_uint2(mh, mc);
-            }
+          const bool plainWord = !__any_sync(full, shifted) && base + 32 * i >= it.homeLen;
+          for (int a0 = 0; a0 < nh; a0 += 4) {
+            unsigned mh[4], mc[4];
+            int gh[4];
+            if (plainWord)
+              nebrTest4<false>(sHome[w], a0, nh, bx, by, bz, sx, sy, sz, k, rrNebr, rrShort, mh, mc, gh);
+            else
+              nebrTest4<true>(sHome[w], a0, nh, bx, by, bz, sx, sy, sz, k, rrNebr, rrShort, mh, mc, gh);
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+              if (a0 + u < nh) sMask[w][i][a0 + u] = make_uint2(mh[u], mc[u]);
           }
         }
         __syncwarp();
-        // ---- emit pass
-        if constexpr (LANE_EMIT) {
-          // lane q of home atom a's group walks the set bits of a's masks in words [i0, i1):
-          // its share of a's entries in list order, with the same limits and the same close and
-          // relevant entries; the group's exclusive prefix of the hit counts places them
-          const int lg = 32 - __clz(nh - 1);  // log2 of nh rounded up to a power of two
-          const int G = 32 >> lg;
-          const int a = lane >> (5 - lg), q = lane & (G - 1);
-          const int i0 = q * nw / G, i1 = (q + 1) * nw / G;
-          int cn = 0, cm = 0, cr = 0;  // this lane's hits, close hits and relevant hits
+        // ---- emit pass: lane q of home atom a's group walks the set bits of a's masks in
+        // words [i0, i1): its share of a's entries in list order, with the same limits and the
+        // same close and relevant entries; the group's exclusive prefix of the hit counts
+        // places them
+        const int lg = 32 - __clz(nh - 1);  // log2 of nh rounded up to a power of two
+        const int G = 32 >> lg;
+        const int a = lane >> (5 - lg), q = lane & (G - 1);
+        const int i0 = q * nw / G, i1 = (q + 1) * nw / G;
+        int cn = 0, cm = 0, cr = 0;  // this lane's hits, close hits and relevant hits
+        for (int i = i0; i < i1; i++) {
+          const uint2 hc = sMask[w][i][a];
+          cn += __popc(hc.x);
+          cm += __popc(hc.x & hc.y);
+          cr += __popc(hc.x & (hc.y | sMetal[w][i]));
+        }
+        int pn = cn, pm = cm, pr = cr;  // inclusive prefix inside the group
+        for (int d = 1; d < G; d <<= 1) {
+          const int yn = __shfl_up_sync(full, pn, d, G);
+          const int ym = __shfl_up_sync(full, pm, d, G);
+          const int yr = __shfl_up_sync(full, pr, d, G);
+          if (q >= d) {
+            pn += yn;
+            pm += ym;
+            pr += yr;
+          }
+        }
+        const int g = __shfl_sync(full, ga, a);
+        int n = __shfl_sync(full, nMy, a) + pn - cn;
+        int m = __shfl_sync(full, mMy, a) + pm - cm;
+        int r = __shfl_sync(full, rMy, a) + pr - cr;
+        const int lastOfGroup = ((lane * G) & 31) + G - 1;  // for lane < nh: home `lane`'s group
+        const int tn = __shfl_sync(full, pn, lastOfGroup);
+        const int tm = __shfl_sync(full, pm, lastOfGroup);
+        const int tr = __shfl_sync(full, pr, lastOfGroup);
+        if (a < nh) {
+          int *row = nbl + (size_t)g * rowStride;
+          const bool carbonHome = g >= metalEnd;
+          int *srow = sl + (size_t)g * kShortMax;
+          unsigned *rrow = rl + (size_t)g * kRelMax;
           for (int i = i0; i < i1; i++) {
             const uint2 hc = sMask[w][i][a];
-            cn += __popc(hc.x);
-            cm += __popc(hc.x & hc.y);
-            cr += __popc(hc.x & (hc.y | sMetal[w][i]));
-          }
-          int pn = cn, pm = cm, pr = cr;  // inclusive prefix inside the group
-          for (int d = 1; d < G; d <<= 1) {
-            const int yn = __shfl_up_sync(full, pn, d, G);
-            const int ym = __shfl_up_sync(full, pm, d, G);
-            const int yr = __shfl_up_sync(full, pr, d, G);
-            if (q >= d) { pn += yn; pm += ym; pr += yr; }
-          }
-          const int g = __shfl_sync(full, ga, a);
-          int n = __shfl_sync(full, nMy, a) + pn - cn;
-          int m = __shfl_sync(full, mMy, a) + pm - cm;
-          int r = __shfl_sync(full, rMy, a) + pr - cr;
-          const int lastOfGroup = ((lane * G) & 31) + G - 1;  // for lane < nh: home `lane`'s group
-          const int tn = __shfl_sync(full, pn, lastOfGroup);
-          const int tm = __shfl_sync(full, pm, lastOfGroup);
-          const int tr = __shfl_sync(full, pr, lastOfGroup);
-          if (a < nh) {
-            int *row = nbl + (size_t)g * rowStride;
-            const bool carbonHome = g >= metalEnd;
-            int *srow = sl + (size_t)g * kShortMax;
-            unsigned *rrow = rl + (size_t)g * kRelMax;
-            for (int i = i0; i < i1; i++) {
-              const uint2 hc = sMask[w][i][a];
-              const unsigned metalW = sMetal[w][i];
-              unsigned bits = hc.x;
-              while (bits) {
-                const int b = __ffs(bits) - 1;
-                bits &= bits - 1;
-                const int k = sK[w][32 * i + b];
-                if (n < nebrMax) row[n] = k;
-                if (carbonHome) {
-                  const bool close = (hc.y >> b) & 1u;
-                  if (close) {
-                    if (m < kShortMax) srow[m] = k;
-                    m++;
-                  }
-                  if (close || ((metalW >> b) & 1u)) {
-                    if (r < kRelMax) rrow[r] = relPack(k - P.atomOff, n);
-                    r++;
-                  }
+            const unsigned metalW = sMetal[w][i];
+            unsigned bits = hc.x;
+            while (bits) {
+              const int b = __ffs(bits) - 1;
+              bits &= bits - 1;
+              const int k = sK[w][32 * i + b];
+              if (n < nebrMax) row[n] = k;
+              if (carbonHome) {
+                const bool close = (hc.y >> b) & 1u;
+                if (close) {
+                  if (m < kShortMax) srow[m] = k;
+                  m++;
                 }
-                n++;
+                if (close || ((metalW >> b) & 1u)) {
+                  if (r < kRelMax) rrow[r] = relPack(k - P.atomOff, n);
+                  r++;
+                }
               }
+              n++;
             }
           }
-          if (lane < nh) { nMy += tn; mMy += tm; rMy += tr; }
-        } else {
-        for (int a = 0; a < nh; a++) {
-          const int g = __float_as_int(sHome[w][a].w);
-          int n = __shfl_sync(full, nMy, a);
-          int *row = nbl + (size_t)g * rowStride;
-          if (g >= metalEnd) {
-            int m = __shfl_sync(full, mMy, a);
-            int r = __shfl_sync(full, rMy, a);
-            int *srow = sl + (size_t)g * kShortMax;
-            unsigned *rrow = rl + (size_t)g * kRelMax;
-            for (int i = 0; i < nw; i++) {
-              const uint2 hc = sMask[w][i][a];
-              const int k = sK[w][32 * i + lane];
-              const int j = n + __popc(hc.x & lower);
-              stIf((hc.x & laneBit) && j < nebrMax, row + j, k);
-              const unsigned mc = hc.x & hc.y;
-              const int jm = m + __popc(mc & lower);
-              stIf((mc & laneBit) && jm < kShortMax, srow + jm, k);
-              const unsigned mr = hc.x & (hc.y | sMetal[w][i]);
-              const int jr = r + __popc(mr & lower);
-              stIf((mr & laneBit) && jr < kRelMax, reinterpret_cast<int *>(rrow + jr), (int)relPack(k - P.atomOff, j));
-              m += __popc(mc);
-              r += __popc(mr);
-              n += __popc(hc.x);
-            }
-            mMy = (lane == a) ? m : mMy;
-            rMy = (lane == a) ? r : rMy;
-          } else {
-            for (int i = 0; i < nw; i++) {
-              const unsigned hx = sMask[w][i][a].x;
-              const int k = sK[w][32 * i + lane];
-              const int j = n + __popc(hx & lower);
-              stIf((hx & laneBit) && j < nebrMax, row + j, k);
-              n += __popc(hx);
-            }
-          }
-          nMy = (lane == a) ? n : nMy;
         }
+        if (lane < nh) {
+          nMy += tn;
+          mMy += tm;
+          rMy += tr;
         }
         __syncwarp();
       }
-      if (lane < nh) {
-        nn[ga] = min(nMy, nebrMax);
-        // -1: the carbon pass walks the full list instead
-        ns[ga] = (ga < metalEnd) ? 0 : (mMy > kShortMax || nMy > nebrMax) ? -1 : mMy;
-        nrl[ga] = (ga < metalEnd) ? 0 : (rMy > kRelMax || nMy > nebrMax || nMy > kRelPosLimit) ? -1 : rMy;
-        want = max(want, nMy);
-        over += (nMy > nebrMax) ? 1 : 0;
-      }
+      nebrFinishHome(lane, nh, ga, nMy, mMy, rMy, metalEnd, nebrMax, nn, ns, nrl, want, over);
+      __syncwarp();
     }
-    for (int off = 16; off > 0; off >>= 1) {
-      want = max(want, __shfl_xor_sync(full, want, off));
-      over += __shfl_xor_sync(full, over, off);
-    }
-    if (lane == 0) {
-      atomicMax(&S->maxNeighbours, want);
-      if (over > 0) {
-        atomicAdd(&S->nebrOverflow, over);
-        setFlag(S, 5 /*SG_ERR_NEBR_OVERFLOW*/);
-      }
-    }
-    __syncwarp();
+    nebrItemStats(lane, st + it.rep, want, over);
   }
 }
 

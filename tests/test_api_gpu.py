@@ -139,9 +139,9 @@ def test_published_record_is_the_current_step_over_many_calls(mode):
 
 
 @pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_MIXED])
-def test_adjacent_state_block_equals_separate_arrays(mode):
-    """r, v, a adjacent in one page-locked block take one copy-engine transfer and an unpack on
-    the device; the state and the trajectory equal those of three separate page-locked arrays."""
+def test_page_locked_block_equals_pageable_arrays(mode):
+    """r, v, a as views of one page-locked block are read in place by the upload kernel,
+    pageable arrays are copied first: the state and the trajectory are the same."""
     torch = pytest.importorskip("torch")
     p, r, v = workloads.small(seed=66)
     n = p.nMol
@@ -152,12 +152,12 @@ def test_adjacent_state_block_equals_separate_arrays(mode):
     one = Simulation(p, mode=mode)
     two = Simulation(p, mode=mode)
     one.set_state(br, bv, ba)
-    two.set_state(_pinned(r), _pinned(v), _pinned(a))
+    two.set_state(r.copy(), v.copy(), a.copy())
     for x, y in zip(one.get_state(), (r, v, a)):
         assert np.array_equal(x, y)
     for _ in range(3):
         t1 = one.step_from_host(br, bv, ba, nsteps=2)
-        t2 = two.step_from_host(_pinned(r), _pinned(v), _pinned(a), nsteps=2)
+        t2 = two.step_from_host(r.copy(), v.copy(), a.copy(), nsteps=2)
         _same_thermo(t1, t2)
     for x, y in zip(one.get_state(), two.get_state()):
         assert np.array_equal(x, y)
