@@ -268,6 +268,19 @@ __device__ __forceinline__ void reduceMixedBody(
       acc[MA_VV_C] += vv;
     }
   }
+  // the replica's constants and state into shared memory for the step control of whichever
+  // block finishes last, loaded by every block while it reduces (nothing writes the state
+  // before the last block has arrived)
+  __shared__ RepState sS;
+  __shared__ RepConst sP;
+  {
+    const int *cs = reinterpret_cast<const int *>(&P);
+    int *cd = reinterpret_cast<int *>(&sP);
+    for (int i = t; i < (int)(sizeof(RepConst) / 4); i += THREADS) cd[i] = cs[i];
+    const int *ss = reinterpret_cast<const int *>(S);
+    int *sd = reinterpret_cast<int *>(&sS);
+    for (int i = t; i < (int)(sizeof(RepState) / 4); i += THREADS) sd[i] = __ldcg(ss + i);
+  }
   __shared__ DF shDF[THREADS / 32][kMixAcc];
   __shared__ float shF[THREADS / 32][kMixMax];
 #pragma unroll
@@ -393,10 +406,6 @@ __device__ __forceinline__ void reduceMixedBody(
   for (int k = 0; k < kMixAcc; k++) A[k] = tot[k];
 #pragma unroll
   for (int k = 0; k < kMixMax; k++) M[k] = totF[k];
-  __shared__ RepState sS;
-  __shared__ RepConst sP;
-  constToShared(&P, &sP);
-  stateToShared(S, &sS);
   stepControlMixed(sP, &sS, A, M, diff64 ? diff64 + diffOff64[rep] : nullptr,
                    diffF ? diffF + diffOffF[rep] : nullptr, forceRebuild);
   stateFromShared(&sS, S);
@@ -424,41 +433,20 @@ __device__ void stepControlMixed(const RepConst &P, RepState *S, const double (&
   const int sc = S->stepCount + 1;
   __shared__ int diffDue, accumNow, printNow;
   __shared__ double cmc[3];
+  const bool metal = P.nMolMe != 0;
+  const double invMe = P.invNMolMe;
+  // the step's scalars in three independent parts, each on lane 0 of its own warp (no two of
+  // them write the same field); the property sums after them
   if (t == 0) {
-    const double nMe = P.nMolMe, invMe = P.invNMolMe;
-    // regime 2 subtracts the metal centre-of-mass velocity from vx in the kinetic energy
+    // kinetic energy (regime 2 subtracts the metal centre-of-mass velocity from vx), thermostat
+    const double nMe = P.nMolMe;
     double vvMetal = A[MA_VX2_M] + A[MA_VVYZ_M];
-    double cmvx = 0.0;
-    if (P.nMolMe != 0) {
-      cmvx = A[MA_VX_M] * invMe;
-      if (P.iRegime == 2) vvMetal = A[MA_VX2_M] - 2.0 * cmvx * A[MA_VX_M] + nMe * cmvx * cmvx + A[MA_VVYZ_M];
+    if (metal && P.iRegime == 2) {
+      const double cmvx = A[MA_VX_M] * invMe;
+      vvMetal = A[MA_VX2_M] - 2.0 * cmvx * A[MA_VX_M] + nMe * cmvx * cmvx + A[MA_VVYZ_M];
     }
     const double vvSum = A[MA_VV_C] + (double)P.massMe * vvMetal;
-    S->red[RS_VSUM_X] = (float)A[MA_VSUM_X]; S->red[RS_VSUM_Y] = (float)A[MA_VSUM_Y];
-    S->red[RS_VSUM_Z] = (float)A[MA_VSUM_Z];
-    S->red[RS_VVMAX] = M[MM_VVMAX];
     S->red[RS_VVSUM] = (float)vvSum;
-    S->red[RS_USUM] = (float)A[MA_USUM];
-    S->red[RS_CM_X] = (float)A[MA_CM_X]; S->red[RS_CM_Y] = (float)A[MA_CM_Y]; S->red[RS_CM_Z] = (float)A[MA_CM_Z];
-    const bool metal = P.nMolMe != 0;
-    S->red[RS_MIN_X] = metal ? M[MM_MIN_X] : 0.f; S->red[RS_MIN_Y] = metal ? M[MM_MIN_Y] : 0.f;
-    S->red[RS_MIN_Z] = metal ? M[MM_MIN_Z] : 0.f;
-    S->red[RS_MAX_X] = metal ? M[MM_MAX_X] : 0.f; S->red[RS_MAX_Y] = metal ? M[MM_MAX_Y] : 0.f;
-    S->red[RS_MAX_Z] = metal ? M[MM_MAX_Z] : 0.f;
-    S->red[RS_FRICT] = (float)A[MA_FRICT];
-    S->cmVel[0] = (float)A[MA_VX_M]; S->cmVel[1] = (float)A[MA_VY_M]; S->cmVel[2] = (float)A[MA_VZ_M];
-    diffDue = 0;
-    if (metal) {
-      S->cmVal = (float)(A[MA_CM_X] * invMe);
-      S->cmVelVal = (float)cmvx;
-      S->frictVal = P.hasFric ? (float)A[MA_FRICT] : 0.f;
-      if (P.iRegime == 2 && sc > P.stepEquil && ((sc - P.stepEquil) % P.stepDiffuse == 0) && diff && diffF) {
-        diffDue = 1;
-        cmc[0] = A[MA_CM_X] * invMe; cmc[1] = A[MA_CM_Y] * invMe; cmc[2] = A[MA_CM_Z] * invMe;
-      }
-    } else {
-      S->cmVal = 0.f; S->cmVelVal = 0.f; S->frictVal = 0.f;
-    }
     const double kin = 0.5 * vvSum * P.invNMol;
     const bool thermo = ((P.iRegime == 2) && (sc > P.stepEquil) && (sc % P.stepThermostat == 0)) ||
                         ((P.iRegime == 1) && (sc % P.stepThermostat == 0));
@@ -470,6 +458,40 @@ __device__ void stepControlMixed(const RepConst &P, RepState *S, const double (&
     } else {
       S->thermoPending = 0;
     }
+    const double pe64 = A[MA_USUM] * P.invNMol;
+    S->ke64 = kin;
+    S->pe64 = pe64;
+    S->virial64 = A[MA_VIRIAL];
+    S->ke = (float)kin;
+    S->pe = (float)pe64;
+    S->te = (float)(kin + pe64);
+  } else if (t == 32) {
+    // the reduced values, the metal centre of mass and its velocity, the friction force
+    S->red[RS_VSUM_X] = (float)A[MA_VSUM_X]; S->red[RS_VSUM_Y] = (float)A[MA_VSUM_Y];
+    S->red[RS_VSUM_Z] = (float)A[MA_VSUM_Z];
+    S->red[RS_VVMAX] = M[MM_VVMAX];
+    S->red[RS_USUM] = (float)A[MA_USUM];
+    S->red[RS_CM_X] = (float)A[MA_CM_X]; S->red[RS_CM_Y] = (float)A[MA_CM_Y]; S->red[RS_CM_Z] = (float)A[MA_CM_Z];
+    S->red[RS_MIN_X] = metal ? M[MM_MIN_X] : 0.f; S->red[RS_MIN_Y] = metal ? M[MM_MIN_Y] : 0.f;
+    S->red[RS_MIN_Z] = metal ? M[MM_MIN_Z] : 0.f;
+    S->red[RS_MAX_X] = metal ? M[MM_MAX_X] : 0.f; S->red[RS_MAX_Y] = metal ? M[MM_MAX_Y] : 0.f;
+    S->red[RS_MAX_Z] = metal ? M[MM_MAX_Z] : 0.f;
+    S->red[RS_FRICT] = (float)A[MA_FRICT];
+    S->cmVel[0] = (float)A[MA_VX_M]; S->cmVel[1] = (float)A[MA_VY_M]; S->cmVel[2] = (float)A[MA_VZ_M];
+    diffDue = 0;
+    if (metal) {
+      S->cmVal = (float)(A[MA_CM_X] * invMe);
+      S->cmVelVal = (float)(A[MA_VX_M] * invMe);
+      S->frictVal = P.hasFric ? (float)A[MA_FRICT] : 0.f;
+      if (P.iRegime == 2 && sc > P.stepEquil && ((sc - P.stepEquil) % P.stepDiffuse == 0) && diff && diffF) {
+        diffDue = 1;
+        cmc[0] = A[MA_CM_X] * invMe; cmc[1] = A[MA_CM_Y] * invMe; cmc[2] = A[MA_CM_Z] * invMe;
+      }
+    } else {
+      S->cmVal = 0.f; S->cmVelVal = 0.f; S->frictVal = 0.f;
+    }
+  } else if (t == 64) {
+    // rebuild criterion, shear drive schedule, deposition count
     if (forceRebuild || S->nebrNow) {
       S->nebrNow = 0;
       S->dispHi = 0.f;
@@ -477,14 +499,8 @@ __device__ void stepControlMixed(const RepConst &P, RepState *S, const double (&
     }
     S->dispHi += sqrtf(M[MM_VVMAX]) * P.deltaT;
     if (S->dispHi > 0.5f * P.rNebrShell) S->nebrNow = 1;
-    S->ke64 = kin;
-    S->pe64 = A[MA_USUM] * P.invNMol;
-    S->virial64 = A[MA_VIRIAL];
-    S->ke = (float)S->ke64;
-    S->pe = (float)S->pe64;
-    S->te = (float)(S->ke64 + S->pe64);
     if (P.iRegime == 2 && metal && sc > P.stepEquil + P.stepCool) {
-      if (S->cmVelVal < 0.005f) S->shear += P.deltaF;
+      if ((float)(A[MA_VX_M] * invMe) < 0.005f) S->shear += P.deltaF;  // cmVelVal
       S->shearCount = 0;
     }
     if (P.iRegime == 1) {
@@ -492,23 +508,34 @@ __device__ void stepControlMixed(const RepConst &P, RepState *S, const double (&
       if (sc > P.stepEquil && nDep < P.nMolMe && (sc - P.stepEquil) % P.stepDeposit == 0)
         S->nMolDeposited = nDep + P.nMolToDeposit;
     }
-    const float vals[7] = {S->te, S->pe, S->ke, 0.f, S->cmVal, S->cmVelVal, S->frictVal};
-    for (int p = 0; p < 7; p++) {
-      if (p == 3) continue;
-      S->props[p][0] = vals[p];
-      S->props[p][1] += vals[p];
-      S->props[p][2] += vals[p] * vals[p];
-    }
+  }
+  __syncthreads();
+  if (t < 7 && t != 3) {
+    // property p = t: value, running sum and sum of squares; the stepAvg snapshot
+    const float val = (t == 0) ? S->te : (t == 1) ? S->pe : (t == 2) ? S->ke : (t == 4) ? S->cmVal
+                    : (t == 5) ? S->cmVelVal : S->frictVal;
+    S->props[t][0] = val;
+    const float s1 = S->props[t][1] + val, s2 = S->props[t][2] + val * val;
     if (sc % P.stepAvg == 0) {
-      for (int p = 0; p < 7; p++) {
-        S->propsSnap[p][0] = S->props[p][0];
-        S->propsSnap[p][1] = S->props[p][1];
-        S->propsSnap[p][2] = S->props[p][2];
-        S->props[p][1] = 0.f;
-        S->props[p][2] = 0.f;
-      }
-      S->snapStep = sc;
+      S->propsSnap[t][0] = val;
+      S->propsSnap[t][1] = s1;
+      S->propsSnap[t][2] = s2;
+      S->props[t][1] = 0.f;
+      S->props[t][2] = 0.f;
+    } else {
+      S->props[t][1] = s1;
+      S->props[t][2] = s2;
     }
+  } else if (t == 3 && sc % P.stepAvg == 0) {
+    // oneStep (p = 3) is timed on the host: its sums are only snapshotted and cleared
+    S->propsSnap[3][0] = S->props[3][0];
+    S->propsSnap[3][1] = S->props[3][1];
+    S->propsSnap[3][2] = S->props[3][2];
+    S->props[3][1] = 0.f;
+    S->props[3][2] = 0.f;
+  }
+  if (t == 32) {
+    if (sc % P.stepAvg == 0) S->snapStep = sc;
     S->stepCount = sc;
   }
   __syncthreads();

@@ -397,7 +397,8 @@ cudaError_t launchScanRank(bool pdl, int cells, int grid, cudaStream_t s, const 
       int rowStride, int nebrMax, int descending, int *__restrict__ blockCount, int nBlockCount
 #define SG_NEBR_ARGS \
   tileRep, active, heavy, work, rc, st, cellStart, sortPos, nn, nbl, ns, sl, nrl, rl, rowStride, nebrMax, descending
-__global__ void __launch_bounds__(kNebrWarps * 32) k_build_nebr(SG_NEBR_PARAMS) {
+// 64 registers a thread, so that eight blocks (32 warps) fit on an SM
+__global__ void __launch_bounds__(kNebrWarps * 32, 8) k_build_nebr(SG_NEBR_PARAMS) {
   pdlEnter();
   clearBlockCount(blockCount, nBlockCount);
   nebrFusedBody(SG_NEBR_ARGS);

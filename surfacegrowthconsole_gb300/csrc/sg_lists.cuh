@@ -251,7 +251,8 @@ struct NebrItem {
 // The warp's next work item; false once the items are exhausted (every warp takes one ticket
 // past the end, and the last one clears the counters for the next rebuild: all warps have read
 // them by then).  Fills the warp's stencil tables: start of each of the 27 cells in sortPos
-// (sQb), its offset in the window (sOff) and its periodic shift (sSh, w = 1 when non-zero).
+// (sQb), its offset in the window (sOff, 32 entries, the last five past any position) and its
+// periodic shift (sSh, w = 1 when non-zero).
 __device__ __forceinline__ bool nebrNextItem(int *work, int nLight, int nHeavy, const int2 *__restrict__ heavy,
                                              const int *__restrict__ active, const int *__restrict__ tileRep,
                                              const RepConst *__restrict__ rc, const int *__restrict__ cellStart,
@@ -301,7 +302,7 @@ __device__ __forceinline__ bool nebrNextItem(int *work, int nLight, int nHeavy, 
     const int v = __shfl_up_sync(full, incl, d);
     if (lane >= d) incl += v;
   }
-  if (lane < 27) sOff[lane] = incl - len;
+  sOff[lane] = (lane < 27) ? incl - len : 0x7fffffff;  // padded: the search needs no bound
   it.total = __shfl_sync(full, incl, 26);
   __syncwarp();
   return true;
@@ -314,7 +315,7 @@ __device__ __forceinline__ float4 nebrCandidate(const float4 *__restrict__ sortP
   o = 0;
 #pragma unroll
   for (int step = 16; step > 0; step >>= 1)
-    if (o + step < 27 && sOff[o + step] <= e) o += step;
+    if (sOff[o + step] <= e) o += step;
   return sortPos[sQb[o] + e - sOff[o]];
 }
 
@@ -350,35 +351,93 @@ __device__ __forceinline__ void nebrItemStats(int lane, RepState *S, int want, i
   __syncwarp();
 }
 
-// Four home atoms (a0 .. a0+3 of the warp's sHome) against this lane's candidate: the hit and
+// A home-atom slot past the item's home atoms: far from every position and from the 1e30 of an
+// empty candidate lane, so its squared distance overflows and it never hits.
+__device__ __forceinline__ float4 nebrNoHome() { return make_float4(-1e30f, -1e30f, -1e30f, __int_as_float(-2)); }
+
+// Store v at p when q, as a predicated store: the warp takes no branch for it.  (No memory
+// clobber: the list build never reads what it stores.)
+__device__ __forceinline__ void stPred(bool q, int *p, int v) {
+  asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %0, 0;\n\t@q st.global.u32 [%1], %2;\n\t}" ::"r"((unsigned)q),
+               "l"(p), "r"(v));
+}
+
+// U home atoms (a0 .. a0+U-1 of the warp's sHome) against this lane's candidate: the hit and
 // close masks of each.  SHIFTED: the word holds a periodic image or the home cell, so the
 // shift is subtracted and the self pair left out.
-template <bool SHIFTED>
-__device__ __forceinline__ void nebrTest4(const float4 *sHome, int a0, int nh, float bx, float by, float bz, float sx,
-                                          float sy, float sz, int k, float rrNebr, float rrShort, unsigned (&mh)[4],
-                                          unsigned (&mc)[4], int (&gh)[4]) {
+template <int U, bool SHIFTED>
+__device__ __forceinline__ void nebrTest(const float4 *sHome, int a0, float bx, float by, float bz, float sx, float sy,
+                                         float sz, int k, float rrNebr, float rrShort, unsigned (&mh)[U],
+                                         unsigned (&mc)[U], int (&gh)[U]) {
   const unsigned full = 0xffffffffu;
 #pragma unroll
-  for (int u = 0; u < 4; u++) {
+  for (int u = 0; u < U; u++) {
     const float4 H = sHome[a0 + u];
     gh[u] = __float_as_int(H.w);
     float dx = H.x - bx, dy = H.y - by, dz = H.z - bz;
-    bool hit;
-    float rr;
     if (SHIFTED) {
       // the reference subtracts the cell shift after the difference: both roundings kept
       dx = dx - sx;
       dy = dy - sy;
       dz = dz - sz;
-      rr = sqDist(dx, dy, dz);
-      hit = (rr < rrNebr) && (gh[u] != k);
-    } else {
-      rr = sqDist(dx, dy, dz);
-      hit = rr < rrNebr;
     }
-    mh[u] = __ballot_sync(full, hit && a0 + u < nh);
+    const float rr = sqDist(dx, dy, dz);
+    mh[u] = __ballot_sync(full, (rr < rrNebr) && (!SHIFTED || gh[u] != k));
     mc[u] = __ballot_sync(full, rr < rrShort);
   }
+}
+
+// Where a work item's lists go.
+struct NebrOut {
+  int *nbl, *sl;
+  unsigned *rl;
+  int rowStride, nebrMax, metalEnd, atomOff;
+  float rrNebr, rrShort;
+};
+
+// Test and store for U home atoms a0 .. a0+U-1 and this lane's candidate k (metalW: the word's
+// metal candidates); nMy, mMy, rMy are the running lengths of home atom `lane`.
+template <int U, bool SHIFTED>
+__device__ __forceinline__ void nebrGroup(const float4 *sHome, int a0, int lane, float bx, float by, float bz, float sx,
+                                          float sy, float sz, int k, unsigned metalW, const NebrOut &O, int &nMy,
+                                          int &mMy, int &rMy) {
+  const unsigned full = 0xffffffffu, lower = (1u << lane) - 1u;
+  unsigned mh[U], mc[U];
+  int gh[U];
+  nebrTest<U, SHIFTED>(sHome, a0, bx, by, bz, sx, sy, sz, k, O.rrNebr, O.rrShort, mh, mc, gh);
+#pragma unroll
+  for (int u = 0; u < U; u++) {
+    const unsigned h = mh[u];
+    if (h == 0u) continue;  // warp-uniform: no entry for this home atom in this word
+    const int a = a0 + u, g = gh[u];
+    const int j = __shfl_sync(full, nMy, a) + __popc(h & lower);
+    stPred(((h >> lane) & 1u) && j < O.nebrMax, O.nbl + (size_t)g * O.rowStride + j, k);
+    if (g >= O.metalEnd) {
+      const unsigned cl = h & mc[u], rv = h & (mc[u] | metalW);
+      if (rv != 0u) {
+        const int jm = __shfl_sync(full, mMy, a) + __popc(cl & lower);
+        const int jr = __shfl_sync(full, rMy, a) + __popc(rv & lower);
+        stPred(((cl >> lane) & 1u) && jm < kShortMax, O.sl + (size_t)g * kShortMax + jm, k);
+        stPred(((rv >> lane) & 1u) && jr < kRelMax, reinterpret_cast<int *>(O.rl + (size_t)g * kRelMax + jr),
+               (int)relPack(k - O.atomOff, j));
+        if (lane == a) {
+          mMy += __popc(cl);
+          rMy += __popc(rv);
+        }
+      }
+    }
+    if (lane == a) nMy += __popc(h);
+  }
+}
+
+template <int U>
+__device__ __forceinline__ void nebrGroupAny(bool shifted, const float4 *sHome, int a0, int lane, float bx, float by,
+                                             float bz, float sx, float sy, float sz, int k, unsigned metalW,
+                                             const NebrOut &O, int &nMy, int &mMy, int &rMy) {
+  if (shifted)
+    nebrGroup<U, true>(sHome, a0, lane, bx, by, bz, sx, sy, sz, k, metalW, O, nMy, mMy, rMy);
+  else
+    nebrGroup<U, false>(sHome, a0, lane, bx, by, bz, sx, sy, sz, k, metalW, O, nMy, mMy, rMy);
 }
 
 __device__ __forceinline__ void nebrFusedBody(const int *__restrict__ tileRep, const int *__restrict__ active,
@@ -390,23 +449,21 @@ __device__ __forceinline__ void nebrFusedBody(const int *__restrict__ tileRep, c
                                               int rowStride, int nebrMax, int descending) {
   __shared__ float4 sHome[kNebrWarps][32];
   __shared__ float4 sSh[kNebrWarps][27];
-  __shared__ int sQb[kNebrWarps][27], sOff[kNebrWarps][27];
+  __shared__ int sQb[kNebrWarps][27], sOff[kNebrWarps][32];
   const unsigned full = 0xffffffffu;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const unsigned lower = (1u << lane) - 1u;
   const int nLight = work[1], nHeavy = work[2];
   NebrItem it;
   while (nebrNextItem(work, nLight, nHeavy, heavy, active, tileRep, rc, cellStart, descending, lane, sSh[w], sQb[w],
                       sOff[w], it)) {
     const RepConst &P = rc[it.rep];
-    const int atomOff = P.atomOff, metalEnd = P.atomOff + P.nMolMe;
-    const float rrNebr = P.rrNebr, rrShort = P.rrShort;
+    const int metalEnd = P.atomOff + P.nMolMe;
+    const NebrOut O{nbl, sl, rl, rowStride, nebrMax, metalEnd, P.atomOff, P.rrNebr, P.rrShort};
     const int total = it.total, nw = (total + 31) >> 5;
     int want = 0, over = 0;
     for (int h0 = it.hFirst; h0 < it.hLast; h0 += 32) {
       const int nh = min(32, it.hLast - h0);
-      float4 Ah = make_float4(0.f, 0.f, 0.f, __int_as_float(-2));
-      if (lane < nh) Ah = sortPos[h0 + lane];
+      const float4 Ah = (lane < nh) ? sortPos[h0 + lane] : nebrNoHome();
       sHome[w][lane] = Ah;
       const int ga = __float_as_int(Ah.w);
       int nMy = 0, mMy = 0, rMy = 0;  // list, close-list and relevant-list lengths of home atom `lane`
@@ -436,38 +493,18 @@ __device__ __forceinline__ void nebrFusedBody(const int *__restrict__ tileRep, c
           shifted = sh.w != 0.f;
         }
         const unsigned metalW = __ballot_sync(full, k >= 0 && k < metalEnd);
-        const bool plainWord = !__any_sync(full, shifted) && 32 * i >= it.homeLen;
-        for (int a0 = 0; a0 < nh; a0 += 4) {
-          unsigned mh[4], mc[4];
-          int gh[4];
-          if (plainWord)
-            nebrTest4<false>(sHome[w], a0, nh, bx, by, bz, sx, sy, sz, k, rrNebr, rrShort, mh, mc, gh);
-          else
-            nebrTest4<true>(sHome[w], a0, nh, bx, by, bz, sx, sy, sz, k, rrNebr, rrShort, mh, mc, gh);
-#pragma unroll
-          for (int u = 0; u < 4; u++) {
-            const unsigned h = mh[u];
-            if (h == 0u) continue;  // warp-uniform
-            const int a = a0 + u, g = gh[u];
-            const int n = __shfl_sync(full, nMy, a);
-            const int j = n + __popc(h & lower);
-            if (((h >> lane) & 1u) && j < nebrMax) nbl[(size_t)g * rowStride + j] = k;
-            if (g >= metalEnd) {
-              const unsigned cl = h & mc[u], rv = h & (mc[u] | metalW);
-              if (rv != 0u) {
-                const int m = __shfl_sync(full, mMy, a), r = __shfl_sync(full, rMy, a);
-                const int jm = m + __popc(cl & lower), jr = r + __popc(rv & lower);
-                if (((cl >> lane) & 1u) && jm < kShortMax) sl[(size_t)g * kShortMax + jm] = k;
-                if (((rv >> lane) & 1u) && jr < kRelMax) rl[(size_t)g * kRelMax + jr] = relPack(k - atomOff, j);
-                if (lane == a) {
-                  mMy += __popc(cl);
-                  rMy += __popc(rv);
-                }
-              }
-            }
-            if (lane == a) nMy += __popc(h);
-          }
-        }
+        const bool shiftWord = __any_sync(full, shifted) || 32 * i < it.homeLen;
+        int a0 = 0;
+        for (; a0 + 4 <= nh; a0 += 4)
+          nebrGroupAny<4>(shiftWord, sHome[w], a0, lane, bx, by, bz, sx, sy, sz, k, metalW, O, nMy, mMy, rMy);
+        // the last one to three home atoms: a group of their size (one of four for three)
+        const int rest = nh - a0;
+        if (rest >= 3)
+          nebrGroupAny<4>(shiftWord, sHome[w], a0, lane, bx, by, bz, sx, sy, sz, k, metalW, O, nMy, mMy, rMy);
+        else if (rest == 2)
+          nebrGroupAny<2>(shiftWord, sHome[w], a0, lane, bx, by, bz, sx, sy, sz, k, metalW, O, nMy, mMy, rMy);
+        else if (rest == 1)
+          nebrGroupAny<1>(shiftWord, sHome[w], a0, lane, bx, by, bz, sx, sy, sz, k, metalW, O, nMy, mMy, rMy);
       }
       nebrFinishHome(lane, nh, ga, nMy, mMy, rMy, metalEnd, nebrMax, nn, ns, nrl, want, over);
       __syncwarp();
@@ -488,7 +525,7 @@ __device__ __forceinline__ void nebrLanesBody(const int *__restrict__ tileRep, c
   __shared__ unsigned sMetal[kNebrWarps][kWin / 32];   // [word]: candidate is a metal atom
   __shared__ float4 sHome[kNebrWarps][32];
   __shared__ float4 sSh[kNebrWarps][27];
-  __shared__ int sQb[kNebrWarps][27], sOff[kNebrWarps][27];
+  __shared__ int sQb[kNebrWarps][27], sOff[kNebrWarps][32];
   const unsigned full = 0xffffffffu;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nLight = work[1], nHeavy = work[2];
@@ -502,8 +539,7 @@ __device__ __forceinline__ void nebrLanesBody(const int *__restrict__ tileRep, c
     int want = 0, over = 0;
     for (int h0 = it.hFirst; h0 < it.hLast; h0 += 32) {
       const int nh = min(32, it.hLast - h0);
-      float4 Ah = make_float4(0.f, 0.f, 0.f, __int_as_float(-2));
-      if (lane < nh) Ah = sortPos[h0 + lane];
+      const float4 Ah = (lane < nh) ? sortPos[h0 + lane] : nebrNoHome();
       sHome[w][lane] = Ah;
       const int ga = __float_as_int(Ah.w);
       int nMy = 0, mMy = 0, rMy = 0;  // list, close-list and relevant-list lengths of home atom `lane`
@@ -540,9 +576,9 @@ __device__ __forceinline__ void nebrLanesBody(const int *__restrict__ tileRep, c
             unsigned mh[4], mc[4];
             int gh[4];
             if (plainWord)
-              nebrTest4<false>(sHome[w], a0, nh, bx, by, bz, sx, sy, sz, k, rrNebr, rrShort, mh, mc, gh);
+              nebrTest<4, false>(sHome[w], a0, bx, by, bz, sx, sy, sz, k, rrNebr, rrShort, mh, mc, gh);
             else
-              nebrTest4<true>(sHome[w], a0, nh, bx, by, bz, sx, sy, sz, k, rrNebr, rrShort, mh, mc, gh);
+              nebrTest<4, true>(sHome[w], a0, bx, by, bz, sx, sy, sz, k, rrNebr, rrShort, mh, mc, gh);
 #pragma unroll
             for (int u = 0; u < 4; u++)
               if (a0 + u < nh) sMask[w][i][a0 + u] = make_uint2(mh[u], mc[u]);
