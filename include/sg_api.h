@@ -129,7 +129,10 @@ int sg_num_atoms(const sg_ctx *ctx, int rep);
 /* Upload / download state of one replica (rep >= 0) or of all replicas concatenated
  * (rep == -1).  Any pointer may be NULL to skip that array.  Layouts as the reference's
  * host arrays hr/hv/ha (SurfaceGrowth.cpp:95-96).  A download first applies a pending
- * thermostat rescale, so it returns exactly the reference's end-of-step velocities. */
+ * thermostat rescale, so it returns exactly the reference's end-of-step velocities.  An upload
+ * reads the host arrays in place from the device where it can (any host memory on a device
+ * that reads through the host's page tables, as a GB300 on NVLink-C2C; page-locked memory
+ * elsewhere) and copies them first otherwise; it has finished with them when the call returns. */
 int sg_set_state(sg_ctx *ctx, int rep, const sg_float4 *r, const sg_float3 *v, const sg_float3 *a);
 int sg_get_state(sg_ctx *ctx, int rep, sg_float4 *r, sg_float3 *v, sg_float3 *a);
 

@@ -36,6 +36,7 @@ constexpr int kMT = 16;           // lanes per metal atom in the density and met
 constexpr int kCT = 4;            // lanes per carbon atom in the carbon-force pass
 constexpr int kNebrWarps = 4;     // warps per block in the neighbour-list build (one home cell each)
 constexpr int kWin = 512;         // candidates per shared-memory window of the list build
+constexpr int kFusedWin = 256;    // candidates per window pass of the fused list build
 constexpr int kRelMax = 48;       // relevant-list capacity per carbon atom
 constexpr int kShortMax = 8;      // close-list capacity per carbon atom (a multiple of 4)
 constexpr int kRelPosLimit = 256; // relevant-list entries record list positions below this
@@ -160,13 +161,11 @@ struct DiffLayout {
   }
 };
 
-// Offsets of the 27 neighbour cells in the reference's visiting order
-// (SurfaceGrowthConsole/ComputeDefs.h:221-231), packed as (dx+1) + 3(dy+1) + 9(dz+1).
-__device__ __constant__ static const signed char kOff27[27][3] = {
-    {0, 0, 0},  {0, 0, 1},  {0, 0, -1},  {0, 1, 0},  {0, 1, 1},  {0, 1, -1},  {0, -1, 0},
-    {0, -1, 1}, {0, -1, -1}, {1, 0, 0},  {1, 0, 1},  {1, 0, -1}, {1, 1, 0},   {1, 1, 1},
-    {1, 1, -1}, {1, -1, 0}, {1, -1, 1},  {1, -1, -1}, {-1, 0, 0}, {-1, 0, 1}, {-1, 0, -1},
-    {-1, 1, 0}, {-1, 1, 1}, {-1, 1, -1}, {-1, -1, 0}, {-1, -1, 1}, {-1, -1, -1}};
+// Offset of stencil cell o (0..26) in the reference's visiting order
+// (SurfaceGrowthConsole/ComputeDefs.h:221-231): x outermost, then y, then z, each in the order
+// 0, +1, -1.  Computed rather than read from a table: the lanes of a warp look up different
+// cells at once, which a constant-memory table would serialise.
+__device__ __forceinline__ int stencilStep(int i) { return i == 2 ? -1 : i; }
 
 // Neighbour cell of local cell c at stencil offset o with the periodic shift
 // (BuildNebrListK, SurfaceGrowth.cu:641-674).
@@ -175,7 +174,7 @@ __device__ __forceinline__ int stencilCell(const RepConst &P, int c, int o, floa
   int ccz = c / (P.cells[0] * P.cells[1]);
   int ccy = (c - ccz * P.cells[0] * P.cells[1]) / P.cells[0];
   int ccx = c - (ccz * P.cells[1] + ccy) * P.cells[0];
-  int mx = ccx + kOff27[o][0], my = ccy + kOff27[o][1], mz = ccz + kOff27[o][2];
+  int mx = ccx + stencilStep(o / 9), my = ccy + stencilStep((o / 3) % 3), mz = ccz + stencilStep(o % 3);
   sx = 0.f; sy = 0.f; sz = 0.f;
   if (mx >= P.cells[0]) { mx = 0; sx = P.region[0]; }
   else if (mx < 0) { mx = P.cells[0] - 1; sx = -P.region[0]; }

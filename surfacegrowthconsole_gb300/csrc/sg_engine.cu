@@ -295,6 +295,13 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
   // list build: one warp per home cell, a grid of a few resident blocks per SM walking the cells
   c->numSMs = numSMs;
   c->pdl = c->opt.programmatic_launch != 0;
+  {
+    int pageable = 0, hostTables = 0;
+    cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, c->opt.device);
+    cudaDeviceGetAttribute(&hostTables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, c->opt.device);
+    // (pageable access without the host's page tables migrates pages on first touch: not used)
+    c->hostDirect = pageable == 1 && hostTables == 1;
+  }
   if (c->opt.persistent_step) {
     if (c->opt.mode != SG_MODE_MIXED) {
       sg_destroy(c);
@@ -586,17 +593,30 @@ static const void *mappedHost(const void *h) {
   return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
 }
 
-// A state upload, enqueued.  Host arrays in page-locked memory are read in place by one kernel
-// (over the host link, without a copy-engine transfer per array); others are copied first, r
-// straight into pos, v and a into the staging buffer.  The same kernel unpacks v and a to
-// float4, clears the low position words and cancels any thermostat rescale still pending from
-// the previous step.  The host arrays must stay valid until the stream has passed the kernel.
+// A state upload, enqueued.  Where the device reads host memory through the host's page tables
+// (a GB300 on NVLink-C2C), the host arrays are read in place by one kernel whatever their
+// allocation: no pointer queries, no copy-engine transfer (a kernel reads the 1.82 MB of a
+// 45,546-atom state in 13.7 us from pageable memory, 13.5 us from page-locked memory).
+// Elsewhere page-locked arrays are read in place and others are copied first, r straight into
+// pos, v and a into the staging buffer.  The same kernel unpacks v and a to float4, clears the
+// low position words and cancels any thermostat rescale still pending from the previous step.
+// The host arrays must stay valid until the stream has passed the kernel.
 static int enqueueSetState(sg_ctx *c, int rep, const sg_float4 *r, const sg_float3 *v, const sg_float3 *a) {
   int off, n, rc;
   if ((rc = repRange(c, rep, off, n))) return rc;
-  const float4 *sr = static_cast<const float4 *>(mappedHost(r));
-  const float *sv = static_cast<const float *>(mappedHost(v));
-  const float *sa = static_cast<const float *>(mappedHost(a));
+  const float4 *sr;
+  const float *sv, *sa;
+  if (c->hostDirect) {
+    // read in place through the host's page tables; r as float4 rows only when 16-byte aligned
+    // (else copied first), v and a row by row at any 4-byte alignment
+    sr = (reinterpret_cast<uintptr_t>(r) & 15) == 0 ? reinterpret_cast<const float4 *>(r) : nullptr;
+    sv = reinterpret_cast<const float *>(v);
+    sa = reinterpret_cast<const float *>(a);
+  } else {
+    sr = static_cast<const float4 *>(mappedHost(r));
+    sv = static_cast<const float *>(mappedHost(v));
+    sa = static_cast<const float *>(mappedHost(a));
+  }
   if (r && !sr) CK(cudaMemcpyAsync(c->pos + off, r, (size_t)n * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
   if (v && !sv) {
     CK(cudaMemcpyAsync(c->stage, v, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, c->stream));

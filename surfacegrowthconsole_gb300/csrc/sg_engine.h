@@ -71,6 +71,10 @@ struct sg_ctx {
   int nebrAlgo = 0;
   bool eamStaged = false;  // MIXED: metal passes with the EAM table staged in shared memory
   bool pdl = false;  // programmatic dependent launch between the kernels of a step
+  // the device reads any host memory through the host's page tables (address translation
+  // services, as over NVLink-C2C): state uploads read the caller's arrays in place, pageable
+  // or page-locked, with no pointer queries and no copies
+  bool hostDirect = false;
   int carbonBlocks = 8;  // carbon pass: resident blocks per SM of its register budget (8, 12, 16)
   // persistent step (MIXED): one cooperative launch per step, grid barriers between phases
   bool persistent = false;

@@ -703,6 +703,17 @@ __global__ void __launch_bounds__(kRedThreads) k_step_reduce(
     ops[s] = slotOp(s);
     x[s] = combine(ops[s], e0[s], e1[s]);
   }
+  // the replica's constants and state into shared memory for the step control of whichever
+  // block finishes last, loaded by every block before its tree (in this launch only the
+  // counter of the blocks changes, and the last block resets its copy)
+  __shared__ RepState sS;
+  __shared__ RepConst sP;
+  constToShared(&P, &sP);
+  {
+    const int *ss = reinterpret_cast<const int *>(S);
+    int *sd = reinterpret_cast<int *>(&sS);
+    for (int i = t; i < (int)(sizeof(RepState) / 4); i += kRedThreads) sd[i] = __ldcg(ss + i);
+  }
   __shared__ float sh[kNumRed][kRedThreads];
   blockTree512<kNumRed>(x, ops, sh);
   __shared__ bool last;
@@ -742,10 +753,6 @@ __global__ void __launch_bounds__(kRedThreads) k_step_reduce(
   float redv[kNumRed];
 #pragma unroll
   for (int s = 0; s < kNumRed; s++) redv[s] = red[s];
-  __shared__ RepState sS;
-  __shared__ RepConst sP;
-  constToShared(&P, &sP);
-  stateToShared(S, &sS);
   if (t == 0) sS.redCounter = 0;  // every block has counted in: ready for the next step
   stepControl(sP, &sS, redv, diffBuf ? diffBuf + diffOff[rep] : nullptr, forceRebuild);
   stateFromShared(&sS, S);
@@ -766,7 +773,10 @@ __device__ void stepControl(const RepConst &P, RepState *S, const float (&red)[k
   const int sc = S->stepCount + 1;
   __shared__ int diffDue, accumNb[16], printNow;
   __shared__ float cmc[3];
+  // the step's scalars in three independent parts, each on lane 0 of its own warp (no two of
+  // them write the same field); the property sums after them
   if (t == 0) {
+    // reduced values, metal centre of mass and its velocity, friction force, diffusion sample
 #pragma unroll
     for (int s = 0; s < kNumRed; s++) S->red[s] = red[s];
     diffDue = 0;
@@ -783,7 +793,9 @@ __device__ void stepControl(const RepConst &P, RepState *S, const float (&red)[k
     } else {
       S->cmVal = 0.f; S->cmVelVal = 0.f; S->frictVal = 0.f;
     }
-    const float vvMax = red[RS_VVMAX], vvSum = red[RS_VVSUM], uSum = red[RS_USUM];
+  } else if (t == 32) {
+    // thermostat decision and energies
+    const float vvSum = red[RS_VVSUM], uSum = red[RS_USUM];
     const bool thermo = ((P.iRegime == 2) && (sc > P.stepEquil) && (sc % P.stepThermostat == 0)) ||
                         ((P.iRegime == 1) && (sc % P.stepThermostat == 0));
     if (thermo) {
@@ -795,20 +807,23 @@ __device__ void stepControl(const RepConst &P, RepState *S, const float (&red)[k
     } else {
       S->thermoPending = 0;
     }
+    const float ke = 0.5f * vvSum / P.nMol, pe = uSum / P.nMol;
+    S->ke = ke;
+    S->pe = pe;
+    S->te = ke + pe;
+    S->ke64 = (double)ke;
+    S->pe64 = (double)pe;
+  } else if (t == 64) {
+    // rebuild criterion, shear drive schedule, deposition
     if (forceRebuild || S->nebrNow) {
       S->nebrNow = 0;
       S->dispHi = 0.f;
       S->rebuilds++;
     }
-    S->dispHi += sqrtf(vvMax) * P.deltaT;
+    S->dispHi += sqrtf(red[RS_VVMAX]) * P.deltaT;
     if (S->dispHi > 0.5f * P.rNebrShell) S->nebrNow = 1;
-    S->ke = 0.5f * vvSum / P.nMol;
-    S->pe = uSum / P.nMol;
-    S->te = S->ke + S->pe;
-    S->ke64 = (double)S->ke;
-    S->pe64 = (double)S->pe;
     if (P.iRegime == 2 && P.nMolMe != 0 && sc > P.stepEquil + P.stepCool) {
-      if (S->cmVelVal < 0.005f) S->shear += P.deltaF;
+      if (S->cmVel[0] / P.nMolMe < 0.005f) S->shear += P.deltaF;  // cmVelVal
       S->shearCount = 0;
     }
     if (P.iRegime == 1) {
@@ -817,26 +832,33 @@ __device__ void stepControl(const RepConst &P, RepState *S, const float (&red)[k
       depositionPlan(P, *S, sc, nDep, nTo, act);
       if (act) S->nMolDeposited = nDep + nTo;
     }
-    // AccumProps(1) for every property but oneStep (host-side)
-    const float vals[7] = {S->te, S->pe, S->ke, 0.f, S->cmVal, S->cmVelVal, S->frictVal};
-#pragma unroll
-    for (int p = 0; p < 7; p++) {
-      if (p == 3) continue;
-      S->props[p][0] = vals[p];
-      S->props[p][1] += vals[p];
-      S->props[p][2] += vals[p] * vals[p];
-    }
+  }
+  __syncthreads();
+  // AccumProps(1) for every property but oneStep (host-side); the stepAvg snapshot
+  if (t < 7 && t != 3) {
+    const float val = (t == 0) ? S->te : (t == 1) ? S->pe : (t == 2) ? S->ke : (t == 4) ? S->cmVal
+                    : (t == 5) ? S->cmVelVal : S->frictVal;
+    S->props[t][0] = val;
+    const float s1 = S->props[t][1] + val, s2 = S->props[t][2] + val * val;
     if (sc % P.stepAvg == 0) {
-#pragma unroll
-      for (int p = 0; p < 7; p++) {
-        S->propsSnap[p][0] = S->props[p][0];
-        S->propsSnap[p][1] = S->props[p][1];
-        S->propsSnap[p][2] = S->props[p][2];
-        S->props[p][1] = 0.f;
-        S->props[p][2] = 0.f;
-      }
-      S->snapStep = sc;
+      S->propsSnap[t][0] = val;
+      S->propsSnap[t][1] = s1;
+      S->propsSnap[t][2] = s2;
+      S->props[t][1] = 0.f;
+      S->props[t][2] = 0.f;
+    } else {
+      S->props[t][1] = s1;
+      S->props[t][2] = s2;
     }
+  } else if (t == 3 && sc % P.stepAvg == 0) {
+    S->propsSnap[3][0] = S->props[3][0];
+    S->propsSnap[3][1] = S->props[3][1];
+    S->propsSnap[3][2] = S->props[3][2];
+    S->props[3][1] = 0.f;
+    S->props[3][2] = 0.f;
+  }
+  if (t == 32) {
+    if (sc % P.stepAvg == 0) S->snapStep = sc;
     S->stepCount = sc;
   }
   __syncthreads();

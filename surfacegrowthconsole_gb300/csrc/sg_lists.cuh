@@ -395,12 +395,13 @@ struct NebrOut {
   float rrNebr, rrShort;
 };
 
-// Test and store for U home atoms a0 .. a0+U-1 and this lane's candidate k (metalW: the word's
-// metal candidates); nMy, mMy, rMy are the running lengths of home atom `lane`.
+// Test U home atoms (a0 .. a0+U-1) against this lane's candidate k of word i, keep the hit and
+// close masks for the close and relevant lists (sMask[i][a]), and store the hits in the rows
+// at once; nMy is the running full-list length of home atom `lane`.
 template <int U, bool SHIFTED>
-__device__ __forceinline__ void nebrGroup(const float4 *sHome, int a0, int lane, float bx, float by, float bz, float sx,
-                                          float sy, float sz, int k, unsigned metalW, const NebrOut &O, int &nMy,
-                                          int &mMy, int &rMy) {
+__device__ __forceinline__ void nebrGroup(const float4 *sHome, uint2 (*sMask)[32], int i, int a0, int lane, float bx,
+                                          float by, float bz, float sx, float sy, float sz, int k,
+                                          const NebrOut &O, int &nMy) {
   const unsigned full = 0xffffffffu, lower = (1u << lane) - 1u;
   unsigned mh[U], mc[U];
   int gh[U];
@@ -408,36 +409,56 @@ __device__ __forceinline__ void nebrGroup(const float4 *sHome, int a0, int lane,
 #pragma unroll
   for (int u = 0; u < U; u++) {
     const unsigned h = mh[u];
+    sMask[i][a0 + u] = make_uint2(h, mc[u]);  // the same value from every lane: no branch
     if (h == 0u) continue;  // warp-uniform: no entry for this home atom in this word
-    const int a = a0 + u, g = gh[u];
+    const int a = a0 + u;
     const int j = __shfl_sync(full, nMy, a) + __popc(h & lower);
-    stPred(((h >> lane) & 1u) && j < O.nebrMax, O.nbl + (size_t)g * O.rowStride + j, k);
-    if (g >= O.metalEnd) {
-      const unsigned cl = h & mc[u], rv = h & (mc[u] | metalW);
-      if (rv != 0u) {
-        const int jm = __shfl_sync(full, mMy, a) + __popc(cl & lower);
-        const int jr = __shfl_sync(full, rMy, a) + __popc(rv & lower);
-        stPred(((cl >> lane) & 1u) && jm < kShortMax, O.sl + (size_t)g * kShortMax + jm, k);
-        stPred(((rv >> lane) & 1u) && jr < kRelMax, reinterpret_cast<int *>(O.rl + (size_t)g * kRelMax + jr),
-               (int)relPack(k - O.atomOff, j));
-        if (lane == a) {
-          mMy += __popc(cl);
-          rMy += __popc(rv);
-        }
-      }
-    }
+    stPred(((h >> lane) & 1u) && j < O.nebrMax, O.nbl + (size_t)gh[u] * O.rowStride + j, k);
     if (lane == a) nMy += __popc(h);
   }
 }
 
 template <int U>
-__device__ __forceinline__ void nebrGroupAny(bool shifted, const float4 *sHome, int a0, int lane, float bx, float by,
-                                             float bz, float sx, float sy, float sz, int k, unsigned metalW,
-                                             const NebrOut &O, int &nMy, int &mMy, int &rMy) {
+__device__ __forceinline__ void nebrGroupAny(bool shifted, const float4 *sHome, uint2 (*sMask)[32], int i, int a0,
+                                             int lane, float bx, float by, float bz, float sx, float sy, float sz,
+                                             int k, const NebrOut &O, int &nMy) {
   if (shifted)
-    nebrGroup<U, true>(sHome, a0, lane, bx, by, bz, sx, sy, sz, k, metalW, O, nMy, mMy, rMy);
+    nebrGroup<U, true>(sHome, sMask, i, a0, lane, bx, by, bz, sx, sy, sz, k, O, nMy);
   else
-    nebrGroup<U, false>(sHome, a0, lane, bx, by, bz, sx, sy, sz, k, metalW, O, nMy, mMy, rMy);
+    nebrGroup<U, false>(sHome, sMask, i, a0, lane, bx, by, bz, sx, sy, sz, k, O, nMy);
+}
+
+// The close and relevant lists of the carbon home atoms for the window pass just tested (nw
+// words, masks in sMask, atom indices in sK, metal candidates in sMetal): the lane of each
+// carbon home atom walks the close and relevant bits of its words (few: a carbon atom has three
+// close neighbours and metal ones only near a cluster); nPass is its full-list length before
+// the pass (the entries' positions), mMy and rMy its running close- and relevant-list lengths.
+__device__ __forceinline__ void nebrCarbonLists(const uint2 (*sMask)[32], const int *sK, const unsigned *sMetal, int nw,
+                                                int nh, int lane, int ga, int nPass, const NebrOut &O, int &mMy,
+                                                int &rMy) {
+  if (lane >= nh || ga < O.metalEnd) return;
+  int n = nPass, m = mMy, r = rMy;
+  int *srow = O.sl + (size_t)ga * kShortMax;
+  unsigned *rrow = O.rl + (size_t)ga * kRelMax;
+  for (int i = 0; i < nw; i++) {
+    const uint2 hc = sMask[i][lane];
+    unsigned bits = hc.x & (hc.y | sMetal[i]);
+    while (bits) {
+      const int b = __ffs(bits) - 1;
+      bits &= bits - 1;
+      const int k = sK[32 * i + b];
+      if ((hc.y >> b) & 1u) {
+        if (m < kShortMax) srow[m] = k;
+        m++;
+      }
+      // its position in the full list
+      if (r < kRelMax) rrow[r] = relPack(k - O.atomOff, n + __popc(hc.x & ((1u << b) - 1u)));
+      r++;
+    }
+    n += __popc(hc.x);
+  }
+  mMy = m;
+  rMy = r;
 }
 
 __device__ __forceinline__ void nebrFusedBody(const int *__restrict__ tileRep, const int *__restrict__ active,
@@ -447,6 +468,9 @@ __device__ __forceinline__ void nebrFusedBody(const int *__restrict__ tileRep, c
                                               int *__restrict__ nn, int *__restrict__ nbl, int *__restrict__ ns,
                                               int *__restrict__ sl, int *__restrict__ nrl, unsigned *__restrict__ rl,
                                               int rowStride, int nebrMax, int descending) {
+  __shared__ int sK[kNebrWarps][kFusedWin];                  // atom index of each window position
+  __shared__ uint2 sMask[kNebrWarps][kFusedWin / 32][32];    // [word][home atom]: {hit, close}
+  __shared__ unsigned sMetal[kNebrWarps][kFusedWin / 32];    // [word]: candidate is a metal atom
   __shared__ float4 sHome[kNebrWarps][32];
   __shared__ float4 sSh[kNebrWarps][27];
   __shared__ int sQb[kNebrWarps][27], sOff[kNebrWarps][32];
@@ -459,52 +483,64 @@ __device__ __forceinline__ void nebrFusedBody(const int *__restrict__ tileRep, c
     const RepConst &P = rc[it.rep];
     const int metalEnd = P.atomOff + P.nMolMe;
     const NebrOut O{nbl, sl, rl, rowStride, nebrMax, metalEnd, P.atomOff, P.rrNebr, P.rrShort};
-    const int total = it.total, nw = (total + 31) >> 5;
+    const int total = it.total;
     int want = 0, over = 0;
     for (int h0 = it.hFirst; h0 < it.hLast; h0 += 32) {
       const int nh = min(32, it.hLast - h0);
       const float4 Ah = (lane < nh) ? sortPos[h0 + lane] : nebrNoHome();
       sHome[w][lane] = Ah;
       const int ga = __float_as_int(Ah.w);
+      const bool carbonHomes = __any_sync(full, lane < nh && ga >= metalEnd);
       int nMy = 0, mMy = 0, rMy = 0;  // list, close-list and relevant-list lengths of home atom `lane`
       __syncwarp();
-      // this lane's candidate of the next word, loaded while the current word is tested
-      int oN = 0;
-      float4 BN = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (lane < total) BN = nebrCandidate(sortPos, sQb[w], sOff[w], lane, oN);
-      for (int i = 0; i < nw; i++) {
-        const int e = 32 * i + lane;
-        const int o = oN;
-        const float4 B = BN;
-        if (e + 32 < total) BN = nebrCandidate(sortPos, sQb[w], sOff[w], e + 32, oN);
-        // this lane's candidate; past the window end it sits at 1e30 and never matches
-        float bx = 1e30f, by = 1e30f, bz = 1e30f, sx = 0.f, sy = 0.f, sz = 0.f;
-        int k = -1;
-        bool shifted = false;
-        if (e < total) {
-          k = __float_as_int(B.w);
-          bx = B.x;
-          by = B.y;
-          bz = B.z;
-          const float4 sh = sSh[w][o];
-          sx = sh.x;
-          sy = sh.y;
-          sz = sh.z;
-          shifted = sh.w != 0.f;
+      for (int base = 0; base < total; base += kFusedWin) {
+        const int nw = (min(kFusedWin, total - base) + 31) >> 5;
+        const int nPass = nMy;
+        // this lane's candidate of the next word, loaded while the current word is tested
+        int oN = 0;
+        float4 BN = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (base + lane < total) BN = nebrCandidate(sortPos, sQb[w], sOff[w], base + lane, oN);
+        for (int i = 0; i < nw; i++) {
+          const int e = base + 32 * i + lane;
+          const int o = oN;
+          const float4 B = BN;
+          if (i + 1 < nw && e + 32 < total) BN = nebrCandidate(sortPos, sQb[w], sOff[w], e + 32, oN);
+          // this lane's candidate; past the window end it sits at 1e30 and never matches
+          float bx = 1e30f, by = 1e30f, bz = 1e30f, sx = 0.f, sy = 0.f, sz = 0.f;
+          int k = -1;
+          bool shifted = false;
+          if (e < total) {
+            k = __float_as_int(B.w);
+            bx = B.x;
+            by = B.y;
+            bz = B.z;
+            const float4 sh = sSh[w][o];
+            sx = sh.x;
+            sy = sh.y;
+            sz = sh.z;
+            shifted = sh.w != 0.f;
+          }
+          if (carbonHomes) {
+            sK[w][32 * i + lane] = k;
+            const unsigned metalW = __ballot_sync(full, k >= 0 && k < metalEnd);
+            if (lane == 0) sMetal[w][i] = metalW;
+          }
+          const bool shiftWord = __any_sync(full, shifted) || base + 32 * i < it.homeLen;
+          int a0 = 0;
+          for (; a0 + 4 <= nh; a0 += 4)
+            nebrGroupAny<4>(shiftWord, sHome[w], sMask[w], i, a0, lane, bx, by, bz, sx, sy, sz, k, O, nMy);
+          // the last one to three home atoms: a group of their size (one of four for three)
+          const int rest = nh - a0;
+          if (rest >= 3)
+            nebrGroupAny<4>(shiftWord, sHome[w], sMask[w], i, a0, lane, bx, by, bz, sx, sy, sz, k, O, nMy);
+          else if (rest == 2)
+            nebrGroupAny<2>(shiftWord, sHome[w], sMask[w], i, a0, lane, bx, by, bz, sx, sy, sz, k, O, nMy);
+          else if (rest == 1)
+            nebrGroupAny<1>(shiftWord, sHome[w], sMask[w], i, a0, lane, bx, by, bz, sx, sy, sz, k, O, nMy);
         }
-        const unsigned metalW = __ballot_sync(full, k >= 0 && k < metalEnd);
-        const bool shiftWord = __any_sync(full, shifted) || 32 * i < it.homeLen;
-        int a0 = 0;
-        for (; a0 + 4 <= nh; a0 += 4)
-          nebrGroupAny<4>(shiftWord, sHome[w], a0, lane, bx, by, bz, sx, sy, sz, k, metalW, O, nMy, mMy, rMy);
-        // the last one to three home atoms: a group of their size (one of four for three)
-        const int rest = nh - a0;
-        if (rest >= 3)
-          nebrGroupAny<4>(shiftWord, sHome[w], a0, lane, bx, by, bz, sx, sy, sz, k, metalW, O, nMy, mMy, rMy);
-        else if (rest == 2)
-          nebrGroupAny<2>(shiftWord, sHome[w], a0, lane, bx, by, bz, sx, sy, sz, k, metalW, O, nMy, mMy, rMy);
-        else if (rest == 1)
-          nebrGroupAny<1>(shiftWord, sHome[w], a0, lane, bx, by, bz, sx, sy, sz, k, metalW, O, nMy, mMy, rMy);
+        __syncwarp();
+        if (carbonHomes) nebrCarbonLists(sMask[w], sK[w], sMetal[w], nw, nh, lane, ga, nPass, O, mMy, rMy);
+        __syncwarp();
       }
       nebrFinishHome(lane, nh, ga, nMy, mMy, rMy, metalEnd, nebrMax, nn, ns, nrl, want, over);
       __syncwarp();

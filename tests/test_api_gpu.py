@@ -163,3 +163,31 @@ def test_page_locked_block_equals_pageable_arrays(mode):
         assert np.array_equal(x, y)
     one.close()
     two.close()
+
+
+@pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_MIXED])
+def test_upload_from_unaligned_pageable_arrays(mode):
+    """r, v and a at 4-byte offsets inside one pageable buffer (r not on a 16-byte boundary)
+    upload exactly, and a step from them equals one from aligned copies."""
+    p, r, v = workloads.small(seed=67)
+    n = p.nMol
+    a = np.random.RandomState(7).normal(size=(n, 3)).astype(np.float32)
+    buf = np.zeros(10 * n + 3, np.float32)
+    hr = buf[1:1 + 4 * n].reshape(n, 4)
+    hv = buf[2 + 4 * n:2 + 7 * n].reshape(n, 3)
+    ha = buf[3 + 7 * n:3 + 10 * n].reshape(n, 3)
+    hr[:], hv[:], ha[:] = r, v, a
+    assert hr.ctypes.data % 16 != 0
+    sim = Simulation(p, mode=mode)
+    sim.set_state(hr, hv, ha)
+    for x, y in zip(sim.get_state(), (r, v, a)):
+        assert np.array_equal(x, y)
+    t1 = sim.step_from_host(hr, hv, ha, nsteps=2)
+    ref = Simulation(p, mode=mode)
+    ref.set_state(r.copy(), v.copy(), a.copy())
+    ref.step(2)
+    _same_thermo(t1, ref.thermo())
+    for x, y in zip(sim.get_state(), ref.get_state()):
+        assert np.array_equal(x, y)
+    sim.close()
+    ref.close()
