@@ -233,20 +233,12 @@ __device__ __forceinline__ float minImg(float d, float L) {
   return d;
 }
 
-// The step control of a replica runs in the last block of its reduction: it copies the replica's
-// RepState into shared memory with all threads, works on that copy (its single-thread scalar
-// code then sees shared-memory latency instead of L2 latency) and writes it back.  No other
-// kernel touches the state meanwhile: the reduction is the only kernel of the step running.
+// The step control of a replica runs in the last block of its reduction on shared-memory copies
+// of the replica's RepState and RepConst (its scalar code then sees shared-memory latency instead
+// of L2 latency), which every reduction block loads while it reduces (nothing writes the state
+// before the last block has arrived; the reduction is the only kernel of the step running), and
+// writes the state back.
 static_assert(sizeof(RepState) % 4 == 0, "RepState is copied as 32-bit words");
-__device__ __forceinline__ void stateToShared(const RepState *g, RepState *s) {
-  const int *src = reinterpret_cast<const int *>(g);
-  int *dst = reinterpret_cast<int *>(s);
-  for (int i = threadIdx.x; i < (int)(sizeof(RepState) / 4); i += blockDim.x) dst[i] = __ldcg(src + i);
-  __syncthreads();
-}
-// The same for the replica's constants, which the step control's single thread reads field by
-// field (from shared memory each read costs tens of cycles instead of an L2 round trip); the
-// copy and the state's share one barrier when this runs first.
 static_assert(sizeof(RepConst) % 4 == 0, "RepConst is copied as 32-bit words");
 __device__ __forceinline__ void constToShared(const RepConst *g, RepConst *s) {
   const int *src = reinterpret_cast<const int *>(g);
