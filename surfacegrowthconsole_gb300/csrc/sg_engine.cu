@@ -665,7 +665,7 @@ extern "C" int sg_get_state(sg_ctx *c, int rep, sg_float4 *r, sg_float3 *v, sg_f
 }
 
 // ---- launch sequences ---------------------------------------------------------------------
-enum { V_SHEAR = 1, V_RDF = 2, V_RDF_ZERO = 4 };
+enum { V_SHEAR = 1, V_RDF = 2, V_RDF_ZERO = 4, G_FROM_HOST = 256 };  // graph keys: a step variant, | G_FROM_HOST
 
 #define LAUNCH_OK() CK(cudaGetLastError())
 
@@ -895,22 +895,20 @@ static int flagsFromMirror(sg_ctx *c) {
   return flags ? checkFlags(c) : SG_OK;
 }
 
-extern "C" int sg_step(sg_ctx *c, int nsteps) {
-  if (!c) return sg_fail(SG_ERR_INVALID, "null context");
-  for (int s = 0; s < nsteps; s++) {
-    const int v = stepVariant(c);
-    int rc = launchStep(c, v);
-    if (rc) return rc;
-    advanceSchedule(c, v, nullptr);
-  }
-  // the replica states come back to the page-locked mirror (flags, and sg_step_thermo's record),
-  // followed by a sequence number the host polls for: a stream synchronisation's wake-up costs
-  // more than this wait.  After 5 ms of polling (long batches of steps, or a failed launch) the
-  // host synchronises the stream instead, which also reports any error.
+// The replica states to the page-locked mirror (flags, and sg_step_thermo's record), followed by
+// a sequence number the host polls for (waitPublished).
+static int enqueuePublish(sg_ctx *c) {
   const int nwords = (int)(sizeof(RepState) * c->nrep / 4);
   k_publish_state<<<1, 256, 0, c->stream>>>(reinterpret_cast<const int *>(c->st), reinterpret_cast<int *>(c->hostSt),
                                             nwords, c->devSeq, c->hostSeq);
   CK(cudaGetLastError());
+  return SG_OK;
+}
+
+// The host's wait for the publish just enqueued: a stream synchronisation's wake-up costs more
+// than polling the sequence number.  After 5 ms of polling (long batches of steps, or a failed
+// launch) the host synchronises the stream instead, which also reports any error.
+static int waitPublished(sg_ctx *c) {
   const unsigned want = ++c->pubSeq;
   const auto t0 = std::chrono::steady_clock::now();
   bool seen = false;
@@ -933,6 +931,18 @@ extern "C" int sg_step(sg_ctx *c, int nsteps) {
   return flagsFromMirror(c);
 }
 
+extern "C" int sg_step(sg_ctx *c, int nsteps) {
+  if (!c) return sg_fail(SG_ERR_INVALID, "null context");
+  for (int s = 0; s < nsteps; s++) {
+    const int v = stepVariant(c);
+    int rc = launchStep(c, v);
+    if (rc) return rc;
+    advanceSchedule(c, v, nullptr);
+  }
+  const int rc = enqueuePublish(c);
+  return rc ? rc : waitPublished(c);
+}
+
 extern "C" long long sg_step_readback_bytes(const sg_ctx *c) {
   return c ? (long long)sizeof(RepState) * c->nrep : 0;
 }
@@ -945,11 +955,63 @@ extern "C" int sg_step_thermo(sg_ctx *c, int nsteps, int rep, sg_thermo *t) {
   return SG_OK;
 }
 
+// One step from host buffers as one graph launch: the upload kernel, the step's kernels and the
+// publish.  The graph holds the buffers' addresses only (the upload kernel reads them when it
+// runs, through the host's page tables), so calls with the same buffers -- a caller's loop --
+// replay it; other buffers replace the context's graphs of this kind.
+static int launchStepFromHost(sg_ctx *c, int rep, const sg_float4 *r, const sg_float3 *v, const sg_float3 *a,
+                              int variant) {
+  const HostBufs key{rep, r, v, a};
+  if (!(key == c->hostGraphBufs)) {
+    for (auto it = c->graphs.begin(); it != c->graphs.end();) {
+      if (it->first & G_FROM_HOST) {
+        cudaGraphExecDestroy(it->second);
+        it = c->graphs.erase(it);
+      } else {
+        ++it;
+      }
+    }
+    c->hostGraphBufs = key;
+  }
+  const int gk = variant | G_FROM_HOST;
+  auto it = c->graphs.find(gk);
+  if (it == c->graphs.end()) {
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueueSetState(c, rep, r, v, a);
+    if (!rc) rc = enqueueStep(c, variant);
+    if (!rc) rc = enqueuePublish(c);
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (rc) return rc;
+    if (e != cudaSuccess) return sg_fail(SG_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    cudaGraphExec_t ex;
+    e = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return sg_fail(SG_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    it = c->graphs.emplace(gk, ex).first;
+  }
+  CK(cudaGraphLaunch(it->second, c->stream));
+  c->lastVariant = variant;
+  return SG_OK;
+}
+
 extern "C" int sg_step_from_host(sg_ctx *c, int rep, const sg_float4 *r, const sg_float3 *v, const sg_float3 *a,
                                  int nsteps, int thermo_rep, sg_thermo *t) {
   if (!c || (t && (thermo_rep < 0 || thermo_rep >= c->nrep)) || nsteps < 0)
     return sg_fail(SG_ERR_INVALID, "sg_step_from_host: bad arguments");
-  int rc = enqueueSetState(c, rep, r, v, a);
+  int rc;
+  if (nsteps == 1 && c->hostDirect && c->opt.use_graphs && !c->persistent && r && v && a &&
+      (reinterpret_cast<uintptr_t>(r) & 15) == 0) {
+    int off, n;
+    if ((rc = repRange(c, rep, off, n))) return rc;
+    const int variant = stepVariant(c);
+    if ((rc = launchStepFromHost(c, rep, r, v, a, variant))) return rc;
+    advanceSchedule(c, variant, nullptr);
+    if ((rc = waitPublished(c))) return rc;
+    if (t) thermoFromState(c, thermo_rep, c->hostSt[thermo_rep], t);
+    return SG_OK;
+  }
+  rc = enqueueSetState(c, rep, r, v, a);
   if (rc) return rc;
   // the upload, the steps and the state records back in one synchronisation
   if ((rc = sg_step(c, nsteps))) return rc;

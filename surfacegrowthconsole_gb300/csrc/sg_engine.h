@@ -21,6 +21,15 @@ struct DevTab {
   BlockTab view() const { return BlockTab{rep, start, n}; }
 };
 
+// The host buffers a step-from-host graph reads (replica, r, v, a).
+struct HostBufs {
+  int rep = -2;
+  const void *r = nullptr, *v = nullptr, *a = nullptr;
+  HostBufs() = default;
+  HostBufs(int rep_, const void *r_, const void *v_, const void *a_) : rep(rep_), r(r_), v(v_), a(a_) {}
+  bool operator==(const HostBufs &o) const { return rep == o.rep && r == o.r && v == o.v && a == o.a; }
+};
+
 struct sg_ctx {
   int nrep = 0, ntot = 0, ctot = 0, nebrMax = 128, rowStride = 128, ntiles = 0;
   sg_options opt;
@@ -83,8 +92,9 @@ struct sg_ctx {
   long long persistWaitCycles = 0;  // longest barrier wait, SM clock cycles
   std::vector<std::pair<void *, size_t>> regions;  // every device buffer with its size
   int anyMetal = 0, anyCarbon = 0, maxHist = 0;
-  // graphs keyed by variant bits
+  // graphs keyed by variant bits (with G_FROM_HOST: upload from hostGraphBufs, step, publish)
   std::map<int, cudaGraphExec_t> graphs;
+  HostBufs hostGraphBufs;
   // host mirror of the schedule
   int stepCount = 0;
   int countRdf = 0;

@@ -191,3 +191,37 @@ def test_upload_from_unaligned_pageable_arrays(mode):
         assert np.array_equal(x, y)
     sim.close()
     ref.close()
+
+
+@pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_MIXED])
+def test_step_from_host_loop_on_the_same_buffers(mode):
+    """A caller's loop: the state refilled into the same buffers, one step from them, again --
+    the library replays one graph of upload, step and publish for the buffers (read when the
+    graph runs) -- equals set_state + step on another context, across an RDF step (a graph of
+    another step variant) and a switch to other buffers."""
+    p, r, v = workloads.small(seed=68)
+    n = p.nMol
+    a0 = np.zeros((n, 3), np.float32)
+    warm = 95  # RDF steps come every 100 steps
+    one = Simulation(p, mode=mode)
+    two = Simulation(p, mode=mode)
+    for s in (one, two):
+        s.set_state(r, v, a0)
+        s.step(warm)
+    hr, hv, ha = np.zeros((n, 4), np.float32), np.zeros((n, 3), np.float32), np.zeros((n, 3), np.float32)
+    for k in range(12):
+        if k == 8:  # other buffers from here on
+            hr, hv, ha = hr.copy(), hv.copy(), ha.copy()
+        st = one.get_state()
+        for x, y in zip((hr, hv, ha), st):
+            x[:] = y
+        t1 = one.step_from_host(hr, hv, ha, nsteps=1)
+        two.set_state(*two.get_state())
+        two.step(1)
+        t2 = two.thermo()
+        assert t1.stepCount == t2.stepCount == warm + k + 1
+        _same_thermo(t1, t2)
+    for x, y in zip(one.get_state(), two.get_state()):
+        assert np.array_equal(x, y)
+    one.close()
+    two.close()
