@@ -744,7 +744,9 @@ static void phaseMark(sg_ctx *c, int k) {
   if (c->opt.phase_timing) cudaEventRecordWithFlags(c->phaseEv[k], c->stream, cudaEventRecordExternal);
 }
 
-static int enqueueStep(sg_ctx *c, int variant) {
+// One step, enqueued; with host arrays (MIXED, all replicas) the integrator starts from them.
+static int enqueueStep(sg_ctx *c, int variant, const sg_float4 *hostR = nullptr, const sg_float3 *hostV = nullptr,
+                       const sg_float3 *hostA = nullptr) {
   int rc;
   const int fr = c->opt.force_rebuild ? 1 : 0;
   if (c->persistent) {
@@ -761,7 +763,7 @@ static int enqueueStep(sg_ctx *c, int variant) {
   }
   phaseMark(c, 0);
   if (c->opt.mode == SG_MODE_MIXED) {
-    if ((rc = sg_mixed_enqueue_integrate(c, fr))) return rc;
+    if ((rc = sg_mixed_enqueue_integrate(c, fr, hostR, hostV, hostA))) return rc;
   } else {
     CK(launchK(c->pdl, k_integrate_first, c->atomTab.n, 128, 0, c->stream, c->atomTab.view(), c->rc, c->st, c->pos,
                c->vel, c->acc, c->cellOf, c->slot, c->cellCount, fr, c->bucket, c->bucketCap,
@@ -955,10 +957,12 @@ extern "C" int sg_step_thermo(sg_ctx *c, int nsteps, int rep, sg_thermo *t) {
   return SG_OK;
 }
 
-// One step from host buffers as one graph launch: the upload kernel, the step's kernels and the
-// publish.  The graph holds the buffers' addresses only (the upload kernel reads them when it
-// runs, through the host's page tables), so calls with the same buffers -- a caller's loop --
-// replay it; other buffers replace the context's graphs of this kind.
+// One step from host buffers as one graph launch: the upload, the step's kernels and the
+// publish.  In MIXED with all replicas uploaded the integrator reads the buffers itself (no
+// upload kernel); otherwise the upload kernel runs first.  The graph holds the buffers'
+// addresses only (read when it runs, through the host's page tables), so calls with the same
+// buffers -- a caller's loop -- replay it; other buffers replace the context's graphs of this
+// kind.
 static int launchStepFromHost(sg_ctx *c, int rep, const sg_float4 *r, const sg_float3 *v, const sg_float3 *a,
                               int variant) {
   const HostBufs key{rep, r, v, a};
@@ -978,8 +982,9 @@ static int launchStepFromHost(sg_ctx *c, int rep, const sg_float4 *r, const sg_f
   if (it == c->graphs.end()) {
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    int rc = enqueueSetState(c, rep, r, v, a);
-    if (!rc) rc = enqueueStep(c, variant);
+    const bool fused = c->opt.mode == SG_MODE_MIXED && rep == -1;
+    int rc = fused ? SG_OK : enqueueSetState(c, rep, r, v, a);
+    if (!rc) rc = fused ? enqueueStep(c, variant, r, v, a) : enqueueStep(c, variant);
     if (!rc) rc = enqueuePublish(c);
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     if (rc) return rc;

@@ -125,7 +125,10 @@ int sg_check_flags(sg_ctx *c);
 // MIXED mode (sg_kernels_mixed.cu)
 int sg_mixed_init(sg_ctx *c);
 void sg_mixed_free(sg_ctx *c);
-int sg_mixed_enqueue_integrate(sg_ctx *c, int forceRebuild);
+// the MIXED integrator; with host arrays (all replicas, hostR 16-byte aligned, read in place)
+// the step starts from them instead of the device state, as after an upload
+int sg_mixed_enqueue_integrate(sg_ctx *c, int forceRebuild, const sg_float4 *hostR = nullptr,
+                               const sg_float3 *hostV = nullptr, const sg_float3 *hostA = nullptr);
 int sg_mixed_enqueue_forces(sg_ctx *c);
 // registers a buffer the library allocated outside devAlloc (autotuner snapshots)
 void sg_register_region(sg_ctx *c, void *p, size_t bytes);

@@ -94,24 +94,67 @@ __device__ __forceinline__ void addHiLo(float &hi, float &lo, float d) {
 // Integrator part 1 with hi/lo positions (same schedule as k_integrate_first: pending
 // thermostat, deposition, kick + drift, wrap, freeze mask, cell histogram on rebuild steps).
 // ============================================================================================
-// Block-table entry e (128 atoms), by a 128-thread block.
+// Floats [3 g0, 3 g1) of a float3 array into shared memory, as float4 where 16-byte aligned.
+__device__ __forceinline__ void stageRows3Range(const float *src, int g0, int g1, float *sm) {
+  const int f0 = 3 * g0, f1 = 3 * g1;
+  const bool aligned = (reinterpret_cast<uintptr_t>(src + f0) & 15) == 0;
+  for (int q = threadIdx.x; 4 * q < f1 - f0; q += blockDim.x) {
+    const int f = f0 + 4 * q;
+    if (aligned && f + 4 <= f1) {
+      const float4 x = *reinterpret_cast<const float4 *>(src + f);
+      sm[4 * q] = x.x; sm[4 * q + 1] = x.y; sm[4 * q + 2] = x.z; sm[4 * q + 3] = x.w;
+    } else {
+      for (int k = 0; k < 4 && f + k < f1; k++) sm[4 * q + k] = src[f + k];
+    }
+  }
+}
+
+// Block-table entry e (128 atoms), by a 128-thread block.  With host arrays (hostR, hostV,
+// hostA: all replicas' r, v, a in global order, read in place through the host's page tables)
+// the step starts from them as an upload would leave the state: the low position words zero,
+// any pending thermostat rescale cancelled, the accelerations stored.
 __device__ __forceinline__ void integrateMixedBody(int e, BlockTab tab, const RepConst *__restrict__ rc, RepState *st,
                                                    float4 *__restrict__ pos, float4 *__restrict__ posLo,
-                                                   float4 *__restrict__ vel, const float4 *__restrict__ acc,
+                                                   float4 *__restrict__ vel, float4 *__restrict__ acc,
                                                    int *__restrict__ cellOf, int *__restrict__ slot,
                                                    int *__restrict__ cellCount, int forceRebuild,
                                                    int *__restrict__ bucket, int cap, int *__restrict__ blockCount,
-                                                   int2 *__restrict__ spill, int *__restrict__ spillCount) {
+                                                   int2 *__restrict__ spill, int *__restrict__ spillCount,
+                                                   const float4 *__restrict__ hostR = nullptr,
+                                                   const float *__restrict__ hostV = nullptr,
+                                                   const float *__restrict__ hostA = nullptr) {
   const int rep = tab.rep[e];
   const RepConst &P = rc[rep];
   RepState *S = st + rep;
   const int g = tab.start[e] + threadIdx.x;
-  if (g >= P.atomOff + P.nMol) return;
+  const int gEnd = P.atomOff + P.nMol;
+  float4 r, lo, v, a;
+  bool pending;
+  if (hostR) {
+    __shared__ float sV[3 * 128], sA[3 * 128];
+    const int g0 = tab.start[e], g1 = min(gEnd, g0 + (int)blockDim.x);
+    if (g < gEnd) r = hostR[g];  // every read over the host link before the barrier
+    stageRows3Range(hostV, g0, g1, sV);
+    stageRows3Range(hostA, g0, g1, sA);
+    __syncthreads();
+    if (g >= gEnd) return;
+    const int t = threadIdx.x;
+    v = make_float4(sV[3 * t], sV[3 * t + 1], sV[3 * t + 2], 0.f);
+    a = make_float4(sA[3 * t], sA[3 * t + 1], sA[3 * t + 2], 0.f);
+    lo = make_float4(0.f, 0.f, 0.f, 0.f);
+    pending = false;
+    acc[g] = a;
+  } else {
+    if (g >= gEnd) return;
+    r = pos[g];
+    lo = posLo[g];
+    v = vel[g];
+    a = acc[g];
+    pending = S->thermoPending != 0;
+  }
   const int local = g - P.atomOff;
   const int sc = S->stepCount + 1;
-  float4 r = pos[g], lo = posLo[g], v = vel[g];
-  const float4 a = acc[g];
-  if (S->thermoPending) {
+  if (pending) {
     if (local >= P.nMolMe) {
       const float b = S->betaC;
       v.x *= b; v.y *= b; v.z *= b;
@@ -162,14 +205,15 @@ __device__ __forceinline__ void integrateMixedBody(int e, BlockTab tab, const Re
 
 __global__ void k_integrate_mixed(BlockTab tab, const RepConst *__restrict__ rc, RepState *st,
                                   float4 *__restrict__ pos, float4 *__restrict__ posLo,
-                                  float4 *__restrict__ vel, const float4 *__restrict__ acc,
+                                  float4 *__restrict__ vel, float4 *__restrict__ acc,
                                   int *__restrict__ cellOf, int *__restrict__ slot,
                                   int *__restrict__ cellCount, int forceRebuild, int *__restrict__ bucket,
                                   int cap, int *__restrict__ blockCount, int2 *__restrict__ spill,
-                                  int *__restrict__ spillCount) {
+                                  int *__restrict__ spillCount, const float4 *__restrict__ hostR,
+                                  const float *__restrict__ hostV, const float *__restrict__ hostA) {
   pdlEnter();
   integrateMixedBody(blockIdx.x, tab, rc, st, pos, posLo, vel, acc, cellOf, slot, cellCount, forceRebuild, bucket, cap,
-                     blockCount, spill, spillCount);
+                     blockCount, spill, spillCount, hostR, hostV, hostA);
 }
 
 // ============================================================================================
@@ -893,11 +937,14 @@ void sg_mixed_free(sg_ctx *c) {
   c->mixed = nullptr;
 }
 
-int sg_mixed_enqueue_integrate(sg_ctx *c, int forceRebuild) {
+int sg_mixed_enqueue_integrate(sg_ctx *c, int forceRebuild, const sg_float4 *hostR, const sg_float3 *hostV,
+                               const sg_float3 *hostA) {
   if (!c->atomTab.n) return SG_OK;
   MCK(launchK(c->pdl, k_integrate_mixed, c->atomTab.n, 128, 0, c->stream, c->atomTab.view(), c->rc, c->st, c->pos, c->posLo, c->vel,
                                                          c->acc, c->cellOf, c->slot, c->cellCount, forceRebuild,
-                c->bucket, c->bucketCap, c->blockCount, c->spill, c->nebrWork + 3));
+                c->bucket, c->bucketCap, c->blockCount, c->spill, c->nebrWork + 3,
+                reinterpret_cast<const float4 *>(hostR), reinterpret_cast<const float *>(hostV),
+                reinterpret_cast<const float *>(hostA)));
   MCK(cudaGetLastError());
   return SG_OK;
 }
