@@ -35,7 +35,7 @@ constexpr int kNumRed = 16;       // values reduced per element in the step redu
 constexpr int kMT = 16;           // lanes per metal atom in the density and metal-force passes
 constexpr int kCT = 4;            // lanes per carbon atom in the carbon-force pass
 constexpr int kNebrWarps = 4;     // warps per block in the neighbour-list build (one home cell each)
-constexpr int kWin = 512;         // candidates per shared-memory window of the list build
+constexpr int kWin = 512;         // candidates per shared-memory window of the lane-placed list build
 constexpr int kFusedWin = 256;    // candidates per window pass of the fused list build
 constexpr int kRelMax = 48;       // relevant-list capacity per carbon atom
 constexpr int kShortMax = 8;      // close-list capacity per carbon atom (a multiple of 4)
