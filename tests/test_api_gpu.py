@@ -225,3 +225,30 @@ def test_step_from_host_loop_on_the_same_buffers(mode):
         assert np.array_equal(x, y)
     one.close()
     two.close()
+
+
+@pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_MIXED])
+def test_step_from_host_one_replica_of_several(mode):
+    """Steps from one replica's buffers in a two-replica context (the graph then holds the upload
+    kernel for that replica) equal set_state of that replica + step, replica by replica."""
+    reps = [workloads.small(seed=s) for s in (69, 70)]
+    plist = [w[0] for w in reps]
+    one = Simulation(plist, mode=mode)
+    two = Simulation(plist, mode=mode)
+    for s in (one, two):
+        for k, (q, r, v) in enumerate(reps):
+            s.set_state(r, v, np.zeros((q.nMol, 3), np.float32), rep=k)
+    n1 = plist[1].nMol
+    hr, hv, ha = np.zeros((n1, 4), np.float32), np.zeros((n1, 3), np.float32), np.zeros((n1, 3), np.float32)
+    for k in range(4):
+        for x, y in zip((hr, hv, ha), one.get_state(1)):
+            x[:] = y
+        t1 = one.step_from_host(hr, hv, ha, nsteps=1, rep=1, thermo_rep=1)
+        two.set_state(*two.get_state(1), rep=1)
+        two.step(1)
+        _same_thermo(t1, two.thermo(1))
+    for k in range(2):
+        for x, y in zip(one.get_state(k), two.get_state(k)):
+            assert np.array_equal(x, y)
+    one.close()
+    two.close()
