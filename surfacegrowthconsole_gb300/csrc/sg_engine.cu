@@ -386,7 +386,9 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
   }
   c->hostSeq = reinterpret_cast<volatile unsigned *>(reinterpret_cast<char *>(c->hostSt) + sizeof(RepState) * n_replicas);
   *c->hostSeq = 0u;
-  if (cudaMalloc(&c->devSeq, sizeof(unsigned)) != cudaSuccess || cudaMemset(c->devSeq, 0, sizeof(unsigned)) != cudaSuccess) {
+  // the sequence counter and, after it, the publish's count of finished blocks
+  if (cudaMalloc(&c->devSeq, 2 * sizeof(unsigned)) != cudaSuccess ||
+      cudaMemset(c->devSeq, 0, 2 * sizeof(unsigned)) != cudaSuccess) {
     sg_destroy(c);
     return sg_fail(SG_ERR_NOMEM, "cudaMalloc(sequence counter)");
   }
@@ -901,8 +903,12 @@ static int flagsFromMirror(sg_ctx *c) {
 // a sequence number the host polls for (waitPublished).
 static int enqueuePublish(sg_ctx *c) {
   const int nwords = (int)(sizeof(RepState) * c->nrep / 4);
-  k_publish_state<<<1, 256, 0, c->stream>>>(reinterpret_cast<const int *>(c->st), reinterpret_cast<int *>(c->hostSt),
-                                            nwords, c->devSeq, c->hostSeq);
+  // a block per 1,024 words (a few replicas), at most 64: many replicas cross the host link in
+  // parallel, one replica in one block
+  const int blocks = std::max(1, std::min(64, (nwords + 1023) / 1024));
+  k_publish_state<<<blocks, 256, 0, c->stream>>>(reinterpret_cast<const int *>(c->st),
+                                                 reinterpret_cast<int *>(c->hostSt), nwords, c->devSeq, c->hostSeq,
+                                                 c->devSeq + 1);
   CK(cudaGetLastError());
   return SG_OK;
 }

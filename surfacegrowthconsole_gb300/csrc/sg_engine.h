@@ -103,7 +103,7 @@ struct sg_ctx {
   float *stage = nullptr;        // 6 floats per atom: two host float3 arrays in transit
   RepState *hostSt = nullptr;    // pinned host mirror of the replica states (read with sg_step)
   volatile unsigned *hostSeq = nullptr;  // pinned, after the mirror: the last published sequence number
-  unsigned *devSeq = nullptr;    // its device-side counter (not a snapshot region)
+  unsigned *devSeq = nullptr;    // its device-side counter, then the publish's block count (not a snapshot region)
   unsigned pubSeq = 0;           // the number the host expects next
   cudaEvent_t phaseEv[9] = {};   // phase boundaries of a step (phase_timing)
   cudaStream_t side = nullptr;   // second stream: the metal force chain runs beside the carbon pass

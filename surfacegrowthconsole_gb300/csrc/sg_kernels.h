@@ -77,7 +77,8 @@ __global__ void k_rdf_ext(const RepConst *rc, const float4 *pos, const int4 *pai
                           int nbins, float range);
 __global__ void k_apply_pending(BlockTab tab, const RepConst *rc, RepState *st, float4 *vel);
 __global__ void k_clear_pending(RepState *st, int nrep);
-__global__ void k_publish_state(const int *src, int *dst, int nwords, unsigned *devSeq, volatile unsigned *hostSeq);
+__global__ void k_publish_state(const int *src, int *dst, int nwords, unsigned *devSeq, volatile unsigned *hostSeq,
+                                unsigned *done);
 __global__ void k_unpack_state(const float4 *sr, const float *sv, const float *sa, float4 *pos, float4 *vel,
                                float4 *acc, float4 *posLo, int n, RepState *st, int nrep);
 __global__ void k_unpack3(const float *src, float4 *dst, int n);

@@ -1238,12 +1238,18 @@ __global__ void __launch_bounds__(kUnpackAtoms) k_unpack_state(const float4 *sr,
 
 // The replica states to the host's page-locked mirror (dst, its device address), then a new
 // sequence number next to it: the host waits for that number instead of a stream
-// synchronisation.  Every thread's copy is made visible system-wide before the number is.
-__global__ void k_publish_state(const int *src, int *dst, int nwords, unsigned *devSeq, volatile unsigned *hostSeq) {
-  for (int i = threadIdx.x; i < nwords; i += blockDim.x) dst[i] = __ldcg(src + i);
+// synchronisation.  The blocks of the grid copy a share of the words each and make them visible
+// system-wide, then count themselves in (done); the last one, which sees every other block's
+// words visible, stores the number (and resets the count for the next publish).
+__global__ void k_publish_state(const int *src, int *dst, int nwords, unsigned *devSeq, volatile unsigned *hostSeq,
+                                unsigned *done) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nwords; i += gridDim.x * blockDim.x)
+    dst[i] = __ldcg(src + i);
   __threadfence_system();
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (threadIdx.x == 0 && atomicAdd(done, 1u) == gridDim.x - 1) {
+    *done = 0;
+    __threadfence();
     const unsigned seq = *devSeq + 1u;
     *devSeq = seq;
     __threadfence_system();
