@@ -23,6 +23,9 @@ LJ, graphene, reductions, thermostat, RDF/diffusion when due).
           CUDA graph of one launch per phase that the headline runs (--no-persistent).
   nve_drift : the total-energy drift of both forms on bulk Ni (4,000 atoms, 300 K, 10 ps NVE),
           the "stated drift" the two forms are compared at.
+  published_configs : both forms on the reference's own published configurations that the
+          engine builds exactly (bulk Au, 55,296 atoms; bulk Cu, 108,000 atoms), device-timed like
+          the headline, beside the published ms/step (--no-published leaves them out).
   e2e   : the same metric through the public C ABI with host buffers: every step uploads the
           state (r, v, a) from pinned host memory, steps, and
           reads the step's thermo record, in one sg_step_from_host call (one wait per step).
@@ -87,10 +90,13 @@ def parse():
     ap.add_argument("--mode", default="mixed", choices=["plain", "mixed"])
     ap.add_argument("--drift-steps", type=int, default=10000)
     ap.add_argument("--cpu-sample-steps", type=int, default=300)
-    ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--e2e-steps", type=int, default=200,
+                    help="steps of the end-to-end window (host-timed: a longer window than the device-timed one)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="leave out the batched comparison of the production line")
+    ap.add_argument("--no-published", action="store_true",
+                    help="leave out the reference's published configurations (bulk Au, bulk Cu)")
     ap.add_argument("--no-persistent", action="store_true", help="leave out the persistent-step measurements")
     ap.add_argument("--workload", default="production", choices=["production", "batched", "diff"])
     ap.add_argument("--replicas", type=int, default=256)
@@ -431,6 +437,49 @@ def main():
         dist.destroy_process_group()
 
 
+# The reference's own published configurations this engine builds exactly (bulk fcc metal,
+# regime 0): name, material (the reference's table order), unit cells per side, published
+# ms/step (GTX 260, 2010; the reference's doc/SurfaceGrowth_compare.pdf p.1 and
+# doc/SurfaceGrowth_user_guide.pdf p.19).
+PUBLISHED = (("bulk Au, 24 x 24 x 24 fcc unit cells (55,296 atoms)", 2, 24, 30.0),
+             ("bulk Cu, 30 x 30 x 30 fcc unit cells (108,000 atoms)", 0, 30, 41.0))
+
+
+def published_configs(local: int, steps: int, warmup: int, flush, stream) -> list:
+    """Both forms on each published configuration: device time of `steps` steps (CUDA events on
+    the library's stream, the L2 flushed before each), lists rebuilt by the reference's rule,
+    300 K, beside the published figure."""
+    import torch
+    from surfacegrowthconsole_gb300 import MODE_MIXED, MODE_PLAIN, workloads
+    from surfacegrowthconsole_gb300.engine import Simulation
+    out = []
+    for name, material, n, ms_pub in PUBLISHED:
+        p, r, v = workloads.bulk_metal(n, 300.0, 5, material=material)
+        pub = p.nMol / (ms_pub * 1e-3)
+        entry = {"config": name, "atoms": p.nMol, "published_ms_per_step": ms_pub,
+                 "published_atom_steps_s": pub, "published_on": "GeForce GTX 260 (2010)"}
+        for fname, mode in (("plain", MODE_PLAIN), ("mixed", MODE_MIXED)):
+            sim = Simulation(p, mode=mode, device=local, stream=stream.cuda_stream)
+            sim.set_state(r, v, np.zeros((p.nMol, 3), np.float32))
+            sim.step(warmup)
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+            torch.cuda.synchronize()
+            with torch.cuda.stream(stream):
+                for e0, e1 in ev:
+                    flush.zero_()
+                    e0.record(stream)
+                    sim.step_async(1)
+                    e1.record(stream)
+            torch.cuda.synchronize()
+            sim.step(0)  # collects device status
+            ms = sum(e0.elapsed_time(e1) for e0, e1 in ev) / steps
+            entry[fname] = {"ms_per_step": ms, "atom_steps_s": p.nMol / (ms * 1e-3),
+                            "over_published": p.nMol / (ms * 1e-3) / pub}
+            sim.close()
+        out.append(entry)
+    return out
+
+
 def nve_drift(mode: int, local: int, steps: int) -> dict:
     """Linear drift of the total energy of bulk Ni (4,000 atoms, 300 K) over `steps` NVE steps."""
     from surfacegrowthconsole_gb300 import MODE_MIXED, workloads
@@ -621,7 +670,9 @@ def run_production(args, rank: int, world: int, local: int, dist):
     hv = torch.empty((p.nMol, 3), dtype=torch.float32, pin_memory=True).numpy()
     ha = torch.empty((p.nMol, 3), dtype=torch.float32, pin_memory=True).numpy()
     hr[:], hv[:], ha[:] = sim.get_state()
-    e2e_steps = max(1, min(args.e2e_steps, args.steps))
+    # a window of its own length: it is timed on the host, whose jitter a window of a few
+    # milliseconds does not average out
+    e2e_steps = max(1, args.e2e_steps)
     s0 = sim.thermo().stepCount
     barrier()
     t0 = time.perf_counter()
@@ -658,6 +709,11 @@ def run_production(args, rank: int, world: int, local: int, dist):
                    "mixed_over_plain": b["mixed_over_plain"], "one_by_one": b["one_by_one"],
                    "timing": "device time of the steps with CUDA events on the library's stream; state larger "
                              "than L2 (no flush)"}
+
+    published = None
+    if not args.no_published and rank == 0:
+        published = published_configs(local, max(5, min(args.steps, 20)), max(3, min(args.warmup, 5)), flush,
+                                      stream)
 
     drift = None
     if args.drift_steps > 0:
@@ -696,6 +752,7 @@ def run_production(args, rank: int, world: int, local: int, dist):
                 "persistent_step": persist,
                 "batched": batched,
                 "nve_drift": drift,
+                "published_configs": published,
                 "cpu_baseline": cpu}
         print(json.dumps(line, default=float))
 

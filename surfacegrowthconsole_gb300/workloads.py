@@ -57,14 +57,15 @@ def batched(n: int = 256, seed: int = 4, steps: int = 5000):
     return out
 
 
-def bulk_metal(n: int = 10, temperature_K: float = 300.0, seed: int = 5):
-    """Bulk fcc Ni (regime 0), n x n x n unit cells (4 n^3 atoms), no thermostat: an NVE system
-    of the EAM alone, the conservative part of the model (the reference's graphene energy omits
-    the second-neighbour angle term its forces apply)."""
+def bulk_metal(n: int = 10, temperature_K: float = 300.0, seed: int = 5, material: int = 3):
+    """Bulk fcc metal (regime 0; material in the reference's table order Cu 0, Ag 1, Au 2, Ni 3,
+    Al 4, Pb 5; default Ni), n x n x n unit cells (4 n^3 atoms), no thermostat: an NVE system of
+    the EAM alone, the conservative part of the model (the reference's graphene energy omits the
+    second-neighbour angle term its forces apply)."""
     from .engine import default_input, init_coords, init_vels, set_params
     inp = default_input()
     inp.iRegime = 0
-    inp.iMaterial = 3
+    inp.iMaterial = material
     inp.ucx = inp.ucy = inp.ucz = n
     inp.temperatureK = temperature_K
     inp.deltaT = DT_1FS
