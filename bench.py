@@ -446,9 +446,9 @@ PUBLISHED = (("bulk Au, 24 x 24 x 24 fcc unit cells (55,296 atoms)", 2, 24, 30.0
 
 
 def published_configs(local: int, steps: int, warmup: int, flush, stream) -> list:
-    """Both forms on each published configuration: device time of `steps` steps (CUDA events on
-    the library's stream, the L2 flushed before each), lists rebuilt by the reference's rule,
-    300 K, beside the published figure."""
+    """Both forms on each published configuration, each autotuned on its own state first: device
+    time of `steps` steps (CUDA events on the library's stream, the L2 flushed before each),
+    lists rebuilt by the reference's rule, 300 K, beside the published figure."""
     import torch
     from surfacegrowthconsole_gb300 import MODE_MIXED, MODE_PLAIN, workloads
     from surfacegrowthconsole_gb300.engine import Simulation
@@ -461,6 +461,7 @@ def published_configs(local: int, steps: int, warmup: int, flush, stream) -> lis
         for fname, mode in (("plain", MODE_PLAIN), ("mixed", MODE_MIXED)):
             sim = Simulation(p, mode=mode, device=local, stream=stream.cuda_stream)
             sim.set_state(r, v, np.zeros((p.nMol, 3), np.float32))
+            shape = sim.autotune(steps=10)
             sim.step(warmup)
             ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
             torch.cuda.synchronize()
@@ -474,7 +475,8 @@ def published_configs(local: int, steps: int, warmup: int, flush, stream) -> lis
             sim.step(0)  # collects device status
             ms = sum(e0.elapsed_time(e1) for e0, e1 in ev) / steps
             entry[fname] = {"ms_per_step": ms, "atom_steps_s": p.nMol / (ms * 1e-3),
-                            "over_published": p.nMol / (ms * 1e-3) / pub}
+                            "over_published": p.nMol / (ms * 1e-3) / pub,
+                            "launch_shape": {k: shape[k] for k in Simulation.SHAPE_FIELDS}}
             sim.close()
         out.append(entry)
     return out
