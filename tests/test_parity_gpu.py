@@ -329,3 +329,28 @@ def test_batched_uneven_replicas_equal_single_runs(mode):
             assert abs(tb.totEnergy - ts.totEnergy) <= 1e-5 * abs(ts.totEnergy), k
         single.close()
     batch.close()
+
+
+@pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_MIXED])
+def test_graphene_without_metal(mode):
+    """A sheet with no metal atoms (960 C, the shear regime's schedule): no metal chain, no
+    relevant-list metal entries, no centre of mass; lists bit-exact against the oracle, a
+    30-step trajectory across the thermostat step against it."""
+    from surfacegrowthconsole_gb300.workloads import DT_1FS, build_workload
+    p, r, v = build_workload(5, 6, [], 300.0, 7, step_limit=100, step_avg=10, step_equil=0, step_rdf=50,
+                             limit_rdf=5, delta_t=DT_1FS)
+    assert p.nMolMe == 0
+    a = np.zeros((p.nMol, 3), np.float32)
+    sim, orc = make_pair(p, r, v, a, mode=mode)
+    sim.build_lists(); orc.build_lists()
+    for x, y in zip(sim.nebr(), orc.nebr()):
+        assert np.array_equal(x, y)
+    sim.step(30); orc.step(30)
+    tg, to = sim.thermo(), orc.thermo()
+    assert tg.stepCount == to.stepCount == 30
+    for k in ("kinEnergy", "potEnergy", "totEnergy"):
+        assert abs(getattr(tg, k) - getattr(to, k)) <= 1e-4 * abs(getattr(to, k)), k
+    rg, vg, _ = sim.get_state()
+    ro, vo, _ = orc.get_state()
+    assert np.all(np.isfinite(rg)) and np.abs(rg[:, :3] - ro[:, :3]).max() < 1e-3
+    sim.close()
