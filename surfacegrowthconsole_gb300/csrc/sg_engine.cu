@@ -852,7 +852,10 @@ static int launchStep(sg_ctx *c, int variant) {
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     int rc = enqueueStep(c, variant);
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
-    if (rc) return rc;
+    if (rc) {
+      if (e == cudaSuccess) cudaGraphDestroy(g);
+      return rc;
+    }
     if (e != cudaSuccess) return sg_fail(SG_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
     c->kernelsPerVariant[variant] = countKernels(g);
     cudaGraphExec_t ex;
@@ -993,7 +996,10 @@ static int launchStepFromHost(sg_ctx *c, int rep, const sg_float4 *r, const sg_f
     if (!rc) rc = fused ? enqueueStep(c, variant, r, v, a) : enqueueStep(c, variant);
     if (!rc) rc = enqueuePublish(c);
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
-    if (rc) return rc;
+    if (rc) {
+      if (e == cudaSuccess) cudaGraphDestroy(g);
+      return rc;
+    }
     if (e != cudaSuccess) return sg_fail(SG_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
     cudaGraphExec_t ex;
     e = cudaGraphInstantiate(&ex, g, 0);
