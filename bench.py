@@ -52,7 +52,7 @@ its own context, for comparison.
 the 66 fit parameters (LJ epsilon, sigma, 64 EAM spline coefficients) over 64 jittered frames of
 the ~20,000-atom graphene + Ni system, forward + adjoint per gradient; metric grads/s.
 Launch shape: before the warm-up, sg_autotune times the lanes per metal atom (4, 8, 16, 32) and
-the list build's blocks per SM (2, 4, 8, 16) on the workload's own state, keeps the fastest and
+the list build's blocks per SM (2, 4, 7, 14) on the workload's own state, keeps the fastest and
 restores the state (--no-tune keeps the defaults, 16 lanes and 8 blocks per SM); the line's
 config carries the choice and the trial timings.
 Multi-GPU (torchrun): replicas only -- each rank runs its own seeded system, no collective on

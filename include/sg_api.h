@@ -76,7 +76,7 @@ typedef struct sg_options {
     int metal_lanes;       /* lanes per metal atom in the density and metal force passes:
                             * 4, 8, 16 or 32 (0: 16) */
     int nebr_blocks_per_sm;/* resident 128-thread blocks per SM of the list build's work queue,
-                            * 1..32 (0: 8) */
+                            * 1..32 (0: 7, the blocks the list build keeps resident) */
     int phase_timing;      /* 1: record CUDA events between the phases of every step */
     int programmatic_launch; /* 1 (default): launch the kernels of a step with programmatic
                             * dependent launch (a kernel is launched once its predecessor's blocks

@@ -323,7 +323,7 @@ extern "C" int sg_create(const sg_simparams *params, int n_replicas, const sg_op
     sg_destroy(c);
     return sg_fail(SG_ERR_INVALID, "nebr_blocks_per_sm %d: 0 (default) or 1..32", c->opt.nebr_blocks_per_sm);
   }
-  setNebrBlocks(c, c->opt.nebr_blocks_per_sm ? c->opt.nebr_blocks_per_sm : 8);
+  setNebrBlocks(c, c->opt.nebr_blocks_per_sm ? c->opt.nebr_blocks_per_sm : 7);
   c->nebrDescending = c->opt.nebr_descending ? 1 : 0;
   c->nebrItemAtoms = c->opt.nebr_item_atoms ? c->opt.nebr_item_atoms : kItemAtoms;
   if (c->opt.nebr_build < 0 || c->opt.nebr_build > 2) {
@@ -1436,7 +1436,7 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
   const int algo0 = c->nebrAlgo;
   const bool staged0 = c->eamStaged;
   const int cb0 = c->carbonBlocks;
-  const int laneChoice[4] = {4, 8, 16, 32}, bpsChoice[4] = {2, 4, 8, 16}, itemChoice[4] = {4, 6, 8, 16};
+  const int laneChoice[4] = {4, 8, 16, 32}, bpsChoice[4] = {2, 4, 7, 14}, itemChoice[4] = {4, 6, 8, 16};
   const int algoChoice[3] = {0, 1, 2}, offOn[2] = {0, 1}, cbChoice[3] = {8, 12, 16};
   float laneMs[4] = {}, bpsMs[4] = {}, orderMs[2] = {}, itemMs[4] = {}, pdlMs[2] = {}, algoMs[3] = {};
   float stagedMs[2] = {}, cbMs[3] = {};
@@ -1580,7 +1580,7 @@ extern "C" int sg_autotune(sg_ctx *c, int steps, char *report, int report_len) {
     snprintf(report, report_len,
              "{\"steps\": %d, \"metal_lanes_ms_per_step\": {\"4\": %.6g, \"8\": %.6g, \"16\": %.6g, "
              "\"32\": %.6g}, \"nebr_blocks_per_sm_ms_per_step_rebuilding\": {\"2\": %.6g, \"4\": %.6g, "
-             "\"8\": %.6g, \"16\": %.6g}, \"nebr_order_ms_per_step_rebuilding\": {\"ascending\": %.6g, "
+             "\"7\": %.6g, \"14\": %.6g}, \"nebr_order_ms_per_step_rebuilding\": {\"ascending\": %.6g, "
              "\"descending\": %.6g}, \"nebr_item_atoms_ms_per_step_rebuilding\": {\"4\": %.6g, "
              "\"6\": %.6g, \"8\": %.6g, \"16\": %.6g}, \"programmatic_launch_ms_per_step\": {\"0\": %.6g, "
              "\"1\": %.6g}, \"nebr_build_ms_per_step_rebuilding\": {\"0\": %.6g, \"1\": %.6g, \"2\": %.6g}, "

@@ -397,8 +397,11 @@ cudaError_t launchScanRank(bool pdl, int cells, int grid, cudaStream_t s, const 
       int rowStride, int nebrMax, int descending, int *__restrict__ blockCount, int nBlockCount
 #define SG_NEBR_ARGS \
   tileRep, active, heavy, work, rc, st, cellStart, sortPos, nn, nbl, ns, sl, nrl, rl, rowStride, nebrMax, descending
-// 64 registers a thread, so that eight blocks (32 warps) fit on an SM
-__global__ void __launch_bounds__(kNebrWarps * 32, 8) k_build_nebr(SG_NEBR_PARAMS) {
+// 72 registers a thread, seven blocks (28 warps) an SM: the kernel is bound by instruction
+// issue, and at 64 registers (eight blocks) the compiler fits the loop's state with extra
+// instructions (on the 45,546-atom workload: 30.5-30.8 us at 72 registers, 31.1-31.4 at 80,
+// 33.0-33.3 at 64)
+__global__ void __launch_bounds__(kNebrWarps * 32, 7) k_build_nebr(SG_NEBR_PARAMS) {
   pdlEnter();
   clearBlockCount(blockCount, nBlockCount);
   nebrFusedBody(SG_NEBR_ARGS);

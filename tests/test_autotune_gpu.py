@@ -73,7 +73,7 @@ def test_bad_shapes_are_refused():
         sim.set_launch_shape({"metal_lanes": 64})
     with pytest.raises(Exception):
         sim.set_launch_shape({"carbon_blocks_per_sm": 9})
-    assert sim.launch_shape() == {"metal_lanes": 16, "nebr_blocks_per_sm": 8, "nebr_descending": 0,
+    assert sim.launch_shape() == {"metal_lanes": 16, "nebr_blocks_per_sm": 7, "nebr_descending": 0,
                                   "nebr_item_atoms": 8, "programmatic_launch": 1, "nebr_build": 0,
                                   "eam_table_smem": 0, "carbon_blocks_per_sm": 8}
     sim.close()
@@ -89,7 +89,7 @@ def test_autotune_restores_the_state(mode):
     rep = tuned.autotune(steps=10)
     shape = tuned.launch_shape()
     assert shape == {f: rep[f] for f in Simulation.SHAPE_FIELDS}
-    assert shape["metal_lanes"] in (4, 8, 16, 32) and shape["nebr_blocks_per_sm"] in (2, 4, 8, 16)
+    assert shape["metal_lanes"] in (4, 8, 16, 32) and shape["nebr_blocks_per_sm"] in (2, 4, 7, 14)
     assert shape["nebr_item_atoms"] in (4, 6, 8, 16) and shape["nebr_build"] in (0, 1, 2)
     for k in ("4", "8", "16", "32"):
         assert rep["metal_lanes_ms_per_step"][k] > 0
