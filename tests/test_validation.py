@@ -76,3 +76,43 @@ def test_valid_system_without_a_device_reports_no_device():
         pytest.skip("a GPU is present")
     rc, msg = _create([_copy(_small())])
     assert rc == SG_ERR_NO_DEVICE, msg
+
+
+def _noalloc(p, pos=1, acc=1):
+    # every block here fails the checks that run before any device call, so the placeholder
+    # pointers are never used; on a machine with a GPU these cases are left to the GPU tests,
+    # which pass real buffers
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present: covered with real buffers by the GPU tests")
+    rc = L.lib().sg_compute_forces_noalloc(C.byref(p), C.c_void_p(pos), C.c_void_p(acc), None)
+    return rc, L.lib().sg_last_error().decode(errors="replace")
+
+
+def test_noalloc_rejects_null_buffers_and_bad_blocks():
+    p = _copy(_small())
+    assert _noalloc(p, pos=0)[0] == SG_ERR_INVALID
+    assert _noalloc(p, acc=0)[0] == SG_ERR_INVALID
+    q = _copy(p)
+    q.nMol = 0
+    assert _noalloc(q)[0] == SG_ERR_INVALID
+    q = _copy(p)
+    q.cells.z = 0
+    assert _noalloc(q)[0] == SG_ERR_INVALID
+
+
+def test_noalloc_rejects_systems_above_its_static_scratch():
+    p = _copy(_small())
+    q = _copy(p)
+    q.nMol = 16384 + 1
+    rc, msg = _noalloc(q)
+    assert rc == SG_ERR_INVALID and "static scratch" in msg
+    # extents whose product wraps a 32-bit int to a small value are still rejected
+    q = _copy(p)
+    q.cells.x, q.cells.y, q.cells.z = 65536, 65536, 1
+    rc, msg = _noalloc(q)
+    assert rc == SG_ERR_INVALID and "static scratch" in msg
+    q = _copy(p)
+    q.iNebrMax = 129
+    rc, msg = _noalloc(q)
+    assert rc == SG_ERR_INVALID and "static scratch" in msg
