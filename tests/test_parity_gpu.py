@@ -331,6 +331,39 @@ def test_batched_uneven_replicas_equal_single_runs(mode):
     batch.close()
 
 
+@pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_MIXED], ids=["plain", "mixed"])
+def test_batched_full_size_sampled_replicas_equal_single_runs(mode):
+    """The batched configuration at its full size (256 replicas, 3.0 M atoms) stepped together;
+    the smallest, the largest and two other replicas are each stepped alone from the same state
+    and compared (PLAIN bit for bit; MIXED close, as above)."""
+    systems = workloads.batched(n=256, seed=4, steps=5000)
+    sizes = np.array([s[0].nMol for s in systems])
+    assert sizes.sum() > 2_900_000
+    batch = Simulation([s[0] for s in systems], mode=mode)
+    for k, (p, r, v) in enumerate(systems):
+        batch.set_state(r, v, np.zeros((p.nMol, 3), np.float32), rep=k)
+    steps = 30
+    batch.step(steps)
+    for k in sorted({int(sizes.argmin()), int(sizes.argmax()), 17, 200}):
+        p, r, v = systems[k]
+        single = Simulation(p, mode=mode)
+        single.set_state(r, v, np.zeros((p.nMol, 3), np.float32))
+        single.step(steps)
+        rb, vb, ab = batch.get_state(rep=k)
+        rs, vs, as_ = single.get_state()
+        tb, ts = batch.thermo(k), single.thermo()
+        assert tb.stepCount == ts.stepCount == steps and tb.rebuilds == ts.rebuilds, k
+        if mode == MODE_PLAIN:
+            assert np.array_equal(rb, rs) and np.array_equal(vb, vs) and np.array_equal(ab, as_), k
+            assert tb.totEnergy == ts.totEnergy, k
+        else:
+            assert np.abs(rb[:, :3] - rs[:, :3]).max() < 1e-4, k
+            ok, err = close(vb, vs, rtol=1e-4); assert ok, (k, err)
+            assert abs(tb.totEnergy - ts.totEnergy) <= 1e-5 * abs(ts.totEnergy), k
+        single.close()
+    batch.close()
+
+
 @pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_MIXED])
 def test_graphene_without_metal(mode):
     """A sheet with no metal atoms (960 C, the shear regime's schedule): no metal chain, no
