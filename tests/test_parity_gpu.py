@@ -202,6 +202,25 @@ def test_trajectory_30_steps_with_thermostat():
     sim.close()
 
 
+def test_trajectory_production_workload():
+    """The 45,546-atom workload (40,000 C + 8 Ni clusters, 700 K, lists rebuilt every step) for 30
+    steps across the thermostat step 25, against the oracle from the same state."""
+    p, r, v = workloads.production(seed=2, steps=100)
+    a = np.zeros((p.nMol, 3), np.float32)
+    sim, orc = make_pair(p, r, v, a, force_rebuild=True)
+    sim.step(30); orc.step(30)
+    tg, to = sim.thermo(), orc.thermo()
+    assert tg.stepCount == to.stepCount == 30
+    assert tg.rebuilds == to.rebuilds == 30
+    for k in ("kinEnergy", "potEnergy", "totEnergy"):
+        assert abs(getattr(tg, k) - getattr(to, k)) <= 1e-4 * abs(getattr(to, k)), k
+    rg, vg, _ = sim.get_state()
+    ro, vo, _ = orc.get_state()
+    assert np.abs(rg[:, :3] - ro[:, :3]).max() < 1e-3
+    ok, err = close(vg, vo, rtol=1e-3); assert ok, err
+    sim.close()
+
+
 def test_forced_rebuild_matches():
     p, r, v, a = perturbed_small(seed=27, jitter=0.0)
     sim, orc = make_pair(p, r, v, a, force_rebuild=True)
