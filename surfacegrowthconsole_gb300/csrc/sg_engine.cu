@@ -1001,6 +1001,7 @@ static int launchStepFromHost(sg_ctx *c, int rep, const sg_float4 *r, const sg_f
       return rc;
     }
     if (e != cudaSuccess) return sg_fail(SG_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    c->kernelsPerVariant[gk] = countKernels(g);  // the upload (if any) and the publish included
     cudaGraphExec_t ex;
     e = cudaGraphInstantiate(&ex, g, 0);
     cudaGraphDestroy(g);
@@ -1008,7 +1009,7 @@ static int launchStepFromHost(sg_ctx *c, int rep, const sg_float4 *r, const sg_f
     it = c->graphs.emplace(gk, ex).first;
   }
   CK(cudaGraphLaunch(it->second, c->stream));
-  c->lastVariant = variant;
+  c->lastVariant = gk;
   return SG_OK;
 }
 

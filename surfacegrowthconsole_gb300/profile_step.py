@@ -2,6 +2,7 @@
 
     python -m surfacegrowthconsole_gb300.profile_step [--workload production|batched|precision]
         [--mode plain|mixed] [--warmup 3] [--steps 1] [--replicas 16] [--shape JSON] [--rdf-step]
+        [--from-host]
 
 Builds the workload (--shape: a launch shape as sg_get_launch_shape reports it, a JSON object
 of its fields, e.g. the one the benchmark's autotuning chose; default: the library's
@@ -11,7 +12,9 @@ from-start profiling off (ncu --profile-from-start off) sees exactly those steps
 Lists are rebuilt every step for the production workload (as its benchmark does) and by the
 reference's rule for the others.  --rdf-step: the production workload with the 0-15 A /
 300-bin RDF extension on, warmed up to the step before an RDF sample, so that the profiled
-step is an RDF step.  Prints the kernel launches per step.
+step is an RDF step.  --from-host: every step is one sg_step_from_host call on the same host
+arrays (r, v, a read from host memory by the step's first kernel, the thermo record published
+back), as an end-to-end caller runs it.  Prints the kernel launches per step.
 """
 from __future__ import annotations
 
@@ -44,6 +47,7 @@ def main() -> None:
     ap.add_argument("--replicas", type=int, default=16)
     ap.add_argument("--shape", default="")
     ap.add_argument("--rdf-step", action="store_true")
+    ap.add_argument("--from-host", action="store_true")
     a = ap.parse_args()
     if a.workload == "production":
         p, r, v = workloads.production(seed=2)
@@ -67,10 +71,22 @@ def main() -> None:
     if a.rdf_step:  # the first profiled step is an RDF step
         warm = max(warm, plist[0].stepRdf - 1)
         warm += (plist[0].stepRdf - 1 - warm) % plist[0].stepRdf
-    sim.step(warm)
+    if a.from_host:
+        # the caller's arrays: the same buffers every call, so the step's graph is captured once
+        rh = np.ascontiguousarray(r, dtype=np.float32)
+        vh = np.ascontiguousarray(v, dtype=np.float32)
+        ah = np.zeros((n, 3), np.float32)
+        for _ in range(warm):
+            sim.step_from_host(rh, vh, ah)
+    else:
+        sim.step(warm)
     rt = _cudart()
     rt.cudaProfilerStart()
-    sim.step(a.steps)
+    if a.from_host:
+        for _ in range(a.steps):
+            sim.step_from_host(rh, vh, ah)
+    else:
+        sim.step(a.steps)
     rt.cudaProfilerStop()
     print(f"{a.workload} {a.mode}: {n} atoms, {sim.kernels_per_step()} kernel launches per step, "
           f"{a.steps} profiled step(s), launch shape {sim.launch_shape()}")
