@@ -119,7 +119,9 @@ int sg_version(void);
 /* ---- context ------------------------------------------------------------------------------
  * Replaces the allocation and upload half of DoComputationsW
  * (SurfaceGrowthConsole/SurfaceGrowth.cu:2040-2126) and SetParametersW (cu:2639-2650).
- * params points to n_replicas consecutive sg_simparams. */
+ * params points to n_replicas consecutive sg_simparams.  A context is used by one host thread
+ * at a time (its calls share the context's stream, graphs and host mirror); separate contexts
+ * may be driven from separate threads. */
 int sg_create(const sg_simparams *params, int n_replicas, const sg_options *opt, sg_ctx **out);
 int sg_destroy(sg_ctx *ctx);
 int sg_num_replicas(const sg_ctx *ctx);
