@@ -28,9 +28,9 @@ LJ, graphene, reductions, thermostat, RDF/diffusion when due).
           the headline, beside the published ms/step (--no-published leaves them out).
   e2e   : the same metric through the public C ABI with host buffers: every step uploads the
           state (r, v, a) from pinned host memory, steps, and
-          reads the step's thermo record, in one sg_step_from_host call (one wait per step),
-          after an untimed warm-up through the next RDF step (each step variant's first call
-          captures its graph).
+          reads the step's thermo record, in one sg_step_from_host call (one wait per step;
+          called as a host program calls it, its arguments built once), after an untimed warm-up
+          through the next RDF step (each step variant's first call captures its graph).
   roofline : the neighbour-list build (the largest share of the step): its compulsory bytes per
           launch / its mean duration (CUDA events around it on the library's stream), against
           the measured HBM copy peak; the kernel is bound by instruction issue, so its issue-slot,
@@ -55,7 +55,7 @@ the 66 fit parameters (LJ epsilon, sigma, 64 EAM spline coefficients) over 64 ji
 the ~20,000-atom graphene + Ni system, forward + adjoint per gradient; metric grads/s.
 Launch shape: before the warm-up, sg_autotune times the lanes per metal atom (4, 8, 16, 32) and
 the list build's blocks per SM (2, 4, 7, 14) on the workload's own state, keeps the fastest and
-restores the state (--no-tune keeps the defaults, 16 lanes and 8 blocks per SM); the line's
+restores the state (--no-tune keeps the defaults, 16 lanes and 7 blocks per SM); the line's
 config carries the choice and the trial timings.
 Multi-GPU (torchrun): replicas only -- each rank runs its own seeded system, no collective on
 the data path; value is the sum over ranks over the slowest rank's time.
@@ -685,12 +685,19 @@ def run_production(args, rank: int, world: int, local: int, dist):
     for _ in range(n_warm):
         sim.step_from_host(hr, hv, ha, nsteps=1)
     s0 = sim.thermo().stepCount
+    # the C ABI call a host program makes (sg_step_from_host), its arguments built once: r, v, a
+    # from pinned host memory, one step, the thermo record of replica 0 back; one call, one wait
+    import ctypes
+    from surfacegrowthconsole_gb300 import _lib
+    step_from_host = _lib.lib().sg_step_from_host
+    th = _lib.Thermo()
+    call_args = (sim._h, -1, hr.ctypes.data_as(ctypes.c_void_p), hv.ctypes.data_as(ctypes.c_void_p),
+                 ha.ctypes.data_as(ctypes.c_void_p), 1, 0, ctypes.byref(th))
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        # r, v, a from pinned host memory, one step, the thermo record back: one call, one
-        # wait (sg_step_from_host)
-        th = sim.step_from_host(hr, hv, ha, nsteps=1)
+        if step_from_host(*call_args):
+            raise RuntimeError(_lib.lib().sg_last_error().decode(errors="replace"))
     barrier()
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     n_rdf_e2e = sum(1 for k in range(1, e2e_steps + 1) if (s0 + k) % p.stepRdf == 0)
