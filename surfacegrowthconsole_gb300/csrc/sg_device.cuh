@@ -252,6 +252,36 @@ __device__ __forceinline__ void stateFromShared(const RepState *s, RepState *g) 
   for (int i = threadIdx.x; i < (int)(sizeof(RepState) / 4); i += blockDim.x) dst[i] = src[i];
 }
 
+// Where a step's last blocks publish the replica states when the step's publish is folded into
+// its reduction (hostSt null: no publish): the host mirror, the device-side sequence counter
+// (seq[0]) with the publish's arrival count (seq[1]), the host's copy of the sequence number.
+struct PublishArgs {
+  RepState *hostSt = nullptr;
+  unsigned *seq = nullptr;
+  volatile unsigned *hostSeq = nullptr;
+  int nrep = 0;
+};
+
+// Replica rep's final state s (shared memory, just written to its device record) into the host
+// mirror; the last replica to arrive then raises the sequence number, after a system-wide fence
+// that orders every replica's mirror words before it (the host reads the number with acquire
+// ordering, then the mirror).  By the whole block.
+__device__ __forceinline__ void publishReplica(const RepState *s, int rep, const PublishArgs &pub) {
+  const int *src = reinterpret_cast<const int *>(s);
+  int *dst = reinterpret_cast<int *>(pub.hostSt + rep);
+  for (int i = threadIdx.x; i < (int)(sizeof(RepState) / 4); i += blockDim.x) dst[i] = src[i];
+  __threadfence_system();
+  __syncthreads();
+  if (threadIdx.x == 0 && atomicAdd(pub.seq + 1, 1u) == (unsigned)pub.nrep - 1u) {
+    pub.seq[1] = 0;
+    __threadfence();
+    const unsigned n = pub.seq[0] + 1u;
+    pub.seq[0] = n;
+    __threadfence_system();
+    *pub.hostSeq = n;
+  }
+}
+
 __device__ __forceinline__ void setFlag(RepState *st, int code) {
   atomicOr(&st->flags, 1 << code);
 }

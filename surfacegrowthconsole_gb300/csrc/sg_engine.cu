@@ -747,8 +747,10 @@ static void phaseMark(sg_ctx *c, int k) {
 }
 
 // One step, enqueued; with host arrays (MIXED, all replicas) the integrator starts from them.
+// hostR/V/A (MIXED, all replicas): the integrator reads the step's state from these host arrays.
+// publish (MIXED): the reduction's last blocks publish the replica states (no publish kernel).
 static int enqueueStep(sg_ctx *c, int variant, const sg_float4 *hostR = nullptr, const sg_float3 *hostV = nullptr,
-                       const sg_float3 *hostA = nullptr) {
+                       const sg_float3 *hostA = nullptr, bool publish = false) {
   int rc;
   const int fr = c->opt.force_rebuild ? 1 : 0;
   if (c->persistent) {
@@ -778,7 +780,7 @@ static int enqueueStep(sg_ctx *c, int variant, const sg_float4 *hostR = nullptr,
   if ((rc = enqueueForces(c, true))) return rc;
   phaseMark(c, 4);
   if (c->opt.mode == SG_MODE_MIXED) {
-    if ((rc = sg_mixed_enqueue_reduce(c, fr))) return rc;
+    if ((rc = sg_mixed_enqueue_reduce(c, fr, publish))) return rc;
   } else {
     CK(launchK(c->pdl, k_step_reduce, c->redTab.n, kRedThreads, 0, c->stream, c->redTab.view(), c->rc, c->st, c->pos, c->vel, c->acc,
                                                               c->fric, c->partial, c->dRedFirst, c->diffBuf,
@@ -968,7 +970,9 @@ extern "C" int sg_step_thermo(sg_ctx *c, int nsteps, int rep, sg_thermo *t) {
 
 // One step from host buffers as one graph launch: the upload, the step's kernels and the
 // publish.  In MIXED with all replicas uploaded the integrator reads the buffers itself (no
-// upload kernel); otherwise the upload kernel runs first.  The graph holds the buffers'
+// upload kernel), and in a step without shear or RDF work (nothing after the reduction) the
+// reduction's last blocks publish the states themselves (no publish kernel); otherwise the
+// upload kernel runs first and the publish kernel last.  The graph holds the buffers'
 // addresses only (read when it runs, through the host's page tables), so calls with the same
 // buffers -- a caller's loop -- replay it; other buffers replace the context's graphs of this
 // kind.
@@ -992,9 +996,10 @@ static int launchStepFromHost(sg_ctx *c, int rep, const sg_float4 *r, const sg_f
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     const bool fused = c->opt.mode == SG_MODE_MIXED && rep == -1;
+    const bool pubInReduce = fused && c->redTab.n > 0 && !(variant & (V_SHEAR | V_RDF));
     int rc = fused ? SG_OK : enqueueSetState(c, rep, r, v, a);
-    if (!rc) rc = fused ? enqueueStep(c, variant, r, v, a) : enqueueStep(c, variant);
-    if (!rc) rc = enqueuePublish(c);
+    if (!rc) rc = fused ? enqueueStep(c, variant, r, v, a, pubInReduce) : enqueueStep(c, variant);
+    if (!rc && !pubInReduce) rc = enqueuePublish(c);
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     if (rc) {
       if (e == cudaSuccess) cudaGraphDestroy(g);

@@ -132,7 +132,9 @@ int sg_mixed_enqueue_integrate(sg_ctx *c, int forceRebuild, const sg_float4 *hos
 int sg_mixed_enqueue_forces(sg_ctx *c);
 // registers a buffer the library allocated outside devAlloc (autotuner snapshots)
 void sg_register_region(sg_ctx *c, void *p, size_t bytes);
-int sg_mixed_enqueue_reduce(sg_ctx *c, int forceRebuild);
+// the MIXED reduction; publish: its last blocks also publish the replica states to the host
+// mirror and raise the sequence number (the step's publish kernel folded in)
+int sg_mixed_enqueue_reduce(sg_ctx *c, int forceRebuild, bool publish = false);
 int sg_mixed_enqueue_persistent(sg_ctx *c, int forceRebuild);
 int sg_mixed_persistent_blocks_per_sm(int metalLanes);
 bool sg_mixed_staging_ok(sg_ctx *c);

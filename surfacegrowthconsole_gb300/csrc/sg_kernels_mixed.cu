@@ -258,7 +258,7 @@ __device__ __forceinline__ void reduceMixedBody(
     const float *__restrict__ fric, float2 *__restrict__ partDF, float *__restrict__ partF,
     const int *__restrict__ redFirst, unsigned *counter, double *__restrict__ diff64,
     const size_t *__restrict__ diffOff64, float *__restrict__ diffF, const size_t *__restrict__ diffOffF,
-    int forceRebuild) {
+    int forceRebuild, const PublishArgs pub = PublishArgs{}) {
   const int rep = tab.rep[e];
   const RepConst &P = rc[rep];
   RepState *S = st + rep;
@@ -453,6 +453,7 @@ __device__ __forceinline__ void reduceMixedBody(
   stepControlMixed(sP, &sS, A, M, diff64 ? diff64 + diffOff64[rep] : nullptr,
                    diffF ? diffF + diffOffF[rep] : nullptr, forceRebuild);
   stateFromShared(&sS, S);
+  if (pub.hostSt) publishReplica(&sS, rep, pub);
 }
 
 template <int APT>
@@ -462,10 +463,10 @@ __global__ void __launch_bounds__(kMixThreads) k_step_reduce_mixed(
     const float *__restrict__ fric, float2 *__restrict__ partDF, float *__restrict__ partF,
     const int *__restrict__ redFirst, unsigned *counter, double *__restrict__ diff64,
     const size_t *__restrict__ diffOff64, float *__restrict__ diffF, const size_t *__restrict__ diffOffF,
-    int forceRebuild) {
+    int forceRebuild, PublishArgs pub) {
   pdlEnter();
   reduceMixedBody<APT, kMixThreads>(blockIdx.x, APT, tab, rc, st, pos, posLo, vel, acc4, fric, partDF, partF, redFirst,
-                                    counter, diff64, diffOff64, diffF, diffOffF, forceRebuild);
+                                    counter, diff64, diffOff64, diffF, diffOffF, forceRebuild, pub);
 }
 
 // Step control in FP64 (same schedule as the PLAIN stepControl: properties, thermostat
@@ -978,7 +979,7 @@ int sg_mixed_enqueue_forces(sg_ctx *c) {
   return SG_OK;
 }
 
-int sg_mixed_enqueue_reduce(sg_ctx *c, int forceRebuild) {
+int sg_mixed_enqueue_reduce(sg_ctx *c, int forceRebuild, bool publish) {
   MixedBufs *m = static_cast<MixedBufs *>(c->mixed);
   if (!c->redTab.n) return SG_OK;
   auto kern = m->mixAtoms == 8 * kMixThreads   ? k_step_reduce_mixed<8>
@@ -987,7 +988,8 @@ int sg_mixed_enqueue_reduce(sg_ctx *c, int forceRebuild) {
                                                : k_step_reduce_mixed<1>;
   MCK(launchK(c->pdl, kern, m->redN, kMixThreads, 0, c->stream,
       BlockTab{m->redRep, m->redStart, m->redN}, c->rc, c->st, c->pos, c->posLo, c->vel, c->acc, c->fric, m->partDF, m->partF,
-      c->dRedFirst, m->counter, m->diff64, m->dDiffOff64, c->diffBuf, c->dDiffOff, forceRebuild));
+      c->dRedFirst, m->counter, m->diff64, m->dDiffOff64, c->diffBuf, c->dDiffOff, forceRebuild,
+      publish ? PublishArgs{c->hostSt, c->devSeq, c->hostSeq, c->nrep} : PublishArgs{}));
   MCK(cudaGetLastError());
   return SG_OK;
 }
