@@ -667,7 +667,9 @@ extern "C" int sg_get_state(sg_ctx *c, int rep, sg_float4 *r, sg_float3 *v, sg_f
 }
 
 // ---- launch sequences ---------------------------------------------------------------------
-enum { V_SHEAR = 1, V_RDF = 2, V_RDF_ZERO = 4, G_FROM_HOST = 256 };  // graph keys: a step variant, | G_FROM_HOST
+// graph keys: a step variant, | G_FROM_HOST (upload from hostGraphBufs, step, publish) or
+// | G_PUBLISH (a MIXED step whose reduction publishes the replica states)
+enum { V_SHEAR = 1, V_RDF = 2, V_RDF_ZERO = 4, G_FROM_HOST = 256, G_PUBLISH = 512 };
 
 #define LAUNCH_OK() CK(cudaGetLastError())
 
@@ -841,18 +843,21 @@ static void advanceSchedule(sg_ctx *c, int variant, bool *rdfPrint) {
   }
 }
 
+// variant | G_PUBLISH: the step's reduction also publishes the replica states (MIXED only).
 static int launchStep(sg_ctx *c, int variant) {
+  const bool publish = (variant & G_PUBLISH) != 0;
+  const int v = variant & ~G_PUBLISH;
   if (!c->opt.use_graphs || c->persistent) {  // the persistent step is one launch: no graph
     c->lastVariant = variant;
     if (c->persistent) c->kernelsPerVariant[variant] = 1 + ((variant & V_SHEAR) ? 1 : 0) +
                                                        ((variant & V_RDF) ? 1 + (c->histExt ? 1 : 0) : 0);
-    return enqueueStep(c, variant);
+    return enqueueStep(c, v, nullptr, nullptr, nullptr, publish);
   }
   auto it = c->graphs.find(variant);
   if (it == c->graphs.end()) {
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    int rc = enqueueStep(c, variant);
+    int rc = enqueueStep(c, v, nullptr, nullptr, nullptr, publish);
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     if (rc) {
       if (e == cudaSuccess) cudaGraphDestroy(g);
@@ -944,16 +949,26 @@ static int waitPublished(sg_ctx *c) {
   return flagsFromMirror(c);
 }
 
+// The steps, then the replica states published to the host mirror.  In MIXED, when the last
+// step has no shear or RDF work (nothing after its reduction), that reduction publishes them;
+// otherwise the publish kernel runs after the steps (and alone for nsteps = 0).
 extern "C" int sg_step(sg_ctx *c, int nsteps) {
   if (!c) return sg_fail(SG_ERR_INVALID, "null context");
+  bool published = false;
   for (int s = 0; s < nsteps; s++) {
     const int v = stepVariant(c);
-    int rc = launchStep(c, v);
+    const bool pub = s == nsteps - 1 && c->opt.mode == SG_MODE_MIXED && !c->persistent && c->redTab.n > 0 &&
+                     !(v & (V_SHEAR | V_RDF));
+    int rc = launchStep(c, pub ? (v | G_PUBLISH) : v);
     if (rc) return rc;
     advanceSchedule(c, v, nullptr);
+    published = pub;
   }
-  const int rc = enqueuePublish(c);
-  return rc ? rc : waitPublished(c);
+  if (!published) {
+    const int rc = enqueuePublish(c);
+    if (rc) return rc;
+  }
+  return waitPublished(c);
 }
 
 extern "C" long long sg_step_readback_bytes(const sg_ctx *c) {
