@@ -139,6 +139,32 @@ def test_published_record_is_the_current_step_over_many_calls(mode):
 
 
 @pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_MIXED])
+def test_published_records_of_every_replica(mode):
+    """Five uneven replicas in one context: the record sg_step_thermo returns for each replica in
+    turn, over 120 single-step calls (RDF steps among them; in MIXED most steps' reductions
+    publish the records themselves, each replica's last block its own), equals sg_get_thermo's
+    after a stream synchronisation, and single steps from host buffers publish every replica's
+    record the same way."""
+    systems = workloads.batched(n=5, seed=6, steps=5000)
+    sim = Simulation([s[0] for s in systems], mode=mode)
+    for k, (p, r, v) in enumerate(systems):
+        sim.set_state(r, v, np.zeros((p.nMol, 3), np.float32), rep=k)
+    for i in range(120):
+        k = i % 5
+        t1 = sim.step_thermo(1, rep=k)
+        t2 = sim.thermo(k)
+        assert t1.stepCount == t2.stepCount == i + 1, (i, k)
+        _same_thermo(t1, t2)
+    hr, hv, ha = (np.ascontiguousarray(x) for x in sim.get_state())
+    for i in range(10):
+        t1 = sim.step_from_host(hr, hv, ha, nsteps=1, thermo_rep=i % 5)
+        t2 = sim.thermo(i % 5)
+        assert t1.stepCount == t2.stepCount == 121 + i, i
+        _same_thermo(t1, t2)
+    sim.close()
+
+
+@pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_MIXED])
 def test_page_locked_block_equals_pageable_arrays(mode):
     """r, v, a as views of one page-locked block are read in place by the upload kernel,
     pageable arrays are copied first: the state and the trajectory are the same."""
