@@ -668,7 +668,7 @@ extern "C" int sg_get_state(sg_ctx *c, int rep, sg_float4 *r, sg_float3 *v, sg_f
 
 // ---- launch sequences ---------------------------------------------------------------------
 // graph keys: a step variant, | G_FROM_HOST (upload from hostGraphBufs, step, publish) or
-// | G_PUBLISH (a MIXED step whose reduction publishes the replica states)
+// | G_PUBLISH (a step whose reduction publishes the replica states)
 enum { V_SHEAR = 1, V_RDF = 2, V_RDF_ZERO = 4, G_FROM_HOST = 256, G_PUBLISH = 512 };
 
 #define LAUNCH_OK() CK(cudaGetLastError())
@@ -750,7 +750,7 @@ static void phaseMark(sg_ctx *c, int k) {
 
 // One step, enqueued; with host arrays (MIXED, all replicas) the integrator starts from them.
 // hostR/V/A (MIXED, all replicas): the integrator reads the step's state from these host arrays.
-// publish (MIXED): the reduction's last blocks publish the replica states (no publish kernel).
+// publish: the reduction's last blocks publish the replica states (no publish kernel).
 static int enqueueStep(sg_ctx *c, int variant, const sg_float4 *hostR = nullptr, const sg_float3 *hostV = nullptr,
                        const sg_float3 *hostA = nullptr, bool publish = false) {
   int rc;
@@ -786,7 +786,9 @@ static int enqueueStep(sg_ctx *c, int variant, const sg_float4 *hostR = nullptr,
   } else {
     CK(launchK(c->pdl, k_step_reduce, c->redTab.n, kRedThreads, 0, c->stream, c->redTab.view(), c->rc, c->st, c->pos, c->vel, c->acc,
                                                               c->fric, c->partial, c->dRedFirst, c->diffBuf,
-                                                              c->dDiffOff, fr));
+                                                              c->dDiffOff, fr,
+                                                              publish ? PublishArgs{c->hostSt, c->devSeq, c->hostSeq, c->nrep}
+                                                                      : PublishArgs{}));
     LAUNCH_OK();
   }
   phaseMark(c, 5);
@@ -843,7 +845,7 @@ static void advanceSchedule(sg_ctx *c, int variant, bool *rdfPrint) {
   }
 }
 
-// variant | G_PUBLISH: the step's reduction also publishes the replica states (MIXED only).
+// variant | G_PUBLISH: the step's reduction also publishes the replica states.
 static int launchStep(sg_ctx *c, int variant) {
   const bool publish = (variant & G_PUBLISH) != 0;
   const int v = variant & ~G_PUBLISH;
@@ -949,16 +951,15 @@ static int waitPublished(sg_ctx *c) {
   return flagsFromMirror(c);
 }
 
-// The steps, then the replica states published to the host mirror.  In MIXED, when the last
-// step has no shear or RDF work (nothing after its reduction), that reduction publishes them;
-// otherwise the publish kernel runs after the steps (and alone for nsteps = 0).
+// The steps, then the replica states published to the host mirror.  When the last step has no
+// shear or RDF work (nothing after its reduction), that reduction publishes them; otherwise the
+// publish kernel runs after the steps (and alone for nsteps = 0).
 extern "C" int sg_step(sg_ctx *c, int nsteps) {
   if (!c) return sg_fail(SG_ERR_INVALID, "null context");
   bool published = false;
   for (int s = 0; s < nsteps; s++) {
     const int v = stepVariant(c);
-    const bool pub = s == nsteps - 1 && c->opt.mode == SG_MODE_MIXED && !c->persistent && c->redTab.n > 0 &&
-                     !(v & (V_SHEAR | V_RDF));
+    const bool pub = s == nsteps - 1 && !c->persistent && c->redTab.n > 0 && !(v & (V_SHEAR | V_RDF));
     int rc = launchStep(c, pub ? (v | G_PUBLISH) : v);
     if (rc) return rc;
     advanceSchedule(c, v, nullptr);
@@ -985,9 +986,9 @@ extern "C" int sg_step_thermo(sg_ctx *c, int nsteps, int rep, sg_thermo *t) {
 
 // One step from host buffers as one graph launch: the upload, the step's kernels and the
 // publish.  In MIXED with all replicas uploaded the integrator reads the buffers itself (no
-// upload kernel), and in a step without shear or RDF work (nothing after the reduction) the
-// reduction's last blocks publish the states themselves (no publish kernel); otherwise the
-// upload kernel runs first and the publish kernel last.  The graph holds the buffers'
+// upload kernel; otherwise the upload kernel runs first), and in a step without shear or RDF
+// work (nothing after the reduction) the reduction's last blocks publish the states themselves
+// (no publish kernel; otherwise the publish kernel runs last).  The graph holds the buffers'
 // addresses only (read when it runs, through the host's page tables), so calls with the same
 // buffers -- a caller's loop -- replay it; other buffers replace the context's graphs of this
 // kind.
@@ -1011,9 +1012,11 @@ static int launchStepFromHost(sg_ctx *c, int rep, const sg_float4 *r, const sg_f
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     const bool fused = c->opt.mode == SG_MODE_MIXED && rep == -1;
-    const bool pubInReduce = fused && c->redTab.n > 0 && !(variant & (V_SHEAR | V_RDF));
+    const bool pubInReduce = c->redTab.n > 0 && !(variant & (V_SHEAR | V_RDF));
     int rc = fused ? SG_OK : enqueueSetState(c, rep, r, v, a);
-    if (!rc) rc = fused ? enqueueStep(c, variant, r, v, a, pubInReduce) : enqueueStep(c, variant);
+    if (!rc)
+      rc = fused ? enqueueStep(c, variant, r, v, a, pubInReduce)
+                 : enqueueStep(c, variant, nullptr, nullptr, nullptr, pubInReduce);
     if (!rc && !pubInReduce) rc = enqueuePublish(c);
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     if (rc) {

@@ -67,7 +67,7 @@ __global__ void k_cmvel(BlockTab tab, const RepConst *rc, RepState *st, const fl
 __global__ void k_step_reduce(BlockTab tab, const RepConst *rc, RepState *st, const float4 *pos,
                               float4 *vel, const float4 *acc, const float *fric, float *partial,
                               const int *redFirst, float *diffBuf, const size_t *diffOff,
-                              int forceRebuild);
+                              int forceRebuild, PublishArgs pub);
 __global__ void k_shear(BlockTab tab, const RepConst *rc, RepState *st, const float4 *pos,
                         float4 *acc);
 __global__ void k_rdf(BlockTab tab, const RepConst *rc, RepState *st, const float4 *pos,

@@ -668,7 +668,7 @@ __global__ void __launch_bounds__(kRedThreads) k_step_reduce(
     BlockTab tab, const RepConst *__restrict__ rc, RepState *st, const float4 *__restrict__ pos,
     float4 *__restrict__ vel, const float4 *__restrict__ acc, const float *__restrict__ fric,
     float *__restrict__ partial, const int *__restrict__ redFirst, float *__restrict__ diffBuf,
-    const size_t *__restrict__ diffOff, int forceRebuild) {
+    const size_t *__restrict__ diffOff, int forceRebuild, PublishArgs pub) {
   pdlEnter();
   const int rep = tab.rep[blockIdx.x];
   const RepConst &P = rc[rep];
@@ -759,6 +759,7 @@ __global__ void __launch_bounds__(kRedThreads) k_step_reduce(
   if (t == 0) sS.redCounter = 0;  // every block has counted in: ready for the next step
   stepControl(sP, &sS, redv, diffBuf ? diffBuf + diffOff[rep] : nullptr, forceRebuild);
   stateFromShared(&sS, S);
+  if (pub.hostSt) publishReplica(&sS, rep, pub);
 }
 
 // Nint of ComputeDefs.h:70-71 (evaluated in double because of the 0.5 literal).

@@ -247,11 +247,11 @@ def test_step_from_host_loop_on_the_same_buffers(mode):
         t2 = two.thermo()
         assert t1.stepCount == t2.stepCount == warm + k + 1
         _same_thermo(t1, t2)
-        # the call's graph: the step's kernels, the publish kernel and the upload kernel in PLAIN;
-        # in MIXED the integrator reads the buffers itself and, in a step without RDF work, the
-        # reduction publishes the record itself
+        # the call's graph: the step's kernels and the upload kernel (in MIXED the integrator
+        # reads the buffers itself); the publish kernel only in an RDF step (otherwise the
+        # reduction publishes the record itself)
         rdf_step = t1.stepCount % p.stepRdf == 0
-        extra = (1 if rdf_step else 0) if mode == MODE_MIXED else 2
+        extra = (1 if rdf_step else 0) + (0 if mode == MODE_MIXED else 1)
         assert one.kernels_per_step() == two.kernels_per_step() + extra, k
     for x, y in zip(one.get_state(), two.get_state()):
         assert np.array_equal(x, y)
