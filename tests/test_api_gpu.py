@@ -165,6 +165,24 @@ def test_published_records_of_every_replica(mode):
 
 
 @pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_MIXED])
+def test_record_after_launch_only_steps(mode):
+    """Steps launched without a wait (sg_step_async) publish nothing; a call with no steps
+    (sg_step_thermo with nsteps 0: the publish kernel alone) then returns the last of them,
+    equal to sg_get_thermo's."""
+    p, r, v = workloads.small(seed=65)
+    sim = Simulation(p, mode=mode)
+    sim.set_state(r, v, np.zeros((p.nMol, 3), np.float32))
+    for n in (7, 1, 93):  # the last batch crosses the RDF step 100
+        sim.step_async(n)
+        t1 = sim.step_thermo(0)
+        t2 = sim.thermo()
+        assert t1.stepCount == t2.stepCount
+        _same_thermo(t1, t2)
+    assert sim.thermo().stepCount == 101
+    sim.close()
+
+
+@pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_MIXED])
 def test_page_locked_block_equals_pageable_arrays(mode):
     """r, v, a as views of one page-locked block are read in place by the upload kernel,
     pageable arrays are copied first: the state and the trajectory are the same."""
