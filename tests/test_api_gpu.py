@@ -183,6 +183,31 @@ def test_record_after_launch_only_steps(mode):
 
 
 @pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_MIXED])
+def test_steps_without_graphs_equal_steps_with_graphs(mode):
+    """use_graphs = 0 enqueues each step's kernels one by one (the publish folded into the last
+    step's reduction all the same): the same states and records as the graphs, over single-step
+    calls, a batch of steps across an RDF step and steps from host buffers."""
+    p, r, v = workloads.small(seed=66)
+    a0 = np.zeros((p.nMol, 3), np.float32)
+    sims = [Simulation(p, mode=mode, use_graphs=g) for g in (True, False)]
+    for sim in sims:
+        sim.set_state(r, v, a0)
+    for i in range(5):
+        t = [sim.step_thermo(1) for sim in sims]
+        _same_thermo(t[0], t[1])
+    t = [sim.step_thermo(97) for sim in sims]  # through the RDF step 100
+    _same_thermo(t[0], t[1])
+    hr, hv, ha = (np.ascontiguousarray(x) for x in sims[0].get_state())
+    for i in range(3):
+        t = [sim.step_from_host(hr, hv, ha, nsteps=1) for sim in sims]
+        _same_thermo(t[0], t[1])
+    for x, y in zip(sims[0].get_state(), sims[1].get_state()):
+        assert np.array_equal(x, y)
+    for sim in sims:
+        sim.close()
+
+
+@pytest.mark.parametrize("mode", [MODE_PLAIN, MODE_MIXED])
 def test_page_locked_block_equals_pageable_arrays(mode):
     """r, v, a as views of one page-locked block are read in place by the upload kernel,
     pageable arrays are copied first: the state and the trajectory are the same."""
